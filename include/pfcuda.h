@@ -1,0 +1,187 @@
+/*
+ * pfcuda.h - C-ABI of the GB300 (sm_103a) GPU-driven fill pipeline.
+ *
+ * The pipeline replaces the stages of pathfinder-cpp's GpuDriven renderer
+ * (RendererD3D11::draw, pathfinder/core/d3d11/renderer.cpp:302-336, and the
+ * compute shaders pathfinder/shaders/d3d11/{bound,dice,bin,propagate,sort,
+ * fill,tile}.comp) with hand-written CUDA kernels, and computes the integer
+ * tile data with the semantics of the reference's CPU tiler
+ * (pathfinder/core/d3d9/tiler.cpp, object_builder.cpp, scene_builder.cpp).
+ *
+ * Conventions
+ *  - Every entry point returns an int status: PF_OK (0) or a pf_status > 0.
+ *    Nothing aborts; the last error text of a context is pf_last_error().
+ *  - Host arrays passed in are borrowed for the duration of the call only.
+ *  - Device memory is owned by the context.  One context per host thread;
+ *    calls on one context are serialised by the caller.
+ *  - A context works on the CUDA stream given in pf_config (0 = a stream the
+ *    context creates).  Entry points return once their work is queued unless
+ *    they hand results back to host memory, in which case they synchronise.
+ */
+#ifndef PFCUDA_H
+#define PFCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PF_ABI_VERSION 1
+
+typedef enum pf_status {
+    PF_OK = 0,
+    PF_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, malformed offsets */
+    PF_ERR_CUDA = 2,             /* a CUDA runtime call failed                */
+    PF_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed                  */
+    PF_ERR_OVERFLOW = 4,         /* a fixed capacity was exceeded             */
+    PF_ERR_KERNEL_LIMIT = 5,     /* a kernel hit an iteration bound           */
+    PF_ERR_NOT_READY = 6         /* no scene uploaded / nothing rendered yet  */
+} pf_status;
+
+/* Fill rules (pathfinder/core/data/data.h:136-141). */
+#define PF_FILL_NONZERO 0u
+#define PF_FILL_EVEN_ODD 1u
+
+/* Point flags (pathfinder/core/data/data.h:120-129). */
+#define PF_POINT_ON_CURVE 0u
+#define PF_POINT_CONTROL_0 1u
+#define PF_POINT_CONTROL_1 2u
+
+/*
+ * One scene in outline form: the data the reference's Scene holds for its
+ * draw paths (Scene::draw_paths -> DrawPath::outline -> Outline::contours,
+ * pathfinder/core/scene.h, pathfinder/core/data/path.h:11-40,
+ * pathfinder/core/data/contour.h:16-30).  Outlines are already transformed
+ * into canvas space (Canvas::push_path, pathfinder/core/canvas.cpp:180-190).
+ *
+ *   points        [n_points][2] float32, x then y
+ *   point_flags   [n_points]    PF_POINT_*
+ *   contour_start [n_contours + 1]  offsets into points (non-decreasing)
+ *   path_start    [n_paths + 1]     offsets into contours (non-decreasing)
+ *   fill_rule     [n_paths]     PF_FILL_*
+ *   color         [n_paths]     RGBA8 solid paint, red in the low byte;
+ *                               src-over (pathfinder/shaders/d3d11/tile.comp:841)
+ *   width,height  canvas size in pixels (Scene view box = (0,0,width,height);
+ *                 its right edge is rounded up to a multiple of 16 as in
+ *                 Scene::set_view_box, pathfinder/core/scene.cpp:170-179)
+ *   clear_color   RGBA8 colour the destination is cleared to
+ */
+typedef struct pf_scene_view {
+    const float *points;
+    const uint8_t *point_flags;
+    const uint32_t *contour_start;
+    const uint32_t *path_start;
+    const uint8_t *fill_rule;
+    const uint32_t *color;
+    uint32_t n_points;
+    uint32_t n_contours;
+    uint32_t n_paths;
+    float width;
+    float height;
+    uint32_t clear_color;
+} pf_scene_view;
+
+/* Context configuration.  Zero-initialise and set what you need. */
+typedef struct pf_config {
+    int device;            /* CUDA device ordinal                                */
+    void *stream;          /* cudaStream_t to run on; NULL = context-owned stream */
+    uint32_t flags;        /* PF_CONFIG_* bits                                    */
+    uint32_t reserved[8];
+} pf_config;
+
+/* Per-frame counters (host copy).  Times are device milliseconds measured
+ * with CUDA events when PF_CONFIG_STAGE_TIMING is set, else 0. */
+typedef struct pf_frame_stats {
+    uint64_t paths, contours, points, segments;
+    uint64_t microlines;   /* flattened leaf lines (d3d9 recursion leaves)        */
+    uint64_t tiles;        /* tiles in all path tile rects                         */
+    uint64_t fills;        /* fills kept after culling                             */
+    uint64_t alpha_tiles;  /* tiles holding at least one fill                      */
+    uint64_t visible_tiles;/* alpha tiles plus solid tiles with a nonzero backdrop */
+    uint64_t composite_entries; /* (framebuffer tile, path tile) pairs after z-cull */
+    uint64_t framebuffer_tiles;
+    uint32_t overflow;     /* nonzero if a predicted capacity overflowed and the   */
+                           /* frame was re-run by the exact two-pass method        */
+    uint32_t kernel_error; /* nonzero if a kernel hit an iteration bound            */
+    float ms_setup, ms_flatten, ms_bin, ms_propagate, ms_lists, ms_composite, ms_total;
+} pf_frame_stats;
+
+#define PF_CONFIG_STAGE_TIMING 0x1u
+
+/*
+ * Canonical integer output of one scene (host memory, owned by the context
+ * until the next call on it).  Tiles are numbered path-major and row-major
+ * inside each path's tile rect (BuiltPath::tile_bounds,
+ * pathfinder/core/data/built_path.cpp:8-34).  Fills are grouped by tile and
+ * sorted inside a tile by (from_x, from_y, to_x, to_y) as u16.
+ */
+typedef struct pf_canon {
+    uint32_t n_paths;
+    const int32_t *path_rect;          /* [n_paths][4] x0,y0,x1,y1 tile rect    */
+    const uint64_t *path_tile_first;   /* [n_paths + 1]                         */
+    const uint64_t *path_column_first; /* [n_paths + 1]                         */
+    uint64_t n_tiles;
+    const uint8_t *tile_alpha;         /* [n_tiles] 1 = alpha tile              */
+    const int8_t *tile_backdrop;       /* [n_tiles] propagated backdrop (int8)  */
+    const uint32_t *tile_fill_count;   /* [n_tiles]                             */
+    uint64_t n_fills;
+    const uint16_t *fills;             /* [n_fills][4] from_x,from_y,to_x,to_y  */
+    uint64_t n_columns;
+    const int32_t *column_backdrop;    /* [n_columns] final column sums (int32) */
+    uint32_t fb_tiles_x, fb_tiles_y;
+    const int32_t *z;                  /* [fb tiles] topmost occluding path, -1 */
+    const uint64_t *fb_list_first;     /* [fb tiles + 1]                        */
+    uint64_t n_list;
+    const uint32_t *fb_list;           /* global tile indices, back to front    */
+} pf_canon;
+
+/* Library and device queries. */
+int pf_abi_version(void);
+int pf_device_count(int *count);
+
+/* Context lifetime. */
+int pf_ctx_create(const pf_config *config, void **ctx);
+int pf_ctx_destroy(void *ctx);
+const char *pf_last_error(void *ctx);
+
+/*
+ * Upload one scene (H2D copies on the context stream).  Replaces
+ * SceneBuilderD3D11::build's CPU packing (pathfinder/core/d3d11/scene_builder.cpp:209-223):
+ * segment extraction, bounds and tile rects are computed on the GPU.
+ */
+int pf_scene_upload(void *ctx, const pf_scene_view *scene);
+
+/*
+ * Render the uploaded scene with the exact two-pass method (count, size,
+ * write), leaving the RGBA8 image on the device.  Replaces
+ * RendererD3D11::draw (pathfinder/core/d3d11/renderer.cpp:302-336).
+ * stats may be NULL.
+ */
+int pf_render(void *ctx, pf_frame_stats *stats);
+
+/* Copy the last rendered image to host memory: RGBA8, row-major,
+ * width_px * height_px * 4 bytes with width_px = ceil(width). */
+int pf_read_image(void *ctx, uint8_t *rgba, size_t capacity_bytes);
+
+/* Device pointer and pitch of the last rendered image (valid until the next
+ * render on this context). */
+int pf_image_device_ptr(void *ctx, void **rgba, uint32_t *width_px, uint32_t *height_px);
+
+/* Canonical integer output of the last rendered scene (synchronises). */
+int pf_read_canon(void *ctx, pf_canon *out);
+
+/*
+ * One call that uploads, renders and reads back: the per-frame work of
+ * Canvas::draw (pathfinder/core/canvas.cpp:557-567) from host buffers to a
+ * host image.
+ */
+int pf_draw(void *ctx, const pf_scene_view *scene, uint8_t *rgba, size_t capacity_bytes,
+            pf_frame_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFCUDA_H */

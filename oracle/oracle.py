@@ -1,0 +1,187 @@
+"""ctypes front end of the CPU oracle.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and bench.py's
+CPU-baseline leg, as the checker or the timed CPU baseline.  The product path
+never imports this module.
+
+``restated``  -> oracle/_build/libpforacle.so, the plain-C restatement
+                 (pf_oracle.c) of the reference's d3d9 CPU tiler plus the FP64
+                 coverage / composite oracle.
+``reference`` -> oracle/_ref/libpfref.so, the reference's own tiler compiled
+                 from its sources (only where the reference tree exists).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Dict, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_ORACLE = os.path.join(HERE, "_build", "libpforacle.so")
+LIB_REF = os.path.join(HERE, "_ref", "libpfref.so")
+REF_ROOT = os.environ.get("PF_REFERENCE_ROOT", "/root/reference")
+
+Z_D3D9 = 0
+Z_D3D11 = 1
+
+
+class SceneView(C.Structure):
+    _fields_ = [
+        ("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_start", C.c_void_p),
+        ("path_start", C.c_void_p), ("fill_rule", C.c_void_p), ("color", C.c_void_p),
+        ("n_points", C.c_uint32), ("n_contours", C.c_uint32), ("n_paths", C.c_uint32),
+        ("width", C.c_float), ("height", C.c_float), ("clear_color", C.c_uint32),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("n_paths", C.c_uint32), ("path_rect", C.c_void_p), ("path_tile_first", C.c_void_p),
+        ("path_column_first", C.c_void_p), ("n_tiles", C.c_uint64), ("tile_alpha", C.c_void_p),
+        ("tile_backdrop", C.c_void_p), ("tile_fill_count", C.c_void_p), ("n_fills", C.c_uint64),
+        ("fills", C.c_void_p), ("n_columns", C.c_uint64), ("column_backdrop", C.c_void_p),
+        ("fb_tiles_x", C.c_uint32), ("fb_tiles_y", C.c_uint32), ("z", C.c_void_p),
+        ("fb_list_first", C.c_void_p), ("n_list", C.c_uint64), ("fb_list", C.c_void_p),
+        ("n_microlines", C.c_uint64), ("path_microlines", C.c_void_p), ("path_fills", C.c_void_p),
+    ]
+
+
+def scene_view(scene) -> "tuple[SceneView, list]":
+    """Build a pf_scene_view over a scenes.Scene; returns (view, keepalive)."""
+    arrs = [np.ascontiguousarray(scene.points, np.float32), np.ascontiguousarray(scene.flags, np.uint8),
+            np.ascontiguousarray(scene.contour_start, np.uint32),
+            np.ascontiguousarray(scene.path_start, np.uint32),
+            np.ascontiguousarray(scene.fill_rule, np.uint8), np.ascontiguousarray(scene.color, np.uint32)]
+    v = SceneView(*(a.ctypes.data for a in arrs), scene.n_points, scene.n_contours, scene.n_paths,
+                  scene.width, scene.height, scene.clear)
+    return v, arrs
+
+
+def _arr(ptr, n, dtype):
+    if n == 0 or not ptr:
+        return np.zeros(0, dtype)
+    buf = (C.c_char * (int(n) * np.dtype(dtype).itemsize)).from_address(ptr)
+    return np.frombuffer(buf, dtype=dtype).copy()
+
+
+def result_to_dict(r: Result) -> Dict[str, np.ndarray]:
+    nfb = r.fb_tiles_x * r.fb_tiles_y
+    d = {
+        "path_rect": _arr(r.path_rect, 4 * r.n_paths, np.int32).reshape(-1, 4),
+        "path_tile_first": _arr(r.path_tile_first, r.n_paths + 1, np.uint64),
+        "path_column_first": _arr(r.path_column_first, r.n_paths + 1, np.uint64),
+        "tile_alpha": _arr(r.tile_alpha, r.n_tiles, np.uint8),
+        "tile_backdrop": _arr(r.tile_backdrop, r.n_tiles, np.int8),
+        "tile_fill_count": _arr(r.tile_fill_count, r.n_tiles, np.uint32),
+        "fills": _arr(r.fills, 4 * r.n_fills, np.uint16).reshape(-1, 4),
+        "column_backdrop": _arr(r.column_backdrop, r.n_columns, np.int32),
+        "fb_tiles": np.array([r.fb_tiles_x, r.fb_tiles_y], np.uint32),
+        "z": _arr(r.z, nfb, np.int32),
+        "fb_list_first": _arr(r.fb_list_first, nfb + 1, np.uint64),
+        "fb_list": _arr(r.fb_list, r.n_list, np.uint32),
+    }
+    if r.path_fills:
+        d["path_fills"] = _arr(r.path_fills, r.n_paths, np.uint32)
+    if r.path_microlines:
+        d["path_microlines"] = _arr(r.path_microlines, r.n_paths, np.uint32)
+    return d
+
+
+def build(reference: bool = False, quiet: bool = True) -> None:
+    """Compile the restatement (and, if asked and possible, the reference harness)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.run(["make", "-C", HERE, "all"], check=True, stdout=out)
+    if reference and os.path.isdir(os.path.join(REF_ROOT, "pathfinder")):
+        subprocess.run(["make", "-C", HERE, "ref", "-j8", f"REF_ROOT={REF_ROOT}"], check=True, stdout=out)
+
+
+_libs: Dict[str, C.CDLL] = {}
+
+
+def _lib(path: str) -> C.CDLL:
+    if path not in _libs:
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"{path} is not built (run oracle.build())")
+        lib = C.CDLL(path)
+        _libs[path] = lib
+    return _libs[path]
+
+
+def have_reference() -> bool:
+    return os.path.exists(LIB_REF)
+
+
+def tile_scene(scene, z_rule: int = Z_D3D11) -> Dict[str, np.ndarray]:
+    """Restated d3d9 tiler over a scene: canonical integer outputs."""
+    lib = _lib(LIB_ORACLE)
+    v, keep = scene_view(scene)
+    r = Result()
+    st = lib.pfo_tile_scene(C.byref(v), C.c_int(z_rule), C.byref(r))
+    if st != 0:
+        raise RuntimeError(f"pfo_tile_scene failed with status {st}")
+    try:
+        d = result_to_dict(r)
+        d["n_microlines"] = int(r.n_microlines)
+        return d
+    finally:
+        lib.pfo_free(C.byref(r))
+
+
+def reference_tile_scene(scene) -> Dict[str, np.ndarray]:
+    """The reference's own tiler (z rule D3D9) over a scene."""
+    lib = _lib(LIB_REF)
+    v, keep = scene_view(scene)
+    r = Result()
+    st = lib.pfref_tile_scene(C.byref(v), C.byref(r))
+    if st != 0:
+        raise RuntimeError(f"pfref_tile_scene failed with status {st}")
+    try:
+        return result_to_dict(r)
+    finally:
+        lib.pfref_free(C.byref(r))
+
+
+def render(scene, z_rule: int = Z_D3D11, threads: int = 1, coverage: bool = False,
+           tiled: Optional[Dict[str, np.ndarray]] = None):
+    """FP64 analytic-area coverage + src-over composite; returns (rgba u8 [H,W,4], coverage|None)."""
+    lib = _lib(LIB_ORACLE)
+    v, keep = scene_view(scene)
+    r = Result()
+    st = lib.pfo_tile_scene(C.byref(v), C.c_int(z_rule), C.byref(r))
+    if st != 0:
+        raise RuntimeError(f"pfo_tile_scene failed with status {st}")
+    try:
+        w = int(np.ceil(scene.width))
+        h = int(np.ceil(scene.height))
+        rgba = np.zeros((h, w, 4), np.uint8)
+        cov = np.zeros((int(r.n_tiles), 16, 16), np.float32) if coverage else None
+        st = lib.pfo_render(C.byref(v), C.byref(r), C.c_void_p(rgba.ctypes.data),
+                            C.c_void_p(cov.ctypes.data if cov is not None else 0), C.c_int(threads))
+        if st != 0:
+            raise RuntimeError(f"pfo_render failed with status {st}")
+        if tiled is not None:
+            tiled.update(result_to_dict(r))
+        return rgba, cov
+    finally:
+        lib.pfo_free(C.byref(r))
+
+
+def composite_lists(d: Dict[str, np.ndarray]):
+    """Per framebuffer tile composite list as a list of int arrays."""
+    first = d["fb_list_first"].astype(np.int64)
+    return [d["fb_list"][first[i]:first[i + 1]] for i in range(len(first) - 1)]
+
+
+def compare(a: Dict[str, np.ndarray], b: Dict[str, np.ndarray], keys=None) -> list:
+    """Names of canonical arrays that differ between two results."""
+    keys = keys or ["path_rect", "path_tile_first", "path_column_first", "tile_alpha",
+                    "tile_backdrop", "tile_fill_count", "fills", "column_backdrop", "fb_tiles",
+                    "fb_list_first", "fb_list"]
+    bad = []
+    for k in keys:
+        if a[k].shape != b[k].shape or not np.array_equal(a[k], b[k]):
+            bad.append(k)
+    return bad

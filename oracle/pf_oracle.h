@@ -1,0 +1,80 @@
+/*
+ * pf_oracle.h - CPU oracle for the GPU-driven fill pipeline.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing on the product path links, loads or
+ * calls this code; only tests/, the smoke check and bench.py's CPU-baseline
+ * leg use it, and only as the checker or the timed CPU baseline.
+ *
+ * Two implementations fill the same pfo_result:
+ *   - pf_oracle.c    : a plain-C restatement of the reference's d3d9 CPU tiler
+ *                      (libpforacle.so, built everywhere);
+ *   - ref_harness.cpp: the reference's own Tiler/ObjectBuilder/SceneBuilderD3D9
+ *                      compiled from its sources (oracle/_ref/libpfref.so, built
+ *                      only where the reference tree is present).
+ */
+#ifndef PF_ORACLE_H
+#define PF_ORACLE_H
+
+#include <stdint.h>
+
+#include "../include/pfcuda.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* z-buffer rule.  D3D9: every solid tile of an opaque path occludes
+ * (pathfinder/core/d3d9/scene_builder.cpp:57-78).  D3D11: solid tiles that the
+ * even-odd rule leaves empty (even backdrop) do not occlude
+ * (pathfinder/shaders/d3d11/propagate.comp:190-198). */
+#define PFO_Z_D3D9 0
+#define PFO_Z_D3D11 1
+
+typedef struct pfo_result {
+    uint32_t n_paths;
+    int32_t *path_rect;          /* [n_paths][4] */
+    uint64_t *path_tile_first;   /* [n_paths + 1] */
+    uint64_t *path_column_first; /* [n_paths + 1] */
+    uint64_t n_tiles;
+    uint8_t *tile_alpha;
+    int8_t *tile_backdrop;
+    uint32_t *tile_fill_count;
+    uint64_t n_fills;
+    uint16_t *fills;             /* [n_fills][4], grouped by tile, sorted inside a tile */
+    uint64_t n_columns;
+    int32_t *column_backdrop;
+    uint32_t fb_tiles_x, fb_tiles_y;
+    int32_t *z;                  /* [fb tiles], -1 = no occluder */
+    uint64_t *fb_list_first;     /* [fb tiles + 1] */
+    uint64_t n_list;
+    uint32_t *fb_list;
+    uint64_t n_microlines;       /* flattened leaf lines that reached the tile walk */
+    uint32_t *path_microlines;   /* [n_paths] leaf lines per path */
+    uint32_t *path_fills;        /* [n_paths] fills per path */
+} pfo_result;
+
+/* Restated tiler: flatten, bin, propagate, z-buffer, composite lists. */
+int pfo_tile_scene(const pf_scene_view *scene, int z_rule, pfo_result *out);
+
+/*
+ * FP64 analytic-area coverage and src-over composite of a tiled scene.
+ * rgba: width_px*height_px*4 bytes (RGBA8).  coverage_f (optional, may be
+ * NULL): [n_tiles*256] float coverage of every alpha tile after the fill
+ * rule, row-major 16x16 (solid and empty tiles are left untouched).
+ * first_tile/n_tiles_limit restrict the coverage pass to a tile range (use
+ * 0 and UINT64_MAX for all).  threads: worker threads (>= 1).
+ */
+int pfo_render(const pf_scene_view *scene, const pfo_result *tiled, uint8_t *rgba,
+               float *coverage_f, int threads);
+
+void pfo_free(pfo_result *r);
+
+/* Reference harness (oracle/_ref/libpfref.so): same output, z rule D3D9. */
+int pfref_tile_scene(const pf_scene_view *scene, pfo_result *out);
+void pfref_free(pfo_result *r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
