@@ -154,6 +154,12 @@ const char *pf_last_error(void *ctx);
 int pf_scene_upload(void *ctx, const pf_scene_view *scene);
 
 /*
+ * Upload a batch of independent scenes (each keeps its own canvas and image).
+ * Host ranges that are contiguous across scenes are copied with one transfer.
+ */
+int pf_scene_upload_batch(void *ctx, const pf_scene_view *scenes, uint32_t n_scenes);
+
+/*
  * Render the uploaded scene with the exact two-pass method (count, size,
  * write), leaving the RGBA8 image on the device.  Replaces
  * RendererD3D11::draw (pathfinder/core/d3d11/renderer.cpp:302-336).
@@ -165,12 +171,23 @@ int pf_render(void *ctx, pf_frame_stats *stats);
  * width_px * height_px * 4 bytes with width_px = ceil(width). */
 int pf_read_image(void *ctx, uint8_t *rgba, size_t capacity_bytes);
 
+/* Same for scene `scene` of an uploaded batch. */
+int pf_read_image_scene(void *ctx, uint32_t scene, uint8_t *rgba, size_t capacity_bytes);
+
 /* Device pointer and pitch of the last rendered image (valid until the next
  * render on this context). */
 int pf_image_device_ptr(void *ctx, void **rgba, uint32_t *width_px, uint32_t *height_px);
 
 /* Canonical integer output of the last rendered scene (synchronises). */
 int pf_read_canon(void *ctx, pf_canon *out);
+int pf_read_canon_scene(void *ctx, uint32_t scene, pf_canon *out);
+
+/*
+ * Coverage after the fill rule of every alpha tile of scene 0 of the last frame,
+ * in tile order: *n_alpha x 256 floats (row-major 16x16).  With out == NULL only
+ * *n_alpha is set.  A test and debugging aid (the frame itself never stores coverage).
+ */
+int pf_read_coverage(void *ctx, float *out, size_t capacity_floats, uint64_t *n_alpha);
 
 /*
  * One call that uploads, renders and reads back: the per-frame work of

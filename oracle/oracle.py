@@ -114,12 +114,12 @@ def have_reference() -> bool:
     return os.path.exists(LIB_REF)
 
 
-def tile_scene(scene, z_rule: int = Z_D3D11) -> Dict[str, np.ndarray]:
+def tile_scene(scene, z_rule: int = Z_D3D11, threads: int = 1) -> Dict[str, np.ndarray]:
     """Restated d3d9 tiler over a scene: canonical integer outputs."""
     lib = _lib(LIB_ORACLE)
     v, keep = scene_view(scene)
     r = Result()
-    st = lib.pfo_tile_scene(C.byref(v), C.c_int(z_rule), C.byref(r))
+    st = lib.pfo_tile_scene_mt(C.byref(v), C.c_int(z_rule), C.c_int(threads), C.byref(r))
     if st != 0:
         raise RuntimeError(f"pfo_tile_scene failed with status {st}")
     try:
@@ -150,7 +150,7 @@ def render(scene, z_rule: int = Z_D3D11, threads: int = 1, coverage: bool = Fals
     lib = _lib(LIB_ORACLE)
     v, keep = scene_view(scene)
     r = Result()
-    st = lib.pfo_tile_scene(C.byref(v), C.c_int(z_rule), C.byref(r))
+    st = lib.pfo_tile_scene_mt(C.byref(v), C.c_int(z_rule), C.c_int(threads), C.byref(r))
     if st != 0:
         raise RuntimeError(f"pfo_tile_scene failed with status {st}")
     try:

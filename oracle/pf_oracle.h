@@ -53,8 +53,10 @@ typedef struct pfo_result {
     uint32_t *path_fills;        /* [n_paths] fills per path */
 } pfo_result;
 
-/* Restated tiler: flatten, bin, propagate, z-buffer, composite lists. */
+/* Restated tiler: flatten, bin, propagate, z-buffer, composite lists.  The _mt
+ * variant tiles paths on `threads` worker threads (same output). */
 int pfo_tile_scene(const pf_scene_view *scene, int z_rule, pfo_result *out);
+int pfo_tile_scene_mt(const pf_scene_view *scene, int z_rule, int threads, pfo_result *out);
 
 /*
  * FP64 analytic-area coverage and src-over composite of a tiled scene.

@@ -1,0 +1,746 @@
+// pf_api.cu - host side of the fill pipeline: context, device buffers, stage order,
+// and the C-ABI of include/pfcuda.h.
+//
+// The exact two-pass frame (pf_render) is the reference's count-then-allocate loop
+// (RendererD3D11::prepare_tiles, pathfinder/core/d3d11/renderer.cpp:510-616) done with
+// exact counts: every stage that appends (segments, leaf lines, fills, composite-list
+// entries) first counts on the GPU, the counts are scanned into offsets, the host reads
+// the total and grows the buffer, and the second pass writes into place.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/pfcuda.h"
+#include "pf_internal.h"
+
+using namespace pfc;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes + bytes / 4, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        cap = want;
+        return cudaSuccess;
+    }
+    template <class T>
+    T *as() const {
+        return static_cast<T *>(p);
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct HostCanon {
+    std::vector<int32_t> rect;
+    std::vector<uint64_t> tile_first, col_first;
+    std::vector<uint8_t> alpha;
+    std::vector<int8_t> backdrop;
+    std::vector<uint32_t> fill_count;
+    std::vector<uint16_t> fills;
+    std::vector<int32_t> col_backdrop;
+    std::vector<int32_t> z;
+    std::vector<uint64_t> list_first;
+    std::vector<uint32_t> list;
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint32_t flags = 0;
+    std::string err;
+
+    // inputs
+    DevBuf points, pflags, cstart, pstart, fill_rule, color, scenes, scene_path_first, scene_contour_first,
+        scene_fb_first;
+    std::vector<SceneDev> h_scenes;
+    std::vector<uint32_t> h_scene_fb_first;
+    uint32_t n_scenes = 0, n_paths = 0, n_contours = 0, n_points = 0, n_fb = 0;
+    uint64_t image_bytes = 0;
+    bool uploaded = false, rendered = false;
+
+    // working buffers
+    DevBuf contour_point_first, contour_path, paths, path_tiles, path_cols, contour_segs, path_contours;
+    DevBuf segs, seg_leaves, leaves, leaf_path;
+    DevBuf tile_fills, tile_cursor, tile_delta, tile_backdrop, tile_path, col_above, col_final, fills;
+    DevBuf z, fb_count, fb_cursor, list, image, status, scan_temp;
+    uint32_t *h_status = nullptr;  // pinned
+
+    // totals of the last frame
+    uint32_t n_segs = 0, n_tiles = 0, n_cols = 0, n_leaves = 0, n_fills = 0, n_list = 0;
+
+    HostCanon canon;
+    cudaEvent_t ev[8] = {};
+};
+
+thread_local std::string g_last_error;
+
+int fail(Ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(Ctx *c, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(c, e == cudaErrorMemoryAllocation ? PF_ERR_OUT_OF_MEMORY : PF_ERR_CUDA, m);
+}
+
+#define PF_CUDA(call)                                              \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call);     \
+    } while (0)
+
+float view_box_right(float width) {
+    // Scene::set_view_box: right = round_up(ceil(right), 16) (pathfinder/core/scene.cpp:175)
+    int32_t w = (int32_t)std::ceil(width);
+    int32_t rem = std::abs(w) % kTile;
+    if (rem != 0) w = w < 0 ? w + rem : w + kTile - rem;
+    return (float)w;
+}
+
+int validate_scene(Ctx *c, const pf_scene_view *s) {
+    if (!s) return fail(c, PF_ERR_INVALID_ARGUMENT, "scene is null");
+    if (!(s->width > 0.0f) || !(s->height > 0.0f) || !std::isfinite(s->width) || !std::isfinite(s->height) ||
+        s->width > 65536.0f || s->height > 65536.0f)
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "canvas size must be finite, positive and at most 65536");
+    if (!s->path_start || !s->contour_start)
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "path_start and contour_start are required");
+    if (s->n_paths && (!s->fill_rule || !s->color))
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "fill_rule and color are required");
+    if (s->n_points && (!s->points || !s->point_flags))
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "points and point_flags are required");
+    if (s->path_start[0] != 0 || s->path_start[s->n_paths] != s->n_contours)
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "path_start must run from 0 to n_contours");
+    if (s->contour_start[0] != 0 || s->contour_start[s->n_contours] != s->n_points)
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "contour_start must run from 0 to n_points");
+    for (uint32_t p = 0; p < s->n_paths; p++)
+        if (s->path_start[p] > s->path_start[p + 1])
+            return fail(c, PF_ERR_INVALID_ARGUMENT, "path_start must be non-decreasing");
+    for (uint32_t k = 0; k < s->n_contours; k++)
+        if (s->contour_start[k] > s->contour_start[k + 1])
+            return fail(c, PF_ERR_INVALID_ARGUMENT, "contour_start must be non-decreasing");
+    return PF_OK;
+}
+
+// Copy n bytes from host to device, merging with the previous copy when the host
+// ranges are contiguous (a batch packed into one host buffer costs one copy per array).
+struct CopyPlan {
+    struct Op {
+        const char *src;
+        char *dst;
+        size_t n;
+    };
+    std::vector<Op> ops;
+    void add(void *dst, const void *src, size_t n) {
+        if (!n) return;
+        const char *s = static_cast<const char *>(src);
+        char *d = static_cast<char *>(dst);
+        if (!ops.empty() && ops.back().src + ops.back().n == s && ops.back().dst + ops.back().n == d) {
+            ops.back().n += n;
+            return;
+        }
+        ops.push_back({s, d, n});
+    }
+    cudaError_t run(cudaStream_t st) {
+        for (auto &o : ops) {
+            cudaError_t e = cudaMemcpyAsync(o.dst, o.src, o.n, cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+};
+
+int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
+    if (!scenes || n == 0) return fail(c, PF_ERR_INVALID_ARGUMENT, "no scenes");
+    uint64_t P = 0, C = 0, N = 0, fb = 0, img = 0, cs = 0, ps = 0;
+    c->h_scenes.assign(n, SceneDev{});
+    c->h_scene_fb_first.assign(n + 1, 0);
+    std::vector<uint32_t> spf(n + 1, 0), scf(n + 1, 0);
+    for (uint32_t i = 0; i < n; i++) {
+        int st = validate_scene(c, &scenes[i]);
+        if (st) return st;
+        const pf_scene_view &s = scenes[i];
+        SceneDev &S = c->h_scenes[i];
+        S.vb_right = view_box_right(s.width);
+        S.vb_bottom = s.height;
+        S.fbw = (uint32_t)std::ceil(S.vb_right / kTile);
+        S.fbh = (uint32_t)std::ceil(s.height / kTile);
+        S.fb_first = (uint32_t)fb;
+        S.img_w = (uint32_t)std::ceil(s.width);
+        S.img_h = (uint32_t)std::ceil(s.height);
+        S.clear = s.clear_color;
+        S.img_offset = img;
+        S.path_first = (uint32_t)N;
+        S.path_end = (uint32_t)(N + s.n_paths);
+        S.contour_first = (uint32_t)C;
+        S.contour_end = (uint32_t)(C + s.n_contours);
+        S.point_first = (uint32_t)P;
+        S.point_end = (uint32_t)(P + s.n_points);
+        S.cstart_base = (uint32_t)cs;
+        S.pstart_base = (uint32_t)ps;
+        spf[i] = (uint32_t)N;
+        scf[i] = (uint32_t)C;
+        c->h_scene_fb_first[i] = (uint32_t)fb;
+        P += s.n_points;
+        C += s.n_contours;
+        N += s.n_paths;
+        fb += uint64_t(S.fbw) * S.fbh;
+        img += uint64_t(S.img_w) * S.img_h * 4;
+        img = (img + 255) & ~uint64_t(255);
+        cs += s.n_contours + 1;
+        ps += s.n_paths + 1;
+    }
+    spf[n] = (uint32_t)N;
+    scf[n] = (uint32_t)C;
+    c->h_scene_fb_first[n] = (uint32_t)fb;
+    if (P >= (1ull << 31) || C >= (1ull << 31) || N >= (1ull << 31) || fb >= (1ull << 31))
+        return fail(c, PF_ERR_OVERFLOW, "batch too large (2^31 points, contours, paths or tiles)");
+    c->n_scenes = n;
+    c->n_points = (uint32_t)P;
+    c->n_contours = (uint32_t)C;
+    c->n_paths = (uint32_t)N;
+    c->n_fb = (uint32_t)fb;
+    c->image_bytes = img;
+
+    PF_CUDA(c->points.ensure(P * 8 + 16));
+    PF_CUDA(c->pflags.ensure(P + 16));
+    PF_CUDA(c->cstart.ensure(cs * 4 + 16));
+    PF_CUDA(c->pstart.ensure(ps * 4 + 16));
+    PF_CUDA(c->fill_rule.ensure(N + 16));
+    PF_CUDA(c->color.ensure(N * 4 + 16));
+    PF_CUDA(c->scenes.ensure(n * sizeof(SceneDev)));
+    PF_CUDA(c->scene_path_first.ensure((n + 1) * 4));
+    PF_CUDA(c->scene_contour_first.ensure((n + 1) * 4));
+    PF_CUDA(c->scene_fb_first.ensure((n + 1) * 4));
+    PF_CUDA(c->image.ensure(img + 256));
+
+    CopyPlan pts, fl, csp, psp, fr, col;
+    for (uint32_t i = 0; i < n; i++) {
+        const pf_scene_view &s = scenes[i];
+        const SceneDev &S = c->h_scenes[i];
+        pts.add(c->points.as<char>() + uint64_t(S.point_first) * 8, s.points, uint64_t(s.n_points) * 8);
+        fl.add(c->pflags.as<char>() + S.point_first, s.point_flags, s.n_points);
+        csp.add(c->cstart.as<char>() + uint64_t(S.cstart_base) * 4, s.contour_start, uint64_t(s.n_contours + 1) * 4);
+        psp.add(c->pstart.as<char>() + uint64_t(S.pstart_base) * 4, s.path_start, uint64_t(s.n_paths + 1) * 4);
+        fr.add(c->fill_rule.as<char>() + S.path_first, s.fill_rule, s.n_paths);
+        col.add(c->color.as<char>() + uint64_t(S.path_first) * 4, s.color, uint64_t(s.n_paths) * 4);
+    }
+    for (CopyPlan *cp : {&pts, &fl, &csp, &psp, &fr, &col}) PF_CUDA(cp->run(c->stream));
+    PF_CUDA(cudaMemcpyAsync(c->scenes.p, c->h_scenes.data(), n * sizeof(SceneDev), cudaMemcpyHostToDevice,
+                            c->stream));
+    PF_CUDA(cudaMemcpyAsync(c->scene_path_first.p, spf.data(), (n + 1) * 4, cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(cudaMemcpyAsync(c->scene_contour_first.p, scf.data(), (n + 1) * 4, cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(cudaMemcpyAsync(c->scene_fb_first.p, c->h_scene_fb_first.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
+                            c->stream));
+    // the host arrays are borrowed only for this call
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    c->uploaded = true;
+    c->rendered = false;
+    return PF_OK;
+}
+
+Batch make_batch(Ctx *c) {
+    Batch b{};
+    b.points = c->points.as<float2>();
+    b.flags = c->pflags.as<uint8_t>();
+    b.contour_start_cat = c->cstart.as<uint32_t>();
+    b.path_start_cat = c->pstart.as<uint32_t>();
+    b.fill_rule = c->fill_rule.as<uint8_t>();
+    b.color = c->color.as<uint32_t>();
+    b.scenes = c->scenes.as<SceneDev>();
+    b.scene_path_first = c->scene_path_first.as<uint32_t>();
+    b.scene_contour_first = c->scene_contour_first.as<uint32_t>();
+    b.n_scenes = c->n_scenes;
+    b.n_paths = c->n_paths;
+    b.n_contours = c->n_contours;
+    b.n_points = c->n_points;
+    b.contour_point_first = c->contour_point_first.as<uint32_t>();
+    b.contour_path = c->contour_path.as<uint32_t>();
+    b.paths = c->paths.as<PathDev>();
+    b.path_tiles = c->path_tiles.as<uint32_t>();
+    b.path_cols = c->path_cols.as<uint32_t>();
+    b.contour_segs = c->contour_segs.as<uint32_t>();
+    b.segs = c->segs.as<SegDev>();
+    b.seg_cap = (uint32_t)std::min<size_t>(c->segs.cap / sizeof(SegDev), 0xffffffffu);
+    b.seg_leaves = c->seg_leaves.as<uint32_t>();
+    b.leaves = c->leaves.as<float4>();
+    b.leaf_path = c->leaf_path.as<uint32_t>();
+    b.leaf_cap = (uint32_t)std::min<size_t>(std::min(c->leaves.cap / 16, c->leaf_path.cap / 4), 0xffffffffu);
+    b.tile_fills = c->tile_fills.as<uint32_t>();
+    b.tile_cursor = c->tile_cursor.as<uint32_t>();
+    b.tile_delta = c->tile_delta.as<int32_t>();
+    b.tile_backdrop = c->tile_backdrop.as<int8_t>();
+    b.tile_path = c->tile_path.as<uint32_t>();
+    b.col_above = c->col_above.as<int32_t>();
+    b.col_final = c->col_final.as<int32_t>();
+    b.fills = c->fills.as<uint2>();
+    b.fill_cap = (uint32_t)std::min<size_t>(c->fills.cap / 8, 0xffffffffu);
+    b.z = c->z.as<int32_t>();
+    b.fb_count = c->fb_count.as<uint32_t>();
+    b.fb_cursor = c->fb_cursor.as<uint32_t>();
+    b.list = c->list.as<uint32_t>();
+    b.list_cap = (uint32_t)std::min<size_t>(c->list.cap / 4, 0xffffffffu);
+    b.n_fb = c->n_fb;
+    b.image = c->image.as<uint8_t>();
+    b.status = c->status.as<uint32_t>();
+    return b;
+}
+
+int read_status(Ctx *c) {
+    PF_CUDA(cudaMemcpyAsync(c->h_status, c->status.p, kStCount * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+int check_kernel_status(Ctx *c) {
+    const uint32_t e = c->h_status[kStErr];
+    if (e & kErrNonFinite) return fail(c, PF_ERR_INVALID_ARGUMENT, "a point coordinate is NaN or infinite");
+    if (e & (kErrDepth | kErrWalk | kErrClip)) {
+        char m[128];
+        std::snprintf(m, sizeof m, "a kernel hit an iteration bound (flags 0x%x)", e);
+        return fail(c, PF_ERR_KERNEL_LIMIT, m);
+    }
+    if (e & (kErrOverflowSeg | kErrOverflowLeaf | kErrOverflowFill | kErrOverflowList))
+        return fail(c, PF_ERR_OVERFLOW, "a buffer capacity was exceeded");
+    return PF_OK;
+}
+
+int scan(Ctx *c, uint32_t *arr, uint32_t n, int slot) {
+    PF_CUDA(c->scan_temp.ensure(scan_temp_bytes(n)));
+    PF_CUDA(scan_exclusive_u32(arr, arr, n, c->status.as<uint32_t>() + slot, c->scan_temp.p, c->stream));
+    return PF_OK;
+}
+
+void record(Ctx *c, int i) {
+    if (c->flags & PF_CONFIG_STAGE_TIMING) cudaEventRecord(c->ev[i], c->stream);
+}
+
+// The exact two-pass frame.
+int render_exact(Ctx *c, pf_frame_stats *stats) {
+    if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
+    cudaStream_t st = c->stream;
+    const uint32_t N = c->n_paths, C = c->n_contours;
+    PF_CUDA(c->status.ensure(kStCount * 4));
+    PF_CUDA(cudaMemsetAsync(c->status.p, 0, kStCount * 4, st));
+    PF_CUDA(c->contour_point_first.ensure((size_t(C) + 1) * 4));
+    PF_CUDA(c->contour_path.ensure(size_t(C) * 4 + 4));
+    PF_CUDA(c->contour_segs.ensure((size_t(C) + 1) * 4));
+    PF_CUDA(c->paths.ensure(size_t(N) * sizeof(PathDev) + 16));
+    PF_CUDA(c->path_tiles.ensure((size_t(N) + 1) * 4));
+    PF_CUDA(c->path_cols.ensure((size_t(N) + 1) * 4));
+    PF_CUDA(c->path_contours.ensure(size_t(N) * 8 + 8));
+    PF_CUDA(c->z.ensure(size_t(c->n_fb) * 4 + 4));
+    PF_CUDA(c->fb_count.ensure((size_t(c->n_fb) + 1) * 4));
+    PF_CUDA(c->fb_cursor.ensure(size_t(c->n_fb) * 4 + 4));
+
+    record(c, 0);
+    // 1. topology, tile rects, segment counts
+    Batch b = make_batch(c);
+    PF_CUDA(launch_normalize(b, c->path_contours.as<uint2>(), st));
+    PF_CUDA(launch_path_setup(b, c->path_contours.as<uint2>(), st));
+    PF_CUDA(cudaMemsetAsync(b.contour_segs + C, 0, 4, st));
+    PF_CUDA(cudaMemsetAsync(b.path_tiles + N, 0, 4, st));
+    PF_CUDA(cudaMemsetAsync(b.path_cols + N, 0, 4, st));
+    PF_CUDA(launch_contour_segments(b, false, st));
+    if (int e = scan(c, b.contour_segs, C + 1, kStSegs)) return e;
+    if (int e = scan(c, b.path_tiles, N + 1, kStTiles)) return e;
+    if (int e = scan(c, b.path_cols, N + 1, kStCols)) return e;
+    PF_CUDA(launch_path_offsets(b, st));
+    if (int e = read_status(c)) return e;
+    if (int e = check_kernel_status(c)) return e;
+    c->n_segs = c->h_status[kStSegs];
+    c->n_tiles = c->h_status[kStTiles];
+    c->n_cols = c->h_status[kStCols];
+    record(c, 1);
+
+    // 2. segments, leaf counts, leaves
+    PF_CUDA(c->segs.ensure(size_t(c->n_segs) * sizeof(SegDev) + 16));
+    PF_CUDA(c->seg_leaves.ensure((size_t(c->n_segs) + 1) * 4));
+    b = make_batch(c);
+    PF_CUDA(launch_contour_segments(b, true, st));
+    PF_CUDA(cudaMemsetAsync(b.seg_leaves + c->n_segs, 0, 4, st));
+    PF_CUDA(launch_flatten(b, c->n_segs, false, st));
+    if (int e = scan(c, b.seg_leaves, c->n_segs + 1, kStLeaves)) return e;
+    if (int e = read_status(c)) return e;
+    if (int e = check_kernel_status(c)) return e;
+    c->n_leaves = c->h_status[kStLeaves];
+    PF_CUDA(c->leaves.ensure(size_t(c->n_leaves) * 16 + 16));
+    PF_CUDA(c->leaf_path.ensure(size_t(c->n_leaves) * 4 + 16));
+    b = make_batch(c);
+    PF_CUDA(launch_flatten(b, c->n_segs, true, st));
+    record(c, 2);
+
+    // 3. fill counts per tile, then fills written grouped by tile
+    const size_t T = c->n_tiles, K = c->n_cols;
+    PF_CUDA(c->tile_fills.ensure((T + 1) * 4));
+    PF_CUDA(c->tile_cursor.ensure(T * 4 + 4));
+    PF_CUDA(c->tile_delta.ensure(T * 4 + 4));
+    PF_CUDA(c->tile_backdrop.ensure(T + 16));
+    PF_CUDA(c->tile_path.ensure(T * 4 + 4));
+    PF_CUDA(c->col_above.ensure(K * 4 + 4));
+    PF_CUDA(c->col_final.ensure(K * 4 + 4));
+    b = make_batch(c);
+    PF_CUDA(cudaMemsetAsync(b.tile_fills, 0, (T + 1) * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.tile_cursor, 0, T * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.tile_delta, 0, T * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.col_above, 0, K * 4, st));
+    PF_CUDA(launch_bin(b, c->n_leaves, false, st));
+    if (int e = scan(c, b.tile_fills, (uint32_t)T + 1, kStFills)) return e;
+    if (int e = read_status(c)) return e;
+    if (int e = check_kernel_status(c)) return e;
+    c->n_fills = c->h_status[kStFills];
+    PF_CUDA(c->fills.ensure(size_t(c->n_fills) * 8 + 16));
+    b = make_batch(c);
+    PF_CUDA(launch_bin(b, c->n_leaves, true, st));
+    record(c, 3);
+
+    // 4. backdrops, z-buffer
+    PF_CUDA(cudaMemsetAsync(b.z, 0xff, size_t(c->n_fb) * 4, st));
+    PF_CUDA(launch_propagate(b, c->n_cols, st));
+    record(c, 4);
+
+    // 5. composite lists
+    PF_CUDA(cudaMemsetAsync(b.fb_count, 0, (size_t(c->n_fb) + 1) * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.fb_cursor, 0, size_t(c->n_fb) * 4, st));
+    PF_CUDA(launch_list(b, c->n_tiles, false, st));
+    if (int e = scan(c, b.fb_count, c->n_fb + 1, kStList)) return e;
+    if (int e = read_status(c)) return e;
+    c->n_list = c->h_status[kStList];
+    PF_CUDA(c->list.ensure(size_t(c->n_list) * 4 + 16));
+    b = make_batch(c);
+    PF_CUDA(launch_list(b, c->n_tiles, true, st));
+    PF_CUDA(launch_list_sort(b, st));
+    record(c, 5);
+
+    // 6. coverage + composite
+    PF_CUDA(launch_composite(b, c->scene_fb_first.as<uint32_t>(), st));
+    record(c, 6);
+    if (int e = read_status(c)) return e;
+    if (int e = check_kernel_status(c)) return e;
+    c->rendered = true;
+
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->paths = c->n_paths;
+        stats->contours = c->n_contours;
+        stats->points = c->n_points;
+        stats->segments = c->n_segs;
+        stats->microlines = c->n_leaves;
+        stats->tiles = c->n_tiles;
+        stats->fills = c->n_fills;
+        stats->composite_entries = c->n_list;
+        stats->framebuffer_tiles = c->n_fb;
+        if (c->flags & PF_CONFIG_STAGE_TIMING) {
+            float ms[6] = {};
+            for (int i = 0; i < 6; i++) cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]);
+            stats->ms_setup = ms[0];
+            stats->ms_flatten = ms[1];
+            stats->ms_bin = ms[2];
+            stats->ms_propagate = ms[3];
+            stats->ms_lists = ms[4];
+            stats->ms_composite = ms[5];
+            cudaEventElapsedTime(&stats->ms_total, c->ev[0], c->ev[6]);
+        }
+    }
+    return PF_OK;
+}
+
+template <class T>
+int d2h(Ctx *c, std::vector<T> &dst, const void *src, size_t n) {
+    dst.resize(n);
+    if (n) PF_CUDA(cudaMemcpyAsync(dst.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+    return PF_OK;
+}
+
+// Canonical integer output of scene `si` of the last frame.
+int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
+    if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
+    if (si >= c->n_scenes) return fail(c, PF_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const SceneDev &S = c->h_scenes[si];
+    const uint32_t p0 = S.path_first, p1 = S.path_end, np = p1 - p0;
+    std::vector<PathDev> paths;
+    std::vector<uint32_t> tf, cf;
+    if (int e = d2h(c, paths, c->paths.as<PathDev>() + p0, np)) return e;
+    if (int e = d2h(c, tf, c->path_tiles.as<uint32_t>() + p0, np + 1)) return e;
+    if (int e = d2h(c, cf, c->path_cols.as<uint32_t>() + p0, np + 1)) return e;
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    const uint32_t t0 = tf[0], t1 = tf[np], k0 = cf[0], k1 = cf[np];
+    HostCanon &h = c->canon;
+    h.rect.resize(size_t(np) * 4);
+    h.tile_first.resize(np + 1);
+    h.col_first.resize(np + 1);
+    for (uint32_t p = 0; p < np; p++) {
+        h.rect[4 * p + 0] = paths[p].rx0;
+        h.rect[4 * p + 1] = paths[p].ry0;
+        h.rect[4 * p + 2] = paths[p].rx1;
+        h.rect[4 * p + 3] = paths[p].ry1;
+    }
+    for (uint32_t p = 0; p <= np; p++) {
+        h.tile_first[p] = tf[p] - t0;
+        h.col_first[p] = cf[p] - k0;
+    }
+    std::vector<uint32_t> tfill;
+    if (int e = d2h(c, tfill, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0) + 1)) return e;
+    if (int e = d2h(c, h.backdrop, c->tile_backdrop.as<int8_t>() + t0, t1 - t0)) return e;
+    if (int e = d2h(c, h.col_backdrop, c->col_final.as<int32_t>() + k0, k1 - k0)) return e;
+    if (int e = d2h(c, h.z, c->z.as<int32_t>() + S.fb_first, size_t(S.fbw) * S.fbh)) return e;
+    std::vector<uint32_t> fbc;
+    if (int e = d2h(c, fbc, c->fb_count.as<uint32_t>() + S.fb_first, size_t(S.fbw) * S.fbh + 1)) return e;
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    const uint32_t f0 = tfill[0], f1 = tfill[t1 - t0];
+    std::vector<uint2> fl;
+    if (int e = d2h(c, fl, c->fills.as<uint2>() + f0, f1 - f0)) return e;
+    const uint32_t l0 = fbc[0], l1 = fbc[size_t(S.fbw) * S.fbh];
+    if (int e = d2h(c, h.list, c->list.as<uint32_t>() + l0, l1 - l0)) return e;
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+
+    const size_t nt = t1 - t0;
+    h.alpha.resize(nt);
+    h.fill_count.resize(nt);
+    h.fills.resize(size_t(f1 - f0) * 4);
+    std::vector<uint64_t> keys;
+    for (size_t t = 0; t < nt; t++) {
+        const uint32_t a = tfill[t] - f0, e = tfill[t + 1] - f0;
+        h.fill_count[t] = e - a;
+        h.alpha[t] = e != a;
+        keys.clear();
+        for (uint32_t k = a; k < e; k++)
+            keys.push_back((uint64_t(fl[k].x & 0xffffu) << 48) | (uint64_t(fl[k].x >> 16) << 32) |
+                           (uint64_t(fl[k].y & 0xffffu) << 16) | uint64_t(fl[k].y >> 16));
+        std::sort(keys.begin(), keys.end());
+        for (uint32_t k = 0; k < e - a; k++) {
+            uint16_t *d = &h.fills[4 * (size_t(a) + k)];
+            d[0] = uint16_t(keys[k] >> 48);
+            d[1] = uint16_t(keys[k] >> 32);
+            d[2] = uint16_t(keys[k] >> 16);
+            d[3] = uint16_t(keys[k]);
+        }
+    }
+    for (auto &z : h.z)
+        if (z >= 0) z -= (int32_t)p0;
+    h.list_first.resize(fbc.size());
+    for (size_t i = 0; i < fbc.size(); i++) h.list_first[i] = fbc[i] - l0;
+    for (auto &g : h.list) g -= t0;
+
+    std::memset(out, 0, sizeof(*out));
+    out->n_paths = np;
+    out->path_rect = h.rect.data();
+    out->path_tile_first = h.tile_first.data();
+    out->path_column_first = h.col_first.data();
+    out->n_tiles = nt;
+    out->tile_alpha = h.alpha.data();
+    out->tile_backdrop = h.backdrop.data();
+    out->tile_fill_count = h.fill_count.data();
+    out->n_fills = f1 - f0;
+    out->fills = h.fills.data();
+    out->n_columns = k1 - k0;
+    out->column_backdrop = h.col_backdrop.data();
+    out->fb_tiles_x = S.fbw;
+    out->fb_tiles_y = S.fbh;
+    out->z = h.z.data();
+    out->fb_list_first = h.list_first.data();
+    out->n_list = l1 - l0;
+    out->fb_list = h.list.data();
+    return PF_OK;
+}
+
+int read_image(Ctx *c, uint32_t si, uint8_t *rgba, size_t cap) {
+    if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
+    if (si >= c->n_scenes) return fail(c, PF_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const SceneDev &S = c->h_scenes[si];
+    const size_t bytes = size_t(S.img_w) * S.img_h * 4;
+    if (!rgba || cap < bytes) return fail(c, PF_ERR_INVALID_ARGUMENT, "image buffer too small");
+    PF_CUDA(cudaMemcpyAsync(rgba, c->image.as<uint8_t>() + S.img_offset, bytes, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+Ctx *as_ctx(void *p) { return static_cast<Ctx *>(p); }
+
+}  // namespace
+
+extern "C" {
+
+int pf_abi_version(void) { return PF_ABI_VERSION; }
+
+int pf_device_count(int *count) {
+    if (!count) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "count is null");
+    cudaError_t e = cudaGetDeviceCount(count);
+    if (e != cudaSuccess) {
+        *count = 0;
+        return fail(nullptr, PF_ERR_CUDA, cudaGetErrorString(e));
+    }
+    return PF_OK;
+}
+
+int pf_ctx_create(const pf_config *config, void **out) {
+    if (!out) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx out pointer is null");
+    *out = nullptr;
+    Ctx *c = new (std::nothrow) Ctx();
+    if (!c) return fail(nullptr, PF_ERR_OUT_OF_MEMORY, "host allocation failed");
+    if (config) {
+        c->device = config->device;
+        c->stream = static_cast<cudaStream_t>(config->stream);
+        c->flags = config->flags;
+    }
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess && !c->stream) {
+        e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        c->own_stream = e == cudaSuccess;
+    }
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, kStCount * 4);
+    for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
+    if (e == cudaSuccess) e = c->status.ensure(kStCount * 4);
+    if (e != cudaSuccess) {
+        int st = cuda_fail(nullptr, e, "pf_ctx_create");
+        pf_ctx_destroy(c);
+        return st;
+    }
+    *out = c;
+    return PF_OK;
+}
+
+int pf_ctx_destroy(void *ctx) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return PF_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    DevBuf *bufs[] = {&c->points, &c->pflags, &c->cstart, &c->pstart, &c->fill_rule, &c->color, &c->scenes,
+                      &c->scene_path_first, &c->scene_contour_first, &c->scene_fb_first, &c->contour_point_first,
+                      &c->contour_path, &c->paths, &c->path_tiles, &c->path_cols, &c->contour_segs,
+                      &c->path_contours, &c->segs, &c->seg_leaves, &c->leaves, &c->leaf_path, &c->tile_fills,
+                      &c->tile_cursor, &c->tile_delta, &c->tile_backdrop, &c->tile_path, &c->col_above,
+                      &c->col_final, &c->fills, &c->z, &c->fb_count, &c->fb_cursor, &c->list, &c->image,
+                      &c->status, &c->scan_temp};
+    for (DevBuf *b : bufs) b->release();
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return PF_OK;
+}
+
+const char *pf_last_error(void *ctx) {
+    Ctx *c = as_ctx(ctx);
+    return c ? c->err.c_str() : g_last_error.c_str();
+}
+
+int pf_scene_upload(void *ctx, const pf_scene_view *scene) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    cudaSetDevice(c->device);
+    return upload(c, scene, 1);
+}
+
+int pf_scene_upload_batch(void *ctx, const pf_scene_view *scenes, uint32_t n_scenes) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    cudaSetDevice(c->device);
+    return upload(c, scenes, n_scenes);
+}
+
+int pf_render(void *ctx, pf_frame_stats *stats) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    cudaSetDevice(c->device);
+    return render_exact(c, stats);
+}
+
+int pf_read_image(void *ctx, uint8_t *rgba, size_t capacity_bytes) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    return read_image(c, 0, rgba, capacity_bytes);
+}
+
+int pf_read_image_scene(void *ctx, uint32_t scene, uint8_t *rgba, size_t capacity_bytes) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    return read_image(c, scene, rgba, capacity_bytes);
+}
+
+int pf_image_device_ptr(void *ctx, void **rgba, uint32_t *width_px, uint32_t *height_px) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !rgba) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
+    *rgba = c->image.p;
+    if (width_px) *width_px = c->h_scenes[0].img_w;
+    if (height_px) *height_px = c->h_scenes[0].img_h;
+    return PF_OK;
+}
+
+int pf_read_canon(void *ctx, pf_canon *out) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !out) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    return read_canon(c, 0, out);
+}
+
+int pf_read_canon_scene(void *ctx, uint32_t scene, pf_canon *out) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !out) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    return read_canon(c, scene, out);
+}
+
+int pf_draw(void *ctx, const pf_scene_view *scene, uint8_t *rgba, size_t capacity_bytes, pf_frame_stats *stats) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    cudaSetDevice(c->device);
+    if (int e = upload(c, scene, 1)) return e;
+    if (int e = render_exact(c, stats)) return e;
+    return read_image(c, 0, rgba, capacity_bytes);
+}
+
+// Coverage after the fill rule of every alpha tile of scene 0, in tile order
+// (n_alpha x 256 floats, row-major 16x16).  A test and debugging aid.
+int pf_read_coverage(void *ctx, float *out, size_t capacity_floats, uint64_t *n_alpha) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !n_alpha) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
+    const SceneDev &S = c->h_scenes[0];
+    std::vector<uint32_t> tf, tfill;
+    if (int e = d2h(c, tf, c->path_tiles.as<uint32_t>() + S.path_first, S.path_end - S.path_first + 1)) return e;
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    const uint32_t t0 = tf.front(), t1 = tf.back();
+    if (int e = d2h(c, tfill, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0) + 1)) return e;
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<uint32_t> alpha;
+    for (uint32_t t = 0; t < t1 - t0; t++)
+        if (tfill[t + 1] != tfill[t]) alpha.push_back(t0 + t);
+    *n_alpha = alpha.size();
+    if (!out) return PF_OK;
+    if (capacity_floats < alpha.size() * 256) return fail(c, PF_ERR_INVALID_ARGUMENT, "coverage buffer too small");
+    DevBuf dt, dout;
+    PF_CUDA(dt.ensure(alpha.size() * 4 + 4));
+    PF_CUDA(dout.ensure(alpha.size() * 1024 + 4));
+    PF_CUDA(cudaMemcpyAsync(dt.p, alpha.data(), alpha.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    Batch b = make_batch(c);
+    PF_CUDA(launch_coverage_dump(b, dt.as<uint32_t>(), (uint32_t)alpha.size(), dout.as<float>(), c->stream));
+    PF_CUDA(cudaMemcpyAsync(out, dout.p, alpha.size() * 1024, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    dt.release();
+    dout.release();
+    return PF_OK;
+}
+
+}  // extern "C"

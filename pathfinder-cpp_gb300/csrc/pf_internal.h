@@ -1,0 +1,146 @@
+// pf_internal.h - device data layout and kernel launchers of the fill pipeline.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pfc {
+
+constexpr int kTile = 16;
+// Coverage is accumulated as int32 fixed point with this many fraction bits:
+// integer sums do not depend on the order fills are visited in.
+constexpr int kCovShift = 20;
+constexpr int kMaxDepth = 32;              // flattening recursion bound (depth of the d3d9 bisection)
+constexpr uint32_t kMaxWalk = 1u << 20;    // tile-walk step bound per line
+constexpr uint32_t kNone = 0xffffffffu;
+
+// Kernel error bits (written with atomicOr into the status word).
+enum : uint32_t {
+    kErrDepth = 1u << 0,    // flattening hit kMaxDepth
+    kErrWalk = 1u << 1,     // a tile walk hit kMaxWalk
+    kErrClip = 1u << 2,     // Cohen-Sutherland clipping did not settle
+    kErrNonFinite = 1u << 3,// a point is NaN or infinite
+    kErrOverflowSeg = 1u << 8,
+    kErrOverflowLeaf = 1u << 9,
+    kErrOverflowFill = 1u << 10,
+    kErrOverflowList = 1u << 11,
+};
+
+// Per scene of a batch (device).
+struct SceneDev {
+    float vb_right;       // view box right edge, rounded up to a multiple of 16
+    float vb_bottom;      // view box bottom edge (canvas height)
+    uint32_t fbw, fbh;    // framebuffer tiles across / down
+    uint32_t fb_first;    // first framebuffer tile of this scene in the batch
+    uint32_t img_w, img_h;
+    uint32_t clear;       // RGBA8
+    uint64_t img_offset;  // byte offset of the scene's image in the batch image buffer
+    uint32_t path_first, path_end;
+    uint32_t contour_first, contour_end;
+    uint32_t point_first, point_end;
+    uint32_t cstart_base, pstart_base;  // offsets of the scene's offset arrays
+};
+
+// Per draw path (device), written by the set-up kernel.
+struct PathDev {
+    int32_t rx0, ry0, rx1, ry1;  // tile rect (BuiltPath::tile_bounds)
+    uint32_t tile_first;         // first global tile
+    uint32_t col_first;          // first global column
+    uint32_t scene;
+    uint32_t flags;              // bit0 even-odd, bit1 occludes (opaque src-over)
+};
+
+// Segment record: points index a, kind, and the second point for closing lines.
+enum : uint32_t { kSegLine = 0, kSegQuad = 1, kSegCubic = 2, kSegClose = 3 };
+struct SegDev {
+    uint32_t a;       // first point (global)
+    uint32_t b;       // kSegClose: the contour's first point; else unused
+    uint32_t kind;
+    uint32_t path;
+};
+
+// Everything the kernels read and write for one batch.
+struct Batch {
+    // inputs (concatenated per-scene arrays)
+    const float2 *points;
+    const uint8_t *flags;
+    const uint32_t *contour_start_cat;   // per scene n_contours+1 entries, scene-local
+    const uint32_t *path_start_cat;      // per scene n_paths+1 entries, scene-local
+    const uint8_t *fill_rule;
+    const uint32_t *color;
+    const SceneDev *scenes;
+    const uint32_t *scene_path_first;    // [n_scenes + 1]
+    const uint32_t *scene_contour_first; // [n_scenes + 1]
+    uint32_t n_scenes, n_paths, n_contours, n_points;
+
+    // normalised topology
+    uint32_t *contour_point_first;       // [n_contours + 1] global
+    uint32_t *contour_path;              // [n_contours]
+    PathDev *paths;                      // [n_paths]
+    uint32_t *path_tiles;                // [n_paths + 1] -> scanned to first tile
+    uint32_t *path_cols;                 // [n_paths + 1] -> scanned to first column
+    uint32_t *contour_segs;              // [n_contours + 1] -> scanned
+
+    // segments / leaves
+    SegDev *segs;
+    uint32_t seg_cap;
+    uint32_t *seg_leaves;                // [segs + 1] -> scanned
+    float4 *leaves;
+    uint32_t *leaf_path;
+    uint32_t leaf_cap;
+
+    // tiles
+    uint32_t *tile_fills;                // [tiles + 1] count -> scanned to first fill
+    uint32_t *tile_cursor;               // [tiles]
+    int32_t *tile_delta;                 // [tiles] summed backdrop deltas
+    int8_t *tile_backdrop;               // [tiles]
+    uint32_t *tile_path;                 // [tiles]
+    int32_t *col_above;                  // [cols] deltas landing above the rect
+    int32_t *col_final;                  // [cols]
+    uint32_t tile_cap, col_cap;
+    uint2 *fills;                        // [fills] packed u16 x4
+    uint32_t fill_cap;
+
+    // framebuffer tiles
+    int32_t *z;                          // [fb tiles]
+    uint32_t *fb_count;                  // [fb + 1] -> scanned
+    uint32_t *fb_cursor;
+    uint32_t *list;
+    uint32_t list_cap;
+    uint32_t n_fb;
+
+    uint8_t *image;                      // batch image buffer
+    uint32_t *status;                    // [16] error bits and totals
+};
+
+// status word slots: error bits, then the totals the scans produce
+enum : int {
+    kStErr = 0,
+    kStSegs = 1,
+    kStTiles = 2,
+    kStCols = 3,
+    kStLeaves = 4,
+    kStFills = 5,
+    kStList = 6,
+    kStCount = 16,
+};
+
+// Scans (exclusive, in place allowed); the total lands in *total (device).
+size_t scan_temp_bytes(uint32_t n);
+cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, void *temp,
+                               cudaStream_t st);
+
+// Stage launchers (all asynchronous on the given stream).
+cudaError_t launch_normalize(const Batch &b, uint2 *path_contours, cudaStream_t st);
+cudaError_t launch_path_setup(const Batch &b, const uint2 *path_contours, cudaStream_t st);
+cudaError_t launch_path_offsets(const Batch &b, cudaStream_t st);
+cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st);
+cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st);
+cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream_t st);
+cudaError_t launch_propagate(const Batch &b, uint32_t n_cols, cudaStream_t st);
+cudaError_t launch_list(const Batch &b, uint32_t n_tiles, bool write, cudaStream_t st);
+cudaError_t launch_list_sort(const Batch &b, cudaStream_t st);
+cudaError_t launch_composite(const Batch &b, const uint32_t *scene_fb_first, cudaStream_t st);
+cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t n, float *out, cudaStream_t st);
+
+}  // namespace pfc

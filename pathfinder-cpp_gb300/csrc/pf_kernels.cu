@@ -1,0 +1,940 @@
+// pf_kernels.cu - the stages of the GPU-driven fill pipeline for sm_103a.
+//
+// Stage map (reference -> here):
+//   SegmentsD3D11::add_path / SegmentsIter   -> k_contour_segments (count + emit)
+//   BuiltPath / round_rect_out_to_tile_bounds -> k_path_setup
+//   dice.comp (here: the d3d9 recursive bisection, tiler.cpp:284-315)  -> k_flatten<count|write>
+//   bin.comp (here: the d3d9 tile walk + add_fill, tiler.cpp:131-279,
+//             object_builder.cpp:19-114)        -> k_bin<count|write>
+//   bound.comp (tile records)                  -> memsets + per-tile counting sort (no linked lists)
+//   propagate.comp / Tiler::prepare_tiles       -> k_propagate
+//   sort.comp                                  -> k_list_count / k_list_write / k_list_sort
+//   fill.comp + tile.comp                      -> k_composite (coverage never leaves the SM)
+//
+// Integer outputs follow the reference's d3d9 CPU tiler bit for bit, so every float
+// operation on that path is written with __f*_rn intrinsics (no FMA contraction), in the
+// same order as the reference's SSE lanes (pathfinder/common/f32x4.h).
+#include "pf_internal.h"
+
+namespace pfc {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+// first index i in [0, n) with a[i] > v (a non-decreasing), n if none
+__device__ __forceinline__ uint32_t upper_bound(const uint32_t *a, uint32_t n, uint32_t v) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] <= v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t global_tid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+inline unsigned grid_for(uint64_t n, int threads = kThreads) {
+    return static_cast<unsigned>((n + threads - 1) / threads);
+}
+
+// ---------------------------------------------------------------------------
+// Normalisation: scene-local offsets -> global offsets.
+
+__global__ void k_normalize_contours(Batch b) {
+    const uint32_t c = global_tid();
+    if (c >= b.n_contours) return;
+    const uint32_t s = upper_bound(b.scene_contour_first, b.n_scenes + 1, c) - 1;
+    const SceneDev &S = b.scenes[s];
+    const uint32_t local = c - S.contour_first;
+    b.contour_point_first[c] = S.point_first + b.contour_start_cat[S.cstart_base + local];
+    if (c == b.n_contours - 1) b.contour_point_first[b.n_contours] = b.n_points;
+}
+
+__global__ void k_normalize_paths(Batch b, uint2 *path_contours) {
+    const uint32_t p = global_tid();
+    if (p >= b.n_paths) return;
+    const uint32_t s = upper_bound(b.scene_path_first, b.n_scenes + 1, p) - 1;
+    const SceneDev &S = b.scenes[s];
+    const uint32_t local = p - S.path_first;
+    const uint32_t c0 = S.contour_first + b.path_start_cat[S.pstart_base + local];
+    const uint32_t c1 = S.contour_first + b.path_start_cat[S.pstart_base + local + 1];
+    path_contours[p] = make_uint2(c0, c1);
+    for (uint32_t c = c0; c < c1; c++) b.contour_path[c] = p;
+    PathDev P{};
+    P.scene = s;
+    P.flags = (b.fill_rule[p] ? 1u : 0u) | (((b.color[p] >> 24) == 0xffu) ? 2u : 0u);
+    b.paths[p] = P;
+}
+
+// ---------------------------------------------------------------------------
+// Per-path bounds and tile rect (one warp per path).
+// Outline::bounds (pathfinder/core/data/path.cpp), RectF::intersection and
+// round_rect_out_to_tile_bounds (pathfinder/core/data/data.h:131-133), Tiler::Tiler
+// (pathfinder/core/d3d9/tiler.cpp:317-335).
+
+__global__ void k_path_setup(Batch b, const uint2 *path_contours) {
+    const uint32_t p = global_tid() >> 5;
+    const int lane = threadIdx.x & 31;
+    if (p >= b.n_paths) return;
+    const uint2 cr = path_contours[p];
+    const uint32_t a = b.contour_point_first[cr.x], e = b.contour_point_first[cr.y];
+    float l = INFINITY, t = INFINITY, r = -INFINITY, bt = -INFINITY;
+    bool bad = false;
+    for (uint32_t i = a + lane; i < e; i += 32) {
+        const float2 q = b.points[i];
+        bad |= !(isfinite(q.x) && isfinite(q.y));
+        l = fminf(l, q.x);
+        t = fminf(t, q.y);
+        r = fmaxf(r, q.x);
+        bt = fmaxf(bt, q.y);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        l = fminf(l, __shfl_xor_sync(0xffffffffu, l, d));
+        t = fminf(t, __shfl_xor_sync(0xffffffffu, t, d));
+        r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, d));
+        bt = fmaxf(bt, __shfl_xor_sync(0xffffffffu, bt, d));
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    if (lane != 0) return;
+    if (bad) atomicOr(&b.status[kStErr], kErrNonFinite);
+    PathDev P = b.paths[p];
+    const SceneDev &S = b.scenes[P.scene];
+    float il, it, ir, ib;
+    if (e == a) {  // no points: the default (invalid) RectF {1, 1, 0, 0}
+        l = 1.0f;
+        t = 1.0f;
+        r = 0.0f;
+        bt = 0.0f;
+    }
+    if (l > S.vb_right || r < 0.0f || t > S.vb_bottom || bt < 0.0f) {
+        il = 1.0f;
+        it = 1.0f;
+        ir = 0.0f;
+        ib = 0.0f;
+    } else {
+        il = l < 0.0f ? 0.0f : l;
+        it = t < 0.0f ? 0.0f : t;
+        ir = S.vb_right < r ? S.vb_right : r;
+        ib = S.vb_bottom < bt ? S.vb_bottom : bt;
+    }
+    const float inv = 1.0f / kTile;
+    P.rx0 = (int32_t)floorf(fmul(il, inv));
+    P.ry0 = (int32_t)floorf(fmul(it, inv));
+    P.rx1 = (int32_t)ceilf(fmul(ir, inv));
+    P.ry1 = (int32_t)ceilf(fmul(ib, inv));
+    const int32_t w = max(P.rx1 - P.rx0, 0), h = max(P.ry1 - P.ry0, 0);
+    b.paths[p] = P;
+    b.path_tiles[p] = (uint32_t)(w * h);
+    b.path_cols[p] = (uint32_t)w;
+}
+
+__global__ void k_path_offsets(Batch b) {
+    const uint32_t p = global_tid();
+    if (p >= b.n_paths) return;
+    b.paths[p].tile_first = b.path_tiles[p];
+    b.paths[p].col_first = b.path_cols[p];
+}
+
+// ---------------------------------------------------------------------------
+// Segments of a contour, as SegmentsIter::get_next(force_closed = true) yields them
+// (pathfinder/core/data/contour.cpp:110-175): stop at the first malformed point pattern;
+// at the end, an implicit closing line unless first ~= last within 1e-4.
+
+template <bool kWrite>
+__global__ void k_contour_segments(Batch b) {
+    const uint32_t c = global_tid();
+    if (c >= b.n_contours) return;
+    const uint32_t a = b.contour_point_first[c], n = b.contour_point_first[c + 1] - a;
+    const uint8_t *fl = b.flags + a;
+    uint32_t out = 0, path = 0;
+    if (kWrite) {
+        out = b.contour_segs[c];
+        path = b.contour_path[c];
+        if (out > b.seg_cap) return;
+    }
+    uint32_t count = 0, head = 0;
+    auto emit = [&](uint32_t kind, uint32_t first, uint32_t second) {
+        if (kWrite) {
+            const uint32_t k = out + count;
+            if (k < b.seg_cap) b.segs[k] = SegDev{first, second, kind, path};
+            else atomicOr(&b.status[kStErr], kErrOverflowSeg);
+        }
+        count++;
+    };
+    if (n != 0) {
+        for (;;) {
+            if (head >= n || fl[head] != 0) break;
+            if (head + 1 < n) {
+                const uint8_t f1 = fl[head + 1];
+                if (f1 == 0) {
+                    emit(kSegLine, a + head, 0);
+                    head += 1;
+                } else if (head + 2 < n) {
+                    const uint8_t f2 = fl[head + 2];
+                    if (f1 == 1 && f2 == 0) {
+                        emit(kSegQuad, a + head, 0);
+                        head += 2;
+                    } else if (head + 3 < n) {
+                        if (f1 == 1 && f2 == 2 && fl[head + 3] == 0) {
+                            emit(kSegCubic, a + head, 0);
+                            head += 3;
+                        } else {
+                            break;
+                        }
+                    } else {
+                        break;
+                    }
+                } else {
+                    break;
+                }
+            } else {
+                if (n > 1) {
+                    const float2 f = b.points[a], l = b.points[a + n - 1];
+                    const float dx = fsub(f.x, l.x), dy = fsub(f.y, l.y);
+                    const float len = __fsqrt_rn(fadd(fmul(dx, dx), fmul(dy, dy)));
+                    if (!(len <= 0.0001f)) emit(kSegClose, a + n - 1, a);
+                }
+                break;
+            }
+        }
+    }
+    if (!kWrite) b.contour_segs[c] = count;
+}
+
+// ---------------------------------------------------------------------------
+// Flattening: the d3d9 recursive bisection (process_segment, tiler.cpp:284-315) run
+// depth first with an explicit stack, so leaves come out in the reference's order.
+// Segment::is_flat_cubic (segment.cpp:12-20), is_flat_quadratic (:22-36), split_cubic
+// at t = 0.5 (:42-100) and split_quadratic (:102-126), with the same operation order.
+
+__device__ __forceinline__ bool flat_cubic(const float bb[4], const float cc[4]) {
+    const float bz[4] = {bb[2], bb[3], bb[0], bb[1]};
+    float uv[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float t = fmul(3.0f, cc[k]);
+        t = fsub(t, bb[k]);
+        t = fsub(t, bb[k]);
+        t = fsub(t, bz[k]);
+        uv[k] = fmul(t, t);
+    }
+    const float m0 = uv[0] > uv[2] ? uv[0] : uv[2];
+    const float m1 = uv[1] > uv[3] ? uv[1] : uv[3];
+    return fadd(m0, m1) <= 1.0f;
+}
+
+__device__ __forceinline__ bool flat_quad(const float bb[4], const float cc[2]) {
+    const float mx = fmul(fadd(bb[0], bb[2]), 0.5f), my = fmul(fadd(bb[1], bb[3]), 0.5f);
+    const float dx = fsub(cc[0], mx), dy = fsub(cc[1], my);
+    return fadd(fmul(dx, dx), fmul(dy, dy)) <= 0.25f;
+}
+
+__device__ __forceinline__ float half_lerp(float a, float b) { return fadd(a, fmul(0.5f, fsub(b, a))); }
+
+template <class Emit>
+__device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, float c1, float c2, float c3,
+                              Emit &&emit, uint32_t *status) {
+    float stk[kMaxDepth][8];
+    int dstk[kMaxDepth];
+    int sp = 0;
+    float bb[4] = {b0, b1, b2, b3}, cc[4] = {c0, c1, c2, c3};
+    int depth = 0;
+    for (;;) {
+        if (depth >= kMaxDepth - 1 || flat_cubic(bb, cc)) {
+            if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
+            emit(bb[0], bb[1], bb[2], bb[3]);
+            if (sp == 0) return;
+            sp--;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                bb[k] = stk[sp][k];
+                cc[k] = stk[sp][4 + k];
+            }
+            depth = dstk[sp];
+            continue;
+        }
+        float p01[2], p12[2], p23[2], p012[2], p123[2], p0123[2];
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            p01[k] = half_lerp(bb[k], cc[k]);
+            p12[k] = half_lerp(cc[k], cc[2 + k]);
+            p23[k] = half_lerp(cc[2 + k], bb[2 + k]);
+            p012[k] = half_lerp(p01[k], p12[k]);
+            p123[k] = half_lerp(p12[k], p23[k]);
+            p0123[k] = half_lerp(p012[k], p123[k]);
+        }
+        // push the second half, continue with the first
+        stk[sp][0] = p0123[0];
+        stk[sp][1] = p0123[1];
+        stk[sp][2] = bb[2];
+        stk[sp][3] = bb[3];
+        stk[sp][4] = p123[0];
+        stk[sp][5] = p123[1];
+        stk[sp][6] = p23[0];
+        stk[sp][7] = p23[1];
+        dstk[sp] = depth + 1;
+        sp++;
+        bb[2] = p0123[0];
+        bb[3] = p0123[1];
+        cc[0] = p01[0];
+        cc[1] = p01[1];
+        cc[2] = p012[0];
+        cc[3] = p012[1];
+        depth++;
+    }
+}
+
+template <class Emit>
+__device__ void flatten_quad(float b0, float b1, float b2, float b3, float c0, float c1, Emit &&emit,
+                             uint32_t *status) {
+    float stk[kMaxDepth][6];
+    int dstk[kMaxDepth];
+    int sp = 0;
+    float bb[4] = {b0, b1, b2, b3}, cc[2] = {c0, c1};
+    int depth = 0;
+    for (;;) {
+        if (depth >= kMaxDepth - 1 || flat_quad(bb, cc)) {
+            if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
+            emit(bb[0], bb[1], bb[2], bb[3]);
+            if (sp == 0) return;
+            sp--;
+#pragma unroll
+            for (int k = 0; k < 4; k++) bb[k] = stk[sp][k];
+            cc[0] = stk[sp][4];
+            cc[1] = stk[sp][5];
+            depth = dstk[sp];
+            continue;
+        }
+        float a[2], q[2], m[2];
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            a[k] = fadd(bb[k], fmul(fsub(cc[k], bb[k]), 0.5f));
+            q[k] = fadd(cc[k], fmul(fsub(bb[2 + k], cc[k]), 0.5f));
+            m[k] = fadd(a[k], fmul(fsub(q[k], a[k]), 0.5f));
+        }
+        stk[sp][0] = m[0];
+        stk[sp][1] = m[1];
+        stk[sp][2] = bb[2];
+        stk[sp][3] = bb[3];
+        stk[sp][4] = q[0];
+        stk[sp][5] = q[1];
+        dstk[sp] = depth + 1;
+        sp++;
+        bb[2] = m[0];
+        bb[3] = m[1];
+        cc[0] = a[0];
+        cc[1] = a[1];
+        depth++;
+    }
+}
+
+template <bool kWrite>
+__global__ void __launch_bounds__(kThreads) k_flatten(Batch b, uint32_t n_segs) {
+    const uint32_t i = global_tid();
+    if (i >= n_segs || i >= b.status[kStSegs]) return;
+    if (kWrite && b.status[kStLeaves] > b.leaf_cap) {
+        if (i == 0) atomicOr(&b.status[kStErr], kErrOverflowLeaf);
+        return;
+    }
+    const SegDev sg = b.segs[i];
+    uint32_t out = kWrite ? b.seg_leaves[i] : 0u;
+    uint32_t count = 0;
+    auto emit = [&](float x0, float y0, float x1, float y1) {
+        if (kWrite) {
+            b.leaves[out + count] = make_float4(x0, y0, x1, y1);
+            b.leaf_path[out + count] = sg.path;
+        }
+        count++;
+    };
+    const float2 p0 = b.points[sg.a];
+    switch (sg.kind) {
+        case kSegLine: {
+            const float2 p1 = b.points[sg.a + 1];
+            emit(p0.x, p0.y, p1.x, p1.y);
+        } break;
+        case kSegClose: {
+            const float2 p1 = b.points[sg.b];
+            emit(p0.x, p0.y, p1.x, p1.y);
+        } break;
+        case kSegQuad: {
+            const float2 c = b.points[sg.a + 1], p2 = b.points[sg.a + 2];
+            flatten_quad(p0.x, p0.y, p2.x, p2.y, c.x, c.y, emit, &b.status[kStErr]);
+        } break;
+        default: {
+            const float2 c0 = b.points[sg.a + 1], c1 = b.points[sg.a + 2], p3 = b.points[sg.a + 3];
+            flatten_cubic(p0.x, p0.y, p3.x, p3.y, c0.x, c0.y, c1.x, c1.y, emit, &b.status[kStErr]);
+        } break;
+    }
+    if (!kWrite) b.seg_leaves[i] = count;
+}
+
+// ---------------------------------------------------------------------------
+// Binning: the d3d9 tile walk of one leaf line (process_line_segment, tiler.cpp:131-279),
+// with clip_line_segment_to_rect (:46-125, clip box top = -inf), ObjectBuilder::add_fill
+// (object_builder.cpp:19-64: cull outside the tile rect, x256 local coordinates, clamp to
+// [0, 4095], round half to even, cull vertical) and adjust_alpha_tile_backdrop (:96-114).
+
+struct WalkCtx {
+    int32_t rx0, ry0, rx1, ry1, rw, rh;
+    float vb_right, vb_bottom;
+};
+
+__device__ __forceinline__ int outcode(const WalkCtx &w, float x, float y) {
+    int o = 0;
+    if (x < 0.0f) o |= 1;
+    else if (x > w.vb_right) o |= 2;
+    if (y > w.vb_bottom) o |= 8;
+    return o;
+}
+
+__device__ __forceinline__ float lerp_clamped(float a, float b, float t) {
+    t = t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t);
+    return fadd(a, fmul(fsub(b, a), t));
+}
+
+__device__ __forceinline__ int clip_line(const WalkCtx &w, float &x0, float &y0, float &x1, float &y1,
+                                         uint32_t *status) {
+    int of = outcode(w, x0, y0), ot = outcode(w, x1, y1);
+    for (int iter = 0; iter < 64; iter++) {
+        if (of == 0 && ot == 0) return 1;
+        if ((of & ot) != 0) return 0;
+        const bool clip_from = of > ot;
+        const int oc = clip_from ? of : ot;
+        float px = clip_from ? x0 : x1, py = clip_from ? y0 : y1;
+        if (oc & 1) {
+            px = 0.0f;
+            py = lerp_clamped(y0, y1, fdiv(fsub(0.0f, x0), fsub(x1, x0)));
+        } else if (oc & 2) {
+            px = w.vb_right;
+            py = lerp_clamped(y0, y1, fdiv(fsub(w.vb_right, x0), fsub(x1, x0)));
+        } else if (oc & 8) {
+            px = lerp_clamped(x0, x1, fdiv(fsub(w.vb_bottom, y0), fsub(y1, y0)));
+            py = w.vb_bottom;
+        }
+        if (clip_from) {
+            x0 = px;
+            y0 = py;
+            of = outcode(w, px, py);
+        } else {
+            x1 = px;
+            y1 = py;
+            ot = outcode(w, px, py);
+        }
+    }
+    atomicOr(status, kErrClip);
+    return 0;
+}
+
+// Quantise a piece of line in tile (tx, ty); returns false when add_fill culls it.
+__device__ __forceinline__ bool quantise(const WalkCtx &w, float x0, float y0, float x1, float y1, int32_t tx,
+                                         int32_t ty, uint2 &packed) {
+    if (!(w.rx0 <= tx && tx <= w.rx1 - 1 && w.ry0 <= ty && ty <= w.ry1 - 1)) return false;
+    const float ox = fmul((float)tx, 16.0f), oy = fmul((float)ty, 16.0f);
+    float v[4] = {fmul(fsub(x0, ox), 256.0f), fmul(fsub(y0, oy), 256.0f), fmul(fsub(x1, ox), 256.0f),
+                  fmul(fsub(y1, oy), 256.0f)};
+    uint32_t q[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        float c = v[k] > 0.0f ? v[k] : 0.0f;
+        c = c < 4095.0f ? c : 4095.0f;
+        q[k] = (uint32_t)rintf(c);
+    }
+    if (q[0] == q[2]) return false;
+    packed = make_uint2(q[0] | (q[1] << 16), q[2] | (q[3] << 16));
+    return true;
+}
+
+// Walk one line; on_fill(local_tile, packed) for every fill kept; on_delta(local_tile or
+// -1 - column, delta) for every backdrop change that lands in the rect or above it.
+template <class OnFill, class OnDelta>
+__device__ void walk_line(const WalkCtx &w, float x0, float y0, float x1, float y1, OnFill &&on_fill,
+                          OnDelta &&on_delta, uint32_t *status) {
+    if (!(isfinite(x0) && isfinite(y0) && isfinite(x1) && isfinite(y1))) return;
+    if (!clip_line(w, x0, y0, x1, y1, status)) return;
+    const float inv = 1.0f / kTile;
+    const int32_t fx = (int32_t)floorf(fmul(x0, inv)), fy = (int32_t)floorf(fmul(y0, inv));
+    const int32_t ex = (int32_t)floorf(fmul(x1, inv)), ey = (int32_t)floorf(fmul(y1, inv));
+    const float vx = fsub(x1, x0), vy = fsub(y1, y0);
+    const int32_t sx = vx < 0.0f ? -1 : 1, sy = vy < 0.0f ? -1 : 1;
+    const float cx = fmul(fadd((float)fx, vx >= 0.0f ? 1.0f : 0.0f), 16.0f);
+    const float cy = fmul(fadd((float)fy, vy >= 0.0f ? 1.0f : 0.0f), 16.0f);
+    float tmx = fdiv(fsub(cx, x0), vx), tmy = fdiv(fsub(cy, y0), vy);
+    const float tdx = fabsf(fdiv(16.0f, vx)), tdy = fabsf(fdiv(16.0f, vy));
+    float curx = x0, cury = y0;
+    int32_t tcx = fx, tcy = fy;
+    int last = 0;  // 0 none, 1 x, 2 y
+    for (uint32_t it = 0;; it++) {
+        if (it >= kMaxWalk) {
+            atomicOr(status, kErrWalk);
+            return;
+        }
+        int next;
+        if (tmx < tmy) next = 1;
+        else if (tmx > tmy) next = 2;
+        else next = sx > 0 ? 1 : 2;
+        float nt = next == 1 ? tmx : tmy;
+        nt = (1.0f < nt) ? 1.0f : nt;
+        if (tcx == ex && tcy == ey) next = 0;
+        const float npx = fadd(x0, fmul(vx, nt)), npy = fadd(y0, fmul(vy, nt));
+        const int32_t lx = tcx - w.rx0, ly = tcy - w.ry0;
+        uint2 q;
+        if (quantise(w, curx, cury, npx, npy, tcx, tcy, q)) on_fill(ly * w.rw + lx, q);
+        if (sy < 0 && next == 2) {
+            if (quantise(w, npx, npy, fmul((float)tcx, 16.0f), fmul((float)tcy, 16.0f), tcx, tcy, q))
+                on_fill(ly * w.rw + lx, q);
+        } else if (sy > 0 && last == 2) {
+            if (quantise(w, fmul((float)tcx, 16.0f), fmul((float)tcy, 16.0f), curx, cury, tcx, tcy, q))
+                on_fill(ly * w.rw + lx, q);
+        }
+        int delta = 0;
+        if (sx < 0 && last == 1) delta = 1;
+        else if (sx > 0 && next == 1) delta = -1;
+        if (delta != 0 && lx >= 0 && lx < w.rw && ly < w.rh) {
+            if (ly < 0) on_delta(-1 - lx, delta);
+            else on_delta(ly * w.rw + lx, delta);
+        }
+        if (next == 1) {
+            tmx = fadd(tmx, tdx);
+            tcx += sx;
+        } else if (next == 2) {
+            tmy = fadd(tmy, tdy);
+            tcy += sy;
+        } else {
+            break;
+        }
+        curx = npx;
+        cury = npy;
+        last = next;
+    }
+}
+
+template <bool kWrite>
+__global__ void __launch_bounds__(kThreads) k_bin(Batch b, uint32_t n_leaves) {
+    const uint32_t i = global_tid();
+    if (i >= n_leaves || i >= b.status[kStLeaves]) return;
+    if (kWrite && b.status[kStFills] > b.fill_cap) {
+        if (i == 0) atomicOr(&b.status[kStErr], kErrOverflowFill);
+        return;
+    }
+    const uint32_t p = b.leaf_path[i];
+    const float4 L = b.leaves[i];
+    const PathDev P = b.paths[p];
+    const SceneDev &S = b.scenes[P.scene];
+    WalkCtx w;
+    w.rx0 = P.rx0;
+    w.ry0 = P.ry0;
+    w.rx1 = P.rx1;
+    w.ry1 = P.ry1;
+    w.rw = max(P.rx1 - P.rx0, 0);
+    w.rh = max(P.ry1 - P.ry0, 0);
+    w.vb_right = S.vb_right;
+    w.vb_bottom = S.vb_bottom;
+    const uint32_t tb = P.tile_first, cb = P.col_first;
+    if (kWrite) {
+        walk_line(
+            w, L.x, L.y, L.z, L.w,
+            [&](int32_t local, uint2 q) {
+                const uint32_t gt = tb + (uint32_t)local;
+                const uint32_t slot = atomicAdd(&b.tile_cursor[gt], 1u);
+                b.fills[b.tile_fills[gt] + slot] = q;
+            },
+            [&](int32_t, int) {}, &b.status[kStErr]);
+    } else {
+        walk_line(
+            w, L.x, L.y, L.z, L.w, [&](int32_t local, uint2) { atomicAdd(&b.tile_fills[tb + (uint32_t)local], 1u); },
+            [&](int32_t where, int d) {
+                if (where >= 0) atomicAdd(&b.tile_delta[tb + (uint32_t)where], d);
+                else atomicAdd(&b.col_above[cb + (uint32_t)(-1 - where)], d);
+            },
+            &b.status[kStErr]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Backdrop propagation down each tile column (Tiler::prepare_tiles, tiler.cpp:369-439:
+// tile backdrop = int8(running int32 column sum), running += int8 tile delta), the
+// z-buffer of occluding solid tiles (d3d11 rule, propagate.comp:190-205: solid tiles the
+// even-odd rule leaves empty do not occlude) and the tile -> path map.
+
+__global__ void __launch_bounds__(kThreads) k_propagate(Batch b, uint32_t n_cols) {
+    const uint32_t gc = global_tid();
+    if (gc >= n_cols || gc >= b.status[kStCols]) return;
+    const uint32_t p = upper_bound(b.path_cols, b.n_paths + 1, gc) - 1;
+    const PathDev P = b.paths[p];
+    const SceneDev &S = b.scenes[P.scene];
+    const int32_t rw = P.rx1 - P.rx0, rh = P.ry1 - P.ry0;
+    const int32_t x = (int32_t)(gc - P.col_first);
+    int32_t run = b.col_above[gc];
+    const bool eo = (P.flags & 1u) != 0, occludes = (P.flags & 2u) != 0;
+    for (int32_t y = 0; y < rh; y++) {
+        const uint32_t gt = P.tile_first + (uint32_t)(y * rw + x);
+        const int8_t bd = (int8_t)run;
+        const int8_t delta = (int8_t)(b.tile_delta[gt] & 0xff);
+        b.tile_backdrop[gt] = bd;
+        b.tile_path[gt] = p;
+        const bool alpha = b.tile_fills[gt + 1] != b.tile_fills[gt];
+        if (!alpha && bd != 0 && occludes && !(eo && ((bd < 0 ? -bd : bd) & 1) == 0)) {
+            const uint32_t fb = S.fb_first + (uint32_t)(P.ry0 + y) * S.fbw + (uint32_t)(P.rx0 + x);
+            atomicMax(&b.z[fb], (int32_t)p);
+        }
+        run += delta;
+    }
+    b.col_final[gc] = run;
+}
+
+// ---------------------------------------------------------------------------
+// Composite lists per framebuffer tile: visible tiles (alpha, or nonzero backdrop,
+// scene_builder.cpp:57-63) of paths at or above the z value, in path order
+// (sort.comp:49-83).
+
+template <bool kWrite>
+__global__ void __launch_bounds__(kThreads) k_list(Batch b, uint32_t n_tiles) {
+    const uint32_t gt = global_tid();
+    if (gt >= n_tiles || gt >= b.status[kStTiles]) return;
+    if (kWrite && b.status[kStList] > b.list_cap) {
+        if (gt == 0) atomicOr(&b.status[kStErr], kErrOverflowList);
+        return;
+    }
+    const bool alpha = b.tile_fills[gt + 1] != b.tile_fills[gt];
+    const int8_t bd = b.tile_backdrop[gt];
+    if (!alpha && bd == 0) return;
+    const uint32_t p = b.tile_path[gt];
+    const PathDev P = b.paths[p];
+    const SceneDev &S = b.scenes[P.scene];
+    const int32_t rw = P.rx1 - P.rx0;
+    const uint32_t local = gt - P.tile_first;
+    const int32_t y = (int32_t)(local / (uint32_t)rw), x = (int32_t)(local % (uint32_t)rw);
+    const uint32_t fb = S.fb_first + (uint32_t)(P.ry0 + y) * S.fbw + (uint32_t)(P.rx0 + x);
+    if ((int32_t)p < b.z[fb]) return;
+    if (kWrite) {
+        const uint32_t slot = atomicAdd(&b.fb_cursor[fb], 1u);
+        b.list[b.fb_count[fb] + slot] = gt;
+    } else {
+        atomicAdd(&b.fb_count[fb], 1u);
+    }
+}
+
+constexpr int kSortThreads = 128;
+constexpr uint32_t kSortSmem = 4096;
+
+__device__ void bitonic_smem(uint32_t *v, uint32_t n_pow2) {
+    for (uint32_t k = 2; k <= n_pow2; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < n_pow2; i += blockDim.x) {
+                const uint32_t ixj = i ^ j;
+                if (ixj > i) {
+                    const uint32_t a = v[i], c = v[ixj];
+                    const bool up = (i & k) == 0;
+                    if ((a > c) == up) {
+                        v[i] = c;
+                        v[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_list_sort(Batch b) {
+    const uint32_t fb = blockIdx.x;
+    const uint32_t first = b.fb_count[fb], n = b.fb_count[fb + 1] - first;
+    if (n <= 1) return;
+    uint32_t *g = b.list + first;
+    if (n <= 32) {
+        // one warp: rank sort (keys are distinct)
+        if (threadIdx.x < 32) {
+            const uint32_t v = threadIdx.x < n ? g[threadIdx.x] : 0xffffffffu;
+            uint32_t rank = 0;
+            for (uint32_t k = 0; k < n; k++) {
+                const uint32_t o = __shfl_sync(0xffffffffu, v, k);
+                rank += (o < v) ? 1u : 0u;
+            }
+            __syncwarp();
+            if (threadIdx.x < n) g[rank] = v;
+        }
+        return;
+    }
+    __shared__ uint32_t sm[kSortSmem];
+    if (n <= kSortSmem) {
+        uint32_t n2 = 64;
+        while (n2 < n) n2 <<= 1;
+        for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) sm[i] = i < n ? g[i] : 0xffffffffu;
+        __syncthreads();
+        bitonic_smem(sm, n2);
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) g[i] = sm[i];
+        return;
+    }
+    // long list: odd-even transposition sort in place (rare; correct for any n)
+    for (uint32_t pass = 0; pass < n; pass++) {
+        for (uint32_t i = 2 * threadIdx.x + (pass & 1); i + 1 < n; i += 2 * blockDim.x) {
+            const uint32_t a = g[i], c = g[i + 1];
+            if (a > c) {
+                g[i] = c;
+                g[i + 1] = a;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Coverage of one alpha tile, accumulated by a warp into shared memory.
+//
+// A fill contributes, to the pixel (i, j) of its tile, the signed area inside the pixel
+// between the fill and the tile bottom (the quantity fill.comp:51-100 looks up in its area
+// LUT).  Along a pixel column that area steps from 0 (rows above the line) to the fill's
+// x-extent (rows below it), so the fill is stored as per-row differences: every piece of
+// the fill inside one cell (i, r) with x-width w and mean in-row depth m adds w(1-m) to
+// row r and w*m to row r+1; a prefix sum down the column restores the area.  Values are
+// int32 fixed point (kCovShift fraction bits), so the result does not depend on fill order.
+
+__device__ __forceinline__ int cov_index(int row, int col) { return row * 16 + col + ((row >> 3) << 4); }
+constexpr int kCovCells = 16 * 16 + 16;
+
+__device__ __forceinline__ void cov_add(int *D, int row, int col, float v) {
+    if (row < 16) atomicAdd(&D[cov_index(row, col)], __float2int_rn(v * (float)(1 << kCovShift)));
+}
+
+__device__ void raster_fill(uint2 f, int *D) {
+    const float x0 = (float)(f.x & 0xffffu) * (1.0f / 256.0f), y0 = (float)(f.x >> 16) * (1.0f / 256.0f);
+    const float x1 = (float)(f.y & 0xffffu) * (1.0f / 256.0f), y1 = (float)(f.y >> 16) * (1.0f / 256.0f);
+    const float s = x0 > x1 ? 1.0f : -1.0f;
+    const float xl = fminf(x0, x1), xr = fmaxf(x0, x1);
+    const float yl = x0 < x1 ? y0 : y1, yr = x0 < x1 ? y1 : y0;
+    const float dydx = (yr - yl) / (xr - xl);
+    const int i0 = (int)floorf(xl), i1 = min((int)ceilf(xr), 16);
+    for (int i = max(i0, 0); i < i1; i++) {
+        const float xa = fmaxf(xl, (float)i), xb = fminf(xr, (float)(i + 1));
+        const float w = xb - xa;
+        if (!(w > 0.0f)) continue;
+        const float ya = xa == xl ? yl : yl + dydx * (xa - xl);
+        const float yb = xb == xr ? yr : yl + dydx * (xb - xl);
+        const float ylo = fminf(ya, yb), yhi = fmaxf(ya, yb);
+        const int r0 = (int)floorf(ylo);
+        const float sw = s * w;
+        if (yhi <= (float)(r0 + 1)) {
+            const float m = 0.5f * (ylo + yhi) - (float)r0;
+            cov_add(D, r0, i, sw * (1.0f - m));
+            cov_add(D, r0 + 1, i, sw * m);
+        } else {
+            const int r1 = min((int)ceilf(yhi) - 1, 15);
+            const float inv_h = 1.0f / (yhi - ylo);
+            for (int r = r0; r <= r1; r++) {
+                const float lo = fmaxf(ylo, (float)r), hi = fminf(yhi, (float)(r + 1));
+                const float hgt = hi - lo;
+                if (!(hgt > 0.0f)) continue;
+                const float wr = sw * hgt * inv_h;
+                const float m = 0.5f * (lo + hi) - (float)r;
+                cov_add(D, r, i, wr * (1.0f - m));
+                cov_add(D, r + 1, i, wr * m);
+            }
+        }
+    }
+}
+
+// Warp computes the coverage of the 8 pixels of every lane (column lane&15, rows
+// (lane>>4)*8 .. +7) of an alpha tile; D must be zeroed on entry and is left dirty.
+__device__ __forceinline__ void alpha_coverage(const Batch &b, uint32_t f0, uint32_t f1, int8_t bd, bool eo, int *D,
+                                               float cov[8]) {
+    const int lane = threadIdx.x & 31;
+    for (uint32_t f = f0 + lane; f < f1; f += 32) raster_fill(b.fills[f], D);
+    __syncwarp();
+    const int col = lane & 15, h = lane >> 4;
+    int acc[8];
+    int run = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        run += D[cov_index(h * 8 + k, col)];
+        acc[k] = run;
+    }
+    const int upper = __shfl_sync(0xffffffffu, run, col);  // rows 0..7 total of this column
+    const int base = (h ? upper : 0) + ((int)bd << kCovShift);
+    const float scale = 1.0f / (float)(1 << kCovShift);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int c = base + acc[k];
+        if (!eo) {
+            cov[k] = fminf(fabsf((float)c) * scale, 1.0f);
+        } else {
+            const float t = (float)(c & ((2 << kCovShift) - 1)) * scale;
+            cov[k] = __saturatef(1.0f - fabsf(1.0f - t));
+        }
+    }
+}
+
+__device__ __forceinline__ void zero_cells(int *D) {
+    const int lane = threadIdx.x & 31;
+    for (int k = lane; k < kCovCells; k += 32) D[k] = 0;
+    __syncwarp();
+}
+
+constexpr int kCompWarps = 4;
+
+__global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b, const uint32_t *scene_fb_first) {
+    __shared__ int cells[kCompWarps][kCovCells];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t fb = blockIdx.x * kCompWarps + warp;
+    if (fb >= b.n_fb) return;
+    int *D = cells[warp];
+    const uint32_t s = upper_bound(scene_fb_first, b.n_scenes + 1, fb) - 1;
+    const SceneDev &S = b.scenes[s];
+    const uint32_t local = fb - S.fb_first;
+    const uint32_t fx = local % S.fbw, fy = local / S.fbw;
+    const int col = lane & 15, h = lane >> 4;
+    const float inv255 = 1.0f / 255.0f;
+    float dr[8], dg[8], db[8], da[8];
+    {
+        const float r = (float)(S.clear & 0xffu) * inv255, g = (float)((S.clear >> 8) & 0xffu) * inv255,
+                    bl = (float)((S.clear >> 16) & 0xffu) * inv255, a = (float)(S.clear >> 24) * inv255;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            dr[k] = r;
+            dg[k] = g;
+            db[k] = bl;
+            da[k] = a;
+        }
+    }
+    const uint32_t e0 = b.fb_count[fb], e1 = b.fb_count[fb + 1];
+    for (uint32_t e = e0; e < e1; e++) {
+        const uint32_t gt = b.list[e];
+        const uint32_t p = b.tile_path[gt];
+        const uint32_t flags = b.paths[p].flags;
+        const uint32_t color = b.color[p];
+        const int8_t bd = b.tile_backdrop[gt];
+        const uint32_t f0 = b.tile_fills[gt], f1 = b.tile_fills[gt + 1];
+        const bool eo = (flags & 1u) != 0;
+        float cov[8];
+        if (f0 == f1) {
+            if (eo && ((bd < 0 ? -bd : bd) & 1) == 0) continue;
+#pragma unroll
+            for (int k = 0; k < 8; k++) cov[k] = 1.0f;
+        } else {
+            zero_cells(D);
+            alpha_coverage(b, f0, f1, bd, eo, D, cov);
+            __syncwarp();
+        }
+        const float pr = (float)(color & 0xffu) * inv255, pg = (float)((color >> 8) & 0xffu) * inv255,
+                    pb = (float)((color >> 16) & 0xffu) * inv255, pa = (float)(color >> 24) * inv255;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const float a = pa * cov[k], ia = 1.0f - a;
+            dr[k] = dr[k] * ia + pr * a;
+            dg[k] = dg[k] * ia + pg * a;
+            db[k] = db[k] * ia + pb * a;
+            da[k] = da[k] * ia + a;
+        }
+    }
+    const uint32_t px = fx * 16 + (uint32_t)col;
+    if (px >= S.img_w) return;
+    uchar4 *img = reinterpret_cast<uchar4 *>(b.image + S.img_offset);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint32_t py = fy * 16 + (uint32_t)(h * 8 + k);
+        if (py < S.img_h) {
+            img[(size_t)py * S.img_w + px] =
+                make_uchar4((unsigned char)__float2uint_rn(__saturatef(dr[k]) * 255.0f),
+                            (unsigned char)__float2uint_rn(__saturatef(dg[k]) * 255.0f),
+                            (unsigned char)__float2uint_rn(__saturatef(db[k]) * 255.0f),
+                            (unsigned char)__float2uint_rn(__saturatef(da[k]) * 255.0f));
+        }
+    }
+}
+
+// Coverage of listed alpha tiles after the fill rule (test output; one warp per tile).
+__global__ void __launch_bounds__(kCompWarps * 32) k_coverage_dump(Batch b, const uint32_t *tiles, uint32_t n,
+                                                                   float *out) {
+    __shared__ int cells[kCompWarps][kCovCells];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t k = blockIdx.x * kCompWarps + warp;
+    if (k >= n) return;
+    int *D = cells[warp];
+    const uint32_t gt = tiles[k];
+    const uint32_t p = b.tile_path[gt];
+    zero_cells(D);
+    float cov[8];
+    alpha_coverage(b, b.tile_fills[gt], b.tile_fills[gt + 1], b.tile_backdrop[gt], (b.paths[p].flags & 1u) != 0, D,
+                   cov);
+    const int col = lane & 15, h = lane >> 4;
+#pragma unroll
+    for (int r = 0; r < 8; r++) out[(size_t)k * 256 + (h * 8 + r) * 16 + col] = cov[r];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers
+
+cudaError_t launch_normalize(const Batch &b, uint2 *path_contours, cudaStream_t st) {
+    if (b.n_contours) k_normalize_contours<<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
+    if (b.n_paths) k_normalize_paths<<<grid_for(b.n_paths), kThreads, 0, st>>>(b, path_contours);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_path_setup(const Batch &b, const uint2 *path_contours, cudaStream_t st) {
+    if (b.n_paths) k_path_setup<<<grid_for(uint64_t(b.n_paths) * 32), kThreads, 0, st>>>(b, path_contours);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_path_offsets(const Batch &b, cudaStream_t st) {
+    if (b.n_paths) k_path_offsets<<<grid_for(b.n_paths), kThreads, 0, st>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st) {
+    if (!b.n_contours) return cudaSuccess;
+    if (write) k_contour_segments<true><<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
+    else k_contour_segments<false><<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st) {
+    if (!n_segs) return cudaSuccess;
+    if (write) k_flatten<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs);
+    else k_flatten<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream_t st) {
+    if (!n_leaves) return cudaSuccess;
+    if (write) k_bin<true><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves);
+    else k_bin<false><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_propagate(const Batch &b, uint32_t n_cols, cudaStream_t st) {
+    if (n_cols) k_propagate<<<grid_for(n_cols), kThreads, 0, st>>>(b, n_cols);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_list(const Batch &b, uint32_t n_tiles, bool write, cudaStream_t st) {
+    if (!n_tiles) return cudaSuccess;
+    if (write) k_list<true><<<grid_for(n_tiles), kThreads, 0, st>>>(b, n_tiles);
+    else k_list<false><<<grid_for(n_tiles), kThreads, 0, st>>>(b, n_tiles);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_list_sort(const Batch &b, cudaStream_t st) {
+    if (b.n_fb) k_list_sort<<<b.n_fb, kSortThreads, 0, st>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_composite(const Batch &b, const uint32_t *scene_fb_first, cudaStream_t st) {
+    if (b.n_fb) k_composite<<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b, scene_fb_first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t n, float *out, cudaStream_t st) {
+    if (n) k_coverage_dump<<<grid_for(n, kCompWarps), kCompWarps * 32, 0, st>>>(b, tiles, n, out);
+    return cudaGetLastError();
+}
+
+}  // namespace pfc

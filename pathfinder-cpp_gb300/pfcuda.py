@@ -1,0 +1,211 @@
+"""Python front end of libpfcuda.so (the C-ABI in include/pfcuda.h).
+
+This mirrors the reference's per-frame flow, ``Canvas::draw``
+(pathfinder/core/canvas.cpp:557-567): a scene is handed to the renderer
+(``Renderer`` = :class:`Renderer` here, one CUDA context), drawn, and the
+destination image read back.  The CUDA library is required: there is no CPU
+fallback, and constructing a :class:`Renderer` without the built library or
+without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libpfcuda.so")
+
+PF_OK = 0
+PF_CONFIG_STAGE_TIMING = 0x1
+
+EXPORTS = [
+    "pf_abi_version", "pf_device_count", "pf_ctx_create", "pf_ctx_destroy", "pf_last_error",
+    "pf_scene_upload", "pf_scene_upload_batch", "pf_render", "pf_read_image", "pf_read_image_scene",
+    "pf_image_device_ptr", "pf_read_canon", "pf_read_canon_scene", "pf_read_coverage", "pf_draw",
+]
+
+
+class SceneView(C.Structure):
+    _fields_ = [
+        ("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_start", C.c_void_p),
+        ("path_start", C.c_void_p), ("fill_rule", C.c_void_p), ("color", C.c_void_p),
+        ("n_points", C.c_uint32), ("n_contours", C.c_uint32), ("n_paths", C.c_uint32),
+        ("width", C.c_float), ("height", C.c_float), ("clear_color", C.c_uint32),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int), ("stream", C.c_void_p), ("flags", C.c_uint32),
+                ("reserved", C.c_uint32 * 8)]
+
+
+class FrameStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "paths", "contours", "points", "segments", "microlines", "tiles", "fills", "alpha_tiles",
+        "visible_tiles", "composite_entries", "framebuffer_tiles")] + [
+        ("overflow", C.c_uint32), ("kernel_error", C.c_uint32)] + [
+        (n, C.c_float) for n in ("ms_setup", "ms_flatten", "ms_bin", "ms_propagate", "ms_lists",
+                                 "ms_composite", "ms_total")]
+
+    def to_dict(self) -> Dict[str, float]:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Canon(C.Structure):
+    _fields_ = [
+        ("n_paths", C.c_uint32), ("path_rect", C.c_void_p), ("path_tile_first", C.c_void_p),
+        ("path_column_first", C.c_void_p), ("n_tiles", C.c_uint64), ("tile_alpha", C.c_void_p),
+        ("tile_backdrop", C.c_void_p), ("tile_fill_count", C.c_void_p), ("n_fills", C.c_uint64),
+        ("fills", C.c_void_p), ("n_columns", C.c_uint64), ("column_backdrop", C.c_void_p),
+        ("fb_tiles_x", C.c_uint32), ("fb_tiles_y", C.c_uint32), ("z", C.c_void_p),
+        ("fb_list_first", C.c_void_p), ("n_list", C.c_uint64), ("fb_list", C.c_void_p),
+    ]
+
+
+class PfError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"pfcuda status {status}: {msg}")
+        self.status = status
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load libpfcuda.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"{path} is not built; run pathfinder-cpp_gb300/build.py")
+        lib = C.CDLL(path)
+        lib.pf_last_error.restype = C.c_char_p
+        lib.pf_last_error.argtypes = [C.c_void_p]
+        for name in EXPORTS:
+            if name != "pf_last_error":
+                getattr(lib, name).restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def scene_view(scene) -> "tuple[SceneView, list]":
+    """pf_scene_view over a scenes.Scene (numpy arrays); returns (view, keepalive)."""
+    arrs = [np.ascontiguousarray(scene.points, np.float32), np.ascontiguousarray(scene.flags, np.uint8),
+            np.ascontiguousarray(scene.contour_start, np.uint32),
+            np.ascontiguousarray(scene.path_start, np.uint32),
+            np.ascontiguousarray(scene.fill_rule, np.uint8), np.ascontiguousarray(scene.color, np.uint32)]
+    v = SceneView(*(a.ctypes.data for a in arrs), scene.n_points, scene.n_contours, scene.n_paths,
+                  scene.width, scene.height, scene.clear)
+    return v, arrs
+
+
+def _arr(ptr, n, dtype):
+    if n == 0 or not ptr:
+        return np.zeros(0, dtype)
+    buf = (C.c_char * (int(n) * np.dtype(dtype).itemsize)).from_address(ptr)
+    return np.frombuffer(buf, dtype=dtype).copy()
+
+
+class Renderer:
+    """One CUDA context: upload scenes, draw them, read images and tile data back."""
+
+    def __init__(self, device: int = 0, stream: int = 0, stage_timing: bool = False):
+        self.lib = load()
+        cfg = Config(device, C.c_void_p(stream or None), PF_CONFIG_STAGE_TIMING if stage_timing else 0)
+        h = C.c_void_p()
+        self._check(self.lib.pf_ctx_create(C.byref(cfg), C.byref(h)), None)
+        self.ctx = h
+        self._sizes: List[tuple] = []
+
+    def _check(self, st: int, ctx) -> None:
+        if st != PF_OK:
+            msg = self.lib.pf_last_error(ctx)
+            raise PfError(st, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if getattr(self, "ctx", None):
+            self.lib.pf_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- frame ---------------------------------------------------------------
+    def upload(self, scenes) -> None:
+        if not isinstance(scenes, (list, tuple)):
+            scenes = [scenes]
+        views, keep = [], []
+        for s in scenes:
+            v, k = scene_view(s)
+            views.append(v)
+            keep.append(k)
+        arr = (SceneView * len(views))(*views)
+        self._check(self.lib.pf_scene_upload_batch(self.ctx, arr, len(views)), self.ctx)
+        self._sizes = [(int(np.ceil(s.width)), int(np.ceil(s.height))) for s in scenes]
+
+    def render(self) -> Dict[str, float]:
+        st = FrameStats()
+        self._check(self.lib.pf_render(self.ctx, C.byref(st)), self.ctx)
+        return st.to_dict()
+
+    def image(self, scene: int = 0) -> np.ndarray:
+        w, h = self._sizes[scene]
+        out = np.empty((h, w, 4), np.uint8)
+        self._check(self.lib.pf_read_image_scene(self.ctx, scene, C.c_void_p(out.ctypes.data), out.nbytes),
+                    self.ctx)
+        return out
+
+    def canon(self, scene: int = 0) -> Dict[str, np.ndarray]:
+        r = Canon()
+        self._check(self.lib.pf_read_canon_scene(self.ctx, scene, C.byref(r)), self.ctx)
+        nfb = r.fb_tiles_x * r.fb_tiles_y
+        return {
+            "path_rect": _arr(r.path_rect, 4 * r.n_paths, np.int32).reshape(-1, 4),
+            "path_tile_first": _arr(r.path_tile_first, r.n_paths + 1, np.uint64),
+            "path_column_first": _arr(r.path_column_first, r.n_paths + 1, np.uint64),
+            "tile_alpha": _arr(r.tile_alpha, r.n_tiles, np.uint8),
+            "tile_backdrop": _arr(r.tile_backdrop, r.n_tiles, np.int8),
+            "tile_fill_count": _arr(r.tile_fill_count, r.n_tiles, np.uint32),
+            "fills": _arr(r.fills, 4 * r.n_fills, np.uint16).reshape(-1, 4),
+            "column_backdrop": _arr(r.column_backdrop, r.n_columns, np.int32),
+            "fb_tiles": np.array([r.fb_tiles_x, r.fb_tiles_y], np.uint32),
+            "z": _arr(r.z, nfb, np.int32),
+            "fb_list_first": _arr(r.fb_list_first, nfb + 1, np.uint64),
+            "fb_list": _arr(r.fb_list, r.n_list, np.uint32),
+        }
+
+    def coverage(self) -> np.ndarray:
+        n = C.c_uint64()
+        self._check(self.lib.pf_read_coverage(self.ctx, None, C.c_size_t(0), C.byref(n)), self.ctx)
+        out = np.empty((n.value, 16, 16), np.float32)
+        self._check(self.lib.pf_read_coverage(self.ctx, C.c_void_p(out.ctypes.data), C.c_size_t(out.size),
+                                              C.byref(n)), self.ctx)
+        return out
+
+    def draw(self, scene) -> np.ndarray:
+        """Upload, render and read back one scene (the whole frame through the C-ABI)."""
+        v, keep = scene_view(scene)
+        w, h = int(np.ceil(scene.width)), int(np.ceil(scene.height))
+        out = np.empty((h, w, 4), np.uint8)
+        self._check(self.lib.pf_draw(self.ctx, C.byref(v), C.c_void_p(out.ctypes.data), out.nbytes, None),
+                    self.ctx)
+        self._sizes = [(w, h)]
+        return out
+
+
+def device_count() -> int:
+    lib = load()
+    n = C.c_int(0)
+    st = lib.pf_device_count(C.byref(n))
+    return n.value if st == PF_OK else 0

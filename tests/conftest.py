@@ -1,0 +1,63 @@
+import glob
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "pathfinder-cpp_gb300")
+for p in (os.path.join(ROOT, "oracle"), PKG, ROOT):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+CANON_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha", "tile_backdrop",
+              "tile_fill_count", "fills", "column_backdrop", "fb_tiles", "z", "fb_list_first", "fb_list"]
+TILE_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha", "tile_backdrop",
+             "tile_fill_count", "fills", "column_backdrop"]
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")
+
+
+def golden_names():
+    return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load_golden(name):
+    import scenes as S
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    w, h, clear = d["meta"]
+    sc = S.Scene(points=d["points"], flags=d["flags"], contour_start=d["contour_start"],
+                 path_start=d["path_start"], fill_rule=d["fill_rule"], color=d["color"],
+                 width=float(w), height=float(h), clear=int(clear))
+    ref = {k: d["ref_" + k] for k in CANON_KEYS}
+    return sc, ref
+
+
+@pytest.fixture(scope="session")
+def oracle_mod():
+    import oracle
+    oracle.build()
+    return oracle
+
+
+@pytest.fixture(scope="session")
+def pf():
+    """The CUDA library, built here if needed; on a machine without a GPU GPU tests are skipped."""
+    import build as pf_build
+    pf_build.build()
+    import pfcuda
+    pfcuda.load()
+    return pfcuda
+
+
+@pytest.fixture(scope="session")
+def renderer(pf):
+    if pf.device_count() < 1:
+        pytest.fail("no CUDA device visible to a GPU test")
+    r = pf.Renderer(stage_timing=True)
+    yield r
+    r.close()

@@ -1,0 +1,192 @@
+"""Generate the golden fixtures from the reference's own d3d9 tiler.
+
+Run in a checkout next to the reference sources (the reference tree is read from
+PF_REFERENCE_ROOT, default /root/reference):
+
+    python tests/golden/make_golden.py
+
+For every scene below it builds oracle/_ref/libpfref.so (the reference's Tiler,
+ObjectBuilder and SceneBuilderD3D9 compiled from their sources, driven by
+oracle/ref_harness.cpp), runs it, and stores the scene together with the
+reference's canonical integer output:
+
+* ``<name>.npz``   - inputs and every canonical array (small scenes), and
+* ``digests.json`` - SHA-256 of every canonical array of the full-size scenes,
+                     plus a digest of their inputs so a test can tell that the
+                     generator still produces the same scene.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "pathfinder-cpp_gb300"))
+
+import oracle  # noqa: E402
+import scenes as S  # noqa: E402
+
+CANON_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha", "tile_backdrop",
+              "tile_fill_count", "fills", "column_backdrop", "fb_tiles", "z", "fb_list_first", "fb_list"]
+INPUT_KEYS = ["points", "flags", "contour_start", "path_start", "fill_rule", "color"]
+
+
+def build_scene(paths, width, height, clear=0) -> S.Scene:
+    """paths: list of (contours, rule, rgba); contours: list of (points[N,2], flags[N])."""
+    pts, fl, cstart, pstart, rules, colors = [], [], [0], [0], [], []
+    for contours, rule, rgba in paths:
+        for p, f in contours:
+            p = np.asarray(p, np.float32).reshape(-1, 2)
+            f = np.asarray(f, np.uint8)
+            assert len(p) == len(f)
+            pts.append(p)
+            fl.append(f)
+            cstart.append(cstart[-1] + len(p))
+        pstart.append(pstart[-1] + len(contours))
+        rules.append(rule)
+        colors.append(int(S.pack_rgba(*rgba)))
+    return S.Scene(points=np.concatenate(pts) if pts else np.zeros((0, 2), np.float32),
+                   flags=np.concatenate(fl) if fl else np.zeros(0, np.uint8),
+                   contour_start=np.asarray(cstart, np.uint32), path_start=np.asarray(pstart, np.uint32),
+                   fill_rule=np.asarray(rules, np.uint8), color=np.asarray(colors, np.uint32),
+                   width=float(width), height=float(height), clear=int(clear))
+
+
+def poly(*xy):
+    p = np.asarray(xy, np.float32).reshape(-1, 2)
+    return p, np.zeros(len(p), np.uint8)
+
+
+def edge_scenes():
+    red, green, blue = (255, 0, 0, 255), (0, 160, 0, 255), (0, 0, 255, 255)
+    half = (20, 40, 200, 128)
+    out = {}
+    # 16x16-aligned square: exact backdrops, no fills inside
+    out["aligned_square"] = build_scene([([poly(16, 16, 48, 16, 48, 48, 16, 48)], 0, red)], 64, 64)
+    # half-pixel offset rectangle: coverage 0.5 on its edges
+    out["half_pixel_rect"] = build_scene([([poly(10.5, 7.5, 37.5, 7.5, 37.5, 40.5, 10.5, 40.5)], 0, blue)], 48, 48)
+    # self-overlapping pentagram, even-odd (hole) and nonzero (filled)
+    star = poly(50, 5, 79, 95, 2, 40, 98, 40, 21, 95)
+    out["star_even_odd"] = build_scene([([star], 1, red), ([poly(*(np.asarray(star[0]).ravel() + 3))], 0, half)],
+                                       100, 100)
+    # crossing the left, right and bottom edges; partly above the top edge (top is never clipped)
+    out["view_box_edges"] = build_scene([
+        ([poly(-30, 20, 90, -40, 130, 60, 40, 140)], 0, green),
+        ([poly(-10, -50, 60, -30, 20, 30)], 1, half),
+        ([poly(70, 70, 140, 75, 75, 160)], 0, blue)], 100, 90)
+    # canvas width not a multiple of 16, tiny shapes, a point exactly on the right edge
+    out["odd_canvas"] = build_scene([
+        ([poly(0, 0, 100, 0, 100, 75, 0, 75)], 0, (255, 255, 255, 255)),
+        ([poly(96, 10, 112, 20, 96, 40)], 0, red),
+        ([poly(3.25, 3.75, 5.5, 3.75, 4.0, 6.0)], 0, blue)], 100, 75, clear=int(S.pack_rgba(10, 20, 30, 255)))
+    # lines through tile corners (the walk's tie rule) and exact tile boundaries
+    out["tile_corners"] = build_scene([
+        ([poly(0, 0, 64, 64, 0, 64)], 0, red),
+        ([poly(64, 0, 0, 64, 64, 64)], 1, half),
+        ([poly(16, 48, 48, 16, 48, 48)], 0, green)], 64, 64)
+    # closing line skipped when first ~= last (1e-4), kept when they differ by more
+    out["closing_line"] = build_scene([
+        ([poly(10, 10, 50, 12, 30, 50, 10.00005, 10.00003)], 0, red),
+        ([poly(16.00001, 20, 40, 30, 15.99, 60.2)], 0, blue)], 64, 64)
+    # malformed point patterns stop the contour; single-point and empty contours; empty path
+    q_bad = (np.asarray([[5, 5], [30, 5], [40, 20], [30, 40], [5, 40]], np.float32),
+             np.asarray([0, 1, 1, 0, 0], np.uint8))
+    c_ok = (np.asarray([[5, 50], [20, 45], [40, 45], [55, 60], [30, 62]], np.float32),
+            np.asarray([0, 1, 2, 0, 0], np.uint8))
+    one = (np.asarray([[60, 60]], np.float32), np.asarray([0], np.uint8))
+    ctl_first = (np.asarray([[10, 10], [20, 20], [30, 10]], np.float32), np.asarray([1, 0, 0], np.uint8))
+    empty = (np.zeros((0, 2), np.float32), np.zeros(0, np.uint8))
+    out["malformed"] = build_scene([([q_bad], 0, red), ([c_ok, one, empty], 0, green), ([], 0, blue),
+                                    ([ctl_first], 0, half)], 64, 64)
+    # quadratics and cubics with coincident control points; degenerate and vertical lines
+    quad = (np.asarray([[4, 30], [32, -10], [60, 30], [32, 62], [4, 30]], np.float32),
+            np.asarray([0, 1, 0, 1, 0], np.uint8))
+    cub = (np.asarray([[8, 8], [8, 8], [56, 56], [56, 8], [56, 8], [56, 8], [8, 56]], np.float32),
+           np.asarray([0, 1, 2, 0, 1, 2, 0], np.uint8))
+    vert = poly(20, 5, 20, 60, 20, 60, 40, 60, 40, 5)
+    out["curves_degenerate"] = build_scene([([quad], 0, red), ([cub], 1, half), ([vert], 0, green)], 64, 64)
+    # a long line from far above the view box into it (walks many tiles above the rect)
+    out["from_far_above"] = build_scene([([poly(30, -900, 50, 40, 10, 50)], 0, red),
+                                         ([poly(5, 20, 60, -3000, 60, 60)], 1, blue)], 64, 64)
+    # entirely outside the view box (left, right, below, above): empty tile rects
+    out["outside"] = build_scene([([poly(-50, 10, -10, 10, -30, 40)], 0, red),
+                                  ([poly(80, 10, 120, 10, 100, 40)], 0, red),
+                                  ([poly(10, 80, 40, 80, 30, 120)], 0, red),
+                                  ([poly(10, -80, 40, -80, 30, -20)], 0, red)], 64, 64)
+    # glyph with holes (inner contour reversed), nonzero
+    outer = poly(8, 8, 56, 8, 56, 56, 8, 56)
+    inner = poly(20, 20, 20, 44, 44, 44, 44, 20)
+    out["hole"] = build_scene([([outer, inner], 0, (0, 0, 0, 255))], 64, 64,
+                              clear=int(S.pack_rgba(255, 255, 255, 255)))
+    # translucent stack over an opaque base (z-buffer must not cull what shows through)
+    out["translucent_stack"] = build_scene([
+        ([poly(0, 0, 64, 0, 64, 64, 0, 64)], 0, (200, 200, 200, 255)),
+        ([poly(4, 4, 60, 10, 30, 60)], 0, (255, 0, 0, 100)),
+        ([poly(10, 50, 60, 50, 35, 2)], 1, (0, 0, 255, 160)),
+        ([poly(20, 20, 40, 20, 40, 40, 20, 40)], 0, (0, 255, 0, 255)),
+        ([poly(0, 30, 64, 34, 64, 36, 0, 40)], 0, (255, 255, 0, 60))], 64, 64)
+    # winding beyond int8: 200 nested copies of one square (backdrop wraps)
+    sq = poly(8, 8, 40, 8, 40, 40, 8, 40)
+    out["int8_wrap"] = build_scene([([sq] * 200, 0, red), ([sq] * 130, 1, half)], 48, 48)
+    return out
+
+
+def generator_scenes():
+    return {
+        "gen_plain_small_s1": S.plain_small(seed=1, n_paths=24, side=256),
+        "gen_large_mixed_s2": S.large_single(seed=2, n_paths=120, side=512),
+        "gen_glyphs_s3": S.glyphs(seed=3, n_paths=400, side=256),
+        "gen_mixed_s4": S.mixed(seed=4, n_paths=96, side=512),
+        "gen_batched_scene_s5": S.batched(n_scenes=3, first_seed=5, hi_paths=64)[2],
+    }
+
+
+def full_scenes():
+    return {"plain_small_1024": S.plain_small()}
+
+
+def digest(a: np.ndarray) -> str:
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.dtype.str.encode() + str(a.shape).encode() + a.tobytes()).hexdigest()
+
+
+def scene_digest(sc: S.Scene) -> str:
+    h = hashlib.sha256()
+    for k in INPUT_KEYS:
+        h.update(digest(getattr(sc, k)).encode())
+    h.update(np.asarray([sc.width, sc.height, sc.clear], np.float64).tobytes())
+    return h.hexdigest()
+
+
+def main() -> None:
+    oracle.build(reference=True)
+    if not oracle.have_reference():
+        raise SystemExit("the reference tiler could not be built (is the reference tree present?)")
+    small = dict(edge_scenes())
+    small.update(generator_scenes())
+    for name, sc in small.items():
+        ref = oracle.reference_tile_scene(sc)
+        arrays = {k: getattr(sc, k) for k in INPUT_KEYS}
+        arrays["meta"] = np.asarray([sc.width, sc.height, sc.clear], np.float64)
+        for k in CANON_KEYS:
+            arrays["ref_" + k] = ref[k]
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
+        print(f"{name}: {sc.n_paths} paths, {len(ref['fills'])} fills, {int(ref['tile_alpha'].sum())} alpha tiles")
+    digests = {}
+    for name, sc in full_scenes().items():
+        ref = oracle.reference_tile_scene(sc)
+        digests[name] = {"scene": scene_digest(sc), "canon": {k: digest(ref[k]) for k in CANON_KEYS},
+                         "fills": int(len(ref["fills"])), "alpha_tiles": int(ref["tile_alpha"].sum())}
+        print(f"{name}: {digests[name]['fills']} fills")
+    with open(os.path.join(HERE, "digests.json"), "w") as f:
+        json.dump(digests, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,105 @@
+"""The restated oracle against the reference's own tiler (golden fixtures, digests, live runs)."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import CANON_KEYS, GOLDEN, golden_names, load_golden
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_restated_tiler_matches_reference_golden(oracle_mod, name):
+    sc, ref = load_golden(name)
+    ours = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D9)
+    for k in CANON_KEYS:
+        assert ours[k].shape == ref[k].shape, k
+        assert np.array_equal(ours[k], ref[k]), k
+
+
+def _digest(a):
+    a = np.ascontiguousarray(a)
+    return hashlib.sha256(a.dtype.str.encode() + str(a.shape).encode() + a.tobytes()).hexdigest()
+
+
+def test_restated_tiler_full_plain_small_digests(oracle_mod):
+    import scenes as S
+    with open(os.path.join(GOLDEN, "digests.json")) as f:
+        want = json.load(f)["plain_small_1024"]
+    sc = S.plain_small()
+    h = hashlib.sha256()
+    for k in ["points", "flags", "contour_start", "path_start", "fill_rule", "color"]:
+        h.update(_digest(getattr(sc, k)).encode())
+    h.update(np.asarray([sc.width, sc.height, sc.clear], np.float64).tobytes())
+    assert h.hexdigest() == want["scene"], "the generator no longer produces the pinned scene"
+    ours = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D9)
+    for k in CANON_KEYS:
+        assert _digest(ours[k]) == want["canon"][k], k
+
+
+def test_restated_tiler_threads_agree(oracle_mod):
+    import ctypes as C
+    import scenes as S
+    sc = S.large_single(seed=9, n_paths=300, side=1024)
+    one = oracle_mod.tile_scene(sc)
+    lib = oracle_mod._lib(oracle_mod.LIB_ORACLE)
+    v, keep = oracle_mod.scene_view(sc)
+    r = oracle_mod.Result()
+    assert lib.pfo_tile_scene_mt(C.byref(v), C.c_int(1), C.c_int(4), C.byref(r)) == 0
+    many = oracle_mod.result_to_dict(r)
+    lib.pfo_free(C.byref(r))
+    assert oracle_mod.compare(one, many) == []
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13, 14])
+def test_restated_tiler_matches_live_reference(oracle_mod, seed):
+    if not os.path.isdir(os.path.join(oracle_mod.REF_ROOT, "pathfinder")):
+        pytest.skip("reference tree not present")
+    oracle_mod.build(reference=True)
+    import scenes as S
+    scs = [S.plain_small(seed=seed, n_paths=16, side=320), S.large_single(seed=seed, n_paths=60, side=700),
+           S.glyphs(seed=seed, n_paths=200, side=300)]
+    for sc in scs:
+        ref = oracle_mod.reference_tile_scene(sc)
+        ours = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D9)
+        assert oracle_mod.compare(ref, ours, CANON_KEYS) == []
+
+
+def test_z_rules_differ_only_on_even_odd_even_backdrop(oracle_mod):
+    sc, _ = load_golden("int8_wrap")
+    d9 = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D9)
+    d11 = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D11)
+    for k in ["tile_alpha", "tile_backdrop", "fills", "column_backdrop"]:
+        assert np.array_equal(d9[k], d11[k])
+
+
+def test_pixel_oracle_known_answers(oracle_mod):
+    # 16x16-aligned square: fully covered inside, untouched outside.  add_fill clamps
+    # tile-local coordinates to 4095/256 px (object_builder.cpp:33-35), so the top edge's
+    # fill stops 1/256 px short of the tile's right edge and the last pixel column of each
+    # tile is covered 255/256 -> alpha 254.
+    sc, _ = load_golden("aligned_square")
+    img, _ = oracle_mod.render(sc)
+    inner = img[16:48, 16:48]
+    assert (inner[:, :, 1:3] == 0).all()
+    cols = inner[:, :, 3].min(axis=0)
+    assert (cols[[15, 31]] == 254).all() and (np.delete(cols, [15, 31]) == 255).all()
+    assert (img[:16] == 0).all() and (img[48:] == 0).all()
+    # half-pixel rectangle: edge pixels half covered (alpha 128 of 255 -> 127.5 rounds to 128)
+    sc, _ = load_golden("half_pixel_rect")
+    img, cov = oracle_mod.render(sc, coverage=True)
+    assert img[20, 10, 3] in (127, 128) and img[20, 37, 3] in (127, 128)
+    assert img[20, 20, 3] == 255 and img[20, 5, 3] == 0
+    # hole: white inside the inner square, black ring
+    sc, _ = load_golden("hole")
+    img, _ = oracle_mod.render(sc)
+    assert (img[30, 30] == [255, 255, 255, 255]).all()
+    assert (img[12, 30] == [0, 0, 0, 255]).all()
+
+
+def test_even_odd_hole_and_nonzero_fill(oracle_mod):
+    sc, _ = load_golden("star_even_odd")
+    img, _ = oracle_mod.render(sc)
+    # the pentagon at the centre of the star is a hole under even-odd (only the translucent copy shows)
+    assert img[52, 50, 0] < 128
