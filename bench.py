@@ -1,0 +1,325 @@
+#!/usr/bin/env python
+"""Benchmark of the GPU-driven fill pipeline on one GB300 (or N replicas).
+
+Workload (default): the batched configuration - 512 independent scenes, path
+count per scene log-uniform in [16, 4096] from the 240-path cubic generator,
+canvas side drawn from {256, 512, 1024, 2048} (scenes.batched()).  One step =
+one pass of the pipeline over the whole batch.
+
+Arms printed in one JSON line (rank 0):
+  value        scenes/s of the batched frame (all 512 scenes in one frame),
+               inputs resident in HBM when the timed region starts;
+  plain        scenes/s of the plain single-scene pipeline (one frame per scene);
+  e2e          scenes/s through the C-ABI from pinned host buffers: upload,
+               frame and read-back of every image inside the timed region;
+  roofline     the composite kernel (fused coverage + src-over), achieved bytes/s
+               from its algorithmic bytes and its CUDA-event time;
+  cpu_baseline the oracle port (restated d3d9 tiler + FP64 coverage/composite)
+               on the host cores over a bounded sample of the batch.
+
+--impl reference times that CPU implementation alone (the reference arm).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "pathfinder-cpp_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "frame ms & scenes/s: batched+learned vs plain CUDA pipeline, 1 GB300, exact tiles"
+UNIT = "scenes/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--scenes", type=int, default=512)
+    ap.add_argument("--cpu-sample-every", type=int, default=32)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(n_scenes, scenes_list):
+    import numpy as np
+    return {
+        "workload": "batched: %d scenes, paths/scene log-uniform 16-4096 (cubic 8-24 seg, control points "
+                    "uniform over the canvas), canvas side in {256,512,1024,2048}, seeds 1000+i" % n_scenes,
+        "scenes": n_scenes,
+        "paths": int(sum(s.n_paths for s in scenes_list)),
+        "points": int(sum(s.n_points for s in scenes_list)),
+        "pixels": int(sum(int(np.ceil(s.width)) * int(np.ceil(s.height)) for s in scenes_list)),
+        "tile": 16,
+        "l2": "inputs and working set larger than L2 (129 MB) every step",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def pack_pinned(scenes_list):
+    """All scenes' arrays packed contiguously (per array) in pinned host memory."""
+    import numpy as np
+    import torch
+    import pfcuda
+    keys = [("points", np.float32, 8), ("flags", np.uint8, 1), ("contour_start", np.uint32, 4),
+            ("path_start", np.uint32, 4), ("fill_rule", np.uint8, 1), ("color", np.uint32, 4)]
+    bufs = {}
+    for k, dt, _ in keys:
+        total = sum(getattr(s, k).nbytes for s in scenes_list)
+        t = torch.empty(max(total, 16), dtype=torch.uint8, pin_memory=True)
+        bufs[k] = t
+    offs = {k: 0 for k, _, _ in keys}
+    views = []
+    for s in scenes_list:
+        ptrs = []
+        for k, dt, _ in keys:
+            a = np.ascontiguousarray(getattr(s, k), dt)
+            dst = bufs[k].numpy()[offs[k]:offs[k] + a.nbytes]
+            dst[:] = a.view(np.uint8).reshape(-1)
+            ptrs.append(bufs[k].data_ptr() + offs[k])
+            offs[k] += a.nbytes
+        views.append(pfcuda.SceneView(*ptrs, s.n_points, s.n_contours, s.n_paths, s.width, s.height, s.clear))
+    h2d = sum(offs.values())
+    return bufs, views, h2d
+
+
+def cpu_baseline(scenes_list, every: int, threads: int):
+    """The oracle port over every `every`-th scene: tiling + FP64 coverage/composite."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    if not os.path.exists(oracle.LIB_ORACLE):
+        oracle.build()
+    sample = scenes_list[::every]
+    t0 = time.perf_counter()
+    for s in sample:
+        oracle.render(s, threads=threads)
+    dt = time.perf_counter() - t0
+    return len(sample) / dt, len(sample), dt
+
+
+def run_reference(args, scenes_list):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    # warm-up, then K timed steps; each step renders the bounded sample
+    for _ in range(max(args.warmup, 0)):
+        cpu_baseline(scenes_list, args.cpu_sample_every, threads)
+    times, n = [], 0
+    for _ in range(args.steps):
+        v, n, dt = cpu_baseline(scenes_list, args.cpu_sample_every, threads)
+        times.append(dt)
+    per_step = sum(times) / len(times)
+    value = n / per_step
+    sample = f"every {args.cpu_sample_every}th scene of the batch ({n} scenes), restated d3d9 tiler + FP64 " \
+             f"coverage and src-over composite"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 tiling, f64 coverage",
+        "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    import numpy as np
+    import scenes as S
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        scenes_list = S.batched(n_scenes=args.scenes)
+        run_reference(args, scenes_list)
+        return
+
+    import torch
+    import pfcuda
+    import build as pf_build
+    if not os.path.exists(pfcuda.LIB_PATH):
+        pf_build.build()
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # replicas: every rank renders its own batch (seeds offset by rank); no data-path collective
+    scenes_list = S.batched(n_scenes=args.scenes, first_seed=1000 + 100000 * rank)
+    bufs, views, h2d_bytes = pack_pinned(scenes_list)
+    stream = torch.cuda.Stream()
+    r = pfcuda.Renderer(device=local_rank, stream=stream.cuda_stream, stage_timing=True)
+    r.upload_views(views)
+    img_bytes = r.image_bytes()
+    img_host = torch.empty(img_bytes, dtype=torch.uint8, pin_memory=True)
+    n_scenes = len(scenes_list)
+
+    def timed(fn, steps):
+        barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = [fn() for _ in range(steps)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms, out
+
+    # 1. batched frame, inputs resident
+    for _ in range(args.warmup):
+        r.render()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ms_batched, stats_b = timed(lambda: r.render(), args.steps)
+    clk = clocks.stop()
+    st = stats_b[-1]
+
+    # 2. plain single-scene pipeline (one frame per scene), inputs resident
+    def plain_pass():
+        last = None
+        launches = 0
+        for i in range(n_scenes):
+            last = r.render(i, 1)
+            launches += last["kernel_launches"]
+        return launches
+    plain_pass()
+    ms_plain, launches_plain = timed(plain_pass, max(1, min(args.steps, 3)))
+
+    # 3. end to end through the C-ABI: pinned H2D upload, frame, D2H of every image
+    def e2e_step():
+        r.upload_views(views)
+        s = r.render()
+        r.read_images(img_host.data_ptr(), img_bytes)
+        return s
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    ms_e2e, _ = timed(e2e_step, args.steps)
+
+    # roofline of the composite kernel (fused coverage + src-over)
+    pixels = sum(int(np.ceil(s.width)) * int(np.ceil(s.height)) for s in scenes_list)
+    comp_bytes = (8 * st["composited_fills"] + 13 * st["composite_entries"]
+                  + 8 * (st["framebuffer_tiles"] + 1) + 4 * pixels)
+    comp_ms = st["ms_composite"]
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback 6.8 TB/s"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+    achieved = comp_bytes / (comp_ms * 1e-3) / 1e9 if comp_ms > 0 else None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, n, dt = cpu_baseline(scenes_list, args.cpu_sample_every, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"every {args.cpu_sample_every}th scene ({n} scenes, {dt:.1f} s): restated d3d9 tiler "
+                         f"+ FP64 coverage/composite"}
+
+    if rank == 0:
+        value = world * n_scenes / (ms_batched * 1e-3)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_batched, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (exact-IEEE tiling), int32 fixed-point coverage", "data": "synthetic",
+            "config": workload_config(n_scenes, scenes_list) | {"parallelism": f"replicas x{world}"},
+            "plain": {"value": world * n_scenes / (ms_plain * 1e-3), "unit": UNIT, "ms_per_step": ms_plain,
+                      "gpu_launches_per_step": launches_plain[-1]},
+            "e2e": {"value": world * n_scenes / (ms_e2e * 1e-3), "unit": UNIT, "ms_per_step": ms_e2e,
+                    "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": img_bytes},
+            "stages_ms": {k: st[k] for k in ("ms_setup", "ms_flatten", "ms_bin", "ms_propagate", "ms_lists",
+                                             "ms_composite", "ms_total")},
+            "frame": {k: st[k] for k in ("paths", "segments", "microlines", "tiles", "fills", "composite_entries",
+                                         "composited_fills", "framebuffer_tiles", "host_syncs")},
+            "roofline": {"kernel": "k_composite", "bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                         "peak_source": peak_src, "algorithmic_bytes": comp_bytes},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+            "gpu_launches": int(st["kernel_launches"]) * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    r.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -106,6 +106,9 @@ typedef struct pf_frame_stats {
                            /* frame was re-run by the exact two-pass method        */
     uint32_t kernel_error; /* nonzero if a kernel hit an iteration bound            */
     float ms_setup, ms_flatten, ms_bin, ms_propagate, ms_lists, ms_composite, ms_total;
+    uint64_t composited_fills; /* fills of the alpha tiles left in composite lists     */
+    uint32_t kernel_launches;  /* CUDA kernels this frame launched                     */
+    uint32_t host_syncs;       /* stream synchronisations this frame waited on        */
 } pf_frame_stats;
 
 #define PF_CONFIG_STAGE_TIMING 0x1u
@@ -167,12 +170,22 @@ int pf_scene_upload_batch(void *ctx, const pf_scene_view *scenes, uint32_t n_sce
  */
 int pf_render(void *ctx, pf_frame_stats *stats);
 
+/* Same, for uploaded scenes [first_scene, first_scene + n_scenes) only: the
+ * single-scene frame of the reference when n_scenes == 1. */
+int pf_render_scenes(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats);
+
 /* Copy the last rendered image to host memory: RGBA8, row-major,
  * width_px * height_px * 4 bytes with width_px = ceil(width). */
 int pf_read_image(void *ctx, uint8_t *rgba, size_t capacity_bytes);
 
 /* Same for scene `scene` of an uploaded batch. */
 int pf_read_image_scene(void *ctx, uint32_t scene, uint8_t *rgba, size_t capacity_bytes);
+
+/* Every image of the uploaded batch in one copy: scene i's RGBA8 image starts at
+ * byte offset_of(i) (pf_image_offset) of dst; the total is pf_image_bytes. */
+int pf_image_bytes(void *ctx, uint64_t *bytes);
+int pf_image_offset(void *ctx, uint32_t scene, uint64_t *offset);
+int pf_read_images(void *ctx, uint8_t *dst, size_t capacity_bytes);
 
 /* Device pointer and pitch of the last rendered image (valid until the next
  * render on this context). */

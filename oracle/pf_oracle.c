@@ -690,6 +690,22 @@ static double apply_rule(double c, int even_odd) {
     return v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
 }
 
+/* coverage after the fill rule of alpha tile g into cov[256] (row-major 16x16) */
+static void alpha_tile_coverage(const pfo_result *r, const uint64_t *fill_first, uint64_t g, int8_t bd, int eo,
+                                double cov[256]) {
+    for (int k = 0; k < 256; k++) cov[k] = (double)bd;
+    for (uint64_t f = fill_first[g]; f < fill_first[g + 1]; f++) {
+        const uint16_t *q = r->fills + 4 * f;
+        const double x0 = q[0] / 256.0, y0 = q[1] / 256.0, x1 = q[2] / 256.0, y1 = q[3] / 256.0;
+        const int i0 = (int)floor(x0 < x1 ? x0 : x1), i1 = (int)ceil(x0 < x1 ? x1 : x0);
+        for (int i = i0; i < i1 && i < 16; i++) {
+            if (i < 0) continue;
+            for (int jj = 0; jj < 16; jj++) cov[jj * 16 + i] += fill_area(x0, y0, x1, y1, i, jj);
+        }
+    }
+    for (int k = 0; k < 256; k++) cov[k] = apply_rule(cov[k], eo);
+}
+
 typedef struct {
     const pf_scene_view *s;
     const pfo_result *r;
@@ -724,20 +740,7 @@ static void *render_worker(void *arg) {
             const int eo = j->s->fill_rule[p] == PF_FILL_EVEN_ODD;
             const int8_t bd = r->tile_backdrop[g];
             if (r->tile_alpha[g]) {
-                for (int k = 0; k < 256; k++) cov[k] = (double)bd;
-                for (uint64_t f = j->fill_first[g]; f < j->fill_first[g + 1]; f++) {
-                    const uint16_t *q = r->fills + 4 * f;
-                    const double x0 = q[0] / 256.0, y0 = q[1] / 256.0, x1 = q[2] / 256.0, y1 = q[3] / 256.0;
-                    const int i0 = (int)floor(x0 < x1 ? x0 : x1), i1 = (int)ceil(x0 < x1 ? x1 : x0);
-                    for (int i = i0; i < i1 && i < 16; i++) {
-                        if (i < 0) continue;
-                        for (int jj = 0; jj < 16; jj++) cov[jj * 16 + i] += fill_area(x0, y0, x1, y1, i, jj);
-                    }
-                }
-                for (int k = 0; k < 256; k++) cov[k] = apply_rule(cov[k], eo);
-                if (j->cov_out) {
-                    for (int k = 0; k < 256; k++) j->cov_out[(size_t)g * 256 + k] = (float)cov[k];
-                }
+                alpha_tile_coverage(r, j->fill_first, g, bd, eo, cov);
             } else {
                 if (eo && (abs((int)bd) % 2) == 0) continue;
                 for (int k = 0; k < 256; k++) cov[k] = 1.0;
@@ -767,6 +770,19 @@ static void *render_worker(void *arg) {
                 }
             }
         }
+    }
+    return NULL;
+}
+
+static void *coverage_worker(void *arg) {
+    render_job *j = (render_job *)arg;
+    const pfo_result *r = j->r;
+    double cov[256];
+    for (uint64_t g = j->first; g < r->n_tiles; g += j->step) {
+        if (!r->tile_alpha[g]) continue;
+        const uint32_t p = j->tile_path[g];
+        alpha_tile_coverage(r, j->fill_first, g, r->tile_backdrop[g], j->s->fill_rule[p] == PF_FILL_EVEN_ODD, cov);
+        for (int k = 0; k < 256; k++) j->cov_out[(size_t)g * 256 + k] = (float)cov[k];
     }
     return NULL;
 }
@@ -801,6 +817,14 @@ int pfo_render(const pf_scene_view *s, const pfo_result *r, uint8_t *rgba, float
     }
     if (threads > 1)
         for (int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+    if (coverage_f) {
+        for (int t = 0; t < threads; t++) {
+            if (threads == 1) coverage_worker(&jobs[t]);
+            else pthread_create(&th[t], NULL, coverage_worker, &jobs[t]);
+        }
+        if (threads > 1)
+            for (int t = 0; t < threads; t++) pthread_join(th[t], NULL);
+    }
     free(jobs);
     free(th);
     free(fill_first);

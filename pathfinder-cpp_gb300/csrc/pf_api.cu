@@ -85,8 +85,11 @@ struct Ctx {
     DevBuf z, fb_count, fb_cursor, list, image, status, scan_temp;
     uint32_t *h_status = nullptr;  // pinned
 
-    // totals of the last frame
+    // the scene range of the last frame and its totals
+    uint32_t r_first = 0, r_count = 0, r_paths = 0, r_contours = 0, r_fb = 0;
+    uint32_t r_path_base = 0, r_contour_base = 0, r_fb_base = 0;
     uint32_t n_segs = 0, n_tiles = 0, n_cols = 0, n_leaves = 0, n_fills = 0, n_list = 0;
+    uint32_t syncs = 0;
 
     HostCanon canon;
     cudaEvent_t ev[8] = {};
@@ -271,10 +274,15 @@ Batch make_batch(Ctx *c) {
     b.scenes = c->scenes.as<SceneDev>();
     b.scene_path_first = c->scene_path_first.as<uint32_t>();
     b.scene_contour_first = c->scene_contour_first.as<uint32_t>();
-    b.n_scenes = c->n_scenes;
-    b.n_paths = c->n_paths;
-    b.n_contours = c->n_contours;
-    b.n_points = c->n_points;
+    b.scene_fb_first = c->scene_fb_first.as<uint32_t>();
+    b.n_scenes_all = c->n_scenes;
+    b.scene_base = c->r_first;
+    b.n_scenes = c->r_count;
+    b.path_base = c->r_path_base;
+    b.n_paths = c->r_paths;
+    b.contour_base = c->r_contour_base;
+    b.n_contours = c->r_contours;
+    b.fb_base = c->r_fb_base;
     b.contour_point_first = c->contour_point_first.as<uint32_t>();
     b.contour_path = c->contour_path.as<uint32_t>();
     b.paths = c->paths.as<PathDev>();
@@ -301,7 +309,7 @@ Batch make_batch(Ctx *c) {
     b.fb_cursor = c->fb_cursor.as<uint32_t>();
     b.list = c->list.as<uint32_t>();
     b.list_cap = (uint32_t)std::min<size_t>(c->list.cap / 4, 0xffffffffu);
-    b.n_fb = c->n_fb;
+    b.n_fb = c->r_fb;
     b.image = c->image.as<uint8_t>();
     b.status = c->status.as<uint32_t>();
     return b;
@@ -310,6 +318,7 @@ Batch make_batch(Ctx *c) {
 int read_status(Ctx *c) {
     PF_CUDA(cudaMemcpyAsync(c->h_status, c->status.p, kStCount * 4, cudaMemcpyDeviceToHost, c->stream));
     PF_CUDA(cudaStreamSynchronize(c->stream));
+    c->syncs++;
     return PF_OK;
 }
 
@@ -336,11 +345,29 @@ void record(Ctx *c, int i) {
     if (c->flags & PF_CONFIG_STAGE_TIMING) cudaEventRecord(c->ev[i], c->stream);
 }
 
-// The exact two-pass frame.
-int render_exact(Ctx *c, pf_frame_stats *stats) {
+void set_range(Ctx *c, uint32_t first, uint32_t count) {
+    const SceneDev &a = c->h_scenes[first], &e = c->h_scenes[first + count - 1];
+    c->r_first = first;
+    c->r_count = count;
+    c->r_path_base = a.path_first;
+    c->r_paths = e.path_end - a.path_first;
+    c->r_contour_base = a.contour_first;
+    c->r_contours = e.contour_end - a.contour_first;
+    c->r_fb_base = a.fb_first;
+    c->r_fb = c->h_scene_fb_first[first + count] - a.fb_first;
+}
+
+// The exact two-pass frame over uploaded scenes [first, first + count).
+int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
     if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
+    if (count == 0 || first >= c->n_scenes || count > c->n_scenes - first)
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "scene range out of bounds");
+    c->rendered = false;
+    set_range(c, first, count);
+    c->syncs = 0;
+    const uint64_t launches0 = launches();
     cudaStream_t st = c->stream;
-    const uint32_t N = c->n_paths, C = c->n_contours;
+    const uint32_t N = c->r_paths, C = c->r_contours;
     PF_CUDA(c->status.ensure(kStCount * 4));
     PF_CUDA(cudaMemsetAsync(c->status.p, 0, kStCount * 4, st));
     PF_CUDA(c->contour_point_first.ensure((size_t(C) + 1) * 4));
@@ -350,9 +377,10 @@ int render_exact(Ctx *c, pf_frame_stats *stats) {
     PF_CUDA(c->path_tiles.ensure((size_t(N) + 1) * 4));
     PF_CUDA(c->path_cols.ensure((size_t(N) + 1) * 4));
     PF_CUDA(c->path_contours.ensure(size_t(N) * 8 + 8));
-    PF_CUDA(c->z.ensure(size_t(c->n_fb) * 4 + 4));
-    PF_CUDA(c->fb_count.ensure((size_t(c->n_fb) + 1) * 4));
-    PF_CUDA(c->fb_cursor.ensure(size_t(c->n_fb) * 4 + 4));
+    const uint32_t NFB = c->r_fb;
+    PF_CUDA(c->z.ensure(size_t(NFB) * 4 + 4));
+    PF_CUDA(c->fb_count.ensure((size_t(NFB) + 1) * 4));
+    PF_CUDA(c->fb_cursor.ensure(size_t(NFB) * 4 + 4));
 
     record(c, 0);
     // 1. topology, tile rects, segment counts
@@ -416,15 +444,15 @@ int render_exact(Ctx *c, pf_frame_stats *stats) {
     record(c, 3);
 
     // 4. backdrops, z-buffer
-    PF_CUDA(cudaMemsetAsync(b.z, 0xff, size_t(c->n_fb) * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.z, 0xff, size_t(NFB) * 4, st));
     PF_CUDA(launch_propagate(b, c->n_cols, st));
     record(c, 4);
 
     // 5. composite lists
-    PF_CUDA(cudaMemsetAsync(b.fb_count, 0, (size_t(c->n_fb) + 1) * 4, st));
-    PF_CUDA(cudaMemsetAsync(b.fb_cursor, 0, size_t(c->n_fb) * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.fb_count, 0, (size_t(NFB) + 1) * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.fb_cursor, 0, size_t(NFB) * 4, st));
     PF_CUDA(launch_list(b, c->n_tiles, false, st));
-    if (int e = scan(c, b.fb_count, c->n_fb + 1, kStList)) return e;
+    if (int e = scan(c, b.fb_count, NFB + 1, kStList)) return e;
     if (int e = read_status(c)) return e;
     c->n_list = c->h_status[kStList];
     PF_CUDA(c->list.ensure(size_t(c->n_list) * 4 + 16));
@@ -434,7 +462,7 @@ int render_exact(Ctx *c, pf_frame_stats *stats) {
     record(c, 5);
 
     // 6. coverage + composite
-    PF_CUDA(launch_composite(b, c->scene_fb_first.as<uint32_t>(), st));
+    PF_CUDA(launch_composite(b, st));
     record(c, 6);
     if (int e = read_status(c)) return e;
     if (int e = check_kernel_status(c)) return e;
@@ -442,15 +470,18 @@ int render_exact(Ctx *c, pf_frame_stats *stats) {
 
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
-        stats->paths = c->n_paths;
-        stats->contours = c->n_contours;
-        stats->points = c->n_points;
+        stats->paths = c->r_paths;
+        stats->contours = c->r_contours;
+        stats->points = c->h_scenes[first + count - 1].point_end - c->h_scenes[first].point_first;
         stats->segments = c->n_segs;
         stats->microlines = c->n_leaves;
         stats->tiles = c->n_tiles;
         stats->fills = c->n_fills;
         stats->composite_entries = c->n_list;
-        stats->framebuffer_tiles = c->n_fb;
+        stats->framebuffer_tiles = NFB;
+        stats->composited_fills = c->h_status[kStListFills];
+        stats->kernel_launches = (uint32_t)(launches() - launches0);
+        stats->host_syncs = c->syncs;
         if (c->flags & PF_CONFIG_STAGE_TIMING) {
             float ms[6] = {};
             for (int i = 0; i < 6; i++) cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]);
@@ -476,9 +507,11 @@ int d2h(Ctx *c, std::vector<T> &dst, const void *src, size_t n) {
 // Canonical integer output of scene `si` of the last frame.
 int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
     if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
-    if (si >= c->n_scenes) return fail(c, PF_ERR_INVALID_ARGUMENT, "scene index out of range");
+    if (si < c->r_first || si >= c->r_first + c->r_count)
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "scene was not rendered by the last frame");
     const SceneDev &S = c->h_scenes[si];
-    const uint32_t p0 = S.path_first, p1 = S.path_end, np = p1 - p0;
+    const uint32_t p0 = S.path_first - c->r_path_base, p1 = S.path_end - c->r_path_base, np = p1 - p0;
+    const uint32_t fb0 = S.fb_first - c->r_fb_base;
     std::vector<PathDev> paths;
     std::vector<uint32_t> tf, cf;
     if (int e = d2h(c, paths, c->paths.as<PathDev>() + p0, np)) return e;
@@ -504,9 +537,9 @@ int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
     if (int e = d2h(c, tfill, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0) + 1)) return e;
     if (int e = d2h(c, h.backdrop, c->tile_backdrop.as<int8_t>() + t0, t1 - t0)) return e;
     if (int e = d2h(c, h.col_backdrop, c->col_final.as<int32_t>() + k0, k1 - k0)) return e;
-    if (int e = d2h(c, h.z, c->z.as<int32_t>() + S.fb_first, size_t(S.fbw) * S.fbh)) return e;
+    if (int e = d2h(c, h.z, c->z.as<int32_t>() + fb0, size_t(S.fbw) * S.fbh)) return e;
     std::vector<uint32_t> fbc;
-    if (int e = d2h(c, fbc, c->fb_count.as<uint32_t>() + S.fb_first, size_t(S.fbw) * S.fbh + 1)) return e;
+    if (int e = d2h(c, fbc, c->fb_count.as<uint32_t>() + fb0, size_t(S.fbw) * S.fbh + 1)) return e;
     PF_CUDA(cudaStreamSynchronize(c->stream));
     const uint32_t f0 = tfill[0], f1 = tfill[t1 - t0];
     std::vector<uint2> fl;
@@ -577,6 +610,36 @@ int read_image(Ctx *c, uint32_t si, uint8_t *rgba, size_t cap) {
 }
 
 Ctx *as_ctx(void *p) { return static_cast<Ctx *>(p); }
+
+}  // namespace
+
+extern "C" int pf_image_bytes(void *ctx, uint64_t *bytes) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !bytes) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
+    *bytes = c->image_bytes;
+    return PF_OK;
+}
+
+extern "C" int pf_image_offset(void *ctx, uint32_t scene, uint64_t *offset) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !offset) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (scene >= c->n_scenes) return fail(c, PF_ERR_INVALID_ARGUMENT, "scene index out of range");
+    *offset = c->h_scenes[scene].img_offset;
+    return PF_OK;
+}
+
+extern "C" int pf_read_images(void *ctx, uint8_t *dst, size_t capacity_bytes) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !dst) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
+    if (capacity_bytes < c->image_bytes) return fail(c, PF_ERR_INVALID_ARGUMENT, "image buffer too small");
+    PF_CUDA(cudaMemcpyAsync(dst, c->image.p, c->image_bytes, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+namespace {
 
 }  // namespace
 
@@ -665,7 +728,14 @@ int pf_render(void *ctx, pf_frame_stats *stats) {
     Ctx *c = as_ctx(ctx);
     if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
     cudaSetDevice(c->device);
-    return render_exact(c, stats);
+    return render_exact(c, 0, c->n_scenes, stats);
+}
+
+int pf_render_scenes(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    cudaSetDevice(c->device);
+    return render_exact(c, first_scene, n_scenes, stats);
 }
 
 int pf_read_image(void *ctx, uint8_t *rgba, size_t capacity_bytes) {
@@ -684,9 +754,9 @@ int pf_image_device_ptr(void *ctx, void **rgba, uint32_t *width_px, uint32_t *he
     Ctx *c = as_ctx(ctx);
     if (!c || !rgba) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
     if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
-    *rgba = c->image.p;
-    if (width_px) *width_px = c->h_scenes[0].img_w;
-    if (height_px) *height_px = c->h_scenes[0].img_h;
+    *rgba = c->image.as<uint8_t>() + c->h_scenes[c->r_first].img_offset;
+    if (width_px) *width_px = c->h_scenes[c->r_first].img_w;
+    if (height_px) *height_px = c->h_scenes[c->r_first].img_h;
     return PF_OK;
 }
 
@@ -707,7 +777,7 @@ int pf_draw(void *ctx, const pf_scene_view *scene, uint8_t *rgba, size_t capacit
     if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
     cudaSetDevice(c->device);
     if (int e = upload(c, scene, 1)) return e;
-    if (int e = render_exact(c, stats)) return e;
+    if (int e = render_exact(c, 0, 1, stats)) return e;
     return read_image(c, 0, rgba, capacity_bytes);
 }
 
@@ -717,9 +787,11 @@ int pf_read_coverage(void *ctx, float *out, size_t capacity_floats, uint64_t *n_
     Ctx *c = as_ctx(ctx);
     if (!c || !n_alpha) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
     if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
-    const SceneDev &S = c->h_scenes[0];
+    const SceneDev &S = c->h_scenes[c->r_first];
     std::vector<uint32_t> tf, tfill;
-    if (int e = d2h(c, tf, c->path_tiles.as<uint32_t>() + S.path_first, S.path_end - S.path_first + 1)) return e;
+    if (int e = d2h(c, tf, c->path_tiles.as<uint32_t>() + (S.path_first - c->r_path_base),
+                    S.path_end - S.path_first + 1))
+        return e;
     PF_CUDA(cudaStreamSynchronize(c->stream));
     const uint32_t t0 = tf.front(), t1 = tf.back();
     if (int e = d2h(c, tfill, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0) + 1)) return e;

@@ -69,9 +69,16 @@ struct Batch {
     const uint8_t *fill_rule;
     const uint32_t *color;
     const SceneDev *scenes;
-    const uint32_t *scene_path_first;    // [n_scenes + 1]
-    const uint32_t *scene_contour_first; // [n_scenes + 1]
-    uint32_t n_scenes, n_paths, n_contours, n_points;
+    const uint32_t *scene_path_first;    // [n_scenes_all + 1]
+    const uint32_t *scene_contour_first; // [n_scenes_all + 1]
+    const uint32_t *scene_fb_first;      // [n_scenes_all + 1]
+    uint32_t n_scenes_all;               // scenes uploaded
+    // the scenes rendered by this frame: a contiguous range of the uploaded ones.
+    // Per-frame arrays are indexed from 0 = the range's first path / contour / framebuffer tile.
+    uint32_t scene_base, n_scenes;
+    uint32_t path_base, n_paths;
+    uint32_t contour_base, n_contours;
+    uint32_t fb_base;
 
     // normalised topology
     uint32_t *contour_point_first;       // [n_contours + 1] global
@@ -122,8 +129,13 @@ enum : int {
     kStLeaves = 4,
     kStFills = 5,
     kStList = 6,
+    kStListFills = 7,  // fills of the alpha tiles that made it into composite lists
     kStCount = 16,
 };
+
+// Kernels launched by this library (host-side counter, all contexts).
+uint64_t launches();
+void count_launches(uint32_t n);
 
 // Scans (exclusive, in place allowed); the total lands in *total (device).
 size_t scan_temp_bytes(uint32_t n);
@@ -140,7 +152,7 @@ cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream
 cudaError_t launch_propagate(const Batch &b, uint32_t n_cols, cudaStream_t st);
 cudaError_t launch_list(const Batch &b, uint32_t n_tiles, bool write, cudaStream_t st);
 cudaError_t launch_list_sort(const Batch &b, cudaStream_t st);
-cudaError_t launch_composite(const Batch &b, const uint32_t *scene_fb_first, cudaStream_t st);
+cudaError_t launch_composite(const Batch &b, cudaStream_t st);
 cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t n, float *out, cudaStream_t st);
 
 }  // namespace pfc

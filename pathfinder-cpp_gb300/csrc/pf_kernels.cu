@@ -14,6 +14,8 @@
 // Integer outputs follow the reference's d3d9 CPU tiler bit for bit, so every float
 // operation on that path is written with __f*_rn intrinsics (no FMA contraction), in the
 // same order as the reference's SSE lanes (pathfinder/common/f32x4.h).
+#include <atomic>
+
 #include "pf_internal.h"
 
 namespace pfc {
@@ -50,26 +52,29 @@ inline unsigned grid_for(uint64_t n, int threads = kThreads) {
 __global__ void k_normalize_contours(Batch b) {
     const uint32_t c = global_tid();
     if (c >= b.n_contours) return;
-    const uint32_t s = upper_bound(b.scene_contour_first, b.n_scenes + 1, c) - 1;
+    const uint32_t cg = b.contour_base + c;
+    const uint32_t s = upper_bound(b.scene_contour_first, b.n_scenes_all + 1, cg) - 1;
     const SceneDev &S = b.scenes[s];
-    const uint32_t local = c - S.contour_first;
+    const uint32_t local = cg - S.contour_first;
     b.contour_point_first[c] = S.point_first + b.contour_start_cat[S.cstart_base + local];
-    if (c == b.n_contours - 1) b.contour_point_first[b.n_contours] = b.n_points;
+    if (c == b.n_contours - 1)
+        b.contour_point_first[b.n_contours] = S.point_first + b.contour_start_cat[S.cstart_base + local + 1];
 }
 
 __global__ void k_normalize_paths(Batch b, uint2 *path_contours) {
     const uint32_t p = global_tid();
     if (p >= b.n_paths) return;
-    const uint32_t s = upper_bound(b.scene_path_first, b.n_scenes + 1, p) - 1;
+    const uint32_t pg = b.path_base + p;
+    const uint32_t s = upper_bound(b.scene_path_first, b.n_scenes_all + 1, pg) - 1;
     const SceneDev &S = b.scenes[s];
-    const uint32_t local = p - S.path_first;
-    const uint32_t c0 = S.contour_first + b.path_start_cat[S.pstart_base + local];
-    const uint32_t c1 = S.contour_first + b.path_start_cat[S.pstart_base + local + 1];
+    const uint32_t local = pg - S.path_first;
+    const uint32_t c0 = S.contour_first + b.path_start_cat[S.pstart_base + local] - b.contour_base;
+    const uint32_t c1 = S.contour_first + b.path_start_cat[S.pstart_base + local + 1] - b.contour_base;
     path_contours[p] = make_uint2(c0, c1);
     for (uint32_t c = c0; c < c1; c++) b.contour_path[c] = p;
     PathDev P{};
     P.scene = s;
-    P.flags = (b.fill_rule[p] ? 1u : 0u) | (((b.color[p] >> 24) == 0xffu) ? 2u : 0u);
+    P.flags = (b.fill_rule[pg] ? 1u : 0u) | (((b.color[pg] >> 24) == 0xffu) ? 2u : 0u);
     b.paths[p] = P;
 }
 
@@ -582,7 +587,7 @@ __global__ void __launch_bounds__(kThreads) k_propagate(Batch b, uint32_t n_cols
         b.tile_path[gt] = p;
         const bool alpha = b.tile_fills[gt + 1] != b.tile_fills[gt];
         if (!alpha && bd != 0 && occludes && !(eo && ((bd < 0 ? -bd : bd) & 1) == 0)) {
-            const uint32_t fb = S.fb_first + (uint32_t)(P.ry0 + y) * S.fbw + (uint32_t)(P.rx0 + x);
+            const uint32_t fb = S.fb_first - b.fb_base + (uint32_t)(P.ry0 + y) * S.fbw + (uint32_t)(P.rx0 + x);
             atomicMax(&b.z[fb], (int32_t)p);
         }
         run += delta;
@@ -612,11 +617,13 @@ __global__ void __launch_bounds__(kThreads) k_list(Batch b, uint32_t n_tiles) {
     const int32_t rw = P.rx1 - P.rx0;
     const uint32_t local = gt - P.tile_first;
     const int32_t y = (int32_t)(local / (uint32_t)rw), x = (int32_t)(local % (uint32_t)rw);
-    const uint32_t fb = S.fb_first + (uint32_t)(P.ry0 + y) * S.fbw + (uint32_t)(P.rx0 + x);
+    const uint32_t fb = S.fb_first - b.fb_base + (uint32_t)(P.ry0 + y) * S.fbw + (uint32_t)(P.rx0 + x);
     if ((int32_t)p < b.z[fb]) return;
     if (kWrite) {
         const uint32_t slot = atomicAdd(&b.fb_cursor[fb], 1u);
         b.list[b.fb_count[fb] + slot] = gt;
+        const uint32_t nf = b.tile_fills[gt + 1] - b.tile_fills[gt];
+        if (nf) atomicAdd(&b.status[kStListFills], nf);
     } else {
         atomicAdd(&b.fb_count[fb], 1u);
     }
@@ -779,15 +786,15 @@ __device__ __forceinline__ void zero_cells(int *D) {
 
 constexpr int kCompWarps = 4;
 
-__global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b, const uint32_t *scene_fb_first) {
+__global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
     __shared__ int cells[kCompWarps][kCovCells];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t fb = blockIdx.x * kCompWarps + warp;
     if (fb >= b.n_fb) return;
     int *D = cells[warp];
-    const uint32_t s = upper_bound(scene_fb_first, b.n_scenes + 1, fb) - 1;
+    const uint32_t s = upper_bound(b.scene_fb_first, b.n_scenes_all + 1, b.fb_base + fb) - 1;
     const SceneDev &S = b.scenes[s];
-    const uint32_t local = fb - S.fb_first;
+    const uint32_t local = b.fb_base + fb - S.fb_first;
     const uint32_t fx = local % S.fbw, fy = local / S.fbw;
     const int col = lane & 15, h = lane >> 4;
     const float inv255 = 1.0f / 255.0f;
@@ -808,7 +815,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b, const ui
         const uint32_t gt = b.list[e];
         const uint32_t p = b.tile_path[gt];
         const uint32_t flags = b.paths[p].flags;
-        const uint32_t color = b.color[p];
+        const uint32_t color = b.color[b.path_base + p];
         const int8_t bd = b.tile_backdrop[gt];
         const uint32_t f0 = b.tile_fills[gt], f1 = b.tile_fills[gt + 1];
         const bool eo = (flags & 1u) != 0;
@@ -873,67 +880,119 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_coverage_dump(Batch b, cons
 // ---------------------------------------------------------------------------
 // launchers
 
+static std::atomic<uint64_t> g_launches{0};
+uint64_t launches() { return g_launches.load(); }
+void count_launches(uint32_t n) { g_launches += n; }
+
 cudaError_t launch_normalize(const Batch &b, uint2 *path_contours, cudaStream_t st) {
-    if (b.n_contours) k_normalize_contours<<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
-    if (b.n_paths) k_normalize_paths<<<grid_for(b.n_paths), kThreads, 0, st>>>(b, path_contours);
+    if (b.n_contours) {
+        k_normalize_contours<<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
+        count_launches(1);
+    }
+    if (b.n_paths) {
+        k_normalize_paths<<<grid_for(b.n_paths), kThreads, 0, st>>>(b, path_contours);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_path_setup(const Batch &b, const uint2 *path_contours, cudaStream_t st) {
-    if (b.n_paths) k_path_setup<<<grid_for(uint64_t(b.n_paths) * 32), kThreads, 0, st>>>(b, path_contours);
+    if (b.n_paths) {
+        k_path_setup<<<grid_for(uint64_t(b.n_paths) * 32), kThreads, 0, st>>>(b, path_contours);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_path_offsets(const Batch &b, cudaStream_t st) {
-    if (b.n_paths) k_path_offsets<<<grid_for(b.n_paths), kThreads, 0, st>>>(b);
+    if (b.n_paths) {
+        k_path_offsets<<<grid_for(b.n_paths), kThreads, 0, st>>>(b);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st) {
     if (!b.n_contours) return cudaSuccess;
-    if (write) k_contour_segments<true><<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
-    else k_contour_segments<false><<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
+    if (write) {
+        k_contour_segments<true><<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
+        count_launches(1);
+    }
+    else {
+        k_contour_segments<false><<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st) {
     if (!n_segs) return cudaSuccess;
-    if (write) k_flatten<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs);
-    else k_flatten<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs);
+    if (write) {
+        k_flatten<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs);
+        count_launches(1);
+    }
+    else {
+        k_flatten<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream_t st) {
     if (!n_leaves) return cudaSuccess;
-    if (write) k_bin<true><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves);
-    else k_bin<false><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves);
+    if (write) {
+        k_bin<true><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves);
+        count_launches(1);
+    }
+    else {
+        k_bin<false><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_propagate(const Batch &b, uint32_t n_cols, cudaStream_t st) {
-    if (n_cols) k_propagate<<<grid_for(n_cols), kThreads, 0, st>>>(b, n_cols);
+    if (n_cols) {
+        k_propagate<<<grid_for(n_cols), kThreads, 0, st>>>(b, n_cols);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_list(const Batch &b, uint32_t n_tiles, bool write, cudaStream_t st) {
     if (!n_tiles) return cudaSuccess;
-    if (write) k_list<true><<<grid_for(n_tiles), kThreads, 0, st>>>(b, n_tiles);
-    else k_list<false><<<grid_for(n_tiles), kThreads, 0, st>>>(b, n_tiles);
+    if (write) {
+        k_list<true><<<grid_for(n_tiles), kThreads, 0, st>>>(b, n_tiles);
+        count_launches(1);
+    }
+    else {
+        k_list<false><<<grid_for(n_tiles), kThreads, 0, st>>>(b, n_tiles);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_list_sort(const Batch &b, cudaStream_t st) {
-    if (b.n_fb) k_list_sort<<<b.n_fb, kSortThreads, 0, st>>>(b);
+    if (b.n_fb) {
+        k_list_sort<<<b.n_fb, kSortThreads, 0, st>>>(b);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
-cudaError_t launch_composite(const Batch &b, const uint32_t *scene_fb_first, cudaStream_t st) {
-    if (b.n_fb) k_composite<<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b, scene_fb_first);
+cudaError_t launch_composite(const Batch &b, cudaStream_t st) {
+    if (b.n_fb) {
+        k_composite<<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t n, float *out, cudaStream_t st) {
-    if (n) k_coverage_dump<<<grid_for(n, kCompWarps), kCompWarps * 32, 0, st>>>(b, tiles, n, out);
+    if (n) {
+        k_coverage_dump<<<grid_for(n, kCompWarps), kCompWarps * 32, 0, st>>>(b, tiles, n, out);
+        count_launches(1);
+    }
     return cudaGetLastError();
 }
 

@@ -100,11 +100,13 @@ cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, uint32_t n, ui
     }
     if (n <= kScanTile) {
         k_scan_tile<<<1, kScanThreads, 0, st>>>(in, out, n, nullptr, total);
+        count_launches(1);
         return cudaGetLastError();
     }
     const uint32_t nb = (n + kScanTile - 1) / kScanTile;
     uint32_t *sums = static_cast<uint32_t *>(temp);
     k_reduce<<<nb, kScanThreads, 0, st>>>(in, n, sums);
+    count_launches(2);
     cudaError_t e = scan_exclusive_u32(sums, sums, nb, total, sums + nb + 1, st);
     if (e != cudaSuccess) return e;
     k_scan_tile<<<nb, kScanThreads, 0, st>>>(in, out, n, sums, nullptr);

@@ -23,8 +23,9 @@ PF_CONFIG_STAGE_TIMING = 0x1
 
 EXPORTS = [
     "pf_abi_version", "pf_device_count", "pf_ctx_create", "pf_ctx_destroy", "pf_last_error",
-    "pf_scene_upload", "pf_scene_upload_batch", "pf_render", "pf_read_image", "pf_read_image_scene",
+    "pf_scene_upload", "pf_scene_upload_batch", "pf_render", "pf_render_scenes", "pf_read_image", "pf_read_image_scene",
     "pf_image_device_ptr", "pf_read_canon", "pf_read_canon_scene", "pf_read_coverage", "pf_draw",
+    "pf_image_bytes", "pf_image_offset", "pf_read_images",
 ]
 
 
@@ -48,7 +49,8 @@ class FrameStats(C.Structure):
         "visible_tiles", "composite_entries", "framebuffer_tiles")] + [
         ("overflow", C.c_uint32), ("kernel_error", C.c_uint32)] + [
         (n, C.c_float) for n in ("ms_setup", "ms_flatten", "ms_bin", "ms_propagate", "ms_lists",
-                                 "ms_composite", "ms_total")]
+                                 "ms_composite", "ms_total")] + [
+        ("composited_fills", C.c_uint64), ("kernel_launches", C.c_uint32), ("host_syncs", C.c_uint32)]
 
     def to_dict(self) -> Dict[str, float]:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -154,9 +156,12 @@ class Renderer:
         self._check(self.lib.pf_scene_upload_batch(self.ctx, arr, len(views)), self.ctx)
         self._sizes = [(int(np.ceil(s.width)), int(np.ceil(s.height))) for s in scenes]
 
-    def render(self) -> Dict[str, float]:
+    def render(self, first: int = 0, count: Optional[int] = None) -> Dict[str, float]:
+        """Exact two-pass frame over uploaded scenes [first, first + count) (default: all)."""
         st = FrameStats()
-        self._check(self.lib.pf_render(self.ctx, C.byref(st)), self.ctx)
+        if count is None:
+            count = len(self._sizes) - first
+        self._check(self.lib.pf_render_scenes(self.ctx, first, count, C.byref(st)), self.ctx)
         return st.to_dict()
 
     def image(self, scene: int = 0) -> np.ndarray:
@@ -184,6 +189,26 @@ class Renderer:
             "fb_list_first": _arr(r.fb_list_first, nfb + 1, np.uint64),
             "fb_list": _arr(r.fb_list, r.n_list, np.uint32),
         }
+
+    def image_bytes(self) -> int:
+        n = C.c_uint64()
+        self._check(self.lib.pf_image_bytes(self.ctx, C.byref(n)), self.ctx)
+        return n.value
+
+    def image_offset(self, scene: int) -> int:
+        n = C.c_uint64()
+        self._check(self.lib.pf_image_offset(self.ctx, scene, C.byref(n)), self.ctx)
+        return n.value
+
+    def read_images(self, dst_ptr: int, capacity: int) -> None:
+        """Copy every image of the batch into host memory at dst_ptr (one transfer)."""
+        self._check(self.lib.pf_read_images(self.ctx, C.c_void_p(dst_ptr), C.c_size_t(capacity)), self.ctx)
+
+    def upload_views(self, views) -> None:
+        """Upload a batch described by ready-made SceneView structs (host pointers)."""
+        arr = (SceneView * len(views))(*views)
+        self._check(self.lib.pf_scene_upload_batch(self.ctx, arr, len(views)), self.ctx)
+        self._sizes = [(int(np.ceil(v.width)), int(np.ceil(v.height))) for v in views]
 
     def coverage(self) -> np.ndarray:
         n = C.c_uint64()
