@@ -81,14 +81,17 @@ struct Ctx {
     // working buffers
     DevBuf contour_point_first, contour_path, paths, path_tiles, path_cols, contour_segs, path_contours;
     DevBuf segs, seg_leaves, leaves, leaf_path;
-    DevBuf tile_fills, tile_cursor, tile_delta, tile_backdrop, tile_path, col_above, col_final, fills;
-    DevBuf z, fb_count, fb_cursor, list, image, status, scan_temp;
+    DevBuf tile_fills, tile_delta, tile_state, col_above, col_final, fills;
+    DevBuf row_first, row_paths, scene_row_first;
+    DevBuf z, fb_count, list, image, status, scan_temp;
     uint32_t *h_status = nullptr;  // pinned
 
     // the scene range of the last frame and its totals
-    uint32_t r_first = 0, r_count = 0, r_paths = 0, r_contours = 0, r_fb = 0;
-    uint32_t r_path_base = 0, r_contour_base = 0, r_fb_base = 0;
-    uint32_t n_segs = 0, n_tiles = 0, n_cols = 0, n_leaves = 0, n_fills = 0, n_list = 0;
+    uint32_t r_first = 0, r_count = 0, r_paths = 0, r_contours = 0, r_fb = 0, r_rows = 0;
+    uint32_t r_path_base = 0, r_contour_base = 0, r_fb_base = 0, r_row_base = 0;
+    uint32_t n_segs = 0, n_tiles = 0, n_cols = 0, n_leaves = 0, n_fills = 0, n_list = 0, n_row_entries = 0;
+    bool lists_dumped = false;
+    std::vector<uint32_t> h_scene_row_first;
     uint32_t syncs = 0;
 
     HostCanon canon;
@@ -179,6 +182,8 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     uint64_t P = 0, C = 0, N = 0, fb = 0, img = 0, cs = 0, ps = 0;
     c->h_scenes.assign(n, SceneDev{});
     c->h_scene_fb_first.assign(n + 1, 0);
+    c->h_scene_row_first.assign(n + 1, 0);
+    uint64_t rows = 0;
     std::vector<uint32_t> spf(n + 1, 0), scf(n + 1, 0);
     for (uint32_t i = 0; i < n; i++) {
         int st = validate_scene(c, &scenes[i]);
@@ -205,6 +210,9 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
         spf[i] = (uint32_t)N;
         scf[i] = (uint32_t)C;
         c->h_scene_fb_first[i] = (uint32_t)fb;
+        S.row_first = (uint32_t)rows;
+        c->h_scene_row_first[i] = (uint32_t)rows;
+        rows += S.fbh;
         P += s.n_points;
         C += s.n_contours;
         N += s.n_paths;
@@ -217,6 +225,7 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     spf[n] = (uint32_t)N;
     scf[n] = (uint32_t)C;
     c->h_scene_fb_first[n] = (uint32_t)fb;
+    c->h_scene_row_first[n] = (uint32_t)rows;
     if (P >= (1ull << 31) || C >= (1ull << 31) || N >= (1ull << 31) || fb >= (1ull << 31))
         return fail(c, PF_ERR_OVERFLOW, "batch too large (2^31 points, contours, paths or tiles)");
     c->n_scenes = n;
@@ -236,6 +245,7 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     PF_CUDA(c->scene_path_first.ensure((n + 1) * 4));
     PF_CUDA(c->scene_contour_first.ensure((n + 1) * 4));
     PF_CUDA(c->scene_fb_first.ensure((n + 1) * 4));
+    PF_CUDA(c->scene_row_first.ensure((n + 1) * 4));
     PF_CUDA(c->image.ensure(img + 256));
 
     CopyPlan pts, fl, csp, psp, fr, col;
@@ -256,6 +266,8 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     PF_CUDA(cudaMemcpyAsync(c->scene_contour_first.p, scf.data(), (n + 1) * 4, cudaMemcpyHostToDevice, c->stream));
     PF_CUDA(cudaMemcpyAsync(c->scene_fb_first.p, c->h_scene_fb_first.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
                             c->stream));
+    PF_CUDA(cudaMemcpyAsync(c->scene_row_first.p, c->h_scene_row_first.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
+                            c->stream));
     // the host arrays are borrowed only for this call
     PF_CUDA(cudaStreamSynchronize(c->stream));
     c->uploaded = true;
@@ -275,6 +287,7 @@ Batch make_batch(Ctx *c) {
     b.scene_path_first = c->scene_path_first.as<uint32_t>();
     b.scene_contour_first = c->scene_contour_first.as<uint32_t>();
     b.scene_fb_first = c->scene_fb_first.as<uint32_t>();
+    b.scene_row_first = c->scene_row_first.as<uint32_t>();
     b.n_scenes_all = c->n_scenes;
     b.scene_base = c->r_first;
     b.n_scenes = c->r_count;
@@ -283,6 +296,7 @@ Batch make_batch(Ctx *c) {
     b.contour_base = c->r_contour_base;
     b.n_contours = c->r_contours;
     b.fb_base = c->r_fb_base;
+    b.row_base = c->r_row_base;
     b.contour_point_first = c->contour_point_first.as<uint32_t>();
     b.contour_path = c->contour_path.as<uint32_t>();
     b.paths = c->paths.as<PathDev>();
@@ -295,21 +309,21 @@ Batch make_batch(Ctx *c) {
     b.leaves = c->leaves.as<float4>();
     b.leaf_path = c->leaf_path.as<uint32_t>();
     b.leaf_cap = (uint32_t)std::min<size_t>(std::min(c->leaves.cap / 16, c->leaf_path.cap / 4), 0xffffffffu);
-    b.tile_fills = c->tile_fills.as<uint32_t>();
-    b.tile_cursor = c->tile_cursor.as<uint32_t>();
+    b.tile_fills = c->tile_fills.p ? c->tile_fills.as<uint32_t>() + 1 : nullptr;
     b.tile_delta = c->tile_delta.as<int32_t>();
-    b.tile_backdrop = c->tile_backdrop.as<int8_t>();
-    b.tile_path = c->tile_path.as<uint32_t>();
+    b.tile_state = c->tile_state.as<uint16_t>();
     b.col_above = c->col_above.as<int32_t>();
     b.col_final = c->col_final.as<int32_t>();
     b.fills = c->fills.as<uint2>();
     b.fill_cap = (uint32_t)std::min<size_t>(c->fills.cap / 8, 0xffffffffu);
+    b.row_first = c->row_first.as<uint32_t>();
+    b.row_paths = c->row_paths.as<uint32_t>();
+    b.row_cap = (uint32_t)std::min<size_t>(c->row_paths.cap / 4, 0xffffffffu);
+    b.n_rows = c->r_rows;
+    b.n_fb = c->r_fb;
     b.z = c->z.as<int32_t>();
     b.fb_count = c->fb_count.as<uint32_t>();
-    b.fb_cursor = c->fb_cursor.as<uint32_t>();
     b.list = c->list.as<uint32_t>();
-    b.list_cap = (uint32_t)std::min<size_t>(c->list.cap / 4, 0xffffffffu);
-    b.n_fb = c->r_fb;
     b.image = c->image.as<uint8_t>();
     b.status = c->status.as<uint32_t>();
     return b;
@@ -355,6 +369,8 @@ void set_range(Ctx *c, uint32_t first, uint32_t count) {
     c->r_contours = e.contour_end - a.contour_first;
     c->r_fb_base = a.fb_first;
     c->r_fb = c->h_scene_fb_first[first + count] - a.fb_first;
+    c->r_row_base = a.row_first;
+    c->r_rows = c->h_scene_row_first[first + count] - a.row_first;
 }
 
 // The exact two-pass frame over uploaded scenes [first, first + count).
@@ -377,36 +393,41 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     PF_CUDA(c->path_tiles.ensure((size_t(N) + 1) * 4));
     PF_CUDA(c->path_cols.ensure((size_t(N) + 1) * 4));
     PF_CUDA(c->path_contours.ensure(size_t(N) * 8 + 8));
-    const uint32_t NFB = c->r_fb;
-    PF_CUDA(c->z.ensure(size_t(NFB) * 4 + 4));
-    PF_CUDA(c->fb_count.ensure((size_t(NFB) + 1) * 4));
-    PF_CUDA(c->fb_cursor.ensure(size_t(NFB) * 4 + 4));
+    const uint32_t NFB = c->r_fb, R = c->r_rows;
+    PF_CUDA(c->row_first.ensure((size_t(R) + 1) * 4));
+    c->lists_dumped = false;
 
     record(c, 0);
-    // 1. topology, tile rects, segment counts
+    // 1. topology, tile rects, segment counts, per-row path counts
     Batch b = make_batch(c);
     PF_CUDA(launch_normalize(b, c->path_contours.as<uint2>(), st));
     PF_CUDA(launch_path_setup(b, c->path_contours.as<uint2>(), st));
     PF_CUDA(cudaMemsetAsync(b.contour_segs + C, 0, 4, st));
     PF_CUDA(cudaMemsetAsync(b.path_tiles + N, 0, 4, st));
     PF_CUDA(cudaMemsetAsync(b.path_cols + N, 0, 4, st));
+    PF_CUDA(cudaMemsetAsync(b.row_first + R, 0, 4, st));
     PF_CUDA(launch_contour_segments(b, false, st));
+    PF_CUDA(launch_rows(b, false, st));
     if (int e = scan(c, b.contour_segs, C + 1, kStSegs)) return e;
     if (int e = scan(c, b.path_tiles, N + 1, kStTiles)) return e;
     if (int e = scan(c, b.path_cols, N + 1, kStCols)) return e;
+    if (int e = scan(c, b.row_first, R + 1, kStRows)) return e;
     PF_CUDA(launch_path_offsets(b, st));
     if (int e = read_status(c)) return e;
     if (int e = check_kernel_status(c)) return e;
     c->n_segs = c->h_status[kStSegs];
     c->n_tiles = c->h_status[kStTiles];
     c->n_cols = c->h_status[kStCols];
+    c->n_row_entries = c->h_status[kStRows];
     record(c, 1);
 
-    // 2. segments, leaf counts, leaves
+    // 2. segments, row lists, leaf counts, leaves
     PF_CUDA(c->segs.ensure(size_t(c->n_segs) * sizeof(SegDev) + 16));
     PF_CUDA(c->seg_leaves.ensure((size_t(c->n_segs) + 1) * 4));
+    PF_CUDA(c->row_paths.ensure(size_t(c->n_row_entries) * 4 + 16));
     b = make_batch(c);
     PF_CUDA(launch_contour_segments(b, true, st));
+    PF_CUDA(launch_rows(b, true, st));
     PF_CUDA(cudaMemsetAsync(b.seg_leaves + c->n_segs, 0, 4, st));
     PF_CUDA(launch_flatten(b, c->n_segs, false, st));
     if (int e = scan(c, b.seg_leaves, c->n_segs + 1, kStLeaves)) return e;
@@ -419,18 +440,15 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     PF_CUDA(launch_flatten(b, c->n_segs, true, st));
     record(c, 2);
 
-    // 3. fill counts per tile, then fills written grouped by tile
+    // 3. fill counts per tile, then fills written grouped by tile (counting sort)
     const size_t T = c->n_tiles, K = c->n_cols;
-    PF_CUDA(c->tile_fills.ensure((T + 1) * 4));
-    PF_CUDA(c->tile_cursor.ensure(T * 4 + 4));
+    PF_CUDA(c->tile_fills.ensure((T + 2) * 4));
     PF_CUDA(c->tile_delta.ensure(T * 4 + 4));
-    PF_CUDA(c->tile_backdrop.ensure(T + 16));
-    PF_CUDA(c->tile_path.ensure(T * 4 + 4));
+    PF_CUDA(c->tile_state.ensure(T * 2 + 16));
     PF_CUDA(c->col_above.ensure(K * 4 + 4));
     PF_CUDA(c->col_final.ensure(K * 4 + 4));
     b = make_batch(c);
-    PF_CUDA(cudaMemsetAsync(b.tile_fills, 0, (T + 1) * 4, st));
-    PF_CUDA(cudaMemsetAsync(b.tile_cursor, 0, T * 4, st));
+    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, (T + 2) * 4, st));
     PF_CUDA(cudaMemsetAsync(b.tile_delta, 0, T * 4, st));
     PF_CUDA(cudaMemsetAsync(b.col_above, 0, K * 4, st));
     PF_CUDA(launch_bin(b, c->n_leaves, false, st));
@@ -443,29 +461,17 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     PF_CUDA(launch_bin(b, c->n_leaves, true, st));
     record(c, 3);
 
-    // 4. backdrops, z-buffer
-    PF_CUDA(cudaMemsetAsync(b.z, 0xff, size_t(NFB) * 4, st));
+    // 4. backdrops
     PF_CUDA(launch_propagate(b, c->n_cols, st));
     record(c, 4);
-
-    // 5. composite lists
-    PF_CUDA(cudaMemsetAsync(b.fb_count, 0, (size_t(NFB) + 1) * 4, st));
-    PF_CUDA(cudaMemsetAsync(b.fb_cursor, 0, size_t(NFB) * 4, st));
-    PF_CUDA(launch_list(b, c->n_tiles, false, st));
-    if (int e = scan(c, b.fb_count, NFB + 1, kStList)) return e;
-    if (int e = read_status(c)) return e;
-    c->n_list = c->h_status[kStList];
-    PF_CUDA(c->list.ensure(size_t(c->n_list) * 4 + 16));
-    b = make_batch(c);
-    PF_CUDA(launch_list(b, c->n_tiles, true, st));
-    PF_CUDA(launch_list_sort(b, st));
     record(c, 5);
 
-    // 6. coverage + composite
+    // 5. coverage + front-to-back composite with the z-cull walk
     PF_CUDA(launch_composite(b, st));
     record(c, 6);
     if (int e = read_status(c)) return e;
     if (int e = check_kernel_status(c)) return e;
+    c->n_list = c->h_status[kStEntries];
     c->rendered = true;
 
     if (stats) {
@@ -480,6 +486,7 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
         stats->composite_entries = c->n_list;
         stats->framebuffer_tiles = NFB;
         stats->composited_fills = c->h_status[kStListFills];
+        stats->alpha_tiles = 0;
         stats->kernel_launches = (uint32_t)(launches() - launches0);
         stats->host_syncs = c->syncs;
         if (c->flags & PF_CONFIG_STAGE_TIMING) {
@@ -504,11 +511,31 @@ int d2h(Ctx *c, std::vector<T> &dst, const void *src, size_t n) {
     return PF_OK;
 }
 
+// Composite lists of the last frame (canonical output only): count, scan, write.
+int dump_lists(Ctx *c) {
+    if (c->lists_dumped) return PF_OK;
+    const uint32_t NFB = c->r_fb;
+    PF_CUDA(c->z.ensure(size_t(NFB) * 4 + 4));
+    PF_CUDA(c->fb_count.ensure((size_t(NFB) + 1) * 4));
+    Batch b = make_batch(c);
+    PF_CUDA(cudaMemsetAsync(b.fb_count + NFB, 0, 4, c->stream));
+    PF_CUDA(launch_list_dump(b, false, c->stream));
+    if (int e = scan(c, b.fb_count, NFB + 1, kStList)) return e;
+    if (int e = read_status(c)) return e;
+    PF_CUDA(c->list.ensure(size_t(c->h_status[kStList]) * 4 + 16));
+    b = make_batch(c);
+    PF_CUDA(launch_list_dump(b, true, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    c->lists_dumped = true;
+    return PF_OK;
+}
+
 // Canonical integer output of scene `si` of the last frame.
 int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
     if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
     if (si < c->r_first || si >= c->r_first + c->r_count)
         return fail(c, PF_ERR_INVALID_ARGUMENT, "scene was not rendered by the last frame");
+    if (int e = dump_lists(c)) return e;
     const SceneDev &S = c->h_scenes[si];
     const uint32_t p0 = S.path_first - c->r_path_base, p1 = S.path_end - c->r_path_base, np = p1 - p0;
     const uint32_t fb0 = S.fb_first - c->r_fb_base;
@@ -533,30 +560,34 @@ int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
         h.tile_first[p] = tf[p] - t0;
         h.col_first[p] = cf[p] - k0;
     }
-    std::vector<uint32_t> tfill;
-    if (int e = d2h(c, tfill, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0) + 1)) return e;
-    if (int e = d2h(c, h.backdrop, c->tile_backdrop.as<int8_t>() + t0, t1 - t0)) return e;
+    // after the fill write pass the fills of tile t are [tile_fills[t - 1], tile_fills[t])
+    std::vector<uint32_t> tend;
+    std::vector<uint16_t> state;
+    if (int e = d2h(c, tend, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0) + 1)) return e;
+    if (int e = d2h(c, state, c->tile_state.as<uint16_t>() + t0, t1 - t0)) return e;
     if (int e = d2h(c, h.col_backdrop, c->col_final.as<int32_t>() + k0, k1 - k0)) return e;
     if (int e = d2h(c, h.z, c->z.as<int32_t>() + fb0, size_t(S.fbw) * S.fbh)) return e;
     std::vector<uint32_t> fbc;
     if (int e = d2h(c, fbc, c->fb_count.as<uint32_t>() + fb0, size_t(S.fbw) * S.fbh + 1)) return e;
     PF_CUDA(cudaStreamSynchronize(c->stream));
-    const uint32_t f0 = tfill[0], f1 = tfill[t1 - t0];
+    const size_t nt = t1 - t0;
+    const uint32_t f0 = tend[0], f1 = tend[nt];  // tend[k] = tile_fills[t0 - 1 + k]
     std::vector<uint2> fl;
     if (int e = d2h(c, fl, c->fills.as<uint2>() + f0, f1 - f0)) return e;
     const uint32_t l0 = fbc[0], l1 = fbc[size_t(S.fbw) * S.fbh];
     if (int e = d2h(c, h.list, c->list.as<uint32_t>() + l0, l1 - l0)) return e;
     PF_CUDA(cudaStreamSynchronize(c->stream));
 
-    const size_t nt = t1 - t0;
     h.alpha.resize(nt);
+    h.backdrop.resize(nt);
     h.fill_count.resize(nt);
     h.fills.resize(size_t(f1 - f0) * 4);
     std::vector<uint64_t> keys;
     for (size_t t = 0; t < nt; t++) {
-        const uint32_t a = tfill[t] - f0, e = tfill[t + 1] - f0;
+        const uint32_t a = tend[t] - f0, e = tend[t + 1] - f0;
         h.fill_count[t] = e - a;
-        h.alpha[t] = e != a;
+        h.alpha[t] = (state[t] >> 8) & 1;
+        h.backdrop[t] = (int8_t)(state[t] & 0xff);
         keys.clear();
         for (uint32_t k = a; k < e; k++)
             keys.push_back((uint64_t(fl[k].x & 0xffffu) << 48) | (uint64_t(fl[k].x >> 16) << 32) |
@@ -693,8 +724,8 @@ int pf_ctx_destroy(void *ctx) {
                       &c->scene_path_first, &c->scene_contour_first, &c->scene_fb_first, &c->contour_point_first,
                       &c->contour_path, &c->paths, &c->path_tiles, &c->path_cols, &c->contour_segs,
                       &c->path_contours, &c->segs, &c->seg_leaves, &c->leaves, &c->leaf_path, &c->tile_fills,
-                      &c->tile_cursor, &c->tile_delta, &c->tile_backdrop, &c->tile_path, &c->col_above,
-                      &c->col_final, &c->fills, &c->z, &c->fb_count, &c->fb_cursor, &c->list, &c->image,
+                      &c->tile_delta, &c->tile_state, &c->col_above, &c->col_final, &c->fills, &c->row_first,
+                      &c->row_paths, &c->scene_row_first, &c->z, &c->fb_count, &c->list, &c->image,
                       &c->status, &c->scan_temp};
     for (DevBuf *b : bufs) b->release();
     for (auto &e : c->ev)
@@ -794,11 +825,12 @@ int pf_read_coverage(void *ctx, float *out, size_t capacity_floats, uint64_t *n_
         return e;
     PF_CUDA(cudaStreamSynchronize(c->stream));
     const uint32_t t0 = tf.front(), t1 = tf.back();
-    if (int e = d2h(c, tfill, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0) + 1)) return e;
+    std::vector<uint16_t> state;
+    if (int e = d2h(c, state, c->tile_state.as<uint16_t>() + t0, size_t(t1 - t0))) return e;
     PF_CUDA(cudaStreamSynchronize(c->stream));
     std::vector<uint32_t> alpha;
     for (uint32_t t = 0; t < t1 - t0; t++)
-        if (tfill[t + 1] != tfill[t]) alpha.push_back(t0 + t);
+        if (state[t] & 0x100u) alpha.push_back(t0 + t);
     *n_alpha = alpha.size();
     if (!out) return PF_OK;
     if (capacity_floats < alpha.size() * 256) return fail(c, PF_ERR_INVALID_ARGUMENT, "coverage buffer too small");

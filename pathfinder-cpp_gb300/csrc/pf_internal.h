@@ -39,6 +39,7 @@ struct SceneDev {
     uint32_t contour_first, contour_end;
     uint32_t point_first, point_end;
     uint32_t cstart_base, pstart_base;  // offsets of the scene's offset arrays
+    uint32_t row_first;                  // first framebuffer-tile row of this scene in the batch
 };
 
 // Per draw path (device), written by the set-up kernel.
@@ -72,13 +73,14 @@ struct Batch {
     const uint32_t *scene_path_first;    // [n_scenes_all + 1]
     const uint32_t *scene_contour_first; // [n_scenes_all + 1]
     const uint32_t *scene_fb_first;      // [n_scenes_all + 1]
+    const uint32_t *scene_row_first;     // [n_scenes_all + 1]
     uint32_t n_scenes_all;               // scenes uploaded
     // the scenes rendered by this frame: a contiguous range of the uploaded ones.
     // Per-frame arrays are indexed from 0 = the range's first path / contour / framebuffer tile.
     uint32_t scene_base, n_scenes;
     uint32_t path_base, n_paths;
     uint32_t contour_base, n_contours;
-    uint32_t fb_base;
+    uint32_t fb_base, row_base;
 
     // normalised topology
     uint32_t *contour_point_first;       // [n_contours + 1] global
@@ -96,25 +98,30 @@ struct Batch {
     uint32_t *leaf_path;
     uint32_t leaf_cap;
 
-    // tiles
-    uint32_t *tile_fills;                // [tiles + 1] count -> scanned to first fill
-    uint32_t *tile_cursor;               // [tiles]
-    int32_t *tile_delta;                 // [tiles] summed backdrop deltas
-    int8_t *tile_backdrop;               // [tiles]
-    uint32_t *tile_path;                 // [tiles]
+    // tiles.  tile_fills points one past the start of its allocation, so tile_fills[-1] == 0:
+    // fill counts -> (scan) first fill of each tile -> (write pass, used as the cursor) one
+    // past the last fill; after the write pass the fills of tile t are
+    // [tile_fills[t - 1], tile_fills[t]).
+    uint32_t *tile_fills;                // [-1 .. tiles]
+    int32_t *tile_delta;                 // [tiles] summed backdrop deltas (bin)
+    uint16_t *tile_state;                // [tiles] propagated int8 backdrop | alpha << 8
     int32_t *col_above;                  // [cols] deltas landing above the rect
     int32_t *col_final;                  // [cols]
-    uint32_t tile_cap, col_cap;
     uint2 *fills;                        // [fills] packed u16 x4
     uint32_t fill_cap;
 
-    // framebuffer tiles
+    // per framebuffer-tile row of each scene: the paths whose tile rect spans the row,
+    // in path order
+    uint32_t *row_first;                 // [rows + 1] counts -> scanned
+    uint32_t *row_paths;
+    uint32_t row_cap;
+    uint32_t n_rows;
+    uint32_t n_fb;
+
+    // composite-list dump (canonical output only)
     int32_t *z;                          // [fb tiles]
     uint32_t *fb_count;                  // [fb + 1] -> scanned
-    uint32_t *fb_cursor;
     uint32_t *list;
-    uint32_t list_cap;
-    uint32_t n_fb;
 
     uint8_t *image;                      // batch image buffer
     uint32_t *status;                    // [16] error bits and totals
@@ -130,6 +137,8 @@ enum : int {
     kStFills = 5,
     kStList = 6,
     kStListFills = 7,  // fills of the alpha tiles that made it into composite lists
+    kStRows = 8,       // entries of the per-row path lists
+    kStEntries = 9,    // composite entries (visible tiles at or above the occluder)
     kStCount = 16,
 };
 
@@ -150,9 +159,9 @@ cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st)
 cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st);
 cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream_t st);
 cudaError_t launch_propagate(const Batch &b, uint32_t n_cols, cudaStream_t st);
-cudaError_t launch_list(const Batch &b, uint32_t n_tiles, bool write, cudaStream_t st);
-cudaError_t launch_list_sort(const Batch &b, cudaStream_t st);
+cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_composite(const Batch &b, cudaStream_t st);
+cudaError_t launch_list_dump(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t n, float *out, cudaStream_t st);
 
 }  // namespace pfc

@@ -14,6 +14,7 @@
 // Integer outputs follow the reference's d3d9 CPU tiler bit for bit, so every float
 // operation on that path is written with __f*_rn intrinsics (no FMA contraction), in the
 // same order as the reference's SSE lanes (pathfinder/common/f32x4.h).
+#include <algorithm>
 #include <atomic>
 
 #include "pf_internal.h"
@@ -544,13 +545,10 @@ __global__ void __launch_bounds__(kThreads) k_bin(Batch b, uint32_t n_leaves) {
     w.vb_bottom = S.vb_bottom;
     const uint32_t tb = P.tile_first, cb = P.col_first;
     if (kWrite) {
+        // tile_fills[t] holds the next free slot of tile t (counting sort, second pass)
         walk_line(
             w, L.x, L.y, L.z, L.w,
-            [&](int32_t local, uint2 q) {
-                const uint32_t gt = tb + (uint32_t)local;
-                const uint32_t slot = atomicAdd(&b.tile_cursor[gt], 1u);
-                b.fills[b.tile_fills[gt] + slot] = q;
-            },
+            [&](int32_t local, uint2 q) { b.fills[atomicAdd(&b.tile_fills[tb + (uint32_t)local], 1u)] = q; },
             [&](int32_t, int) {}, &b.status[kStErr]);
     } else {
         walk_line(
@@ -565,132 +563,75 @@ __global__ void __launch_bounds__(kThreads) k_bin(Batch b, uint32_t n_leaves) {
 
 // ---------------------------------------------------------------------------
 // Backdrop propagation down each tile column (Tiler::prepare_tiles, tiler.cpp:369-439:
-// tile backdrop = int8(running int32 column sum), running += int8 tile delta), the
-// z-buffer of occluding solid tiles (d3d11 rule, propagate.comp:190-205: solid tiles the
-// even-odd rule leaves empty do not occlude) and the tile -> path map.
+// tile backdrop = int8(running int32 column sum), running += int8 tile delta).  Every tile
+// gets a 2-byte state: its propagated backdrop and whether it holds fills (alpha tile).
 
 __global__ void __launch_bounds__(kThreads) k_propagate(Batch b, uint32_t n_cols) {
     const uint32_t gc = global_tid();
     if (gc >= n_cols || gc >= b.status[kStCols]) return;
     const uint32_t p = upper_bound(b.path_cols, b.n_paths + 1, gc) - 1;
     const PathDev P = b.paths[p];
-    const SceneDev &S = b.scenes[P.scene];
     const int32_t rw = P.rx1 - P.rx0, rh = P.ry1 - P.ry0;
     const int32_t x = (int32_t)(gc - P.col_first);
     int32_t run = b.col_above[gc];
-    const bool eo = (P.flags & 1u) != 0, occludes = (P.flags & 2u) != 0;
     for (int32_t y = 0; y < rh; y++) {
         const uint32_t gt = P.tile_first + (uint32_t)(y * rw + x);
-        const int8_t bd = (int8_t)run;
         const int8_t delta = (int8_t)(b.tile_delta[gt] & 0xff);
-        b.tile_backdrop[gt] = bd;
-        b.tile_path[gt] = p;
-        const bool alpha = b.tile_fills[gt + 1] != b.tile_fills[gt];
-        if (!alpha && bd != 0 && occludes && !(eo && ((bd < 0 ? -bd : bd) & 1) == 0)) {
-            const uint32_t fb = S.fb_first - b.fb_base + (uint32_t)(P.ry0 + y) * S.fbw + (uint32_t)(P.rx0 + x);
-            atomicMax(&b.z[fb], (int32_t)p);
-        }
+        const bool alpha = b.tile_fills[gt] != b.tile_fills[(int64_t)gt - 1];
+        b.tile_state[gt] = (uint16_t)((uint8_t)(int8_t)run) | (alpha ? 0x100u : 0u);
         run += delta;
     }
     b.col_final[gc] = run;
 }
 
 // ---------------------------------------------------------------------------
-// Composite lists per framebuffer tile: visible tiles (alpha, or nonzero backdrop,
-// scene_builder.cpp:57-63) of paths at or above the z value, in path order
-// (sort.comp:49-83).
+// Per framebuffer-tile row of each scene: the scene's paths whose tile rect spans the row,
+// in path order (one block per row; a block scan keeps the order, no sort is needed).
+
+constexpr int kRowThreads = 256;
 
 template <bool kWrite>
-__global__ void __launch_bounds__(kThreads) k_list(Batch b, uint32_t n_tiles) {
-    const uint32_t gt = global_tid();
-    if (gt >= n_tiles || gt >= b.status[kStTiles]) return;
-    if (kWrite && b.status[kStList] > b.list_cap) {
-        if (gt == 0) atomicOr(&b.status[kStErr], kErrOverflowList);
-        return;
-    }
-    const bool alpha = b.tile_fills[gt + 1] != b.tile_fills[gt];
-    const int8_t bd = b.tile_backdrop[gt];
-    if (!alpha && bd == 0) return;
-    const uint32_t p = b.tile_path[gt];
-    const PathDev P = b.paths[p];
-    const SceneDev &S = b.scenes[P.scene];
-    const int32_t rw = P.rx1 - P.rx0;
-    const uint32_t local = gt - P.tile_first;
-    const int32_t y = (int32_t)(local / (uint32_t)rw), x = (int32_t)(local % (uint32_t)rw);
-    const uint32_t fb = S.fb_first - b.fb_base + (uint32_t)(P.ry0 + y) * S.fbw + (uint32_t)(P.rx0 + x);
-    if ((int32_t)p < b.z[fb]) return;
-    if (kWrite) {
-        const uint32_t slot = atomicAdd(&b.fb_cursor[fb], 1u);
-        b.list[b.fb_count[fb] + slot] = gt;
-        const uint32_t nf = b.tile_fills[gt + 1] - b.tile_fills[gt];
-        if (nf) atomicAdd(&b.status[kStListFills], nf);
-    } else {
-        atomicAdd(&b.fb_count[fb], 1u);
-    }
-}
-
-constexpr int kSortThreads = 128;
-constexpr uint32_t kSortSmem = 4096;
-
-__device__ void bitonic_smem(uint32_t *v, uint32_t n_pow2) {
-    for (uint32_t k = 2; k <= n_pow2; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < n_pow2; i += blockDim.x) {
-                const uint32_t ixj = i ^ j;
-                if (ixj > i) {
-                    const uint32_t a = v[i], c = v[ixj];
-                    const bool up = (i & k) == 0;
-                    if ((a > c) == up) {
-                        v[i] = c;
-                        v[ixj] = a;
-                    }
-                }
-            }
-            __syncthreads();
+__global__ void __launch_bounds__(kRowThreads) k_rows(Batch b) {
+    __shared__ uint32_t warp_counts[kRowThreads / 32];
+    __shared__ uint32_t chunk_total;
+    const uint32_t r = blockIdx.x;
+    const uint32_t rg = b.row_base + r;
+    const uint32_t s = upper_bound(b.scene_row_first, b.n_scenes_all + 1, rg) - 1;
+    const SceneDev &S = b.scenes[s];
+    const int32_t y = (int32_t)(rg - S.row_first);
+    const uint32_t p0 = S.path_first - b.path_base, p1 = S.path_end - b.path_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t out = kWrite ? b.row_first[r] : 0u;
+    uint32_t total = 0;
+    for (uint32_t base = p0; base < p1; base += kRowThreads) {
+        const uint32_t p = base + threadIdx.x;
+        bool spans = false;
+        if (p < p1) {
+            const int4 rect = *reinterpret_cast<const int4 *>(&b.paths[p].rx0);
+            spans = rect.y <= y && y < rect.w && rect.x < rect.z;
         }
-    }
-}
-
-__global__ void __launch_bounds__(kSortThreads) k_list_sort(Batch b) {
-    const uint32_t fb = blockIdx.x;
-    const uint32_t first = b.fb_count[fb], n = b.fb_count[fb + 1] - first;
-    if (n <= 1) return;
-    uint32_t *g = b.list + first;
-    if (n <= 32) {
-        // one warp: rank sort (keys are distinct)
-        if (threadIdx.x < 32) {
-            const uint32_t v = threadIdx.x < n ? g[threadIdx.x] : 0xffffffffu;
-            uint32_t rank = 0;
-            for (uint32_t k = 0; k < n; k++) {
-                const uint32_t o = __shfl_sync(0xffffffffu, v, k);
-                rank += (o < v) ? 1u : 0u;
-            }
-            __syncwarp();
-            if (threadIdx.x < n) g[rank] = v;
-        }
-        return;
-    }
-    __shared__ uint32_t sm[kSortSmem];
-    if (n <= kSortSmem) {
-        uint32_t n2 = 64;
-        while (n2 < n) n2 <<= 1;
-        for (uint32_t i = threadIdx.x; i < n2; i += blockDim.x) sm[i] = i < n ? g[i] : 0xffffffffu;
+        const uint32_t ballot = __ballot_sync(0xffffffffu, spans);
+        if (lane == 0) warp_counts[warp] = __popc(ballot);
         __syncthreads();
-        bitonic_smem(sm, n2);
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) g[i] = sm[i];
-        return;
-    }
-    // long list: odd-even transposition sort in place (rare; correct for any n)
-    for (uint32_t pass = 0; pass < n; pass++) {
-        for (uint32_t i = 2 * threadIdx.x + (pass & 1); i + 1 < n; i += 2 * blockDim.x) {
-            const uint32_t a = g[i], c = g[i + 1];
-            if (a > c) {
-                g[i] = c;
-                g[i + 1] = a;
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (int k = 0; k < kRowThreads / 32; k++) {
+                const uint32_t c = warp_counts[k];
+                warp_counts[k] = run;
+                run += c;
             }
+            chunk_total = run;
         }
         __syncthreads();
+        if (kWrite && spans) {
+            const uint32_t rank = warp_counts[warp] + __popc(ballot & ((1u << lane) - 1u));
+            if (out + rank < b.row_cap) b.row_paths[out + rank] = p;
+        }
+        out += chunk_total;
+        total += chunk_total;
+        __syncthreads();
     }
+    if (!kWrite && threadIdx.x == 0) b.row_first[r] = total;
 }
 
 // ---------------------------------------------------------------------------
@@ -786,73 +727,156 @@ __device__ __forceinline__ void zero_cells(int *D) {
 
 constexpr int kCompWarps = 4;
 
+// One framebuffer tile: walk the paths spanning its row from the topmost down, test 32
+// candidates at a time (one per lane), and visit the visible tiles in order.  A visible tile
+// is an alpha tile or a solid tile with a nonzero backdrop (scene_builder.cpp:57-63); the
+// walk ends at the first occluding tile - a solid, opaque tile whose fill rule covers it
+// (the d3d11 z-buffer rule, propagate.comp:190-205) - so the tiles visited are exactly the
+// framebuffer tile's composite list after z-culling (sort.comp:49-83), in reverse order.
+// visit(p, gt, state) returns true to stop the walk.
+template <class Visit>
+__device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint32_t fx, uint32_t fy, Visit &&visit) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t k_lo = b.row_first[row], k_hi = b.row_first[row + 1];
+    for (uint32_t top = k_hi; top > k_lo; top = top > k_lo + 32 ? top - 32 : k_lo) {
+        const int64_t k = (int64_t)top - 1 - lane;
+        uint32_t p = 0, gt = 0, st = 0;
+        bool vis = false;
+        if (k >= (int64_t)k_lo) {
+            p = b.row_paths[k];
+            const int4 rect = *reinterpret_cast<const int4 *>(&b.paths[p].rx0);
+            if ((int32_t)fx >= rect.x && (int32_t)fx < rect.z) {
+                gt = b.paths[p].tile_first + ((int32_t)fy - rect.y) * (rect.z - rect.x) + ((int32_t)fx - rect.x);
+                st = b.tile_state[gt];
+                vis = st != 0;
+            }
+        }
+        uint32_t mask = __ballot_sync(0xffffffffu, vis);
+        while (mask) {
+            const int l = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const uint32_t pl = __shfl_sync(0xffffffffu, p, l);
+            const uint32_t gtl = __shfl_sync(0xffffffffu, gt, l);
+            const uint32_t stl = __shfl_sync(0xffffffffu, st, l);
+            if (visit(pl, gtl, stl)) return;
+        }
+    }
+}
+
+__device__ __forceinline__ bool solid_hidden(bool eo, int8_t bd) { return eo && ((bd < 0 ? -bd : bd) & 1) == 0; }
+
 __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
     __shared__ int cells[kCompWarps][kCovCells];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t fb = blockIdx.x * kCompWarps + warp;
-    if (fb >= b.n_fb) return;
     int *D = cells[warp];
-    const uint32_t s = upper_bound(b.scene_fb_first, b.n_scenes_all + 1, b.fb_base + fb) - 1;
-    const SceneDev &S = b.scenes[s];
-    const uint32_t local = b.fb_base + fb - S.fb_first;
-    const uint32_t fx = local % S.fbw, fy = local / S.fbw;
     const int col = lane & 15, h = lane >> 4;
     const float inv255 = 1.0f / 255.0f;
-    float dr[8], dg[8], db[8], da[8];
-    {
-        const float r = (float)(S.clear & 0xffu) * inv255, g = (float)((S.clear >> 8) & 0xffu) * inv255,
-                    bl = (float)((S.clear >> 16) & 0xffu) * inv255, a = (float)(S.clear >> 24) * inv255;
+    const uint32_t n_warps = gridDim.x * kCompWarps;
+    uint32_t entries = 0, comp_fills = 0;
+    for (uint32_t fb = blockIdx.x * kCompWarps + warp; fb < b.n_fb; fb += n_warps) {
+        const uint32_t fbg = b.fb_base + fb;
+        const uint32_t s = upper_bound(b.scene_fb_first, b.n_scenes_all + 1, fbg) - 1;
+        const SceneDev &S = b.scenes[s];
+        const uint32_t local = fbg - S.fb_first;
+        const uint32_t fx = local % S.fbw, fy = local / S.fbw;
+        // front to back: acc = sum of T * premultiplied source, T = product of (1 - a) above
+        float ar[8], ag[8], ab[8], aa[8], tr[8];
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            dr[k] = r;
-            dg[k] = g;
-            db[k] = bl;
-            da[k] = a;
+            ar[k] = ag[k] = ab[k] = aa[k] = 0.0f;
+            tr[k] = 1.0f;
+        }
+        walk_fb_tile(b, S.row_first - b.row_base + fy, fx, fy, [&](uint32_t p, uint32_t gt, uint32_t st) -> bool {
+            const uint32_t flags = b.paths[p].flags;
+            const bool eo = (flags & 1u) != 0;
+            const int8_t bd = (int8_t)(st & 0xffu);
+            float cov[8];
+            bool stop = false;
+            entries++;
+            if (!(st & 0x100u)) {
+                if (solid_hidden(eo, bd)) return false;
+#pragma unroll
+                for (int k = 0; k < 8; k++) cov[k] = 1.0f;
+                stop = (flags & 2u) != 0;
+            } else {
+                const uint32_t f0 = b.tile_fills[(int64_t)gt - 1], f1 = b.tile_fills[gt];
+                comp_fills += f1 - f0;
+                zero_cells(D);
+                alpha_coverage(b, f0, f1, bd, eo, D, cov);
+                __syncwarp();
+            }
+            const uint32_t color = b.color[b.path_base + p];
+            const float pr = (float)(color & 0xffu) * inv255, pg = (float)((color >> 8) & 0xffu) * inv255,
+                        pb = (float)((color >> 16) & 0xffu) * inv255, pa = (float)(color >> 24) * inv255;
+            bool opaque = true;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const float a = pa * cov[k], w = tr[k] * a;
+                ar[k] += w * pr;
+                ag[k] += w * pg;
+                ab[k] += w * pb;
+                aa[k] += w;
+                tr[k] *= 1.0f - a;
+                opaque &= tr[k] == 0.0f;
+            }
+            return stop || __all_sync(0xffffffffu, opaque);
+        });
+        const uint32_t px = fx * 16 + (uint32_t)col;
+        if (px < S.img_w) {
+            const float cr = (float)(S.clear & 0xffu) * inv255, cg = (float)((S.clear >> 8) & 0xffu) * inv255,
+                        cb = (float)((S.clear >> 16) & 0xffu) * inv255, ca = (float)(S.clear >> 24) * inv255;
+            uchar4 *img = reinterpret_cast<uchar4 *>(b.image + S.img_offset);
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const uint32_t py = fy * 16 + (uint32_t)(h * 8 + k);
+                if (py < S.img_h) {
+                    img[(size_t)py * S.img_w + px] =
+                        make_uchar4((unsigned char)__float2uint_rn(__saturatef(ar[k] + tr[k] * cr) * 255.0f),
+                                    (unsigned char)__float2uint_rn(__saturatef(ag[k] + tr[k] * cg) * 255.0f),
+                                    (unsigned char)__float2uint_rn(__saturatef(ab[k] + tr[k] * cb) * 255.0f),
+                                    (unsigned char)__float2uint_rn(__saturatef(aa[k] + tr[k] * ca) * 255.0f));
+                }
+            }
         }
     }
-    const uint32_t e0 = b.fb_count[fb], e1 = b.fb_count[fb + 1];
-    for (uint32_t e = e0; e < e1; e++) {
-        const uint32_t gt = b.list[e];
-        const uint32_t p = b.tile_path[gt];
+    if (lane == 0 && entries) {
+        atomicAdd(&b.status[kStEntries], entries);
+        atomicAdd(&b.status[kStListFills], comp_fills);
+    }
+}
+
+// Composite lists and z per framebuffer tile for the canonical output (not part of a frame):
+// the same walk as k_composite, written back to front.
+template <bool kWrite>
+__global__ void __launch_bounds__(kCompWarps * 32) k_list_dump(Batch b) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t fb = blockIdx.x * kCompWarps + warp;
+    if (fb >= b.n_fb) return;
+    const uint32_t fbg = b.fb_base + fb;
+    const uint32_t s = upper_bound(b.scene_fb_first, b.n_scenes_all + 1, fbg) - 1;
+    const SceneDev &S = b.scenes[s];
+    const uint32_t local = fbg - S.fb_first;
+    const uint32_t fx = local % S.fbw, fy = local / S.fbw;
+    uint32_t n = 0, first = 0, count = 0;
+    int32_t z = -1;
+    if (kWrite) {
+        first = b.fb_count[fb];
+        count = b.fb_count[fb + 1] - first;
+    }
+    walk_fb_tile(b, S.row_first - b.row_base + fy, fx, fy, [&](uint32_t p, uint32_t gt, uint32_t st) -> bool {
+        if (kWrite && lane == 0) b.list[first + count - 1 - n] = gt;
+        n++;
         const uint32_t flags = b.paths[p].flags;
-        const uint32_t color = b.color[b.path_base + p];
-        const int8_t bd = b.tile_backdrop[gt];
-        const uint32_t f0 = b.tile_fills[gt], f1 = b.tile_fills[gt + 1];
-        const bool eo = (flags & 1u) != 0;
-        float cov[8];
-        if (f0 == f1) {
-            if (eo && ((bd < 0 ? -bd : bd) & 1) == 0) continue;
-#pragma unroll
-            for (int k = 0; k < 8; k++) cov[k] = 1.0f;
-        } else {
-            zero_cells(D);
-            alpha_coverage(b, f0, f1, bd, eo, D, cov);
-            __syncwarp();
+        const int8_t bd = (int8_t)(st & 0xffu);
+        if (!(st & 0x100u) && (flags & 2u) && !solid_hidden((flags & 1u) != 0, bd)) {
+            z = (int32_t)p;
+            return true;
         }
-        const float pr = (float)(color & 0xffu) * inv255, pg = (float)((color >> 8) & 0xffu) * inv255,
-                    pb = (float)((color >> 16) & 0xffu) * inv255, pa = (float)(color >> 24) * inv255;
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            const float a = pa * cov[k], ia = 1.0f - a;
-            dr[k] = dr[k] * ia + pr * a;
-            dg[k] = dg[k] * ia + pg * a;
-            db[k] = db[k] * ia + pb * a;
-            da[k] = da[k] * ia + a;
-        }
-    }
-    const uint32_t px = fx * 16 + (uint32_t)col;
-    if (px >= S.img_w) return;
-    uchar4 *img = reinterpret_cast<uchar4 *>(b.image + S.img_offset);
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const uint32_t py = fy * 16 + (uint32_t)(h * 8 + k);
-        if (py < S.img_h) {
-            img[(size_t)py * S.img_w + px] =
-                make_uchar4((unsigned char)__float2uint_rn(__saturatef(dr[k]) * 255.0f),
-                            (unsigned char)__float2uint_rn(__saturatef(dg[k]) * 255.0f),
-                            (unsigned char)__float2uint_rn(__saturatef(db[k]) * 255.0f),
-                            (unsigned char)__float2uint_rn(__saturatef(da[k]) * 255.0f));
-        }
+        return false;
+    });
+    if (lane == 0) {
+        if (kWrite) b.z[fb] = z;
+        else b.fb_count[fb] = n;
     }
 }
 
@@ -865,11 +889,11 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_coverage_dump(Batch b, cons
     if (k >= n) return;
     int *D = cells[warp];
     const uint32_t gt = tiles[k];
-    const uint32_t p = b.tile_path[gt];
+    const uint32_t p = upper_bound(b.path_tiles, b.n_paths + 1, gt) - 1;
     zero_cells(D);
     float cov[8];
-    alpha_coverage(b, b.tile_fills[gt], b.tile_fills[gt + 1], b.tile_backdrop[gt], (b.paths[p].flags & 1u) != 0, D,
-                   cov);
+    alpha_coverage(b, b.tile_fills[(int64_t)gt - 1], b.tile_fills[gt], (int8_t)(b.tile_state[gt] & 0xffu),
+                   (b.paths[p].flags & 1u) != 0, D, cov);
     const int col = lane & 15, h = lane >> 4;
 #pragma unroll
     for (int r = 0; r < 8; r++) out[(size_t)k * 256 + (h * 8 + r) * 16 + col] = cov[r];
@@ -884,115 +908,82 @@ static std::atomic<uint64_t> g_launches{0};
 uint64_t launches() { return g_launches.load(); }
 void count_launches(uint32_t n) { g_launches += n; }
 
+#define PF_LAUNCH(...)           \
+    do {                         \
+        __VA_ARGS__;             \
+        count_launches(1);       \
+    } while (0)
+
 cudaError_t launch_normalize(const Batch &b, uint2 *path_contours, cudaStream_t st) {
-    if (b.n_contours) {
-        k_normalize_contours<<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
-        count_launches(1);
-    }
-    if (b.n_paths) {
-        k_normalize_paths<<<grid_for(b.n_paths), kThreads, 0, st>>>(b, path_contours);
-        count_launches(1);
-    }
+    if (b.n_contours) PF_LAUNCH(k_normalize_contours<<<grid_for(b.n_contours), kThreads, 0, st>>>(b));
+    if (b.n_paths) PF_LAUNCH(k_normalize_paths<<<grid_for(b.n_paths), kThreads, 0, st>>>(b, path_contours));
     return cudaGetLastError();
 }
 
 cudaError_t launch_path_setup(const Batch &b, const uint2 *path_contours, cudaStream_t st) {
-    if (b.n_paths) {
-        k_path_setup<<<grid_for(uint64_t(b.n_paths) * 32), kThreads, 0, st>>>(b, path_contours);
-        count_launches(1);
-    }
+    if (b.n_paths) PF_LAUNCH(k_path_setup<<<grid_for(uint64_t(b.n_paths) * 32), kThreads, 0, st>>>(b, path_contours));
     return cudaGetLastError();
 }
 
 cudaError_t launch_path_offsets(const Batch &b, cudaStream_t st) {
-    if (b.n_paths) {
-        k_path_offsets<<<grid_for(b.n_paths), kThreads, 0, st>>>(b);
-        count_launches(1);
-    }
+    if (b.n_paths) PF_LAUNCH(k_path_offsets<<<grid_for(b.n_paths), kThreads, 0, st>>>(b));
     return cudaGetLastError();
 }
 
 cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st) {
     if (!b.n_contours) return cudaSuccess;
-    if (write) {
-        k_contour_segments<true><<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
-        count_launches(1);
-    }
-    else {
-        k_contour_segments<false><<<grid_for(b.n_contours), kThreads, 0, st>>>(b);
-        count_launches(1);
-    }
+    if (write) PF_LAUNCH(k_contour_segments<true><<<grid_for(b.n_contours), kThreads, 0, st>>>(b));
+    else PF_LAUNCH(k_contour_segments<false><<<grid_for(b.n_contours), kThreads, 0, st>>>(b));
     return cudaGetLastError();
 }
 
 cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st) {
     if (!n_segs) return cudaSuccess;
-    if (write) {
-        k_flatten<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs);
-        count_launches(1);
-    }
-    else {
-        k_flatten<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs);
-        count_launches(1);
-    }
+    if (write) PF_LAUNCH(k_flatten<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
+    else PF_LAUNCH(k_flatten<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
     return cudaGetLastError();
 }
 
 cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream_t st) {
     if (!n_leaves) return cudaSuccess;
-    if (write) {
-        k_bin<true><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves);
-        count_launches(1);
-    }
-    else {
-        k_bin<false><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves);
-        count_launches(1);
-    }
+    if (write) PF_LAUNCH(k_bin<true><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves));
+    else PF_LAUNCH(k_bin<false><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves));
     return cudaGetLastError();
 }
 
 cudaError_t launch_propagate(const Batch &b, uint32_t n_cols, cudaStream_t st) {
-    if (n_cols) {
-        k_propagate<<<grid_for(n_cols), kThreads, 0, st>>>(b, n_cols);
-        count_launches(1);
-    }
+    if (n_cols) PF_LAUNCH(k_propagate<<<grid_for(n_cols), kThreads, 0, st>>>(b, n_cols));
     return cudaGetLastError();
 }
 
-cudaError_t launch_list(const Batch &b, uint32_t n_tiles, bool write, cudaStream_t st) {
-    if (!n_tiles) return cudaSuccess;
-    if (write) {
-        k_list<true><<<grid_for(n_tiles), kThreads, 0, st>>>(b, n_tiles);
-        count_launches(1);
-    }
-    else {
-        k_list<false><<<grid_for(n_tiles), kThreads, 0, st>>>(b, n_tiles);
-        count_launches(1);
-    }
-    return cudaGetLastError();
-}
-
-cudaError_t launch_list_sort(const Batch &b, cudaStream_t st) {
-    if (b.n_fb) {
-        k_list_sort<<<b.n_fb, kSortThreads, 0, st>>>(b);
-        count_launches(1);
-    }
+cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st) {
+    if (!b.n_rows) return cudaSuccess;
+    if (write) PF_LAUNCH(k_rows<true><<<b.n_rows, kRowThreads, 0, st>>>(b));
+    else PF_LAUNCH(k_rows<false><<<b.n_rows, kRowThreads, 0, st>>>(b));
     return cudaGetLastError();
 }
 
 cudaError_t launch_composite(const Batch &b, cudaStream_t st) {
-    if (b.n_fb) {
-        k_composite<<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b);
-        count_launches(1);
-    }
+    if (!b.n_fb) return cudaSuccess;
+    int dev = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_composite, kCompWarps * 32, 0);
+    const uint64_t want = grid_for(b.n_fb, kCompWarps);
+    const unsigned grid = (unsigned)std::min<uint64_t>(want, uint64_t(std::max(per_sm, 1)) * sms);
+    PF_LAUNCH(k_composite<<<grid, kCompWarps * 32, 0, st>>>(b));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_list_dump(const Batch &b, bool write, cudaStream_t st) {
+    if (!b.n_fb) return cudaSuccess;
+    if (write) PF_LAUNCH(k_list_dump<true><<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
+    else PF_LAUNCH(k_list_dump<false><<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
     return cudaGetLastError();
 }
 
 cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t n, float *out, cudaStream_t st) {
-    if (n) {
-        k_coverage_dump<<<grid_for(n, kCompWarps), kCompWarps * 32, 0, st>>>(b, tiles, n, out);
-        count_launches(1);
-    }
+    if (n) PF_LAUNCH(k_coverage_dump<<<grid_for(n, kCompWarps), kCompWarps * 32, 0, st>>>(b, tiles, n, out));
     return cudaGetLastError();
 }
 
