@@ -317,8 +317,8 @@ Batch make_batch(Ctx *c) {
     b.fills = c->fills.as<uint2>();
     b.fill_cap = (uint32_t)std::min<size_t>(c->fills.cap / 8, 0xffffffffu);
     b.row_first = c->row_first.as<uint32_t>();
-    b.row_paths = c->row_paths.as<uint32_t>();
-    b.row_cap = (uint32_t)std::min<size_t>(c->row_paths.cap / 4, 0xffffffffu);
+    b.row_paths = c->row_paths.as<uint4>();
+    b.row_cap = (uint32_t)std::min<size_t>(c->row_paths.cap / 16, 0xffffffffu);
     b.n_rows = c->r_rows;
     b.n_fb = c->r_fb;
     b.z = c->z.as<int32_t>();
@@ -339,7 +339,7 @@ int read_status(Ctx *c) {
 int check_kernel_status(Ctx *c) {
     const uint32_t e = c->h_status[kStErr];
     if (e & kErrNonFinite) return fail(c, PF_ERR_INVALID_ARGUMENT, "a point coordinate is NaN or infinite");
-    if (e & (kErrDepth | kErrWalk | kErrClip)) {
+    if (e & (kErrDepth | kErrWalk | kErrClip | kErrScanWait)) {
         char m[128];
         std::snprintf(m, sizeof m, "a kernel hit an iteration bound (flags 0x%x)", e);
         return fail(c, PF_ERR_KERNEL_LIMIT, m);
@@ -351,7 +351,8 @@ int check_kernel_status(Ctx *c) {
 
 int scan(Ctx *c, uint32_t *arr, uint32_t n, int slot) {
     PF_CUDA(c->scan_temp.ensure(scan_temp_bytes(n)));
-    PF_CUDA(scan_exclusive_u32(arr, arr, n, c->status.as<uint32_t>() + slot, c->scan_temp.p, c->stream));
+    PF_CUDA(scan_exclusive_u32(arr, arr, n, c->status.as<uint32_t>() + slot, c->scan_temp.p, c->stream,
+                               c->status.as<uint32_t>() + kStErr));
     return PF_OK;
 }
 
@@ -424,7 +425,7 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     // 2. segments, row lists, leaf counts, leaves
     PF_CUDA(c->segs.ensure(size_t(c->n_segs) * sizeof(SegDev) + 16));
     PF_CUDA(c->seg_leaves.ensure((size_t(c->n_segs) + 1) * 4));
-    PF_CUDA(c->row_paths.ensure(size_t(c->n_row_entries) * 4 + 16));
+    PF_CUDA(c->row_paths.ensure(size_t(c->n_row_entries) * 16 + 16));
     b = make_batch(c);
     PF_CUDA(launch_contour_segments(b, true, st));
     PF_CUDA(launch_rows(b, true, st));

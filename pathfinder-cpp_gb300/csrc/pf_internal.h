@@ -1,6 +1,7 @@
 // pf_internal.h - device data layout and kernel launchers of the fill pipeline.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -14,12 +15,18 @@ constexpr int kMaxDepth = 32;              // flattening recursion bound (depth 
 constexpr uint32_t kMaxWalk = 1u << 20;    // tile-walk step bound per line
 constexpr uint32_t kNone = 0xffffffffu;
 
+// Learned sizer: per-path features -> 64 -> 64 -> (log1p leaf lines, log1p fills).
+constexpr int kSizerIn = 12, kSizerHidden = 64, kSizerOut = 2;
+constexpr int kSizerParams = kSizerHidden * kSizerIn + kSizerHidden + kSizerHidden * kSizerHidden + kSizerHidden +
+                             kSizerOut * kSizerHidden + kSizerOut;  // 5122
+
 // Kernel error bits (written with atomicOr into the status word).
 enum : uint32_t {
     kErrDepth = 1u << 0,    // flattening hit kMaxDepth
     kErrWalk = 1u << 1,     // a tile walk hit kMaxWalk
     kErrClip = 1u << 2,     // Cohen-Sutherland clipping did not settle
     kErrNonFinite = 1u << 3,// a point is NaN or infinite
+    kErrScanWait = 1u << 4, // a scan's look-back wait hit its bound
     kErrOverflowSeg = 1u << 8,
     kErrOverflowLeaf = 1u << 9,
     kErrOverflowFill = 1u << 10,
@@ -113,7 +120,8 @@ struct Batch {
     // per framebuffer-tile row of each scene: the paths whose tile rect spans the row,
     // in path order
     uint32_t *row_first;                 // [rows + 1] counts -> scanned
-    uint32_t *row_paths;
+    uint4 *row_paths;                    // {path, rx0 | rx1 << 16, tile of (0, row) in the path's rect
+                                         //  numbering, path flags}
     uint32_t row_cap;
     uint32_t n_rows;
     uint32_t n_fb;
@@ -149,7 +157,7 @@ void count_launches(uint32_t n);
 // Scans (exclusive, in place allowed); the total lands in *total (device).
 size_t scan_temp_bytes(uint32_t n);
 cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, void *temp,
-                               cudaStream_t st);
+                               cudaStream_t st, uint32_t *err);
 
 // Stage launchers (all asynchronous on the given stream).
 cudaError_t launch_normalize(const Batch &b, uint2 *path_contours, cudaStream_t st);
@@ -163,5 +171,14 @@ cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_composite(const Batch &b, cudaStream_t st);
 cudaError_t launch_list_dump(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t n, float *out, cudaStream_t st);
+
+// Learned sizer (pf_sizer.cu).
+cudaError_t launch_features(const Batch &b, const uint2 *path_contours, const float4 *bounds, float *feat,
+                            cudaStream_t st);
+cudaError_t launch_mlp_predict(const __nv_bfloat16 *w, const float *feat, uint32_t n, float *out, cudaStream_t st);
+cudaError_t launch_mlp_grad(const __nv_bfloat16 *w, const float *feat, const float *target, const uint32_t *index,
+                            uint32_t n, float *grad, float *loss, cudaStream_t st);
+cudaError_t launch_adam(float *master, __nv_bfloat16 *w, float *grad, float *m, float *v, float lr, int step,
+                        cudaStream_t st);
 
 }  // namespace pfc

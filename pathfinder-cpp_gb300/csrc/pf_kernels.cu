@@ -606,8 +606,9 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(Batch b) {
     for (uint32_t base = p0; base < p1; base += kRowThreads) {
         const uint32_t p = base + threadIdx.x;
         bool spans = false;
+        int4 rect = make_int4(0, 0, 0, 0);
         if (p < p1) {
-            const int4 rect = *reinterpret_cast<const int4 *>(&b.paths[p].rx0);
+            rect = *reinterpret_cast<const int4 *>(&b.paths[p].rx0);
             spans = rect.y <= y && y < rect.w && rect.x < rect.z;
         }
         const uint32_t ballot = __ballot_sync(0xffffffffu, spans);
@@ -625,7 +626,13 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(Batch b) {
         __syncthreads();
         if (kWrite && spans) {
             const uint32_t rank = warp_counts[warp] + __popc(ballot & ((1u << lane) - 1u));
-            if (out + rank < b.row_cap) b.row_paths[out + rank] = p;
+            // tile index of column 0 of this row in the path's numbering (may underflow by rx0;
+            // adding fx >= rx0 brings it back into range)
+            const uint32_t row_tile = b.paths[p].tile_first + (uint32_t)(y - rect.y) * (uint32_t)(rect.z - rect.x) -
+                                      (uint32_t)rect.x;
+            if (out + rank < b.row_cap)
+                b.row_paths[out + rank] = make_uint4(p, (uint32_t)rect.x | ((uint32_t)rect.z << 16), row_tile,
+                                                     b.paths[p].flags);
         }
         out += chunk_total;
         total += chunk_total;
@@ -740,13 +747,13 @@ __device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint3
     const uint32_t k_lo = b.row_first[row], k_hi = b.row_first[row + 1];
     for (uint32_t top = k_hi; top > k_lo; top = top > k_lo + 32 ? top - 32 : k_lo) {
         const int64_t k = (int64_t)top - 1 - lane;
-        uint32_t p = 0, gt = 0, st = 0;
+        uint4 e = make_uint4(0, 0, 0, 0);
+        uint32_t gt = 0, st = 0;
         bool vis = false;
         if (k >= (int64_t)k_lo) {
-            p = b.row_paths[k];
-            const int4 rect = *reinterpret_cast<const int4 *>(&b.paths[p].rx0);
-            if ((int32_t)fx >= rect.x && (int32_t)fx < rect.z) {
-                gt = b.paths[p].tile_first + ((int32_t)fy - rect.y) * (rect.z - rect.x) + ((int32_t)fx - rect.x);
+            e = b.row_paths[k];
+            if (fx >= (e.y & 0xffffu) && fx < (e.y >> 16)) {
+                gt = e.z + fx;
                 st = b.tile_state[gt];
                 vis = st != 0;
             }
@@ -755,10 +762,11 @@ __device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint3
         while (mask) {
             const int l = __ffs(mask) - 1;
             mask &= mask - 1;
-            const uint32_t pl = __shfl_sync(0xffffffffu, p, l);
+            const uint32_t pl = __shfl_sync(0xffffffffu, e.x, l);
             const uint32_t gtl = __shfl_sync(0xffffffffu, gt, l);
             const uint32_t stl = __shfl_sync(0xffffffffu, st, l);
-            if (visit(pl, gtl, stl)) return;
+            const uint32_t fl = __shfl_sync(0xffffffffu, e.w, l);
+            if (visit(pl, gtl, stl, fl)) return;
         }
     }
 }
@@ -786,8 +794,8 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
             ar[k] = ag[k] = ab[k] = aa[k] = 0.0f;
             tr[k] = 1.0f;
         }
-        walk_fb_tile(b, S.row_first - b.row_base + fy, fx, fy, [&](uint32_t p, uint32_t gt, uint32_t st) -> bool {
-            const uint32_t flags = b.paths[p].flags;
+        walk_fb_tile(b, S.row_first - b.row_base + fy, fx, fy,
+                     [&](uint32_t p, uint32_t gt, uint32_t st, uint32_t flags) -> bool {
             const bool eo = (flags & 1u) != 0;
             const int8_t bd = (int8_t)(st & 0xffu);
             float cov[8];
@@ -863,10 +871,10 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_list_dump(Batch b) {
         first = b.fb_count[fb];
         count = b.fb_count[fb + 1] - first;
     }
-    walk_fb_tile(b, S.row_first - b.row_base + fy, fx, fy, [&](uint32_t p, uint32_t gt, uint32_t st) -> bool {
+    walk_fb_tile(b, S.row_first - b.row_base + fy, fx, fy,
+                 [&](uint32_t p, uint32_t gt, uint32_t st, uint32_t flags) -> bool {
         if (kWrite && lane == 0) b.list[first + count - 1 - n] = gt;
         n++;
-        const uint32_t flags = b.paths[p].flags;
         const int8_t bd = (int8_t)(st & 0xffu);
         if (!(st & 0x100u) && (flags & 2u) && !solid_hidden((flags & 1u) != 0, bd)) {
             z = (int32_t)p;

@@ -1,18 +1,27 @@
-// pf_scan.cu - exclusive prefix sums over uint32 arrays (reduce, scan the block sums, scan-add).
+// pf_scan.cu - exclusive prefix sums over uint32 arrays: single pass, decoupled look-back.
 //
 // Used to turn per-contour segment counts, per-segment leaf counts, per-tile fill
-// counts and per-framebuffer-tile list lengths into offsets, which replaces the
-// reference's atomic allocation and linked lists (pathfinder/shaders/d3d11/bin.comp:100-103,
+// counts and per-row path counts into offsets, which replaces the reference's atomic
+// allocation and linked lists (pathfinder/shaders/d3d11/bin.comp:100-103,
 // propagate.comp:179,210) with a deterministic, gap-free layout.
+//
+// Each block scans one tile of kScanTile elements (uint4 loads), publishes its aggregate,
+// then resolves its prefix by looking back over the predecessors' published aggregates /
+// inclusive prefixes (a status word per tile: flag in the top 2 bits, value below).  Tiles
+// are taken in launch order from an atomic ticket so a block only ever waits on tiles that
+// started before it.  Every wait is bounded: after kSpinLimit polls the block records an
+// error bit and stops.
 #include "pf_internal.h"
 
 namespace pfc {
 
 namespace {
 
-constexpr int kScanThreads = 512;
-constexpr int kScanItems = 8;
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;                               // 4 x uint4 per thread
 constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096
+constexpr uint64_t kFlagAgg = 1ull << 62, kFlagInc = 2ull << 62, kValMask = (1ull << 62) - 1;
+constexpr uint32_t kSpinLimit = 1u << 24;
 
 __device__ __forceinline__ uint32_t warp_inclusive(uint32_t v) {
     const int lane = threadIdx.x & 31;
@@ -24,92 +33,113 @@ __device__ __forceinline__ uint32_t warp_inclusive(uint32_t v) {
     return v;
 }
 
-// Block-wide exclusive scan of one value per thread; returns the block total in *total.
-__device__ __forceinline__ uint32_t block_exclusive(uint32_t v, uint32_t *total) {
+// state[0] = ticket counter, state[1 + t] = status of tile t
+__global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t *in, uint32_t *out, uint32_t n,
+                                                       unsigned long long *state, uint32_t *total,
+                                                       uint32_t *err) {
     __shared__ uint32_t warp_sums[kScanThreads / 32];
+    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_prefix;
+    if (threadIdx.x == 0) s_tile = (uint32_t)atomicAdd(&state[0], 1ull);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t base = (uint64_t)tile * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    if (base + kScanItems <= n && ((reinterpret_cast<uintptr_t>(in + base) & 15) == 0)) {
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; q++) {
+            const uint4 x = *reinterpret_cast<const uint4 *>(in + base + 4 * q);
+            v[4 * q + 0] = x.x;
+            v[4 * q + 1] = x.y;
+            v[4 * q + 2] = x.z;
+            v[4 * q + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) v[k] = base + k < n ? in[base + k] : 0u;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) sum += v[k];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t inc = warp_inclusive(v);
+    const uint32_t inc = warp_inclusive(sum);
     if (lane == 31) warp_sums[warp] = inc;
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = lane < kScanThreads / 32 ? warp_sums[lane] : 0u;
+        const uint32_t w = lane < kScanThreads / 32 ? warp_sums[lane] : 0u;
         const uint32_t wi = warp_inclusive(w);
         if (lane < kScanThreads / 32) warp_sums[lane] = wi - w;
-        if (lane == kScanThreads / 32 - 1) *total = wi;
+        const uint32_t agg = __shfl_sync(0xffffffffu, wi, kScanThreads / 32 - 1);
+        // publish, look back, publish the inclusive prefix
+        if (lane == 0) {
+            volatile unsigned long long *st = state + 1;
+            if (tile == 0) {
+                st[0] = kFlagInc | agg;
+                s_prefix = 0;
+            } else {
+                st[tile] = kFlagAgg | agg;
+                uint64_t prefix = 0;
+                int64_t t = (int64_t)tile - 1;
+                uint32_t spins = 0;
+                while (t >= 0) {
+                    const unsigned long long s = st[t];
+                    const uint64_t flag = s & ~kValMask;
+                    if (flag == 0) {
+                        if (++spins > kSpinLimit) {
+                            atomicOr(err, kErrScanWait);
+                            break;
+                        }
+                        continue;
+                    }
+                    prefix += s & kValMask;
+                    if (flag == kFlagInc) break;
+                    t--;
+                }
+                __threadfence();
+                st[tile] = kFlagInc | (prefix + agg);
+                s_prefix = (uint32_t)prefix;
+            }
+        }
     }
     __syncthreads();
-    const uint32_t r = warp_sums[warp] + inc - v;
-    __syncthreads();
-    return r;
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_reduce(const uint32_t *__restrict__ in, uint32_t n,
-                                                         uint32_t *__restrict__ block_sums) {
-    const uint32_t base = blockIdx.x * kScanTile;
-    uint32_t s = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        const uint32_t i = base + k * kScanThreads + threadIdx.x;
-        if (i < n) s += in[i];
+    uint32_t run = s_prefix + warp_sums[warp] + inc - sum;
+    if (tile == gridDim.x - 1 && threadIdx.x == kScanThreads - 1 && total) {
+        total[0] = run + sum;
     }
-    __shared__ uint32_t total;
-    block_exclusive(s, &total);
-    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
-}
-
-// Exclusive scan of one tile per block, plus an optional per-block offset.
-__global__ void __launch_bounds__(kScanThreads) k_scan_tile(const uint32_t *in, uint32_t *out, uint32_t n,
-                                                            const uint32_t *__restrict__ block_offsets,
-                                                            uint32_t *total_out) {
-    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    uint32_t v[kScanItems];
-    uint32_t s = 0;
+    if (base + kScanItems <= n && ((reinterpret_cast<uintptr_t>(out + base) & 15) == 0)) {
+        uint32_t o[kScanItems];
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        const uint32_t i = base + k;
-        v[k] = i < n ? in[i] : 0u;
-        s += v[k];
-    }
-    __shared__ uint32_t total;
-    uint32_t run = block_exclusive(s, &total);
-    if (block_offsets) run += block_offsets[blockIdx.x];
+        for (int k = 0; k < kScanItems; k++) {
+            o[k] = run;
+            run += v[k];
+        }
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) {
-        const uint32_t i = base + k;
-        if (i < n) out[i] = run;
-        run += v[k];
+        for (int q = 0; q < kScanItems / 4; q++)
+            *reinterpret_cast<uint4 *>(out + base + 4 * q) = make_uint4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            if (base + k < n) out[base + k] = run;
+            run += v[k];
+        }
     }
-    if (total_out && threadIdx.x == 0) *total_out = total;
 }
 
 }  // namespace
 
 size_t scan_temp_bytes(uint32_t n) {
-    size_t bytes = 0;
-    while (n > kScanTile) {
-        n = (n + kScanTile - 1) / kScanTile;
-        bytes += (size_t(n) + 1) * sizeof(uint32_t);
-    }
-    return bytes + 64;
+    const size_t tiles = (size_t(n) + kScanTile - 1) / kScanTile;
+    return (tiles + 1) * sizeof(unsigned long long) + 64;
 }
 
 cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, void *temp,
-                               cudaStream_t st) {
-    if (n == 0) {
-        return cudaMemsetAsync(total, 0, sizeof(uint32_t), st);
-    }
-    if (n <= kScanTile) {
-        k_scan_tile<<<1, kScanThreads, 0, st>>>(in, out, n, nullptr, total);
-        count_launches(1);
-        return cudaGetLastError();
-    }
-    const uint32_t nb = (n + kScanTile - 1) / kScanTile;
-    uint32_t *sums = static_cast<uint32_t *>(temp);
-    k_reduce<<<nb, kScanThreads, 0, st>>>(in, n, sums);
-    count_launches(2);
-    cudaError_t e = scan_exclusive_u32(sums, sums, nb, total, sums + nb + 1, st);
+                               cudaStream_t st, uint32_t *err) {
+    if (n == 0) return cudaMemsetAsync(total, 0, sizeof(uint32_t), st);
+    const uint32_t tiles = (n + kScanTile - 1) / kScanTile;
+    cudaError_t e = cudaMemsetAsync(temp, 0, (size_t(tiles) + 1) * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
-    k_scan_tile<<<nb, kScanThreads, 0, st>>>(in, out, n, sums, nullptr);
+    k_scan<<<tiles, kScanThreads, 0, st>>>(in, out, n, static_cast<unsigned long long *>(temp), total, err);
+    count_launches(1);
     return cudaGetLastError();
 }
 

@@ -95,8 +95,6 @@ constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kH * kI, kOffW2 = kOffB1 + kH, kOffB
               kOffW3 = kOffB2 + kH, kOffB3 = kOffW3 + kO * kH, kParams = kOffB3 + kO;
 static_assert(kParams == kSizerParams, "parameter count");
 
-__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
-
 // Weights are stored and used in bf16; accumulation is fp32.
 __device__ __forceinline__ void load_params_smem(const __nv_bfloat16 *w, float *s) {
     for (int i = threadIdx.x; i < kParams; i += blockDim.x) s[i] = __bfloat162float(w[i]);
