@@ -242,16 +242,32 @@ def main():
             ms = float(t.item())
         return ms, out
 
-    # 1. batched frame, inputs resident
+    learned = os.path.exists(pfcuda.DEFAULT_WEIGHTS)
+    if learned:
+        r.sizer_load(pfcuda.DEFAULT_WEIGHTS)
+
+    # 1. batched exact two-pass frame, inputs resident
     for _ in range(args.warmup):
         r.render()
+    ms_exact, stats_e = timed(lambda: r.render(), args.steps)
+
+    # 2. batched learned one-pass frame (the headline), inputs resident
+    frame = r.render_learned if learned else r.render
+    for _ in range(args.warmup):
+        frame()
     clocks = ClockSampler(local_rank)
     clocks.start()
-    ms_batched, stats_b = timed(lambda: r.render(), args.steps)
+    ms_batched, stats_b = timed(frame, args.steps)
     clk = clocks.stop()
     st = stats_b[-1]
+    sizer = None
+    if learned:
+        over, pool = r.sizer_last_frame()
+        sizer = {"frames_redone_exactly": int(sum(s["overflow"] for s in stats_b)), "paths_over_budget": over,
+                 "spill_pool_slots_used": pool, "host_syncs": st["host_syncs"],
+                 "exact_host_syncs": stats_e[-1]["host_syncs"]}
 
-    # 2. plain single-scene pipeline (one frame per scene), inputs resident
+    # 3. plain single-scene pipeline (one exact frame per scene), inputs resident
     def plain_pass():
         last = None
         launches = 0
@@ -262,10 +278,10 @@ def main():
     plain_pass()
     ms_plain, launches_plain = timed(plain_pass, max(1, min(args.steps, 3)))
 
-    # 3. end to end through the C-ABI: pinned H2D upload, frame, D2H of every image
+    # 4. end to end through the C-ABI: pinned H2D upload, frame, D2H of every image
     def e2e_step():
         r.upload_views(views)
-        s = r.render()
+        s = frame()
         r.read_images(img_host.data_ptr(), img_bytes)
         return s
     for _ in range(max(1, args.warmup // 2)):
@@ -300,14 +316,18 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_batched, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (exact-IEEE tiling), int32 fixed-point coverage", "data": "synthetic",
             "config": workload_config(n_scenes, scenes_list) | {"parallelism": f"replicas x{world}"},
+            "frame": "batched learned one-pass" if learned else "batched exact two-pass",
+            "batched_exact": {"value": world * n_scenes / (ms_exact * 1e-3), "unit": UNIT, "ms_per_step": ms_exact},
             "plain": {"value": world * n_scenes / (ms_plain * 1e-3), "unit": UNIT, "ms_per_step": ms_plain,
                       "gpu_launches_per_step": launches_plain[-1]},
+            "speedup_vs_plain": ms_plain / ms_batched,
+            "sizer": sizer,
             "e2e": {"value": world * n_scenes / (ms_e2e * 1e-3), "unit": UNIT, "ms_per_step": ms_e2e,
                     "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": img_bytes},
             "stages_ms": {k: st[k] for k in ("ms_setup", "ms_flatten", "ms_bin", "ms_propagate", "ms_lists",
                                              "ms_composite", "ms_total")},
-            "frame": {k: st[k] for k in ("paths", "segments", "microlines", "tiles", "fills", "composite_entries",
-                                         "composited_fills", "framebuffer_tiles", "host_syncs")},
+            "counts": {k: st[k] for k in ("paths", "segments", "microlines", "tiles", "fills", "composite_entries",
+                                          "composited_fills", "framebuffer_tiles", "host_syncs")},
             "roofline": {"kernel": "k_composite", "bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
                          "peak_source": peak_src, "algorithmic_bytes": comp_bytes},

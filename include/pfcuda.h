@@ -174,6 +174,48 @@ int pf_render(void *ctx, pf_frame_stats *stats);
  * single-scene frame of the reference when n_scenes == 1. */
 int pf_render_scenes(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats);
 
+/*
+ * The learned one-pass frame over uploaded scenes [first_scene, first_scene + n_scenes):
+ * a per-path MLP (the "sizer", below) predicts every path's leaf-line and fill counts, the
+ * frame lays out per-path leaf regions and the fill capacity from those predictions, and
+ * flattens, stores and counts leaf lines in one pass (one host synchronisation after
+ * set-up instead of the exact method's count-then-allocate passes).  Output is identical
+ * to pf_render_scenes.  If a prediction is too small the frame is redone by the exact
+ * method and stats->overflow is set.  Needs sizer weights (pf_sizer_load / _init).
+ */
+int pf_render_learned(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats);
+
+/*
+ * Learned sizer: features (12 per path) -> 64 -> 64 -> (log1p leaf lines, log1p fills),
+ * bf16 weights, fp32 accumulation, trained on the GPU with the library's own forward,
+ * backward and Adam kernels.  It replaces the reference's buffer sizing by readback and
+ * retry (pathfinder/core/d3d11/renderer.cpp:540-577).  Budgets per path are
+ * ceil(expm1(prediction) * mul + add); leaf lines past a path's budget spill into a shared
+ * pool of pool_fraction x (sum of budgets) slots, and only an exhausted pool (or fills past
+ * the summed fill estimate) sends the frame to the exact method.
+ */
+int pf_sizer_param_count(void);
+int pf_sizer_init(void *ctx, uint64_t seed);
+int pf_sizer_set_params(void *ctx, const float *params, size_t n);
+int pf_sizer_get_params(void *ctx, float *params, size_t n);
+int pf_sizer_set_margin(void *ctx, float mul, float add, float pool_fraction);
+int pf_sizer_last_frame(void *ctx, uint32_t *paths_over_budget, uint32_t *pool_slots_used);
+int pf_sizer_predict(void *ctx, const float *features, uint32_t n, float *out);
+int pf_sizer_gradient(void *ctx, const float *features, const float *targets, uint32_t n, float *grad,
+                      float *loss);
+int pf_sizer_train(void *ctx, const float *features, const float *targets, uint32_t n, uint32_t epochs,
+                   uint32_t batch, float lr, uint64_t seed, float *epoch_losses);
+int pf_sizer_save(void *ctx, const char *path);
+int pf_sizer_load(void *ctx, const char *path);
+
+/* Per-path features (n_paths x 12) and exact leaf-line / fill counts of the last frame
+ * (the sizer's inputs and training labels). */
+int pf_path_features(void *ctx, float *out, size_t capacity_floats);
+int pf_path_counts(void *ctx, uint32_t *leaves, uint32_t *fills, size_t capacity);
+
+/* The last frame's 16 status words: error bits, stage totals and counters (debug aid). */
+int pf_debug_counters(void *ctx, uint32_t *out, size_t n);
+
 /* Copy the last rendered image to host memory: RGBA8, row-major,
  * width_px * height_px * 4 bytes with width_px = ceil(width). */
 int pf_read_image(void *ctx, uint8_t *rgba, size_t capacity_bytes);

@@ -79,7 +79,14 @@ struct Ctx {
     bool uploaded = false, rendered = false;
 
     // working buffers
-    DevBuf contour_point_first, contour_path, paths, path_tiles, path_cols, contour_segs, path_contours;
+    DevBuf contour_point_first, contour_path, paths, path_tiles, path_cols, contour_segs, path_contours, path_bounds;
+    // learned sizer: weights (bf16 used by the kernels, fp32 master + Adam moments for training)
+    DevBuf sz_w, sz_master, sz_m, sz_v, sz_grad, sz_loss, sz_feat, sz_target, sz_index, sz_pred;
+    DevBuf path_feat, path_pred, path_leaf_first, path_leaf_budget, path_leaf_cursor, path_fill_budget;
+    int sz_step = 0;
+    bool sz_ready = false;
+    float sz_mul = 1.25f, sz_add = 8.0f, sz_pool = 0.10f;
+    uint32_t last_paths_over = 0, last_pool_used = 0;
     DevBuf segs, seg_leaves, leaves, leaf_path;
     DevBuf tile_fills, tile_delta, tile_state, col_above, col_final, fills;
     DevBuf row_first, row_paths, scene_row_first;
@@ -300,6 +307,10 @@ Batch make_batch(Ctx *c) {
     b.contour_point_first = c->contour_point_first.as<uint32_t>();
     b.contour_path = c->contour_path.as<uint32_t>();
     b.paths = c->paths.as<PathDev>();
+    b.path_bounds = c->path_bounds.as<float4>();
+    b.path_leaf_first = c->path_leaf_first.as<uint32_t>();
+    b.path_leaf_budget = c->path_leaf_budget.as<uint32_t>();
+    b.path_leaf_cursor = c->path_leaf_cursor.as<uint32_t>();
     b.path_tiles = c->path_tiles.as<uint32_t>();
     b.path_cols = c->path_cols.as<uint32_t>();
     b.contour_segs = c->contour_segs.as<uint32_t>();
@@ -374,15 +385,14 @@ void set_range(Ctx *c, uint32_t first, uint32_t count) {
     c->r_rows = c->h_scene_row_first[first + count] - a.row_first;
 }
 
-// The exact two-pass frame over uploaded scenes [first, first + count).
-int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
+int begin_frame(Ctx *c, uint32_t first, uint32_t count) {
     if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
     if (count == 0 || first >= c->n_scenes || count > c->n_scenes - first)
         return fail(c, PF_ERR_INVALID_ARGUMENT, "scene range out of bounds");
     c->rendered = false;
+    c->lists_dumped = false;
     set_range(c, first, count);
     c->syncs = 0;
-    const uint64_t launches0 = launches();
     cudaStream_t st = c->stream;
     const uint32_t N = c->r_paths, C = c->r_contours;
     PF_CUDA(c->status.ensure(kStCount * 4));
@@ -394,12 +404,16 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     PF_CUDA(c->path_tiles.ensure((size_t(N) + 1) * 4));
     PF_CUDA(c->path_cols.ensure((size_t(N) + 1) * 4));
     PF_CUDA(c->path_contours.ensure(size_t(N) * 8 + 8));
-    const uint32_t NFB = c->r_fb, R = c->r_rows;
-    PF_CUDA(c->row_first.ensure((size_t(R) + 1) * 4));
-    c->lists_dumped = false;
+    PF_CUDA(c->path_bounds.ensure(size_t(N) * 16 + 16));
+    PF_CUDA(c->row_first.ensure((size_t(c->r_rows) + 1) * 4));
+    return PF_OK;
+}
 
-    record(c, 0);
-    // 1. topology, tile rects, segment counts, per-row path counts
+// Stage 1: topology, tile rects, segment counts, per-row path counts (and, for a learned
+// frame, the sizer's per-path budgets), ending with the frame's first host synchronisation.
+int stage_setup(Ctx *c, bool learned) {
+    cudaStream_t st = c->stream;
+    const uint32_t N = c->r_paths, C = c->r_contours, R = c->r_rows;
     Batch b = make_batch(c);
     PF_CUDA(launch_normalize(b, c->path_contours.as<uint2>(), st));
     PF_CUDA(launch_path_setup(b, c->path_contours.as<uint2>(), st));
@@ -414,67 +428,50 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     if (int e = scan(c, b.path_cols, N + 1, kStCols)) return e;
     if (int e = scan(c, b.row_first, R + 1, kStRows)) return e;
     PF_CUDA(launch_path_offsets(b, st));
+    if (learned) {
+        PF_CUDA(c->path_feat.ensure(size_t(N) * kSizerIn * 4 + 16));
+        PF_CUDA(c->path_pred.ensure(size_t(N) * kSizerOut * 4 + 16));
+        PF_CUDA(c->path_leaf_first.ensure((size_t(N) + 1) * 4));
+        PF_CUDA(c->path_leaf_budget.ensure(size_t(N) * 4 + 16));
+        PF_CUDA(c->path_leaf_cursor.ensure(size_t(N) * 4 + 16));
+        PF_CUDA(c->path_fill_budget.ensure((size_t(N) + 1) * 4));
+        b = make_batch(c);
+        PF_CUDA(launch_features(b, c->path_contours.as<uint2>(), c->path_feat.as<float>(), st));
+        PF_CUDA(launch_mlp_predict(c->sz_w.as<__nv_bfloat16>(), c->path_feat.as<float>(), N, c->path_pred.as<float>(),
+                                   st));
+        PF_CUDA(launch_budgets(b, c->path_pred.as<float>(), c->sz_mul, c->sz_add, b.path_leaf_first,
+                               c->path_fill_budget.as<uint32_t>(), st));
+        PF_CUDA(cudaMemcpyAsync(b.path_leaf_budget, b.path_leaf_first, size_t(N) * 4, cudaMemcpyDeviceToDevice, st));
+        PF_CUDA(cudaMemsetAsync(b.path_leaf_first + N, 0, 4, st));
+        PF_CUDA(cudaMemsetAsync(c->path_fill_budget.as<uint32_t>() + N, 0, 4, st));
+        PF_CUDA(cudaMemsetAsync(b.path_leaf_cursor, 0, size_t(N) * 4, st));
+        if (int e = scan(c, b.path_leaf_first, N + 1, kStLeafBudget)) return e;
+        if (int e = scan(c, c->path_fill_budget.as<uint32_t>(), N + 1, kStFillBudget)) return e;
+    }
     if (int e = read_status(c)) return e;
     if (int e = check_kernel_status(c)) return e;
     c->n_segs = c->h_status[kStSegs];
     c->n_tiles = c->h_status[kStTiles];
     c->n_cols = c->h_status[kStCols];
     c->n_row_entries = c->h_status[kStRows];
-    record(c, 1);
-
-    // 2. segments, row lists, leaf counts, leaves
     PF_CUDA(c->segs.ensure(size_t(c->n_segs) * sizeof(SegDev) + 16));
     PF_CUDA(c->seg_leaves.ensure((size_t(c->n_segs) + 1) * 4));
     PF_CUDA(c->row_paths.ensure(size_t(c->n_row_entries) * 16 + 16));
-    b = make_batch(c);
-    PF_CUDA(launch_contour_segments(b, true, st));
-    PF_CUDA(launch_rows(b, true, st));
-    PF_CUDA(cudaMemsetAsync(b.seg_leaves + c->n_segs, 0, 4, st));
-    PF_CUDA(launch_flatten(b, c->n_segs, false, st));
-    if (int e = scan(c, b.seg_leaves, c->n_segs + 1, kStLeaves)) return e;
-    if (int e = read_status(c)) return e;
-    if (int e = check_kernel_status(c)) return e;
-    c->n_leaves = c->h_status[kStLeaves];
-    PF_CUDA(c->leaves.ensure(size_t(c->n_leaves) * 16 + 16));
-    PF_CUDA(c->leaf_path.ensure(size_t(c->n_leaves) * 4 + 16));
-    b = make_batch(c);
-    PF_CUDA(launch_flatten(b, c->n_segs, true, st));
-    record(c, 2);
-
-    // 3. fill counts per tile, then fills written grouped by tile (counting sort)
     const size_t T = c->n_tiles, K = c->n_cols;
     PF_CUDA(c->tile_fills.ensure((T + 2) * 4));
     PF_CUDA(c->tile_delta.ensure(T * 4 + 4));
     PF_CUDA(c->tile_state.ensure(T * 2 + 16));
     PF_CUDA(c->col_above.ensure(K * 4 + 4));
     PF_CUDA(c->col_final.ensure(K * 4 + 4));
-    b = make_batch(c);
-    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, (T + 2) * 4, st));
-    PF_CUDA(cudaMemsetAsync(b.tile_delta, 0, T * 4, st));
-    PF_CUDA(cudaMemsetAsync(b.col_above, 0, K * 4, st));
-    PF_CUDA(launch_bin(b, c->n_leaves, false, st));
-    if (int e = scan(c, b.tile_fills, (uint32_t)T + 1, kStFills)) return e;
-    if (int e = read_status(c)) return e;
-    if (int e = check_kernel_status(c)) return e;
-    c->n_fills = c->h_status[kStFills];
-    PF_CUDA(c->fills.ensure(size_t(c->n_fills) * 8 + 16));
-    b = make_batch(c);
-    PF_CUDA(launch_bin(b, c->n_leaves, true, st));
-    record(c, 3);
+    return PF_OK;
+}
 
-    // 4. backdrops
-    PF_CUDA(launch_propagate(b, c->n_cols, st));
-    record(c, 4);
-    record(c, 5);
-
-    // 5. coverage + front-to-back composite with the z-cull walk
-    PF_CUDA(launch_composite(b, st));
-    record(c, 6);
+int finish_frame(Ctx *c, uint32_t first, uint32_t count, uint64_t launches0, pf_frame_stats *stats) {
+    const uint32_t NFB = c->r_fb;
     if (int e = read_status(c)) return e;
     if (int e = check_kernel_status(c)) return e;
     c->n_list = c->h_status[kStEntries];
     c->rendered = true;
-
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->paths = c->r_paths;
@@ -503,6 +500,123 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
         }
     }
     return PF_OK;
+}
+
+// The exact two-pass frame over uploaded scenes [first, first + count).
+int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
+    if (int e = begin_frame(c, first, count)) return e;
+    const uint64_t launches0 = launches();
+    cudaStream_t st = c->stream;
+    record(c, 0);
+    if (int e = stage_setup(c, false)) return e;
+    record(c, 1);
+
+    // 2. segments, row lists, leaf counts, leaves
+    Batch b = make_batch(c);
+    PF_CUDA(launch_contour_segments(b, true, st));
+    PF_CUDA(launch_rows(b, true, st));
+    PF_CUDA(cudaMemsetAsync(b.seg_leaves + c->n_segs, 0, 4, st));
+    PF_CUDA(launch_flatten(b, c->n_segs, false, st));
+    if (int e = scan(c, b.seg_leaves, c->n_segs + 1, kStLeaves)) return e;
+    if (int e = read_status(c)) return e;
+    if (int e = check_kernel_status(c)) return e;
+    c->n_leaves = c->h_status[kStLeaves];
+    PF_CUDA(c->leaves.ensure(size_t(c->n_leaves) * 16 + 16));
+    PF_CUDA(c->leaf_path.ensure(size_t(c->n_leaves) * 4 + 16));
+    b = make_batch(c);
+    PF_CUDA(launch_flatten(b, c->n_segs, true, st));
+    record(c, 2);
+
+    // 3. fill counts per tile, then fills written grouped by tile (counting sort)
+    const size_t T = c->n_tiles, K = c->n_cols;
+    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, (T + 2) * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.tile_delta, 0, T * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.col_above, 0, K * 4, st));
+    PF_CUDA(launch_bin(b, c->n_leaves, false, st));
+    if (int e = scan(c, b.tile_fills, (uint32_t)T + 1, kStFills)) return e;
+    if (int e = read_status(c)) return e;
+    if (int e = check_kernel_status(c)) return e;
+    c->n_fills = c->h_status[kStFills];
+    PF_CUDA(c->fills.ensure(size_t(c->n_fills) * 8 + 16));
+    b = make_batch(c);
+    PF_CUDA(launch_bin(b, c->n_leaves, true, st));
+    record(c, 3);
+
+    // 4. backdrops
+    PF_CUDA(launch_propagate(b, c->n_cols, st));
+    record(c, 4);
+    record(c, 5);
+    // 5. coverage + front-to-back composite with the z-cull walk
+    PF_CUDA(launch_composite(b, st));
+    record(c, 6);
+    return finish_frame(c, first, count, launches0, stats);
+}
+
+// The learned one-pass frame: per-path leaf regions and the fill capacity come from the
+// sizer's predictions, so leaf lines are produced once (flattened, stored and counted in the
+// same kernel) and the frame synchronises only after set-up.  If a path overruns its leaf
+// budget or the fills overrun the capacity, the frame is redone by the exact two-pass method
+// (the reference's own recovery, renderer.cpp:540-577, made exact).
+int render_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
+    if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights loaded");
+    if (int e = begin_frame(c, first, count)) return e;
+    const uint64_t launches0 = launches();
+    cudaStream_t st = c->stream;
+    record(c, 0);
+    if (int e = stage_setup(c, true)) return e;
+    // per-path regions, then a shared spill pool sized as a fraction of them
+    const uint64_t leaf_regions = c->h_status[kStLeafBudget];
+    const uint64_t leaf_pool = uint64_t(double(leaf_regions) * c->sz_pool) + 4096;
+    const uint64_t leaf_slots = leaf_regions + leaf_pool;
+    const uint64_t fill_cap = uint64_t(c->h_status[kStFillBudget]);
+    if (leaf_slots >= 0xffffffffull || fill_cap >= 0xffffffffull) return render_exact(c, first, count, stats);
+    PF_CUDA(c->leaves.ensure(leaf_slots * 16 + 16));
+    PF_CUDA(c->leaf_path.ensure(leaf_slots * 4 + 16));
+    PF_CUDA(c->fills.ensure(std::max<uint64_t>(fill_cap, 1) * 8 + 16));
+    record(c, 1);
+
+    const size_t T = c->n_tiles, K = c->n_cols;
+    Batch b = make_batch(c);
+    b.fill_cap = (uint32_t)std::min<uint64_t>(fill_cap, b.fill_cap);  // the predicted capacity is the limit
+    b.leaf_pool_first = (uint32_t)leaf_regions;
+    b.leaf_pool_cap = (uint32_t)leaf_pool;
+    PF_CUDA(launch_contour_segments(b, true, st));
+    PF_CUDA(launch_rows(b, true, st));
+    PF_CUDA(cudaMemsetAsync(b.leaf_path, 0xff, leaf_slots * 4, st));
+    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, (T + 2) * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.tile_delta, 0, T * 4, st));
+    PF_CUDA(cudaMemsetAsync(b.col_above, 0, K * 4, st));
+    PF_CUDA(launch_flatten_bin_count(b, c->n_segs, st));
+    record(c, 2);
+    if (int e = scan(c, b.tile_fills, (uint32_t)T + 1, kStFills)) return e;
+    // the leaf slots (with gaps) are what the fill pass walks
+    const uint32_t slots32 = (uint32_t)leaf_slots;
+    PF_CUDA(cudaMemcpyAsync(b.status + kStLeaves, &slots32, 4, cudaMemcpyHostToDevice, st));
+    PF_CUDA(launch_bin(b, slots32, true, st));
+    record(c, 3);
+    PF_CUDA(launch_propagate(b, c->n_cols, st));
+    record(c, 4);
+    record(c, 5);
+    PF_CUDA(launch_composite(b, st));
+    record(c, 6);
+    if (int e = read_status(c)) return e;
+    const uint32_t err = c->h_status[kStErr];
+    if (err & (kErrOverflowLeaf | kErrOverflowFill)) {
+        // a prediction was too small: redo the frame exactly
+        const int e = render_exact(c, first, count, stats);
+        if (stats) stats->overflow = 1;
+        return e;
+    }
+    c->n_leaves = c->h_status[kStLeafCount];
+    c->n_fills = c->h_status[kStFills];
+    c->last_paths_over = c->h_status[kStPathsOver];
+    c->last_pool_used = c->h_status[kStPoolUsed];
+    const int e = finish_frame(c, first, count, launches0, stats);
+    if (stats) {
+        stats->microlines = c->n_leaves;
+        stats->overflow = 0;
+    }
+    return e;
 }
 
 template <class T>
@@ -721,7 +835,10 @@ int pf_ctx_destroy(void *ctx) {
     if (!c) return PF_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    DevBuf *bufs[] = {&c->points, &c->pflags, &c->cstart, &c->pstart, &c->fill_rule, &c->color, &c->scenes,
+    DevBuf *bufs[] = {&c->sz_w, &c->sz_master, &c->sz_m, &c->sz_v, &c->sz_grad, &c->sz_loss, &c->sz_feat,
+                      &c->sz_target, &c->sz_index, &c->sz_pred, &c->path_feat, &c->path_pred, &c->path_leaf_first,
+                      &c->path_leaf_budget, &c->path_leaf_cursor, &c->path_fill_budget, &c->path_bounds,
+                      &c->points, &c->pflags, &c->cstart, &c->pstart, &c->fill_rule, &c->color, &c->scenes,
                       &c->scene_path_first, &c->scene_contour_first, &c->scene_fb_first, &c->contour_point_first,
                       &c->contour_path, &c->paths, &c->path_tiles, &c->path_cols, &c->contour_segs,
                       &c->path_contours, &c->segs, &c->seg_leaves, &c->leaves, &c->leaf_path, &c->tile_fills,
@@ -846,6 +963,301 @@ int pf_read_coverage(void *ctx, float *out, size_t capacity_floats, uint64_t *n_
     dt.release();
     dout.release();
     return PF_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Learned sizer: weights, training, prediction (see pf_sizer.cu).
+
+namespace {
+
+int sizer_alloc(Ctx *c) {
+    PF_CUDA(c->sz_w.ensure(kSizerParams * 2 + 16));
+    PF_CUDA(c->sz_master.ensure(kSizerParams * 4 + 16));
+    PF_CUDA(c->sz_m.ensure(kSizerParams * 4 + 16));
+    PF_CUDA(c->sz_v.ensure(kSizerParams * 4 + 16));
+    PF_CUDA(c->sz_grad.ensure(kSizerParams * 4 + 16));
+    PF_CUDA(c->sz_loss.ensure(16));
+    return PF_OK;
+}
+
+// fp32 master -> device (master, bf16 copy); Adam moments and gradient cleared
+int sizer_upload(Ctx *c, const float *params) {
+    if (int e = sizer_alloc(c)) return e;
+    std::vector<__nv_bfloat16> w(kSizerParams);
+    for (int i = 0; i < kSizerParams; i++) w[i] = __float2bfloat16_rn(params[i]);
+    PF_CUDA(cudaMemcpyAsync(c->sz_master.p, params, kSizerParams * 4, cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(cudaMemcpyAsync(c->sz_w.p, w.data(), kSizerParams * 2, cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(cudaMemsetAsync(c->sz_m.p, 0, kSizerParams * 4, c->stream));
+    PF_CUDA(cudaMemsetAsync(c->sz_v.p, 0, kSizerParams * 4, c->stream));
+    PF_CUDA(cudaMemsetAsync(c->sz_grad.p, 0, kSizerParams * 4, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    c->sz_step = 0;
+    c->sz_ready = true;
+    return PF_OK;
+}
+
+int upload_dataset(Ctx *c, const float *feat, const float *target, uint32_t n) {
+    PF_CUDA(c->sz_feat.ensure(size_t(n) * kSizerIn * 4 + 16));
+    PF_CUDA(c->sz_target.ensure(size_t(n) * kSizerOut * 4 + 16));
+    PF_CUDA(cudaMemcpyAsync(c->sz_feat.p, feat, size_t(n) * kSizerIn * 4, cudaMemcpyHostToDevice, c->stream));
+    if (target)
+        PF_CUDA(cudaMemcpyAsync(c->sz_target.p, target, size_t(n) * kSizerOut * 4, cudaMemcpyHostToDevice, c->stream));
+    return PF_OK;
+}
+
+struct SizerFileHeader {
+    char magic[4];     // "PFSZ"
+    uint32_t version;  // 1
+    uint32_t n_in, hidden, n_out, n_params;
+    uint32_t step;
+    float budget_mul, budget_add;
+    uint32_t reserved[7];
+};
+
+}  // namespace
+
+extern "C" {
+
+int pf_sizer_init(void *ctx, uint64_t seed) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    cudaSetDevice(c->device);
+    // He-uniform initialisation from a splitmix64 stream
+    std::vector<float> w(kSizerParams, 0.0f);
+    uint64_t z = seed;
+    auto next = [&]() {
+        z += 0x9E3779B97F4A7C15ull;
+        uint64_t x = z;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        x ^= x >> 31;
+        return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+    };
+    const int H = kSizerHidden, I = kSizerIn, O = kSizerOut;
+    const int oW1 = 0, oW2 = H * I + H, oW3 = oW2 + H * H + H;
+    for (int i = 0; i < H * I; i++) w[oW1 + i] = (float)((next() * 2 - 1) * std::sqrt(6.0 / I));
+    for (int i = 0; i < H * H; i++) w[oW2 + i] = (float)((next() * 2 - 1) * std::sqrt(6.0 / H));
+    for (int i = 0; i < O * H; i++) w[oW3 + i] = (float)((next() * 2 - 1) * std::sqrt(3.0 / H));
+    return sizer_upload(c, w.data());
+}
+
+int pf_sizer_param_count(void) { return kSizerParams; }
+
+int pf_sizer_set_params(void *ctx, const float *params, size_t n) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !params || n != (size_t)kSizerParams) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad sizer parameters");
+    cudaSetDevice(c->device);
+    return sizer_upload(c, params);
+}
+
+int pf_sizer_get_params(void *ctx, float *params, size_t n) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !params || n != (size_t)kSizerParams) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad sizer parameters");
+    if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights");
+    PF_CUDA(cudaMemcpyAsync(params, c->sz_master.p, kSizerParams * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+int pf_sizer_set_margin(void *ctx, float mul, float add, float pool) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !(mul > 0.0f) || !(add >= 0.0f) || !(pool >= 0.0f)) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad margin");
+    c->sz_mul = mul;
+    c->sz_add = add;
+    c->sz_pool = pool;
+    return PF_OK;
+}
+
+// Budget statistics of the last learned frame: paths that overran their leaf budget and
+// leaf slots taken from the spill pool.
+int pf_sizer_last_frame(void *ctx, uint32_t *paths_over, uint32_t *pool_used) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !paths_over || !pool_used) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    *paths_over = c->last_paths_over;
+    *pool_used = c->last_pool_used;
+    return PF_OK;
+}
+
+int pf_sizer_predict(void *ctx, const float *feat, uint32_t n, float *out) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || (n && (!feat || !out))) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights");
+    cudaSetDevice(c->device);
+    if (int e = upload_dataset(c, feat, nullptr, n)) return e;
+    PF_CUDA(c->sz_pred.ensure(size_t(n) * kSizerOut * 4 + 16));
+    PF_CUDA(launch_mlp_predict(c->sz_w.as<__nv_bfloat16>(), c->sz_feat.as<float>(), n, c->sz_pred.as<float>(),
+                               c->stream));
+    PF_CUDA(cudaMemcpyAsync(out, c->sz_pred.p, size_t(n) * kSizerOut * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+// Gradient of the mean squared error over (feat, target) at the current weights (bf16
+// forward, fp32 accumulation), without updating them.  grad: kSizerParams floats.
+int pf_sizer_gradient(void *ctx, const float *feat, const float *target, uint32_t n, float *grad, float *loss) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !feat || !target || !grad || n == 0) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights");
+    cudaSetDevice(c->device);
+    if (int e = upload_dataset(c, feat, target, n)) return e;
+    PF_CUDA(cudaMemsetAsync(c->sz_grad.p, 0, kSizerParams * 4, c->stream));
+    PF_CUDA(cudaMemsetAsync(c->sz_loss.p, 0, 4, c->stream));
+    PF_CUDA(launch_mlp_grad(c->sz_w.as<__nv_bfloat16>(), c->sz_feat.as<float>(), c->sz_target.as<float>(), nullptr,
+                            n, c->sz_grad.as<float>(), c->sz_loss.as<float>(), c->stream));
+    PF_CUDA(cudaMemcpyAsync(grad, c->sz_grad.p, kSizerParams * 4, cudaMemcpyDeviceToHost, c->stream));
+    float l = 0.0f;
+    PF_CUDA(cudaMemcpyAsync(&l, c->sz_loss.p, 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaMemsetAsync(c->sz_grad.p, 0, kSizerParams * 4, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    if (loss) *loss = l / (float)(size_t(n) * kSizerOut);
+    return PF_OK;
+}
+
+// Adam training on the GPU: `epochs` passes over (feat, target) in shuffled mini-batches.
+// losses (optional): mean squared error of every epoch.
+int pf_sizer_train(void *ctx, const float *feat, const float *target, uint32_t n, uint32_t epochs, uint32_t batch,
+                   float lr, uint64_t seed, float *losses) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !feat || !target || n == 0 || batch == 0) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights");
+    cudaSetDevice(c->device);
+    if (int e = upload_dataset(c, feat, target, n)) return e;
+    PF_CUDA(c->sz_index.ensure(size_t(n) * 4 + 16));
+    std::vector<uint32_t> perm(n);
+    for (uint32_t i = 0; i < n; i++) perm[i] = i;
+    uint64_t z = seed ^ 0x5DEECE66Dull;
+    for (uint32_t ep = 0; ep < epochs; ep++) {
+        for (uint32_t i = n - 1; i > 0; i--) {  // Fisher-Yates with splitmix64
+            z += 0x9E3779B97F4A7C15ull;
+            uint64_t x = z;
+            x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+            x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+            x ^= x >> 31;
+            std::swap(perm[i], perm[x % (i + 1)]);
+        }
+        PF_CUDA(cudaMemcpyAsync(c->sz_index.p, perm.data(), size_t(n) * 4, cudaMemcpyHostToDevice, c->stream));
+        PF_CUDA(cudaMemsetAsync(c->sz_loss.p, 0, 4, c->stream));
+        for (uint32_t off = 0; off < n; off += batch) {
+            const uint32_t m = std::min(batch, n - off);
+            PF_CUDA(launch_mlp_grad(c->sz_w.as<__nv_bfloat16>(), c->sz_feat.as<float>(), c->sz_target.as<float>(),
+                                    c->sz_index.as<uint32_t>() + off, m, c->sz_grad.as<float>(),
+                                    c->sz_loss.as<float>(), c->stream));
+            PF_CUDA(launch_adam(c->sz_master.as<float>(), c->sz_w.as<__nv_bfloat16>(), c->sz_grad.as<float>(),
+                                c->sz_m.as<float>(), c->sz_v.as<float>(), lr, ++c->sz_step, c->stream));
+        }
+        if (losses) {
+            float l = 0.0f;
+            PF_CUDA(cudaMemcpyAsync(&l, c->sz_loss.p, 4, cudaMemcpyDeviceToHost, c->stream));
+            PF_CUDA(cudaStreamSynchronize(c->stream));
+            losses[ep] = l / (float)(size_t(n) * kSizerOut);
+        }
+    }
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+int pf_sizer_save(void *ctx, const char *path) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !path) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights");
+    std::vector<float> w(kSizerParams), m(kSizerParams), v(kSizerParams);
+    PF_CUDA(cudaMemcpyAsync(w.data(), c->sz_master.p, kSizerParams * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaMemcpyAsync(m.data(), c->sz_m.p, kSizerParams * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaMemcpyAsync(v.data(), c->sz_v.p, kSizerParams * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    SizerFileHeader h{};
+    std::memcpy(h.magic, "PFSZ", 4);
+    h.version = 1;
+    h.n_in = kSizerIn;
+    h.hidden = kSizerHidden;
+    h.n_out = kSizerOut;
+    h.n_params = kSizerParams;
+    h.step = (uint32_t)c->sz_step;
+    h.budget_mul = c->sz_mul;
+    h.budget_add = c->sz_add;
+    FILE *f = std::fopen(path, "wb");
+    if (!f) return fail(c, PF_ERR_INVALID_ARGUMENT, std::string("cannot write ") + path);
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(w.data(), 4, w.size(), f) == w.size() &&
+              std::fwrite(m.data(), 4, m.size(), f) == m.size() && std::fwrite(v.data(), 4, v.size(), f) == v.size();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? PF_OK : fail(c, PF_ERR_INVALID_ARGUMENT, std::string("short write to ") + path);
+}
+
+int pf_sizer_load(void *ctx, const char *path) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !path) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    cudaSetDevice(c->device);
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return fail(c, PF_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);
+    SizerFileHeader h{};
+    std::vector<float> w(kSizerParams), m(kSizerParams), v(kSizerParams);
+    bool ok = std::fread(&h, sizeof h, 1, f) == 1 && std::memcmp(h.magic, "PFSZ", 4) == 0 && h.version == 1 &&
+              h.n_in == (uint32_t)kSizerIn && h.hidden == (uint32_t)kSizerHidden && h.n_out == (uint32_t)kSizerOut &&
+              h.n_params == (uint32_t)kSizerParams && std::fread(w.data(), 4, w.size(), f) == w.size() &&
+              std::fread(m.data(), 4, m.size(), f) == m.size() && std::fread(v.data(), 4, v.size(), f) == v.size();
+    std::fclose(f);
+    if (!ok) return fail(c, PF_ERR_INVALID_ARGUMENT, std::string("not a sizer weight file: ") + path);
+    if (int e = sizer_upload(c, w.data())) return e;
+    PF_CUDA(cudaMemcpyAsync(c->sz_m.p, m.data(), kSizerParams * 4, cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(cudaMemcpyAsync(c->sz_v.p, v.data(), kSizerParams * 4, cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    c->sz_step = (int)h.step;
+    if (h.budget_mul > 0.0f) c->sz_mul = h.budget_mul;
+    if (h.budget_add >= 0.0f) c->sz_add = h.budget_add;
+    return PF_OK;
+}
+
+// Per-path features of the last frame (n_paths x 12 floats).
+int pf_path_features(void *ctx, float *out, size_t capacity_floats) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !out) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
+    const size_t n = c->r_paths;
+    if (capacity_floats < n * kSizerIn) return fail(c, PF_ERR_INVALID_ARGUMENT, "buffer too small");
+    PF_CUDA(c->path_feat.ensure(n * kSizerIn * 4 + 16));
+    Batch b = make_batch(c);
+    PF_CUDA(launch_features(b, c->path_contours.as<uint2>(), c->path_feat.as<float>(), c->stream));
+    PF_CUDA(cudaMemcpyAsync(out, c->path_feat.p, n * kSizerIn * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+// Exact per-path leaf-line and fill counts of the last exact frame (training labels).
+int pf_path_counts(void *ctx, uint32_t *leaves, uint32_t *fills, size_t capacity) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !leaves || !fills) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
+    const size_t n = c->r_paths;
+    if (capacity < n) return fail(c, PF_ERR_INVALID_ARGUMENT, "buffer too small");
+    DevBuf dl, df;
+    PF_CUDA(dl.ensure(n * 4 + 16));
+    PF_CUDA(df.ensure(n * 4 + 16));
+    Batch b = make_batch(c);
+    PF_CUDA(launch_path_counts(b, c->path_contours.as<uint2>(), dl.as<uint32_t>(), df.as<uint32_t>(), c->stream));
+    PF_CUDA(cudaMemcpyAsync(leaves, dl.p, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaMemcpyAsync(fills, df.p, n * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    dl.release();
+    df.release();
+    return PF_OK;
+}
+
+// The frame's status words (error bits, totals, counters; 16 x u32) of the last frame.
+int pf_debug_counters(void *ctx, uint32_t *out, size_t n) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !out) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (int e = read_status(c)) return e;
+    for (size_t i = 0; i < n && i < (size_t)kStCount; i++) out[i] = c->h_status[i];
+    return PF_OK;
+}
+
+int pf_render_learned(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    cudaSetDevice(c->device);
+    return render_learned(c, first_scene, n_scenes, stats);
 }
 
 }  // extern "C"

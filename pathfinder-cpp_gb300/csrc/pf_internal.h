@@ -93,6 +93,12 @@ struct Batch {
     uint32_t *contour_point_first;       // [n_contours + 1] global
     uint32_t *contour_path;              // [n_contours]
     PathDev *paths;                      // [n_paths]
+    float4 *path_bounds;                 // [n_paths] outline bounds (min x, min y, max x, max y)
+    // learned frame: per-path leaf regions laid out from the sizer's budgets
+    uint32_t *path_leaf_first;           // [n_paths + 1] budgets -> scanned
+    uint32_t *path_leaf_budget;          // [n_paths]
+    uint32_t *path_leaf_cursor;          // [n_paths]
+    uint32_t leaf_pool_first, leaf_pool_cap;  // shared spill pool after the per-path regions
     uint32_t *path_tiles;                // [n_paths + 1] -> scanned to first tile
     uint32_t *path_cols;                 // [n_paths + 1] -> scanned to first column
     uint32_t *contour_segs;              // [n_contours + 1] -> scanned
@@ -147,6 +153,12 @@ enum : int {
     kStListFills = 7,  // fills of the alpha tiles that made it into composite lists
     kStRows = 8,       // entries of the per-row path lists
     kStEntries = 9,    // composite entries (visible tiles at or above the occluder)
+    kStLeafBudget = 10,// learned frame: sum of per-path leaf budgets
+    kStFillBudget = 11,// learned frame: sum of per-path fill estimates
+    kStLeafCount = 12, // learned frame: leaf lines produced (kept or not)
+    kStPoolUsed = 13,  // learned frame: leaf slots taken from the spill pool
+    kStPathsOver = 14, // learned frame: paths that overran their leaf budget
+    kStWalkChunks = 15,// composite: 32-candidate chunks walked (all framebuffer tiles)
     kStCount = 16,
 };
 
@@ -173,8 +185,12 @@ cudaError_t launch_list_dump(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t n, float *out, cudaStream_t st);
 
 // Learned sizer (pf_sizer.cu).
-cudaError_t launch_features(const Batch &b, const uint2 *path_contours, const float4 *bounds, float *feat,
-                            cudaStream_t st);
+cudaError_t launch_features(const Batch &b, const uint2 *path_contours, float *feat, cudaStream_t st);
+cudaError_t launch_budgets(const Batch &b, const float *pred, float mul, float add, uint32_t *leaf_budget,
+                           uint32_t *fill_budget, cudaStream_t st);
+cudaError_t launch_path_counts(const Batch &b, const uint2 *path_contours, uint32_t *leaves, uint32_t *fills,
+                               cudaStream_t st);
+cudaError_t launch_flatten_bin_count(const Batch &b, uint32_t n_segs, cudaStream_t st);
 cudaError_t launch_mlp_predict(const __nv_bfloat16 *w, const float *feat, uint32_t n, float *out, cudaStream_t st);
 cudaError_t launch_mlp_grad(const __nv_bfloat16 *w, const float *feat, const float *target, const uint32_t *index,
                             uint32_t n, float *grad, float *loss, cudaStream_t st);

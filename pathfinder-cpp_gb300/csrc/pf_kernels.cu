@@ -131,6 +131,7 @@ __global__ void k_path_setup(Batch b, const uint2 *path_contours) {
         ir = S.vb_right < r ? S.vb_right : r;
         ib = S.vb_bottom < bt ? S.vb_bottom : bt;
     }
+    b.path_bounds[p] = make_float4(l, t, r, bt);
     const float inv = 1.0f / kTile;
     P.rx0 = (int32_t)floorf(fmul(il, inv));
     P.ry0 = (int32_t)floorf(fmul(it, inv));
@@ -245,55 +246,90 @@ __device__ __forceinline__ bool flat_quad(const float bb[4], const float cc[2]) 
 
 __device__ __forceinline__ float half_lerp(float a, float b) { return fadd(a, fmul(0.5f, fsub(b, a))); }
 
-template <class Emit>
-__device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, float c1, float c2, float c3,
-                              Emit &&emit, uint32_t *status) {
-    float stk[kMaxDepth][8];
-    int dstk[kMaxDepth];
-    int sp = 0;
-    float bb[4] = {b0, b1, b2, b3}, cc[4] = {c0, c1, c2, c3};
-    int depth = 0;
-    for (;;) {
-        if (depth >= kMaxDepth - 1 || flat_cubic(bb, cc)) {
-            if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
-            emit(bb[0], bb[1], bb[2], bb[3]);
-            if (sp == 0) return;
-            sp--;
+// One de Casteljau half split (segment.cpp:62-95), keeping the first (right == false) or the
+// second half.
+__device__ __forceinline__ void split_cubic_half(float bb[4], float cc[4], bool right) {
+    float p01[2], p12[2], p23[2], p012[2], p123[2], p0123[2];
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                bb[k] = stk[sp][k];
-                cc[k] = stk[sp][4 + k];
-            }
-            depth = dstk[sp];
-            continue;
-        }
-        float p01[2], p12[2], p23[2], p012[2], p123[2], p0123[2];
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            p01[k] = half_lerp(bb[k], cc[k]);
-            p12[k] = half_lerp(cc[k], cc[2 + k]);
-            p23[k] = half_lerp(cc[2 + k], bb[2 + k]);
-            p012[k] = half_lerp(p01[k], p12[k]);
-            p123[k] = half_lerp(p12[k], p23[k]);
-            p0123[k] = half_lerp(p012[k], p123[k]);
-        }
-        // push the second half, continue with the first
-        stk[sp][0] = p0123[0];
-        stk[sp][1] = p0123[1];
-        stk[sp][2] = bb[2];
-        stk[sp][3] = bb[3];
-        stk[sp][4] = p123[0];
-        stk[sp][5] = p123[1];
-        stk[sp][6] = p23[0];
-        stk[sp][7] = p23[1];
-        dstk[sp] = depth + 1;
-        sp++;
+    for (int k = 0; k < 2; k++) {
+        p01[k] = half_lerp(bb[k], cc[k]);
+        p12[k] = half_lerp(cc[k], cc[2 + k]);
+        p23[k] = half_lerp(cc[2 + k], bb[2 + k]);
+        p012[k] = half_lerp(p01[k], p12[k]);
+        p123[k] = half_lerp(p12[k], p23[k]);
+        p0123[k] = half_lerp(p012[k], p123[k]);
+    }
+    if (!right) {
         bb[2] = p0123[0];
         bb[3] = p0123[1];
         cc[0] = p01[0];
         cc[1] = p01[1];
         cc[2] = p012[0];
         cc[3] = p012[1];
+    } else {
+        bb[0] = p0123[0];
+        bb[1] = p0123[1];
+        cc[0] = p123[0];
+        cc[1] = p123[1];
+        cc[2] = p23[0];
+        cc[3] = p23[1];
+    }
+}
+
+__device__ __forceinline__ void split_quad_half(float bb[4], float cc[2], bool right) {
+    float a[2], q[2], m[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        a[k] = fadd(bb[k], fmul(fsub(cc[k], bb[k]), 0.5f));
+        q[k] = fadd(cc[k], fmul(fsub(bb[2 + k], cc[k]), 0.5f));
+        m[k] = fadd(a[k], fmul(fsub(q[k], a[k]), 0.5f));
+    }
+    if (!right) {
+        bb[2] = m[0];
+        bb[3] = m[1];
+        cc[0] = a[0];
+        cc[1] = a[1];
+    } else {
+        bb[0] = m[0];
+        bb[1] = m[1];
+        cc[0] = q[0];
+        cc[1] = q[1];
+    }
+}
+
+// Depth-first traversal of the bisection tree without a stack: the current node is kept in
+// registers with its path from the root (one bit per level, 1 = second half).  Descending
+// splits the current node; moving to the next sibling re-derives that node from the root by
+// the same sequence of splits, so every node is bit-identical to the recursive algorithm's.
+template <class Emit>
+__device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, float c1, float c2, float c3,
+                              Emit &&emit, uint32_t *status) {
+    float bb[4] = {b0, b1, b2, b3}, cc[4] = {c0, c1, c2, c3};
+    uint32_t bits = 0;
+    int depth = 0;
+    for (;;) {
+        if (depth >= kMaxDepth - 1 || flat_cubic(bb, cc)) {
+            if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
+            emit(bb[0], bb[1], bb[2], bb[3]);
+            while (depth > 0 && (bits & 1u)) {
+                bits >>= 1;
+                depth--;
+            }
+            if (depth == 0) return;
+            bits |= 1u;
+            bb[0] = b0;
+            bb[1] = b1;
+            bb[2] = b2;
+            bb[3] = b3;
+            cc[0] = c0;
+            cc[1] = c1;
+            cc[2] = c2;
+            cc[3] = c3;
+            for (int l = depth - 1; l >= 0; l--) split_cubic_half(bb, cc, (bits >> l) & 1u);
+            continue;
+        }
+        split_cubic_half(bb, cc, false);
+        bits <<= 1;
         depth++;
     }
 }
@@ -301,43 +337,30 @@ __device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, 
 template <class Emit>
 __device__ void flatten_quad(float b0, float b1, float b2, float b3, float c0, float c1, Emit &&emit,
                              uint32_t *status) {
-    float stk[kMaxDepth][6];
-    int dstk[kMaxDepth];
-    int sp = 0;
     float bb[4] = {b0, b1, b2, b3}, cc[2] = {c0, c1};
+    uint32_t bits = 0;
     int depth = 0;
     for (;;) {
         if (depth >= kMaxDepth - 1 || flat_quad(bb, cc)) {
             if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
             emit(bb[0], bb[1], bb[2], bb[3]);
-            if (sp == 0) return;
-            sp--;
-#pragma unroll
-            for (int k = 0; k < 4; k++) bb[k] = stk[sp][k];
-            cc[0] = stk[sp][4];
-            cc[1] = stk[sp][5];
-            depth = dstk[sp];
+            while (depth > 0 && (bits & 1u)) {
+                bits >>= 1;
+                depth--;
+            }
+            if (depth == 0) return;
+            bits |= 1u;
+            bb[0] = b0;
+            bb[1] = b1;
+            bb[2] = b2;
+            bb[3] = b3;
+            cc[0] = c0;
+            cc[1] = c1;
+            for (int l = depth - 1; l >= 0; l--) split_quad_half(bb, cc, (bits >> l) & 1u);
             continue;
         }
-        float a[2], q[2], m[2];
-#pragma unroll
-        for (int k = 0; k < 2; k++) {
-            a[k] = fadd(bb[k], fmul(fsub(cc[k], bb[k]), 0.5f));
-            q[k] = fadd(cc[k], fmul(fsub(bb[2 + k], cc[k]), 0.5f));
-            m[k] = fadd(a[k], fmul(fsub(q[k], a[k]), 0.5f));
-        }
-        stk[sp][0] = m[0];
-        stk[sp][1] = m[1];
-        stk[sp][2] = bb[2];
-        stk[sp][3] = bb[3];
-        stk[sp][4] = q[0];
-        stk[sp][5] = q[1];
-        dstk[sp] = depth + 1;
-        sp++;
-        bb[2] = m[0];
-        bb[3] = m[1];
-        cc[0] = a[0];
-        cc[1] = a[1];
+        split_quad_half(bb, cc, false);
+        bits <<= 1;
         depth++;
     }
 }
@@ -531,6 +554,7 @@ __global__ void __launch_bounds__(kThreads) k_bin(Batch b, uint32_t n_leaves) {
         return;
     }
     const uint32_t p = b.leaf_path[i];
+    if (p == kNone) return;  // unused slot of a learned frame's leaf region
     const float4 L = b.leaves[i];
     const PathDev P = b.paths[p];
     const SceneDev &S = b.scenes[P.scene];
@@ -559,6 +583,93 @@ __global__ void __launch_bounds__(kThreads) k_bin(Batch b, uint32_t n_leaves) {
             },
             &b.status[kStErr]);
     }
+}
+
+// Learned frame: flatten one segment, store each leaf line in its path's leaf region (laid out
+// from the sizer's budget; slots are reserved eight at a time) and walk it at once for the
+// fill and backdrop counts.  Counts stay exact even when a path overruns its budget (the
+// overflow bit then sends the frame to the exact two-pass method).
+constexpr int kLeafBatch = 8;
+
+__global__ void __launch_bounds__(kThreads) k_flatten_bin_count(Batch b, uint32_t n_segs) {
+    const uint32_t i = global_tid();
+    if (i >= n_segs || i >= b.status[kStSegs]) return;
+    const SegDev sg = b.segs[i];
+    const PathDev P = b.paths[sg.path];
+    const SceneDev &S = b.scenes[P.scene];
+    WalkCtx w;
+    w.rx0 = P.rx0;
+    w.ry0 = P.ry0;
+    w.rx1 = P.rx1;
+    w.ry1 = P.ry1;
+    w.rw = max(P.rx1 - P.rx0, 0);
+    w.rh = max(P.ry1 - P.ry0, 0);
+    w.vb_right = S.vb_right;
+    w.vb_bottom = S.vb_bottom;
+    const uint32_t tb = P.tile_first, cb = P.col_first;
+    const uint32_t region = b.path_leaf_first[sg.path], budget = b.path_leaf_budget[sg.path];
+    float4 pend[kLeafBatch];
+    int npend = 0;
+    uint32_t produced = 0;
+    auto flush = [&]() {
+        if (!npend) return;
+        const uint32_t slot = atomicAdd(&b.path_leaf_cursor[sg.path], (uint32_t)npend);
+        const uint32_t in_region = slot >= budget ? 0u : min((uint32_t)npend, budget - slot);
+        for (uint32_t k = 0; k < in_region; k++) {
+            b.leaves[region + slot + k] = pend[k];
+            b.leaf_path[region + slot + k] = sg.path;
+        }
+        if (in_region < (uint32_t)npend) {
+            // the path overran its budget: spill into the shared pool
+            const uint32_t extra = (uint32_t)npend - in_region;
+            if (slot <= budget && slot + npend > budget) atomicAdd(&b.status[kStPathsOver], 1u);
+            const uint32_t q = atomicAdd(&b.status[kStPoolUsed], extra);
+            for (uint32_t k = 0; k < extra; k++) {
+                if (q + k < b.leaf_pool_cap) {
+                    b.leaves[b.leaf_pool_first + q + k] = pend[in_region + k];
+                    b.leaf_path[b.leaf_pool_first + q + k] = sg.path;
+                } else {
+                    atomicOr(&b.status[kStErr], kErrOverflowLeaf);
+                }
+            }
+        }
+        npend = 0;
+    };
+    auto emit = [&](float x0, float y0, float x1, float y1) {
+        pend[npend++] = make_float4(x0, y0, x1, y1);
+        if (npend == kLeafBatch) flush();
+        produced++;
+        walk_line(
+            w, x0, y0, x1, y1, [&](int32_t local, uint2) { atomicAdd(&b.tile_fills[tb + (uint32_t)local], 1u); },
+            [&](int32_t where, int d) {
+                if (where >= 0) atomicAdd(&b.tile_delta[tb + (uint32_t)where], d);
+                else atomicAdd(&b.col_above[cb + (uint32_t)(-1 - where)], d);
+            },
+            &b.status[kStErr]);
+    };
+    const float2 p0 = b.points[sg.a];
+    switch (sg.kind) {
+        case kSegLine: {
+            const float2 p1 = b.points[sg.a + 1];
+            emit(p0.x, p0.y, p1.x, p1.y);
+        } break;
+        case kSegClose: {
+            const float2 p1 = b.points[sg.b];
+            emit(p0.x, p0.y, p1.x, p1.y);
+        } break;
+        case kSegQuad: {
+            const float2 c = b.points[sg.a + 1], p2 = b.points[sg.a + 2];
+            flatten_quad(p0.x, p0.y, p2.x, p2.y, c.x, c.y, emit, &b.status[kStErr]);
+        } break;
+        default: {
+            const float2 c0 = b.points[sg.a + 1], c1 = b.points[sg.a + 2], p3 = b.points[sg.a + 3];
+            flatten_cubic(p0.x, p0.y, p3.x, p3.y, c0.x, c0.y, c1.x, c1.y, emit, &b.status[kStErr]);
+        } break;
+    }
+    flush();
+    const unsigned active = __activemask();
+    const uint32_t total = __reduce_add_sync(active, produced);
+    if ((int)(threadIdx.x & 31) == __ffs(active) - 1) atomicAdd(&b.status[kStLeafCount], total);
 }
 
 // ---------------------------------------------------------------------------
@@ -742,10 +853,12 @@ constexpr int kCompWarps = 4;
 // framebuffer tile's composite list after z-culling (sort.comp:49-83), in reverse order.
 // visit(p, gt, state) returns true to stop the walk.
 template <class Visit>
-__device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint32_t fx, uint32_t fy, Visit &&visit) {
+__device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint32_t fx, uint32_t fy, Visit &&visit,
+                                             uint32_t &chunks) {
     const int lane = threadIdx.x & 31;
     const uint32_t k_lo = b.row_first[row], k_hi = b.row_first[row + 1];
     for (uint32_t top = k_hi; top > k_lo; top = top > k_lo + 32 ? top - 32 : k_lo) {
+        chunks++;
         const int64_t k = (int64_t)top - 1 - lane;
         uint4 e = make_uint4(0, 0, 0, 0);
         uint32_t gt = 0, st = 0;
@@ -780,7 +893,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
     const int col = lane & 15, h = lane >> 4;
     const float inv255 = 1.0f / 255.0f;
     const uint32_t n_warps = gridDim.x * kCompWarps;
-    uint32_t entries = 0, comp_fills = 0;
+    uint32_t entries = 0, comp_fills = 0, chunks = 0;
     for (uint32_t fb = blockIdx.x * kCompWarps + warp; fb < b.n_fb; fb += n_warps) {
         const uint32_t fbg = b.fb_base + fb;
         const uint32_t s = upper_bound(b.scene_fb_first, b.n_scenes_all + 1, fbg) - 1;
@@ -828,7 +941,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
                 opaque &= tr[k] == 0.0f;
             }
             return stop || __all_sync(0xffffffffu, opaque);
-        });
+        }, chunks);
         const uint32_t px = fx * 16 + (uint32_t)col;
         if (px < S.img_w) {
             const float cr = (float)(S.clear & 0xffu) * inv255, cg = (float)((S.clear >> 8) & 0xffu) * inv255,
@@ -851,6 +964,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
         atomicAdd(&b.status[kStEntries], entries);
         atomicAdd(&b.status[kStListFills], comp_fills);
     }
+    if (lane == 0 && chunks) atomicAdd(&b.status[kStWalkChunks], chunks);
 }
 
 // Composite lists and z per framebuffer tile for the canonical output (not part of a frame):
@@ -865,7 +979,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_list_dump(Batch b) {
     const SceneDev &S = b.scenes[s];
     const uint32_t local = fbg - S.fb_first;
     const uint32_t fx = local % S.fbw, fy = local / S.fbw;
-    uint32_t n = 0, first = 0, count = 0;
+    uint32_t n = 0, first = 0, count = 0, n_chunks = 0;
     int32_t z = -1;
     if (kWrite) {
         first = b.fb_count[fb];
@@ -881,7 +995,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_list_dump(Batch b) {
             return true;
         }
         return false;
-    });
+    }, n_chunks);
     if (lane == 0) {
         if (kWrite) b.z[fb] = z;
         else b.fb_count[fb] = n;
@@ -956,6 +1070,11 @@ cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream
     if (!n_leaves) return cudaSuccess;
     if (write) PF_LAUNCH(k_bin<true><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves));
     else PF_LAUNCH(k_bin<false><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flatten_bin_count(const Batch &b, uint32_t n_segs, cudaStream_t st) {
+    if (n_segs) PF_LAUNCH(k_flatten_bin_count<<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
     return cudaGetLastError();
 }
 

@@ -32,48 +32,51 @@ __device__ __forceinline__ float turn(float2 a, float2 b, float2 c) {
     return fabsf(atan2f(cr, dt));
 }
 
-// One warp per path: features from the path's segments (after k_contour_segments<write>)
-// and its bounds / tile rect (after k_path_setup).
-__global__ void k_features(Batch b, const uint2 *path_contours, const float4 *bounds, float *feat) {
+// One warp per path: features from the path's points and point flags (they do not need the
+// segment records, so they are ready before the first host synchronisation of a frame) and
+// its bounds / tile rect (after k_path_setup):
+//   0 segments   1 lines   2 quadratics   3 cubics   4 contours   5 box width   6 box height
+//   7 box area   8 control-polygon length   9 summed turning angle   10 tiles in the rect
+//   11 even-odd flag
+// (log1p of every count / length; the reference's outlines are already in canvas space, so
+// the transform-scale feature is replaced by the tile count of the clipped rect).
+__global__ void k_features(Batch b, const uint2 *path_contours, float *feat) {
     const uint32_t p = global_tid() >> 5;
     const int lane = threadIdx.x & 31;
     if (p >= b.n_paths) return;
     const uint2 cr = path_contours[p];
-    const uint32_t s0 = b.contour_segs[cr.x], s1 = b.contour_segs[cr.y];
-    float n_line = 0, n_quad = 0, n_cubic = 0, length = 0, turning = 0;
-    for (uint32_t i = s0 + lane; i < s1; i += 32) {
-        const SegDev sg = b.segs[i];
-        const float2 p0 = b.points[sg.a];
-        if (sg.kind == kSegLine || sg.kind == kSegClose) {
-            n_line += 1;
-            length += leg_len(p0, b.points[sg.kind == kSegClose ? sg.b : sg.a + 1]);
-        } else if (sg.kind == kSegQuad) {
-            n_quad += 1;
-            const float2 c = b.points[sg.a + 1], p2 = b.points[sg.a + 2];
-            length += leg_len(p0, c) + leg_len(c, p2);
-            turning += turn(p0, c, p2);
-        } else {
-            n_cubic += 1;
-            const float2 c0 = b.points[sg.a + 1], c1 = b.points[sg.a + 2], p3 = b.points[sg.a + 3];
-            length += leg_len(p0, c0) + leg_len(c0, c1) + leg_len(c1, p3);
-            turning += turn(p0, c0, c1) + turn(c0, c1, p3);
+    float n_on = 0, n_c0 = 0, n_c1 = 0, length = 0, turning = 0;
+    for (uint32_t c = cr.x; c < cr.y; c++) {
+        const uint32_t a = b.contour_point_first[c], e = b.contour_point_first[c + 1], n = e - a;
+        for (uint32_t i = lane; i < n; i += 32) {
+            const uint8_t f = b.flags[a + i];
+            n_on += f == 0;
+            n_c0 += f == 1;
+            n_c1 += f == 2;
+            if (n > 1) {
+                const float2 q0 = b.points[a + (i == 0 ? n - 1 : i - 1)], q1 = b.points[a + i],
+                             q2 = b.points[a + (i + 1 == n ? 0 : i + 1)];
+                length += leg_len(q1, q2);
+                turning += turn(q0, q1, q2);
+            }
         }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
-        n_line += __shfl_xor_sync(0xffffffffu, n_line, d);
-        n_quad += __shfl_xor_sync(0xffffffffu, n_quad, d);
-        n_cubic += __shfl_xor_sync(0xffffffffu, n_cubic, d);
+        n_on += __shfl_xor_sync(0xffffffffu, n_on, d);
+        n_c0 += __shfl_xor_sync(0xffffffffu, n_c0, d);
+        n_c1 += __shfl_xor_sync(0xffffffffu, n_c1, d);
         length += __shfl_xor_sync(0xffffffffu, length, d);
         turning += __shfl_xor_sync(0xffffffffu, turning, d);
     }
     if (lane != 0) return;
-    const float4 bb = bounds[p];
+    const float4 bb = b.path_bounds[p];
     const float w = fmaxf(bb.z - bb.x, 0.0f), h = fmaxf(bb.w - bb.y, 0.0f);
     const PathDev P = b.paths[p];
     const float tiles = (float)max(P.rx1 - P.rx0, 0) * (float)max(P.ry1 - P.ry0, 0);
+    const float n_cubic = n_c1, n_quad = fmaxf(n_c0 - n_c1, 0.0f), n_line = fmaxf(n_on - n_c0, 0.0f);
     float *f = feat + (size_t)p * kSizerIn;
-    f[0] = log1pf(n_line + n_quad + n_cubic);
+    f[0] = log1pf(n_on);
     f[1] = log1pf(n_line);
     f[2] = log1pf(n_quad);
     f[3] = log1pf(n_cubic);
@@ -85,6 +88,29 @@ __global__ void k_features(Batch b, const uint2 *path_contours, const float4 *bo
     f[9] = log1pf(turning);
     f[10] = log1pf(tiles);
     f[11] = (P.flags & 1u) ? 1.0f : 0.0f;
+}
+
+// Per-path leaf budget (and fill estimate) from the sizer's prediction:
+// budget = ceil(expm1(prediction) * mul + add).
+__global__ void k_budgets(Batch b, const float *pred, float mul, float add, uint32_t *leaf_budget,
+                          uint32_t *fill_budget) {
+    const uint32_t p = global_tid();
+    if (p >= b.n_paths) return;
+    const float l = fmaxf(expm1f(fminf(pred[2 * p + 0], 30.0f)), 0.0f);
+    const float f = fmaxf(expm1f(fminf(pred[2 * p + 1], 30.0f)), 0.0f);
+    leaf_budget[p] = (uint32_t)fminf(ceilf(l * mul + add), 1.0e9f);
+    fill_budget[p] = (uint32_t)fminf(ceilf(f * mul + add), 1.0e9f);
+}
+
+// Exact per-path counts of the last exact frame (training labels): leaf lines and fills.
+__global__ void k_path_counts(Batch b, const uint2 *path_contours, uint32_t *leaves, uint32_t *fills) {
+    const uint32_t p = global_tid();
+    if (p >= b.n_paths) return;
+    const uint2 cr = path_contours[p];
+    const uint32_t s0 = b.contour_segs[cr.x], s1 = b.contour_segs[cr.y];
+    leaves[p] = b.seg_leaves[s1] - b.seg_leaves[s0];
+    const uint32_t t0 = b.path_tiles[p], t1 = b.path_tiles[p + 1];
+    fills[p] = b.tile_fills[(int64_t)t1 - 1] - b.tile_fills[(int64_t)t0 - 1];
 }
 
 // ---------------------------------------------------------------------------
@@ -249,11 +275,29 @@ __global__ void k_adam(float *master, __nv_bfloat16 *w, float *grad, float *m, f
 
 }  // namespace
 
-cudaError_t launch_features(const Batch &b, const uint2 *path_contours, const float4 *bounds, float *feat,
-                            cudaStream_t st) {
+cudaError_t launch_features(const Batch &b, const uint2 *path_contours, float *feat, cudaStream_t st) {
     if (b.n_paths) {
         k_features<<<(unsigned)((uint64_t(b.n_paths) * 32 + kThreads - 1) / kThreads), kThreads, 0, st>>>(
-            b, path_contours, bounds, feat);
+            b, path_contours, feat);
+        count_launches(1);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_budgets(const Batch &b, const float *pred, float mul, float add, uint32_t *leaf_budget,
+                           uint32_t *fill_budget, cudaStream_t st) {
+    if (b.n_paths) {
+        k_budgets<<<(b.n_paths + kThreads - 1) / kThreads, kThreads, 0, st>>>(b, pred, mul, add, leaf_budget,
+                                                                             fill_budget);
+        count_launches(1);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_path_counts(const Batch &b, const uint2 *path_contours, uint32_t *leaves, uint32_t *fills,
+                               cudaStream_t st) {
+    if (b.n_paths) {
+        k_path_counts<<<(b.n_paths + kThreads - 1) / kThreads, kThreads, 0, st>>>(b, path_contours, leaves, fills);
         count_launches(1);
     }
     return cudaGetLastError();

@@ -25,8 +25,15 @@ EXPORTS = [
     "pf_abi_version", "pf_device_count", "pf_ctx_create", "pf_ctx_destroy", "pf_last_error",
     "pf_scene_upload", "pf_scene_upload_batch", "pf_render", "pf_render_scenes", "pf_read_image", "pf_read_image_scene",
     "pf_image_device_ptr", "pf_read_canon", "pf_read_canon_scene", "pf_read_coverage", "pf_draw",
-    "pf_image_bytes", "pf_image_offset", "pf_read_images",
+    "pf_image_bytes", "pf_image_offset", "pf_read_images", "pf_render_learned", "pf_sizer_param_count",
+    "pf_sizer_init", "pf_sizer_set_params", "pf_sizer_get_params", "pf_sizer_set_margin", "pf_sizer_predict",
+    "pf_sizer_gradient", "pf_sizer_train", "pf_sizer_save", "pf_sizer_load", "pf_path_features", "pf_path_counts",
+    "pf_sizer_last_frame", "pf_debug_counters",
 ]
+
+N_FEATURES = 12
+N_OUTPUTS = 2
+DEFAULT_WEIGHTS = os.path.join(HERE, "weights", "sizer.bin")
 
 
 class SceneView(C.Structure):
@@ -190,6 +197,11 @@ class Renderer:
             "fb_list": _arr(r.fb_list, r.n_list, np.uint32),
         }
 
+    def debug_counters(self) -> np.ndarray:
+        out = np.zeros(16, np.uint32)
+        self._check(self.lib.pf_debug_counters(self.ctx, C.c_void_p(out.ctypes.data), C.c_size_t(16)), self.ctx)
+        return out
+
     def image_bytes(self) -> int:
         n = C.c_uint64()
         self._check(self.lib.pf_image_bytes(self.ctx, C.byref(n)), self.ctx)
@@ -209,6 +221,86 @@ class Renderer:
         arr = (SceneView * len(views))(*views)
         self._check(self.lib.pf_scene_upload_batch(self.ctx, arr, len(views)), self.ctx)
         self._sizes = [(int(np.ceil(v.width)), int(np.ceil(v.height))) for v in views]
+
+    # -- learned frame and sizer -------------------------------------------------
+    def render_learned(self, first: int = 0, count: Optional[int] = None) -> Dict[str, float]:
+        """One-pass frame with sizer-predicted buffers (falls back to the exact frame on overflow)."""
+        st = FrameStats()
+        if count is None:
+            count = len(self._sizes) - first
+        self._check(self.lib.pf_render_learned(self.ctx, first, count, C.byref(st)), self.ctx)
+        return st.to_dict()
+
+    def sizer_init(self, seed: int = 0) -> None:
+        self._check(self.lib.pf_sizer_init(self.ctx, C.c_uint64(seed)), self.ctx)
+
+    def sizer_params(self) -> np.ndarray:
+        n = self.lib.pf_sizer_param_count()
+        out = np.empty(n, np.float32)
+        self._check(self.lib.pf_sizer_get_params(self.ctx, C.c_void_p(out.ctypes.data), C.c_size_t(n)), self.ctx)
+        return out
+
+    def set_sizer_params(self, params: np.ndarray) -> None:
+        params = np.ascontiguousarray(params, np.float32)
+        self._check(self.lib.pf_sizer_set_params(self.ctx, C.c_void_p(params.ctypes.data), C.c_size_t(params.size)),
+                    self.ctx)
+
+    def sizer_margin(self, mul: float, add: float, pool: float = 0.10) -> None:
+        self._check(self.lib.pf_sizer_set_margin(self.ctx, C.c_float(mul), C.c_float(add), C.c_float(pool)),
+                    self.ctx)
+
+    def sizer_last_frame(self):
+        """(paths over their leaf budget, spill-pool slots used) of the last learned frame."""
+        a, b = C.c_uint32(), C.c_uint32()
+        self._check(self.lib.pf_sizer_last_frame(self.ctx, C.byref(a), C.byref(b)), self.ctx)
+        return a.value, b.value
+
+    def sizer_predict(self, feat: np.ndarray) -> np.ndarray:
+        feat = np.ascontiguousarray(feat, np.float32)
+        out = np.empty((feat.shape[0], N_OUTPUTS), np.float32)
+        self._check(self.lib.pf_sizer_predict(self.ctx, C.c_void_p(feat.ctypes.data), C.c_uint32(feat.shape[0]),
+                                              C.c_void_p(out.ctypes.data)), self.ctx)
+        return out
+
+    def sizer_gradient(self, feat: np.ndarray, target: np.ndarray):
+        feat = np.ascontiguousarray(feat, np.float32)
+        target = np.ascontiguousarray(target, np.float32)
+        grad = np.empty(self.lib.pf_sizer_param_count(), np.float32)
+        loss = C.c_float()
+        self._check(self.lib.pf_sizer_gradient(self.ctx, C.c_void_p(feat.ctypes.data), C.c_void_p(target.ctypes.data),
+                                               C.c_uint32(feat.shape[0]), C.c_void_p(grad.ctypes.data),
+                                               C.byref(loss)), self.ctx)
+        return grad, loss.value
+
+    def sizer_train(self, feat: np.ndarray, target: np.ndarray, epochs: int, batch: int = 4096, lr: float = 1e-3,
+                    seed: int = 0) -> np.ndarray:
+        feat = np.ascontiguousarray(feat, np.float32)
+        target = np.ascontiguousarray(target, np.float32)
+        losses = np.zeros(epochs, np.float32)
+        self._check(self.lib.pf_sizer_train(self.ctx, C.c_void_p(feat.ctypes.data), C.c_void_p(target.ctypes.data),
+                                            C.c_uint32(feat.shape[0]), C.c_uint32(epochs), C.c_uint32(batch),
+                                            C.c_float(lr), C.c_uint64(seed), C.c_void_p(losses.ctypes.data)),
+                    self.ctx)
+        return losses
+
+    def sizer_save(self, path: str) -> None:
+        self._check(self.lib.pf_sizer_save(self.ctx, path.encode()), self.ctx)
+
+    def sizer_load(self, path: str = DEFAULT_WEIGHTS) -> None:
+        self._check(self.lib.pf_sizer_load(self.ctx, path.encode()), self.ctx)
+
+    def path_features(self, n_paths: int) -> np.ndarray:
+        out = np.empty((n_paths, N_FEATURES), np.float32)
+        self._check(self.lib.pf_path_features(self.ctx, C.c_void_p(out.ctypes.data), C.c_size_t(out.size)),
+                    self.ctx)
+        return out
+
+    def path_counts(self, n_paths: int):
+        leaves = np.empty(n_paths, np.uint32)
+        fills = np.empty(n_paths, np.uint32)
+        self._check(self.lib.pf_path_counts(self.ctx, C.c_void_p(leaves.ctypes.data), C.c_void_p(fills.ctypes.data),
+                                            C.c_size_t(n_paths)), self.ctx)
+        return leaves, fills
 
     def coverage(self) -> np.ndarray:
         n = C.c_uint64()

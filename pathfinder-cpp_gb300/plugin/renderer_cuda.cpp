@@ -1,0 +1,94 @@
+// renderer_cuda.cpp - see renderer_cuda.h.
+#include "renderer_cuda.h"
+
+#include <cmath>
+
+#include "common/logger.h"
+#include "core/scene.h"
+
+namespace Pathfinder {
+
+void SceneBuilderCuda::build(Scene *scene, Renderer *renderer) {
+    (void)renderer;
+    this->scene = scene;
+    points_.clear();
+    flags_.clear();
+    contour_start_.assign(1, 0);
+    path_start_.assign(1, 0);
+    color_.clear();
+    fill_rule_.clear();
+    for (const DrawPath &path : scene->draw_paths) {
+        for (const Contour &contour : path.outline.contours) {
+            for (size_t i = 0; i < contour.points.size(); i++) {
+                points_.push_back(contour.points[i].x);
+                points_.push_back(contour.points[i].y);
+                flags_.push_back(static_cast<uint8_t>(contour.flags[i]));
+            }
+            contour_start_.push_back(static_cast<uint32_t>(flags_.size()));
+        }
+        path_start_.push_back(static_cast<uint32_t>(contour_start_.size() - 1));
+        const ColorU c = scene->get_paint(path.paint).get_base_color();
+        color_.push_back(uint32_t(c.r_) | uint32_t(c.g_) << 8 | uint32_t(c.b_) << 16 | uint32_t(c.a_) << 24);
+        fill_rule_.push_back(path.fill_rule == FillRule::EvenOdd ? PF_FILL_EVEN_ODD : PF_FILL_NONZERO);
+    }
+    const RectF vb = scene->get_view_box();
+    view_ = pf_scene_view{};
+    view_.points = points_.data();
+    view_.point_flags = flags_.data();
+    view_.contour_start = contour_start_.data();
+    view_.path_start = path_start_.data();
+    view_.fill_rule = fill_rule_.data();
+    view_.color = color_.data();
+    view_.n_points = static_cast<uint32_t>(flags_.size());
+    view_.n_contours = static_cast<uint32_t>(contour_start_.size() - 1);
+    view_.n_paths = static_cast<uint32_t>(color_.size());
+    view_.width = vb.width();
+    view_.height = vb.height();
+    view_.clear_color = 0;
+}
+
+RendererCuda::RendererCuda(const std::shared_ptr<Device> &device, const std::shared_ptr<Queue> &queue,
+                           int cuda_device)
+    : Renderer(device, queue) {
+    pf_config cfg{};
+    cfg.device = cuda_device;
+    if (pf_ctx_create(&cfg, &ctx_) != PF_OK) {
+        Logger::error(std::string("RendererCuda: ") + pf_last_error(nullptr));
+        ctx_ = nullptr;
+    }
+}
+
+RendererCuda::~RendererCuda() {
+    if (ctx_) pf_ctx_destroy(ctx_);
+}
+
+bool RendererCuda::load_sizer(const std::string &path) {
+    learned_ = ctx_ && pf_sizer_load(ctx_, path.c_str()) == PF_OK;
+    return learned_;
+}
+
+void RendererCuda::draw(const std::shared_ptr<SceneBuilder> &scene_builder, bool clear_dst_texture) {
+    // errors are logged and the frame skipped, as the reference does (renderer.cpp:551-553)
+    auto *builder = dynamic_cast<SceneBuilderCuda *>(scene_builder.get());
+    if (!ctx_ || !builder) {
+        Logger::error("RendererCuda: needs a SceneBuilderCuda and a CUDA context");
+        return;
+    }
+    pf_scene_view view = builder->view();
+    if (!clear_dst_texture) view.clear_color = 0;
+    int st = pf_scene_upload(ctx_, &view);
+    if (st == PF_OK) st = learned_ ? pf_render_learned(ctx_, 0, 1, &stats_) : pf_render(ctx_, &stats_);
+    if (st == PF_OK) {
+        const size_t w = static_cast<size_t>(std::ceil(view.width)), h = static_cast<size_t>(std::ceil(view.height));
+        pixels_.resize(w * h * 4);
+        st = pf_read_image(ctx_, pixels_.data(), pixels_.size());
+        if (st == PF_OK && dest_texture_) {
+            auto encoder = device->create_command_encoder("RendererCuda upload");
+            encoder->write_texture(dest_texture_, RectI({0, 0}, {int(w), int(h)}), pixels_.data());
+            queue->submit(encoder, fence);
+        }
+    }
+    if (st != PF_OK) Logger::error(std::string("RendererCuda: ") + pf_last_error(ctx_));
+}
+
+}  // namespace Pathfinder
