@@ -112,6 +112,9 @@ typedef struct pf_frame_stats {
 } pf_frame_stats;
 
 #define PF_CONFIG_STAGE_TIMING 0x1u
+/* Count the composite's work (entries, composited fills) into pf_frame_stats; off by default
+ * because the counters cost a few atomics per block. */
+#define PF_CONFIG_FRAME_COUNTERS 0x2u
 
 /*
  * Canonical integer output of one scene (host memory, owned by the context
@@ -148,6 +151,7 @@ int pf_device_count(int *count);
 int pf_ctx_create(const pf_config *config, void **ctx);
 int pf_ctx_destroy(void *ctx);
 const char *pf_last_error(void *ctx);
+int pf_ctx_set_flags(void *ctx, uint32_t flags); /* PF_CONFIG_* bits */
 
 /*
  * Upload one scene (H2D copies on the context stream).  Replaces

@@ -337,6 +337,7 @@ Batch make_batch(Ctx *c) {
     b.list = c->list.as<uint32_t>();
     b.image = c->image.as<uint8_t>();
     b.status = c->status.as<uint32_t>();
+    b.counters = (c->flags & PF_CONFIG_FRAME_COUNTERS) ? 1u : 0u;
     return b;
 }
 
@@ -1241,6 +1242,14 @@ int pf_path_counts(void *ctx, uint32_t *leaves, uint32_t *fills, size_t capacity
     PF_CUDA(cudaStreamSynchronize(c->stream));
     dl.release();
     df.release();
+    return PF_OK;
+}
+
+// Change the PF_CONFIG_* flags of a context (stage timing, frame counters).
+int pf_ctx_set_flags(void *ctx, uint32_t flags) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    c->flags = flags;
     return PF_OK;
 }
 

@@ -139,6 +139,7 @@ struct Batch {
 
     uint8_t *image;                      // batch image buffer
     uint32_t *status;                    // [16] error bits and totals
+    uint32_t counters;                   // nonzero: the composite adds its work counters to status
 };
 
 // status word slots: error bits, then the totals the scans produce

@@ -246,90 +246,55 @@ __device__ __forceinline__ bool flat_quad(const float bb[4], const float cc[2]) 
 
 __device__ __forceinline__ float half_lerp(float a, float b) { return fadd(a, fmul(0.5f, fsub(b, a))); }
 
-// One de Casteljau half split (segment.cpp:62-95), keeping the first (right == false) or the
-// second half.
-__device__ __forceinline__ void split_cubic_half(float bb[4], float cc[4], bool right) {
-    float p01[2], p12[2], p23[2], p012[2], p123[2], p0123[2];
+template <class Emit>
+__device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, float c1, float c2, float c3,
+                              Emit &&emit, uint32_t *status) {
+    float stk[kMaxDepth][8];
+    int dstk[kMaxDepth];
+    int sp = 0;
+    float bb[4] = {b0, b1, b2, b3}, cc[4] = {c0, c1, c2, c3};
+    int depth = 0;
+    for (;;) {
+        if (depth >= kMaxDepth - 1 || flat_cubic(bb, cc)) {
+            if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
+            emit(bb[0], bb[1], bb[2], bb[3]);
+            if (sp == 0) return;
+            sp--;
 #pragma unroll
-    for (int k = 0; k < 2; k++) {
-        p01[k] = half_lerp(bb[k], cc[k]);
-        p12[k] = half_lerp(cc[k], cc[2 + k]);
-        p23[k] = half_lerp(cc[2 + k], bb[2 + k]);
-        p012[k] = half_lerp(p01[k], p12[k]);
-        p123[k] = half_lerp(p12[k], p23[k]);
-        p0123[k] = half_lerp(p012[k], p123[k]);
-    }
-    if (!right) {
+            for (int k = 0; k < 4; k++) {
+                bb[k] = stk[sp][k];
+                cc[k] = stk[sp][4 + k];
+            }
+            depth = dstk[sp];
+            continue;
+        }
+        float p01[2], p12[2], p23[2], p012[2], p123[2], p0123[2];
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            p01[k] = half_lerp(bb[k], cc[k]);
+            p12[k] = half_lerp(cc[k], cc[2 + k]);
+            p23[k] = half_lerp(cc[2 + k], bb[2 + k]);
+            p012[k] = half_lerp(p01[k], p12[k]);
+            p123[k] = half_lerp(p12[k], p23[k]);
+            p0123[k] = half_lerp(p012[k], p123[k]);
+        }
+        // push the second half, continue with the first
+        stk[sp][0] = p0123[0];
+        stk[sp][1] = p0123[1];
+        stk[sp][2] = bb[2];
+        stk[sp][3] = bb[3];
+        stk[sp][4] = p123[0];
+        stk[sp][5] = p123[1];
+        stk[sp][6] = p23[0];
+        stk[sp][7] = p23[1];
+        dstk[sp] = depth + 1;
+        sp++;
         bb[2] = p0123[0];
         bb[3] = p0123[1];
         cc[0] = p01[0];
         cc[1] = p01[1];
         cc[2] = p012[0];
         cc[3] = p012[1];
-    } else {
-        bb[0] = p0123[0];
-        bb[1] = p0123[1];
-        cc[0] = p123[0];
-        cc[1] = p123[1];
-        cc[2] = p23[0];
-        cc[3] = p23[1];
-    }
-}
-
-__device__ __forceinline__ void split_quad_half(float bb[4], float cc[2], bool right) {
-    float a[2], q[2], m[2];
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        a[k] = fadd(bb[k], fmul(fsub(cc[k], bb[k]), 0.5f));
-        q[k] = fadd(cc[k], fmul(fsub(bb[2 + k], cc[k]), 0.5f));
-        m[k] = fadd(a[k], fmul(fsub(q[k], a[k]), 0.5f));
-    }
-    if (!right) {
-        bb[2] = m[0];
-        bb[3] = m[1];
-        cc[0] = a[0];
-        cc[1] = a[1];
-    } else {
-        bb[0] = m[0];
-        bb[1] = m[1];
-        cc[0] = q[0];
-        cc[1] = q[1];
-    }
-}
-
-// Depth-first traversal of the bisection tree without a stack: the current node is kept in
-// registers with its path from the root (one bit per level, 1 = second half).  Descending
-// splits the current node; moving to the next sibling re-derives that node from the root by
-// the same sequence of splits, so every node is bit-identical to the recursive algorithm's.
-template <class Emit>
-__device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, float c1, float c2, float c3,
-                              Emit &&emit, uint32_t *status) {
-    float bb[4] = {b0, b1, b2, b3}, cc[4] = {c0, c1, c2, c3};
-    uint32_t bits = 0;
-    int depth = 0;
-    for (;;) {
-        if (depth >= kMaxDepth - 1 || flat_cubic(bb, cc)) {
-            if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
-            emit(bb[0], bb[1], bb[2], bb[3]);
-            while (depth > 0 && (bits & 1u)) {
-                bits >>= 1;
-                depth--;
-            }
-            if (depth == 0) return;
-            bits |= 1u;
-            bb[0] = b0;
-            bb[1] = b1;
-            bb[2] = b2;
-            bb[3] = b3;
-            cc[0] = c0;
-            cc[1] = c1;
-            cc[2] = c2;
-            cc[3] = c3;
-            for (int l = depth - 1; l >= 0; l--) split_cubic_half(bb, cc, (bits >> l) & 1u);
-            continue;
-        }
-        split_cubic_half(bb, cc, false);
-        bits <<= 1;
         depth++;
     }
 }
@@ -337,30 +302,43 @@ __device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, 
 template <class Emit>
 __device__ void flatten_quad(float b0, float b1, float b2, float b3, float c0, float c1, Emit &&emit,
                              uint32_t *status) {
+    float stk[kMaxDepth][6];
+    int dstk[kMaxDepth];
+    int sp = 0;
     float bb[4] = {b0, b1, b2, b3}, cc[2] = {c0, c1};
-    uint32_t bits = 0;
     int depth = 0;
     for (;;) {
         if (depth >= kMaxDepth - 1 || flat_quad(bb, cc)) {
             if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
             emit(bb[0], bb[1], bb[2], bb[3]);
-            while (depth > 0 && (bits & 1u)) {
-                bits >>= 1;
-                depth--;
-            }
-            if (depth == 0) return;
-            bits |= 1u;
-            bb[0] = b0;
-            bb[1] = b1;
-            bb[2] = b2;
-            bb[3] = b3;
-            cc[0] = c0;
-            cc[1] = c1;
-            for (int l = depth - 1; l >= 0; l--) split_quad_half(bb, cc, (bits >> l) & 1u);
+            if (sp == 0) return;
+            sp--;
+#pragma unroll
+            for (int k = 0; k < 4; k++) bb[k] = stk[sp][k];
+            cc[0] = stk[sp][4];
+            cc[1] = stk[sp][5];
+            depth = dstk[sp];
             continue;
         }
-        split_quad_half(bb, cc, false);
-        bits <<= 1;
+        float a[2], q[2], m[2];
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            a[k] = fadd(bb[k], fmul(fsub(cc[k], bb[k]), 0.5f));
+            q[k] = fadd(cc[k], fmul(fsub(bb[2 + k], cc[k]), 0.5f));
+            m[k] = fadd(a[k], fmul(fsub(q[k], a[k]), 0.5f));
+        }
+        stk[sp][0] = m[0];
+        stk[sp][1] = m[1];
+        stk[sp][2] = bb[2];
+        stk[sp][3] = bb[3];
+        stk[sp][4] = q[0];
+        stk[sp][5] = q[1];
+        dstk[sp] = depth + 1;
+        sp++;
+        bb[2] = m[0];
+        bb[3] = m[1];
+        cc[0] = a[0];
+        cc[1] = a[1];
         depth++;
     }
 }
@@ -770,50 +748,89 @@ __device__ __forceinline__ void cov_add(int *D, int row, int col, float v) {
     if (row < 16) atomicAdd(&D[cov_index(row, col)], __float2int_rn(v * (float)(1 << kCovShift)));
 }
 
-__device__ void raster_fill(uint2 f, int *D) {
-    const float x0 = (float)(f.x & 0xffffu) * (1.0f / 256.0f), y0 = (float)(f.x >> 16) * (1.0f / 256.0f);
-    const float x1 = (float)(f.y & 0xffffu) * (1.0f / 256.0f), y1 = (float)(f.y >> 16) * (1.0f / 256.0f);
-    const float s = x0 > x1 ? 1.0f : -1.0f;
-    const float xl = fminf(x0, x1), xr = fmaxf(x0, x1);
-    const float yl = x0 < x1 ? y0 : y1, yr = x0 < x1 ? y1 : y0;
-    const float dydx = (yr - yl) / (xr - xl);
-    const int i0 = (int)floorf(xl), i1 = min((int)ceilf(xr), 16);
-    for (int i = max(i0, 0); i < i1; i++) {
-        const float xa = fmaxf(xl, (float)i), xb = fminf(xr, (float)(i + 1));
-        const float w = xb - xa;
-        if (!(w > 0.0f)) continue;
-        const float ya = xa == xl ? yl : yl + dydx * (xa - xl);
-        const float yb = xb == xr ? yr : yl + dydx * (xb - xl);
-        const float ylo = fminf(ya, yb), yhi = fmaxf(ya, yb);
-        const int r0 = (int)floorf(ylo);
-        const float sw = s * w;
-        if (yhi <= (float)(r0 + 1)) {
-            const float m = 0.5f * (ylo + yhi) - (float)r0;
-            cov_add(D, r0, i, sw * (1.0f - m));
-            cov_add(D, r0 + 1, i, sw * m);
-        } else {
-            const int r1 = min((int)ceilf(yhi) - 1, 15);
-            const float inv_h = 1.0f / (yhi - ylo);
-            for (int r = r0; r <= r1; r++) {
-                const float lo = fmaxf(ylo, (float)r), hi = fminf(yhi, (float)(r + 1));
-                const float hgt = hi - lo;
-                if (!(hgt > 0.0f)) continue;
-                const float wr = sw * hgt * inv_h;
-                const float m = 0.5f * (lo + hi) - (float)r;
-                cov_add(D, r, i, wr * (1.0f - m));
-                cov_add(D, r + 1, i, wr * m);
-            }
+// Per-fill set-up shared by the (fill, column) work items of one alpha tile.
+struct FillPrep {
+    float xl, yl, xr, yr, dydx, s;
+    int i0;
+    int first;  // first work item of this fill
+};
+
+// The piece of fill `fp` inside pixel column i: per-row differences into D.
+__device__ __forceinline__ void raster_column(const FillPrep &fp, int i, int *D) {
+    const float xa = fmaxf(fp.xl, (float)i), xb = fminf(fp.xr, (float)(i + 1));
+    const float w = xb - xa;
+    if (!(w > 0.0f)) return;
+    const float ya = xa == fp.xl ? fp.yl : fp.yl + fp.dydx * (xa - fp.xl);
+    const float yb = xb == fp.xr ? fp.yr : fp.yl + fp.dydx * (xb - fp.xl);
+    const float ylo = fminf(ya, yb), yhi = fmaxf(ya, yb);
+    const int r0 = (int)floorf(ylo);
+    const float sw = fp.s * w;
+    if (yhi <= (float)(r0 + 1)) {
+        const float m = 0.5f * (ylo + yhi) - (float)r0;
+        cov_add(D, r0, i, sw * (1.0f - m));
+        cov_add(D, r0 + 1, i, sw * m);
+    } else {
+        const int r1 = min((int)ceilf(yhi) - 1, 15);
+        const float inv_h = 1.0f / (yhi - ylo);
+        for (int r = r0; r <= r1; r++) {
+            const float lo = fmaxf(ylo, (float)r), hi = fminf(yhi, (float)(r + 1));
+            const float hgt = hi - lo;
+            if (!(hgt > 0.0f)) continue;
+            const float wr = sw * hgt * inv_h;
+            const float m = 0.5f * (lo + hi) - (float)r;
+            cov_add(D, r, i, wr * (1.0f - m));
+            cov_add(D, r + 1, i, wr * m);
         }
     }
 }
 
 // Warp computes the coverage of the 8 pixels of every lane (column lane&15, rows
 // (lane>>4)*8 .. +7) of an alpha tile; D must be zeroed on entry and is left dirty.
+// Fills are rasterised as (fill, pixel column) work items spread over the lanes, 32 fills
+// at a time, so a tile of a few wide fills still keeps the warp busy.
 __device__ __forceinline__ void alpha_coverage(const Batch &b, uint32_t f0, uint32_t f1, int8_t bd, bool eo, int *D,
-                                               float cov[8]) {
+                                               FillPrep *prep, float cov[8]) {
     const int lane = threadIdx.x & 31;
-    for (uint32_t f = f0 + lane; f < f1; f += 32) raster_fill(b.fills[f], D);
-    __syncwarp();
+    for (uint32_t base = f0; base < f1; base += 32) {
+        const uint32_t f = base + lane;
+        int items = 0;
+        FillPrep fp;
+        if (f < f1) {
+            const uint2 q = b.fills[f];
+            const float x0 = (float)(q.x & 0xffffu) * (1.0f / 256.0f), y0 = (float)(q.x >> 16) * (1.0f / 256.0f);
+            const float x1 = (float)(q.y & 0xffffu) * (1.0f / 256.0f), y1 = (float)(q.y >> 16) * (1.0f / 256.0f);
+            fp.s = x0 > x1 ? 1.0f : -1.0f;
+            fp.xl = fminf(x0, x1);
+            fp.xr = fmaxf(x0, x1);
+            fp.yl = x0 < x1 ? y0 : y1;
+            fp.yr = x0 < x1 ? y1 : y0;
+            fp.dydx = (fp.yr - fp.yl) / (fp.xr - fp.xl);
+            fp.i0 = max((int)floorf(fp.xl), 0);
+            items = max(min((int)ceilf(fp.xr), 16) - fp.i0, 0);
+        }
+        int incl = items;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += t;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        fp.first = incl - items;
+        prep[lane] = fp;
+        __syncwarp();
+        for (int k = lane; k < total; k += 32) {
+            // fill of item k: the last fill whose first item is <= k
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (prep[mid].first <= k && mid < (int)min(32u, f1 - base)) lo = mid;
+                else hi = mid - 1;
+            }
+            const FillPrep &g = prep[lo];
+            raster_column(g, g.i0 + (k - g.first), D);
+        }
+        __syncwarp();
+    }
     const int col = lane & 15, h = lane >> 4;
     int acc[8];
     int run = 0;
@@ -888,13 +905,14 @@ __device__ __forceinline__ bool solid_hidden(bool eo, int8_t bd) { return eo && 
 
 __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
     __shared__ int cells[kCompWarps][kCovCells];
+    __shared__ FillPrep prep[kCompWarps][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int *D = cells[warp];
     const int col = lane & 15, h = lane >> 4;
     const float inv255 = 1.0f / 255.0f;
-    const uint32_t n_warps = gridDim.x * kCompWarps;
     uint32_t entries = 0, comp_fills = 0, chunks = 0;
-    for (uint32_t fb = blockIdx.x * kCompWarps + warp; fb < b.n_fb; fb += n_warps) {
+    const uint32_t fb = blockIdx.x * kCompWarps + warp;
+    if (fb < b.n_fb) {
         const uint32_t fbg = b.fb_base + fb;
         const uint32_t s = upper_bound(b.scene_fb_first, b.n_scenes_all + 1, fbg) - 1;
         const SceneDev &S = b.scenes[s];
@@ -923,7 +941,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
                 const uint32_t f0 = b.tile_fills[(int64_t)gt - 1], f1 = b.tile_fills[gt];
                 comp_fills += f1 - f0;
                 zero_cells(D);
-                alpha_coverage(b, f0, f1, bd, eo, D, cov);
+                alpha_coverage(b, f0, f1, bd, eo, D, prep[warp], cov);
                 __syncwarp();
             }
             const uint32_t color = b.color[b.path_base + p];
@@ -960,11 +978,22 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
             }
         }
     }
-    if (lane == 0 && entries) {
-        atomicAdd(&b.status[kStEntries], entries);
-        atomicAdd(&b.status[kStListFills], comp_fills);
+    if (b.counters) {
+        // one reduction per block into the frame counters
+        __shared__ uint32_t red[kCompWarps][3];
+        if (lane == 0) {
+            red[warp][0] = entries;
+            red[warp][1] = comp_fills;
+            red[warp][2] = chunks;
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            uint32_t v = 0;
+            for (int w = 0; w < kCompWarps; w++) v += red[w][threadIdx.x];
+            const int slot = threadIdx.x == 0 ? kStEntries : (threadIdx.x == 1 ? kStListFills : kStWalkChunks);
+            if (v) atomicAdd(&b.status[slot], v);
+        }
     }
-    if (lane == 0 && chunks) atomicAdd(&b.status[kStWalkChunks], chunks);
 }
 
 // Composite lists and z per framebuffer tile for the canonical output (not part of a frame):
@@ -1006,6 +1035,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_list_dump(Batch b) {
 __global__ void __launch_bounds__(kCompWarps * 32) k_coverage_dump(Batch b, const uint32_t *tiles, uint32_t n,
                                                                    float *out) {
     __shared__ int cells[kCompWarps][kCovCells];
+    __shared__ FillPrep prep[kCompWarps][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t k = blockIdx.x * kCompWarps + warp;
     if (k >= n) return;
@@ -1015,7 +1045,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_coverage_dump(Batch b, cons
     zero_cells(D);
     float cov[8];
     alpha_coverage(b, b.tile_fills[(int64_t)gt - 1], b.tile_fills[gt], (int8_t)(b.tile_state[gt] & 0xffu),
-                   (b.paths[p].flags & 1u) != 0, D, cov);
+                   (b.paths[p].flags & 1u) != 0, D, prep[warp], cov);
     const int col = lane & 15, h = lane >> 4;
 #pragma unroll
     for (int r = 0; r < 8; r++) out[(size_t)k * 256 + (h * 8 + r) * 16 + col] = cov[r];
@@ -1091,14 +1121,7 @@ cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st) {
 }
 
 cudaError_t launch_composite(const Batch &b, cudaStream_t st) {
-    if (!b.n_fb) return cudaSuccess;
-    int dev = 0, sms = 152, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_composite, kCompWarps * 32, 0);
-    const uint64_t want = grid_for(b.n_fb, kCompWarps);
-    const unsigned grid = (unsigned)std::min<uint64_t>(want, uint64_t(std::max(per_sm, 1)) * sms);
-    PF_LAUNCH(k_composite<<<grid, kCompWarps * 32, 0, st>>>(b));
+    if (b.n_fb) PF_LAUNCH(k_composite<<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
     return cudaGetLastError();
 }
 

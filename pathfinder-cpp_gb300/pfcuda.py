@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libpfcuda.so")
 
 PF_OK = 0
 PF_CONFIG_STAGE_TIMING = 0x1
+PF_CONFIG_FRAME_COUNTERS = 0x2
 
 EXPORTS = [
     "pf_abi_version", "pf_device_count", "pf_ctx_create", "pf_ctx_destroy", "pf_last_error",
@@ -28,7 +29,7 @@ EXPORTS = [
     "pf_image_bytes", "pf_image_offset", "pf_read_images", "pf_render_learned", "pf_sizer_param_count",
     "pf_sizer_init", "pf_sizer_set_params", "pf_sizer_get_params", "pf_sizer_set_margin", "pf_sizer_predict",
     "pf_sizer_gradient", "pf_sizer_train", "pf_sizer_save", "pf_sizer_load", "pf_path_features", "pf_path_counts",
-    "pf_sizer_last_frame", "pf_debug_counters",
+    "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags",
 ]
 
 N_FEATURES = 12
@@ -120,9 +121,10 @@ def _arr(ptr, n, dtype):
 class Renderer:
     """One CUDA context: upload scenes, draw them, read images and tile data back."""
 
-    def __init__(self, device: int = 0, stream: int = 0, stage_timing: bool = False):
+    def __init__(self, device: int = 0, stream: int = 0, stage_timing: bool = False, counters: bool = False):
         self.lib = load()
-        cfg = Config(device, C.c_void_p(stream or None), PF_CONFIG_STAGE_TIMING if stage_timing else 0)
+        flags = (PF_CONFIG_STAGE_TIMING if stage_timing else 0) | (PF_CONFIG_FRAME_COUNTERS if counters else 0)
+        cfg = Config(device, C.c_void_p(stream or None), flags)
         h = C.c_void_p()
         self._check(self.lib.pf_ctx_create(C.byref(cfg), C.byref(h)), None)
         self.ctx = h
@@ -196,6 +198,10 @@ class Renderer:
             "fb_list_first": _arr(r.fb_list_first, nfb + 1, np.uint64),
             "fb_list": _arr(r.fb_list, r.n_list, np.uint32),
         }
+
+    def set_flags(self, stage_timing: bool = False, counters: bool = False) -> None:
+        flags = (PF_CONFIG_STAGE_TIMING if stage_timing else 0) | (PF_CONFIG_FRAME_COUNTERS if counters else 0)
+        self._check(self.lib.pf_ctx_set_flags(self.ctx, C.c_uint32(flags)), self.ctx)
 
     def debug_counters(self) -> np.ndarray:
         out = np.zeros(16, np.uint32)

@@ -58,6 +58,6 @@ def pf():
 def renderer(pf):
     if pf.device_count() < 1:
         pytest.fail("no CUDA device visible to a GPU test")
-    r = pf.Renderer(stage_timing=True)
+    r = pf.Renderer(stage_timing=True, counters=True)
     yield r
     r.close()
