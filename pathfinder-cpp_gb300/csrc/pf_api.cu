@@ -83,6 +83,7 @@ struct Ctx {
     // learned sizer: weights (bf16 used by the kernels, fp32 master + Adam moments for training)
     DevBuf sz_w, sz_master, sz_m, sz_v, sz_grad, sz_loss, sz_feat, sz_target, sz_index, sz_pred;
     DevBuf path_feat, path_pred, path_leaf_first, path_leaf_budget, path_leaf_cursor, path_fill_budget;
+    DevBuf bin_list, bin_ctl, path_leaf_range;
     int sz_step = 0;
     bool sz_ready = false;
     float sz_mul = 1.25f, sz_add = 8.0f, sz_pool = 0.10f;
@@ -311,6 +312,12 @@ Batch make_batch(Ctx *c) {
     b.path_leaf_first = c->path_leaf_first.as<uint32_t>();
     b.path_leaf_budget = c->path_leaf_budget.as<uint32_t>();
     b.path_leaf_cursor = c->path_leaf_cursor.as<uint32_t>();
+    b.leaf_pool_first = 0xffffffffu;  // no spill pool unless a learned frame sets one
+    b.leaf_pool_cap = 0;
+    b.path_leaf_range = c->path_leaf_range.as<uint2>();
+    b.path_contours = c->path_contours.as<uint2>();
+    b.bin_list = c->bin_list.as<uint32_t>();
+    b.bin_ctl = c->bin_ctl.as<uint32_t>();
     b.path_tiles = c->path_tiles.as<uint32_t>();
     b.path_cols = c->path_cols.as<uint32_t>();
     b.contour_segs = c->contour_segs.as<uint32_t>();
@@ -407,6 +414,9 @@ int begin_frame(Ctx *c, uint32_t first, uint32_t count) {
     PF_CUDA(c->path_contours.ensure(size_t(N) * 8 + 8));
     PF_CUDA(c->path_bounds.ensure(size_t(N) * 16 + 16));
     PF_CUDA(c->row_first.ensure((size_t(c->r_rows) + 1) * 4));
+    PF_CUDA(c->bin_list.ensure(size_t(N) * 16 + 16));
+    PF_CUDA(c->bin_ctl.ensure(64));
+    PF_CUDA(c->path_leaf_range.ensure(size_t(N) * 8 + 16));
     return PF_OK;
 }
 
@@ -528,19 +538,22 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     PF_CUDA(launch_flatten(b, c->n_segs, true, st));
     record(c, 2);
 
-    // 3. fill counts per tile, then fills written grouped by tile (counting sort)
+    // 3. fill counts per tile, then fills written grouped by tile (counting sort); paths are
+    //    binned by CTAs owning their tiles, so the tile counters need no clearing
     const size_t T = c->n_tiles, K = c->n_cols;
-    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, (T + 2) * 4, st));
-    PF_CUDA(cudaMemsetAsync(b.tile_delta, 0, T * 4, st));
+    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, 4, st));  // tile_fills[-1]
+    PF_CUDA(cudaMemsetAsync(b.tile_fills + T, 0, 4, st));
     PF_CUDA(cudaMemsetAsync(b.col_above, 0, K * 4, st));
-    PF_CUDA(launch_bin(b, c->n_leaves, false, st));
+    PF_CUDA(cudaMemsetAsync(b.bin_ctl, 0, 64, st));
+    PF_CUDA(launch_bin_classify(b, false, st));
+    PF_CUDA(launch_bin_paths(b, false, c->n_leaves, st));
     if (int e = scan(c, b.tile_fills, (uint32_t)T + 1, kStFills)) return e;
     if (int e = read_status(c)) return e;
     if (int e = check_kernel_status(c)) return e;
     c->n_fills = c->h_status[kStFills];
     PF_CUDA(c->fills.ensure(size_t(c->n_fills) * 8 + 16));
     b = make_batch(c);
-    PF_CUDA(launch_bin(b, c->n_leaves, true, st));
+    PF_CUDA(launch_bin_paths(b, true, c->n_leaves, st));
     record(c, 3);
 
     // 4. backdrops
@@ -584,16 +597,19 @@ int render_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats
     PF_CUDA(launch_contour_segments(b, true, st));
     PF_CUDA(launch_rows(b, true, st));
     PF_CUDA(cudaMemsetAsync(b.leaf_path, 0xff, leaf_slots * 4, st));
-    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, (T + 2) * 4, st));
-    PF_CUDA(cudaMemsetAsync(b.tile_delta, 0, T * 4, st));
+    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, 4, st));  // tile_fills[-1]
+    PF_CUDA(cudaMemsetAsync(b.tile_fills + T, 0, 4, st));
     PF_CUDA(cudaMemsetAsync(b.col_above, 0, K * 4, st));
-    PF_CUDA(launch_flatten_bin_count(b, c->n_segs, st));
+    PF_CUDA(cudaMemsetAsync(b.bin_ctl, 0, 64, st));
+    PF_CUDA(launch_flatten_budget(b, c->n_segs, st));
     record(c, 2);
-    if (int e = scan(c, b.tile_fills, (uint32_t)T + 1, kStFills)) return e;
-    // the leaf slots (with gaps) are what the fill pass walks
+    // the leaf slots (regions with gaps, then the pool) are what the global pass walks
     const uint32_t slots32 = (uint32_t)leaf_slots;
     PF_CUDA(cudaMemcpyAsync(b.status + kStLeaves, &slots32, 4, cudaMemcpyHostToDevice, st));
-    PF_CUDA(launch_bin(b, slots32, true, st));
+    PF_CUDA(launch_bin_classify(b, true, st));
+    PF_CUDA(launch_bin_paths(b, false, slots32, st));
+    if (int e = scan(c, b.tile_fills, (uint32_t)T + 1, kStFills)) return e;
+    PF_CUDA(launch_bin_paths(b, true, slots32, st));
     record(c, 3);
     PF_CUDA(launch_propagate(b, c->n_cols, st));
     record(c, 4);
@@ -839,6 +855,7 @@ int pf_ctx_destroy(void *ctx) {
     DevBuf *bufs[] = {&c->sz_w, &c->sz_master, &c->sz_m, &c->sz_v, &c->sz_grad, &c->sz_loss, &c->sz_feat,
                       &c->sz_target, &c->sz_index, &c->sz_pred, &c->path_feat, &c->path_pred, &c->path_leaf_first,
                       &c->path_leaf_budget, &c->path_leaf_cursor, &c->path_fill_budget, &c->path_bounds,
+                      &c->bin_list, &c->bin_ctl, &c->path_leaf_range,
                       &c->points, &c->pflags, &c->cstart, &c->pstart, &c->fill_rule, &c->color, &c->scenes,
                       &c->scene_path_first, &c->scene_contour_first, &c->scene_fb_first, &c->contour_point_first,
                       &c->contour_path, &c->paths, &c->path_tiles, &c->path_cols, &c->contour_segs,

@@ -99,6 +99,11 @@ struct Batch {
     uint32_t *path_leaf_budget;          // [n_paths]
     uint32_t *path_leaf_cursor;          // [n_paths]
     uint32_t leaf_pool_first, leaf_pool_cap;  // shared spill pool after the per-path regions
+    // per-path binning: leaf range of every path, paths bucketed by tile count
+    uint2 *path_leaf_range;              // [n_paths] [first, end) in the leaf buffer
+    const uint2 *path_contours;          // [n_paths] [first, end) contours of each path
+    uint32_t *bin_list;                  // [4][n_paths] paths of each size class
+    uint32_t *bin_ctl;                   // [16] class counts, work tickets
     uint32_t *path_tiles;                // [n_paths + 1] -> scanned to first tile
     uint32_t *path_cols;                 // [n_paths + 1] -> scanned to first column
     uint32_t *contour_segs;              // [n_contours + 1] -> scanned
@@ -191,7 +196,11 @@ cudaError_t launch_budgets(const Batch &b, const float *pred, float mul, float a
                            uint32_t *fill_budget, cudaStream_t st);
 cudaError_t launch_path_counts(const Batch &b, const uint2 *path_contours, uint32_t *leaves, uint32_t *fills,
                                cudaStream_t st);
-cudaError_t launch_flatten_bin_count(const Batch &b, uint32_t n_segs, cudaStream_t st);
+cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t st);
+// Binning by path: classify (leaf ranges, size classes), then count or write.  `pool` is
+// true in a learned frame (leaves past the per-path regions are binned by the global pass).
+cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st);
+cudaError_t launch_bin_paths(const Batch &b, bool write, uint32_t n_leaf_slots, cudaStream_t st);
 cudaError_t launch_mlp_predict(const __nv_bfloat16 *w, const float *feat, uint32_t n, float *out, cudaStream_t st);
 cudaError_t launch_mlp_grad(const __nv_bfloat16 *w, const float *feat, const float *target, const uint32_t *index,
                             uint32_t n, float *grad, float *loss, cudaStream_t st);

@@ -523,6 +523,8 @@ __device__ void walk_line(const WalkCtx &w, float x0, float y0, float x1, float 
     }
 }
 
+__device__ __forceinline__ int path_class(const PathDev &P);
+
 template <bool kWrite>
 __global__ void __launch_bounds__(kThreads) k_bin(Batch b, uint32_t n_leaves) {
     const uint32_t i = global_tid();
@@ -533,8 +535,10 @@ __global__ void __launch_bounds__(kThreads) k_bin(Batch b, uint32_t n_leaves) {
     }
     const uint32_t p = b.leaf_path[i];
     if (p == kNone) return;  // unused slot of a learned frame's leaf region
-    const float4 L = b.leaves[i];
     const PathDev P = b.paths[p];
+    // paths that fit a CTA are binned by k_bin_paths, except leaves in the spill pool
+    if (i < b.leaf_pool_first && path_class(P) < 3) return;
+    const float4 L = b.leaves[i];
     const SceneDev &S = b.scenes[P.scene];
     WalkCtx w;
     w.rx0 = P.rx0;
@@ -563,28 +567,16 @@ __global__ void __launch_bounds__(kThreads) k_bin(Batch b, uint32_t n_leaves) {
     }
 }
 
-// Learned frame: flatten one segment, store each leaf line in its path's leaf region (laid out
-// from the sizer's budget; slots are reserved eight at a time) and walk it at once for the
-// fill and backdrop counts.  Counts stay exact even when a path overruns its budget (the
-// overflow bit then sends the frame to the exact two-pass method).
+// Learned frame: flatten one segment and store its leaf lines in the path's leaf region,
+// laid out from the sizer's budget (slots reserved eight at a time); lines past the budget
+// spill into the shared pool.  An exhausted pool sets the overflow bit and the frame is
+// redone by the exact two-pass method.
 constexpr int kLeafBatch = 8;
 
-__global__ void __launch_bounds__(kThreads) k_flatten_bin_count(Batch b, uint32_t n_segs) {
+__global__ void __launch_bounds__(kThreads) k_flatten_budget(Batch b, uint32_t n_segs) {
     const uint32_t i = global_tid();
     if (i >= n_segs || i >= b.status[kStSegs]) return;
     const SegDev sg = b.segs[i];
-    const PathDev P = b.paths[sg.path];
-    const SceneDev &S = b.scenes[P.scene];
-    WalkCtx w;
-    w.rx0 = P.rx0;
-    w.ry0 = P.ry0;
-    w.rx1 = P.rx1;
-    w.ry1 = P.ry1;
-    w.rw = max(P.rx1 - P.rx0, 0);
-    w.rh = max(P.ry1 - P.ry0, 0);
-    w.vb_right = S.vb_right;
-    w.vb_bottom = S.vb_bottom;
-    const uint32_t tb = P.tile_first, cb = P.col_first;
     const uint32_t region = b.path_leaf_first[sg.path], budget = b.path_leaf_budget[sg.path];
     float4 pend[kLeafBatch];
     int npend = 0;
@@ -598,7 +590,6 @@ __global__ void __launch_bounds__(kThreads) k_flatten_bin_count(Batch b, uint32_
             b.leaf_path[region + slot + k] = sg.path;
         }
         if (in_region < (uint32_t)npend) {
-            // the path overran its budget: spill into the shared pool
             const uint32_t extra = (uint32_t)npend - in_region;
             if (slot <= budget && slot + npend > budget) atomicAdd(&b.status[kStPathsOver], 1u);
             const uint32_t q = atomicAdd(&b.status[kStPoolUsed], extra);
@@ -617,13 +608,6 @@ __global__ void __launch_bounds__(kThreads) k_flatten_bin_count(Batch b, uint32_
         pend[npend++] = make_float4(x0, y0, x1, y1);
         if (npend == kLeafBatch) flush();
         produced++;
-        walk_line(
-            w, x0, y0, x1, y1, [&](int32_t local, uint2) { atomicAdd(&b.tile_fills[tb + (uint32_t)local], 1u); },
-            [&](int32_t where, int d) {
-                if (where >= 0) atomicAdd(&b.tile_delta[tb + (uint32_t)where], d);
-                else atomicAdd(&b.col_above[cb + (uint32_t)(-1 - where)], d);
-            },
-            &b.status[kStErr]);
     };
     const float2 p0 = b.points[sg.a];
     switch (sg.kind) {
@@ -648,6 +632,159 @@ __global__ void __launch_bounds__(kThreads) k_flatten_bin_count(Batch b, uint32_
     const unsigned active = __activemask();
     const uint32_t total = __reduce_add_sync(active, produced);
     if ((int)(threadIdx.x & 31) == __ffs(active) - 1) atomicAdd(&b.status[kStLeafCount], total);
+}
+
+// ---------------------------------------------------------------------------
+// Binning by path.  A path's tiles belong to it alone, so one CTA can bin all of a path's
+// leaf lines with shared-memory counters (count pass) and shared-memory cursors (write pass)
+// and write its tiles' counts / deltas / end offsets out densely: no global atomics and no
+// memsets for those tiles.  Paths are bucketed by tile count; each class has its own CTA
+// shape; paths above the largest class, and leaves in a learned frame's spill pool, go
+// through the per-leaf global-atomic k_bin.
+
+__host__ __device__ constexpr uint32_t class_tiles(int c) { return c == 0 ? 1024u : c == 1 ? 4096u : 16384u; }
+__host__ __device__ constexpr int class_threads(int c) { return c == 2 ? 1024 : 256; }
+constexpr uint32_t kMaxCols = 4096;  // widest tile rect (65536 px canvas)
+// bin_ctl slots
+enum : int { kCtlCount = 0, kCtlTicketCount = 4, kCtlTicketWrite = 8, kCtlTicketZero = 12 };
+
+__device__ __forceinline__ int size_class(uint32_t tiles) {
+    return tiles <= class_tiles(0) ? 0 : tiles <= class_tiles(1) ? 1 : tiles <= class_tiles(2) ? 2 : 3;
+}
+
+// -1: no columns (nothing to bin); 3: binned by the global pass (too many tiles for a CTA, or
+// columns but no tile rows, where only deltas above the rect can land)
+__device__ __forceinline__ int path_class(const PathDev &P) {
+    const int32_t rw = max(P.rx1 - P.rx0, 0), rh = max(P.ry1 - P.ry0, 0);
+    if (rw == 0) return -1;
+    if (rh == 0) return 3;
+    return size_class((uint32_t)rw * (uint32_t)rh);
+}
+
+__global__ void k_bin_classify(Batch b, bool learned) {
+    const uint32_t p = global_tid();
+    const int lane = threadIdx.x & 31;
+    int cls = -1;
+    if (p < b.n_paths) {
+        const PathDev P = b.paths[p];
+        const uint32_t tiles = (uint32_t)max(P.rx1 - P.rx0, 0) * (uint32_t)max(P.ry1 - P.ry0, 0);
+        uint2 range;
+        if (learned) {
+            const uint32_t f = b.path_leaf_first[p];
+            range = make_uint2(f, f + min(b.path_leaf_cursor[p], b.path_leaf_budget[p]));
+        } else {
+            const uint2 pc = b.path_contours[p];
+            range = make_uint2(b.seg_leaves[b.contour_segs[pc.x]], b.seg_leaves[b.contour_segs[pc.y]]);
+        }
+        b.path_leaf_range[p] = range;
+        (void)tiles;
+        cls = path_class(P);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const uint32_t m = __ballot_sync(0xffffffffu, cls == c);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&b.bin_ctl[kCtlCount + c], (uint32_t)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (cls == c) b.bin_list[(size_t)c * b.n_paths + base + __popc(m & ((1u << lane) - 1u))] = p;
+    }
+}
+
+template <bool kWrite, int kCls>
+__global__ void __launch_bounds__(class_threads(kCls)) k_bin_paths(Batch b) {
+    extern __shared__ uint32_t sm[];
+    constexpr uint32_t kT = class_tiles(kCls);
+    constexpr uint32_t kCols = kT < kMaxCols ? kT : kMaxCols;
+    uint32_t *cnt = sm;                                           // counts, then cursors
+    int32_t *dlt = reinterpret_cast<int32_t *>(sm + kT);          // backdrop deltas
+    int32_t *above = reinterpret_cast<int32_t *>(sm + 2 * kT);    // deltas above the rect
+    __shared__ uint32_t s_item;
+    if (kWrite && b.status[kStFills] > b.fill_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&b.status[kStErr], kErrOverflowFill);
+        return;
+    }
+    const uint32_t *list = b.bin_list + (size_t)kCls * b.n_paths;
+    const uint32_t n_items = b.bin_ctl[kCtlCount + kCls];
+    uint32_t *ticket = &b.bin_ctl[(kWrite ? kCtlTicketWrite : kCtlTicketCount) + kCls];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(ticket, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        __syncthreads();
+        if (item >= n_items) return;
+        const uint32_t p = list[item];
+        const PathDev P = b.paths[p];
+        const SceneDev &S = b.scenes[P.scene];
+        WalkCtx w;
+        w.rx0 = P.rx0;
+        w.ry0 = P.ry0;
+        w.rx1 = P.rx1;
+        w.ry1 = P.ry1;
+        w.rw = P.rx1 - P.rx0;
+        w.rh = P.ry1 - P.ry0;
+        w.vb_right = S.vb_right;
+        w.vb_bottom = S.vb_bottom;
+        const uint32_t T = (uint32_t)(w.rw * w.rh), tb = P.tile_first, cb = P.col_first;
+        const uint2 range = b.path_leaf_range[p];
+        if (!kWrite) {
+            for (uint32_t t = threadIdx.x; t < T; t += blockDim.x) {
+                cnt[t] = 0;
+                dlt[t] = 0;
+            }
+            for (uint32_t x = threadIdx.x; x < (uint32_t)w.rw; x += blockDim.x) above[x] = 0;
+        } else {
+            for (uint32_t t = threadIdx.x; t < T; t += blockDim.x) cnt[t] = b.tile_fills[tb + t];
+        }
+        __syncthreads();
+        for (uint32_t i = range.x + threadIdx.x; i < range.y; i += blockDim.x) {
+            const float4 L = b.leaves[i];
+            if (kWrite) {
+                walk_line(
+                    w, L.x, L.y, L.z, L.w, [&](int32_t local, uint2 q) { b.fills[atomicAdd(&cnt[local], 1u)] = q; },
+                    [&](int32_t, int) {}, &b.status[kStErr]);
+            } else {
+                walk_line(
+                    w, L.x, L.y, L.z, L.w, [&](int32_t local, uint2) { atomicAdd(&cnt[local], 1u); },
+                    [&](int32_t where, int d) {
+                        if (where >= 0) atomicAdd(&dlt[where], d);
+                        else atomicAdd(&above[-1 - where], d);
+                    },
+                    &b.status[kStErr]);
+            }
+        }
+        __syncthreads();
+        for (uint32_t t = threadIdx.x; t < T; t += blockDim.x) {
+            b.tile_fills[tb + t] = cnt[t];
+            if (!kWrite) b.tile_delta[tb + t] = dlt[t];
+        }
+        if (!kWrite)
+            for (uint32_t x = threadIdx.x; x < (uint32_t)w.rw; x += blockDim.x) b.col_above[cb + x] = above[x];
+        (void)kCols;
+        __syncthreads();
+    }
+}
+
+// Zero the tile counters of the paths too large for a CTA (the global pass adds into them).
+__global__ void k_bin_zero_large(Batch b) {
+    __shared__ uint32_t s_item;
+    const uint32_t *list = b.bin_list + (size_t)3 * b.n_paths;
+    const uint32_t n_items = b.bin_ctl[kCtlCount + 3];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&b.bin_ctl[kCtlTicketZero], 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        __syncthreads();
+        if (item >= n_items) return;
+        const PathDev P = b.paths[list[item]];
+        const uint32_t rw = (uint32_t)(P.rx1 - P.rx0), T = rw * (uint32_t)(P.ry1 - P.ry0);
+        for (uint32_t t = threadIdx.x; t < T; t += blockDim.x) {
+            b.tile_fills[P.tile_first + t] = 0;
+            b.tile_delta[P.tile_first + t] = 0;
+        }
+        for (uint32_t x = threadIdx.x; x < rw; x += blockDim.x) b.col_above[P.col_first + x] = 0;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1103,9 +1240,51 @@ cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream
     return cudaGetLastError();
 }
 
-cudaError_t launch_flatten_bin_count(const Batch &b, uint32_t n_segs, cudaStream_t st) {
-    if (n_segs) PF_LAUNCH(k_flatten_bin_count<<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
+cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t st) {
+    if (n_segs) PF_LAUNCH(k_flatten_budget<<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
     return cudaGetLastError();
+}
+
+cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st) {
+    if (b.n_paths) PF_LAUNCH(k_bin_classify<<<grid_for(b.n_paths), kThreads, 0, st>>>(b, learned));
+    return cudaGetLastError();
+}
+
+template <bool kWrite, int kCls>
+static cudaError_t launch_class(const Batch &b, int sms, cudaStream_t st) {
+    const size_t smem = (2 * size_t(class_tiles(kCls)) + std::min<uint32_t>(class_tiles(kCls), kMaxCols)) * 4;
+    static bool configured = false;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_bin_paths<kWrite, kCls>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin_paths<kWrite, kCls>, class_threads(kCls), smem);
+    const unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)sms;
+    PF_LAUNCH(k_bin_paths<kWrite, kCls><<<grid, class_threads(kCls), smem, st>>>(b));
+    return cudaGetLastError();
+}
+
+// Count pass: per-path CTAs, zero the large paths, then the global pass (large paths, pool).
+// Write pass: per-path CTAs, then the global pass.
+cudaError_t launch_bin_paths(const Batch &b, bool write, uint32_t n_leaf_slots, cudaStream_t st) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e;
+    if (!write) {
+        if ((e = launch_class<false, 0>(b, sms, st)) != cudaSuccess) return e;
+        if ((e = launch_class<false, 1>(b, sms, st)) != cudaSuccess) return e;
+        if ((e = launch_class<false, 2>(b, sms, st)) != cudaSuccess) return e;
+        PF_LAUNCH(k_bin_zero_large<<<sms * 4, 256, 0, st>>>(b));
+    } else {
+        if ((e = launch_class<true, 0>(b, sms, st)) != cudaSuccess) return e;
+        if ((e = launch_class<true, 1>(b, sms, st)) != cudaSuccess) return e;
+        if ((e = launch_class<true, 2>(b, sms, st)) != cudaSuccess) return e;
+    }
+    return launch_bin(b, n_leaf_slots, write, st);
 }
 
 cudaError_t launch_propagate(const Batch &b, uint32_t n_cols, cudaStream_t st) {

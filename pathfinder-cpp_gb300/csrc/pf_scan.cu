@@ -21,7 +21,7 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;                               // 4 x uint4 per thread
 constexpr uint32_t kScanTile = kScanThreads * kScanItems;  // 4096
 constexpr uint64_t kFlagAgg = 1ull << 62, kFlagInc = 2ull << 62, kValMask = (1ull << 62) - 1;
-constexpr uint32_t kSpinLimit = 1u << 24;
+constexpr uint32_t kSpinLimit = 1u << 20;
 
 __device__ __forceinline__ uint32_t warp_inclusive(uint32_t v) {
     const int lane = threadIdx.x & 31;
@@ -70,32 +70,41 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(const uint32_t *in, uint3
         const uint32_t wi = warp_inclusive(w);
         if (lane < kScanThreads / 32) warp_sums[lane] = wi - w;
         const uint32_t agg = __shfl_sync(0xffffffffu, wi, kScanThreads / 32 - 1);
-        // publish, look back, publish the inclusive prefix
-        if (lane == 0) {
-            volatile unsigned long long *st = state + 1;
-            if (tile == 0) {
+        // publish the aggregate, then look back over a window of 32 predecessors at a time
+        // (lane l reads tile `base - l`); stop at the nearest inclusive prefix
+        volatile unsigned long long *st = state + 1;
+        if (tile == 0) {
+            if (lane == 0) {
                 st[0] = kFlagInc | agg;
                 s_prefix = 0;
-            } else {
-                st[tile] = kFlagAgg | agg;
-                uint64_t prefix = 0;
-                int64_t t = (int64_t)tile - 1;
-                uint32_t spins = 0;
-                while (t >= 0) {
-                    const unsigned long long s = st[t];
-                    const uint64_t flag = s & ~kValMask;
-                    if (flag == 0) {
-                        if (++spins > kSpinLimit) {
-                            atomicOr(err, kErrScanWait);
-                            break;
-                        }
-                        continue;
+            }
+        } else {
+            if (lane == 0) st[tile] = kFlagAgg | agg;
+            uint64_t prefix = 0;
+            int64_t base = (int64_t)tile - 1;
+            uint32_t spins = 0;
+            for (;;) {
+                const int64_t idx = base - lane;
+                const unsigned long long sv = idx >= 0 ? st[idx] : kFlagInc;
+                const uint64_t flag = sv & ~kValMask;
+                const uint32_t inc_mask = __ballot_sync(0xffffffffu, flag == kFlagInc);
+                const uint32_t wait_mask = __ballot_sync(0xffffffffu, flag == 0);
+                const uint32_t upto = inc_mask ? (inc_mask & (0u - inc_mask)) * 2u - 1u : 0xffffffffu;
+                if (wait_mask & upto) {
+                    if (++spins > kSpinLimit) {
+                        if (lane == 0) atomicOr(err, kErrScanWait);
+                        break;
                     }
-                    prefix += s & kValMask;
-                    if (flag == kFlagInc) break;
-                    t--;
+                    continue;
                 }
-                __threadfence();
+                uint64_t v = (upto >> lane) & 1u ? (sv & kValMask) : 0;
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+                prefix += v;
+                if (inc_mask) break;
+                base -= 32;
+            }
+            if (lane == 0) {
                 st[tile] = kFlagInc | (prefix + agg);
                 s_prefix = (uint32_t)prefix;
             }
