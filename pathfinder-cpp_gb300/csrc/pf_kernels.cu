@@ -642,14 +642,17 @@ __global__ void __launch_bounds__(kThreads) k_flatten_budget(Batch b, uint32_t n
 // shape; paths above the largest class, and leaves in a learned frame's spill pool, go
 // through the per-leaf global-atomic k_bin.
 
-__host__ __device__ constexpr uint32_t class_tiles(int c) { return c == 0 ? 1024u : c == 1 ? 4096u : 16384u; }
-__host__ __device__ constexpr int class_threads(int c) { return c == 2 ? 1024 : 256; }
+// Classes 0 and 1 are binned by CTAs; a CTA for larger rects would need so much shared memory
+// that too few fit on an SM, so class 2 and above use the per-leaf global pass.
+__host__ __device__ constexpr uint32_t class_tiles(int c) { return c == 0 ? 1024u : 4096u; }
+__host__ __device__ constexpr int class_threads(int) { return 256; }
 constexpr uint32_t kMaxCols = 4096;  // widest tile rect (65536 px canvas)
+static_assert(class_tiles(1) <= 4096, "a class-1 rect fits the column buffer");
 // bin_ctl slots
 enum : int { kCtlCount = 0, kCtlTicketCount = 4, kCtlTicketWrite = 8, kCtlTicketZero = 12 };
 
 __device__ __forceinline__ int size_class(uint32_t tiles) {
-    return tiles <= class_tiles(0) ? 0 : tiles <= class_tiles(1) ? 1 : tiles <= class_tiles(2) ? 2 : 3;
+    return tiles <= class_tiles(0) ? 0 : tiles <= class_tiles(1) ? 1 : 3;
 }
 
 // -1: no columns (nothing to bin); 3: binned by the global pass (too many tiles for a CTA, or
@@ -1277,12 +1280,10 @@ cudaError_t launch_bin_paths(const Batch &b, bool write, uint32_t n_leaf_slots, 
     if (!write) {
         if ((e = launch_class<false, 0>(b, sms, st)) != cudaSuccess) return e;
         if ((e = launch_class<false, 1>(b, sms, st)) != cudaSuccess) return e;
-        if ((e = launch_class<false, 2>(b, sms, st)) != cudaSuccess) return e;
         PF_LAUNCH(k_bin_zero_large<<<sms * 4, 256, 0, st>>>(b));
     } else {
         if ((e = launch_class<true, 0>(b, sms, st)) != cudaSuccess) return e;
         if ((e = launch_class<true, 1>(b, sms, st)) != cudaSuccess) return e;
-        if ((e = launch_class<true, 2>(b, sms, st)) != cudaSuccess) return e;
     }
     return launch_bin(b, n_leaf_slots, write, st);
 }
