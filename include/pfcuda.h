@@ -205,6 +205,18 @@ int pf_sizer_get_params(void *ctx, float *params, size_t n);
 int pf_sizer_set_margin(void *ctx, float mul, float add, float pool_fraction);
 int pf_sizer_last_frame(void *ctx, uint32_t *paths_over_budget, uint32_t *pool_slots_used);
 int pf_sizer_predict(void *ctx, const float *features, uint32_t n, float *out);
+
+/*
+ * pf_sizer_predict without any device allocation, for callers that cannot call cudaMalloc
+ * (a render loop that must not stall the device, a CUDA-graph capture in progress, or GPU
+ * memory owned by another allocator).  No counterpart in the reference.  Features and
+ * predictions are staged in a fixed device array of 16384 paths (about 0.9 MB, held by every
+ * GPU that loads the library until exit); larger n is rejected with PF_ERR_INVALID_ARGUMENT.
+ * The first call on a device looks the array up (cudaGetSymbolAddress) - make it before any
+ * stream capture.  Calls share the array: calls whose GPU work overlaps race; serialise them.
+ * The context must already hold sizer weights.
+ */
+int pf_sizer_predict_noalloc(void *ctx, const float *features, uint32_t n, float *out);
 int pf_sizer_gradient(void *ctx, const float *features, const float *targets, uint32_t n, float *grad,
                       float *loss);
 int pf_sizer_train(void *ctx, const float *features, const float *targets, uint32_t n, uint32_t epochs,

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1287,3 +1288,69 @@ int pf_render_learned(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_fra
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Sizer prediction that allocates nothing.
+//
+// Some callers cannot call cudaMalloc: a render loop that plans the next frame's buffers
+// while it must not stall the device (cudaMalloc can synchronise it), code recording a
+// CUDA-graph capture (a plain cudaMalloc is not allowed there), or a host whose GPU memory
+// belongs to another allocator (an engine's own pool) and may not grow.  For them this
+// variant of pf_sizer_predict stages features and predictions in a fixed, file-scope device
+// array instead of context buffers.  It needs a context that already holds sizer weights
+// (pf_sizer_load / pf_sizer_init, which do allocate, once).
+//
+// Limit: kNoAllocMaxPaths paths per call (the array is (12 + 2) floats per path, about
+// 0.9 MB, and every GPU that loads this library keeps it until the process exits).
+// The first call on a device looks up the array's device address (cudaGetSymbolAddress, with
+// that device current); make that first call before any stream capture.  All calls share the
+// array and it keeps the last call's contents; nothing in it has to start at zero (each call
+// overwrites the rows it uses).  Calls whose GPU work overlaps - from two threads, or on two
+// streams - race on the array: serialise them.
+
+namespace {
+
+constexpr uint32_t kNoAllocMaxPaths = 16384;
+static __device__ __align__(256) float g_sizer_noalloc_scratch[kNoAllocMaxPaths * (kSizerIn + kSizerOut)];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+float *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// device address of the scratch array on `device` (looked up once per device)
+cudaError_t noalloc_scratch(int device, float **out) {
+    if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_sizer_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[device] = static_cast<float *>(p);
+    }
+    *out = g_noalloc_ptr[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int pf_sizer_predict_noalloc(void *ctx, const float *features, uint32_t n, float *out) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    if (n && (!features || !out)) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (n > kNoAllocMaxPaths) {
+        return fail(c, PF_ERR_INVALID_ARGUMENT,
+                    "pf_sizer_predict_noalloc: " + std::to_string(n) + " paths exceed its limit of " +
+                        std::to_string(kNoAllocMaxPaths) + " per call");
+    }
+    if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights");
+    if (n == 0) return PF_OK;
+    PF_CUDA(cudaSetDevice(c->device));
+    float *scratch = nullptr;
+    PF_CUDA(noalloc_scratch(c->device, &scratch));
+    float *feat = scratch, *pred = scratch + size_t(kNoAllocMaxPaths) * kSizerIn;
+    PF_CUDA(cudaMemcpyAsync(feat, features, size_t(n) * kSizerIn * 4, cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(launch_mlp_predict(c->sz_w.as<__nv_bfloat16>(), feat, n, pred, c->stream));
+    PF_CUDA(cudaMemcpyAsync(out, pred, size_t(n) * kSizerOut * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}

@@ -29,7 +29,7 @@ EXPORTS = [
     "pf_image_bytes", "pf_image_offset", "pf_read_images", "pf_render_learned", "pf_sizer_param_count",
     "pf_sizer_init", "pf_sizer_set_params", "pf_sizer_get_params", "pf_sizer_set_margin", "pf_sizer_predict",
     "pf_sizer_gradient", "pf_sizer_train", "pf_sizer_save", "pf_sizer_load", "pf_path_features", "pf_path_counts",
-    "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags",
+    "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags", "pf_sizer_predict_noalloc",
 ]
 
 N_FEATURES = 12
