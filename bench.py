@@ -46,6 +46,9 @@ def parse_args():
     ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--cpu-sample-every", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-frames", action="store_true",
+                    help="only the batched exact and learned frames (warm-up + steps each), a short summary "
+                         "line instead of the benchmark line: the command the committed launch lists profile")
     return ap.parse_args()
 
 
@@ -266,6 +269,13 @@ def main():
         sizer = {"frames_redone_exactly": int(sum(s["overflow"] for s in stats_b)), "paths_over_budget": over,
                  "spill_pool_slots_used": pool, "host_syncs": st["host_syncs"],
                  "exact_host_syncs": stats_e[-1]["host_syncs"]}
+
+    if args.profile_frames:
+        if rank == 0:
+            print(json.dumps({"profile_frames": True, "exact_ms": ms_exact, "learned_ms": ms_batched,
+                              "exact_stats": stats_e[-1], "learned_stats": st}), flush=True)
+        r.close()
+        return
 
     # 3. plain single-scene pipeline (one exact frame per scene), inputs resident
     def plain_pass():

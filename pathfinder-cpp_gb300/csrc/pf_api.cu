@@ -89,8 +89,8 @@ struct Ctx {
     bool sz_ready = false;
     float sz_mul = 1.25f, sz_add = 8.0f, sz_pool = 0.10f;
     uint32_t last_paths_over = 0, last_pool_used = 0;
-    DevBuf segs, seg_leaves, leaves, leaf_path;
-    DevBuf tile_fills, tile_delta, tile_state, col_above, col_final, fills;
+    DevBuf segs, seg_leaves, leaves, pool_path, pool_cnt, pool_idx;
+    DevBuf tile_fills, tile_state, col_above, col_final, fills, path_fill, path_cls;
     DevBuf row_first, row_paths, scene_row_first;
     DevBuf z, fb_count, list, image, status, scan_temp;
     uint32_t *h_status = nullptr;  // pinned
@@ -98,7 +98,9 @@ struct Ctx {
     // the scene range of the last frame and its totals
     uint32_t r_first = 0, r_count = 0, r_paths = 0, r_contours = 0, r_fb = 0, r_rows = 0;
     uint32_t r_path_base = 0, r_contour_base = 0, r_fb_base = 0, r_row_base = 0;
-    uint32_t n_segs = 0, n_tiles = 0, n_cols = 0, n_leaves = 0, n_fills = 0, n_list = 0, n_row_entries = 0;
+    uint32_t n_segs = 0, n_tiles = 0, n_cols = 0, n_leaves = 0, n_list = 0, n_row_entries = 0;
+    uint64_t n_fills = 0;
+    uint64_t fill_hint = 0;  // fills of the largest frame so far: the next frame's starting capacity
     bool lists_dumped = false;
     std::vector<uint32_t> h_scene_row_first;
     uint32_t syncs = 0;
@@ -326,10 +328,13 @@ Batch make_batch(Ctx *c) {
     b.seg_cap = (uint32_t)std::min<size_t>(c->segs.cap / sizeof(SegDev), 0xffffffffu);
     b.seg_leaves = c->seg_leaves.as<uint32_t>();
     b.leaves = c->leaves.as<float4>();
-    b.leaf_path = c->leaf_path.as<uint32_t>();
-    b.leaf_cap = (uint32_t)std::min<size_t>(std::min(c->leaves.cap / 16, c->leaf_path.cap / 4), 0xffffffffu);
-    b.tile_fills = c->tile_fills.p ? c->tile_fills.as<uint32_t>() + 1 : nullptr;
-    b.tile_delta = c->tile_delta.as<int32_t>();
+    b.leaf_cap = (uint32_t)std::min<size_t>(c->leaves.cap / 16, 0xffffffffu);
+    b.pool_path = nullptr;  // set by a learned frame
+    b.pool_cnt = nullptr;
+    b.pool_idx = nullptr;
+    b.tile_fills = c->tile_fills.as<uint32_t>();
+    b.path_fill = c->path_fill.as<uint32_t>();
+    b.path_cls = c->path_cls.as<uint8_t>();
     b.tile_state = c->tile_state.as<uint16_t>();
     b.col_above = c->col_above.as<int32_t>();
     b.col_final = c->col_final.as<int32_t>();
@@ -415,7 +420,9 @@ int begin_frame(Ctx *c, uint32_t first, uint32_t count) {
     PF_CUDA(c->path_contours.ensure(size_t(N) * 8 + 8));
     PF_CUDA(c->path_bounds.ensure(size_t(N) * 16 + 16));
     PF_CUDA(c->row_first.ensure((size_t(c->r_rows) + 1) * 4));
-    PF_CUDA(c->bin_list.ensure(size_t(N) * 16 + 16));
+    PF_CUDA(c->bin_list.ensure(size_t(N) * 20 + 16));
+    PF_CUDA(c->path_fill.ensure(size_t(N) * 4 + 16));
+    PF_CUDA(c->path_cls.ensure(size_t(N) + 16));
     PF_CUDA(c->bin_ctl.ensure(64));
     PF_CUDA(c->path_leaf_range.ensure(size_t(N) * 8 + 16));
     return PF_OK;
@@ -470,17 +477,53 @@ int stage_setup(Ctx *c, bool learned) {
     PF_CUDA(c->seg_leaves.ensure((size_t(c->n_segs) + 1) * 4));
     PF_CUDA(c->row_paths.ensure(size_t(c->n_row_entries) * 16 + 16));
     const size_t T = c->n_tiles, K = c->n_cols;
-    PF_CUDA(c->tile_fills.ensure((T + 2) * 4));
-    PF_CUDA(c->tile_delta.ensure(T * 4 + 4));
+    PF_CUDA(c->tile_fills.ensure(T * 4 + 16));
     PF_CUDA(c->tile_state.ensure(T * 2 + 16));
     PF_CUDA(c->col_above.ensure(K * 4 + 4));
     PF_CUDA(c->col_final.ensure(K * 4 + 4));
     return PF_OK;
 }
 
+// Binning and composite of a frame whose leaf lines are in place.  The fills buffer starts
+// at the largest frame's size (or about three fills per line); a frame that overruns it is
+// counted to the exact total, the buffer grows, and binning and composite run again.  Ends
+// with the status words read back.
+int bin_and_composite(Ctx *c, Batch b, bool learned) {
+    cudaStream_t st = c->stream;
+    for (int attempt = 0;; attempt++) {
+        PF_CUDA(cudaMemsetAsync(b.bin_ctl, 0, 64, st));
+        PF_CUDA(cudaMemsetAsync(b.status + kStFill64, 0, 8, st));
+        PF_CUDA(launch_bin_classify(b, learned, st));
+        PF_CUDA(launch_bin_paths(b, st));
+        record(c, 3);
+        record(c, 4);
+        record(c, 5);
+        PF_CUDA(launch_composite(b, st));
+        record(c, 6);
+        if (int e = read_status(c)) return e;
+        const uint32_t err = c->h_status[kStErr];
+        const uint64_t need = uint64_t(c->h_status[kStFill64]) | uint64_t(c->h_status[kStFill64 + 1]) << 32;
+        if (!(err & kErrOverflowFill) || (err & kErrOverflowLeaf)) {
+            c->n_fills = need;
+            c->fill_hint = std::max(c->fill_hint, need);
+            return PF_OK;
+        }
+        if (attempt > 0 || need >= 0xffffffffull)
+            return fail(c, PF_ERR_OVERFLOW, "the frame's fills exceed what one frame can index (2^32)");
+        PF_CUDA(c->fills.ensure(need * 8 + 16));
+        c->fill_hint = std::max(c->fill_hint, need);
+        b.fills = c->fills.as<uint2>();
+        b.fill_cap = (uint32_t)std::min<size_t>(c->fills.cap / 8, 0xffffffffu);
+        // clear the error word and the composite's counters before the second run
+        const uint32_t zero = 0;
+        for (int slot : {(int)kStErr, (int)kStListFills, (int)kStEntries, (int)kStWalkChunks})
+            PF_CUDA(cudaMemcpyAsync(b.status + slot, &zero, 4, cudaMemcpyHostToDevice, st));
+    }
+}
+
+// Statistics of the frame; the status words were read back by bin_and_composite.
 int finish_frame(Ctx *c, uint32_t first, uint32_t count, uint64_t launches0, pf_frame_stats *stats) {
     const uint32_t NFB = c->r_fb;
-    if (int e = read_status(c)) return e;
     if (int e = check_kernel_status(c)) return e;
     c->n_list = c->h_status[kStEntries];
     c->rendered = true;
@@ -534,36 +577,15 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     if (int e = check_kernel_status(c)) return e;
     c->n_leaves = c->h_status[kStLeaves];
     PF_CUDA(c->leaves.ensure(size_t(c->n_leaves) * 16 + 16));
-    PF_CUDA(c->leaf_path.ensure(size_t(c->n_leaves) * 4 + 16));
     b = make_batch(c);
     PF_CUDA(launch_flatten(b, c->n_segs, true, st));
     record(c, 2);
 
-    // 3. fill counts per tile, then fills written grouped by tile (counting sort); paths are
-    //    binned by CTAs owning their tiles, so the tile counters need no clearing
-    const size_t T = c->n_tiles, K = c->n_cols;
-    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, 4, st));  // tile_fills[-1]
-    PF_CUDA(cudaMemsetAsync(b.tile_fills + T, 0, 4, st));
-    PF_CUDA(cudaMemsetAsync(b.col_above, 0, K * 4, st));
-    PF_CUDA(cudaMemsetAsync(b.bin_ctl, 0, 64, st));
-    PF_CUDA(launch_bin_classify(b, false, st));
-    PF_CUDA(launch_bin_paths(b, false, c->n_leaves, st));
-    if (int e = scan(c, b.tile_fills, (uint32_t)T + 1, kStFills)) return e;
-    if (int e = read_status(c)) return e;
-    if (int e = check_kernel_status(c)) return e;
-    c->n_fills = c->h_status[kStFills];
-    PF_CUDA(c->fills.ensure(size_t(c->n_fills) * 8 + 16));
+    // 3. binning (one CTA per path: counts, backdrops, fill offsets, fills grouped by tile),
+    //    then coverage and the front-to-back composite with the z-cull walk
+    PF_CUDA(c->fills.ensure(std::max<uint64_t>(c->fill_hint, uint64_t(c->n_leaves) * 3) * 8 + 16));
     b = make_batch(c);
-    PF_CUDA(launch_bin_paths(b, true, c->n_leaves, st));
-    record(c, 3);
-
-    // 4. backdrops
-    PF_CUDA(launch_propagate(b, c->n_cols, st));
-    record(c, 4);
-    record(c, 5);
-    // 5. coverage + front-to-back composite with the z-cull walk
-    PF_CUDA(launch_composite(b, st));
-    record(c, 6);
+    if (int e = bin_and_composite(c, b, false)) return e;
     return finish_frame(c, first, count, launches0, stats);
 }
 
@@ -583,50 +605,39 @@ int render_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats
     const uint64_t leaf_regions = c->h_status[kStLeafBudget];
     const uint64_t leaf_pool = uint64_t(double(leaf_regions) * c->sz_pool) + 4096;
     const uint64_t leaf_slots = leaf_regions + leaf_pool;
-    const uint64_t fill_cap = uint64_t(c->h_status[kStFillBudget]);
-    if (leaf_slots >= 0xffffffffull || fill_cap >= 0xffffffffull) return render_exact(c, first, count, stats);
+    const uint64_t fill_pred = uint64_t(c->h_status[kStFillBudget]);
+    if (leaf_slots >= 0xffffffffull) return render_exact(c, first, count, stats);
+    const uint32_t N = c->r_paths;
     PF_CUDA(c->leaves.ensure(leaf_slots * 16 + 16));
-    PF_CUDA(c->leaf_path.ensure(leaf_slots * 4 + 16));
-    PF_CUDA(c->fills.ensure(std::max<uint64_t>(fill_cap, 1) * 8 + 16));
+    PF_CUDA(c->pool_path.ensure(leaf_pool * 4 + 16));
+    PF_CUDA(c->pool_idx.ensure(leaf_pool * 4 + 16));
+    PF_CUDA(c->pool_cnt.ensure((size_t(N) + 2) * 4));
+    PF_CUDA(c->fills.ensure(std::min<uint64_t>(std::max(fill_pred, c->fill_hint), 0xfffffffeull) * 8 + 16));
     record(c, 1);
 
-    const size_t T = c->n_tiles, K = c->n_cols;
     Batch b = make_batch(c);
-    b.fill_cap = (uint32_t)std::min<uint64_t>(fill_cap, b.fill_cap);  // the predicted capacity is the limit
     b.leaf_pool_first = (uint32_t)leaf_regions;
     b.leaf_pool_cap = (uint32_t)leaf_pool;
+    b.pool_path = c->pool_path.as<uint32_t>();
+    b.pool_idx = c->pool_idx.as<uint32_t>();
     PF_CUDA(launch_contour_segments(b, true, st));
     PF_CUDA(launch_rows(b, true, st));
-    PF_CUDA(cudaMemsetAsync(b.leaf_path, 0xff, leaf_slots * 4, st));
-    PF_CUDA(cudaMemsetAsync(c->tile_fills.p, 0, 4, st));  // tile_fills[-1]
-    PF_CUDA(cudaMemsetAsync(b.tile_fills + T, 0, 4, st));
-    PF_CUDA(cudaMemsetAsync(b.col_above, 0, K * 4, st));
-    PF_CUDA(cudaMemsetAsync(b.bin_ctl, 0, 64, st));
     PF_CUDA(launch_flatten_budget(b, c->n_segs, st));
     record(c, 2);
-    // the leaf slots (regions with gaps, then the pool) are what the global pass walks
-    const uint32_t slots32 = (uint32_t)leaf_slots;
-    PF_CUDA(cudaMemcpyAsync(b.status + kStLeaves, &slots32, 4, cudaMemcpyHostToDevice, st));
-    PF_CUDA(launch_bin_classify(b, true, st));
-    PF_CUDA(launch_bin_paths(b, false, slots32, st));
-    if (int e = scan(c, b.tile_fills, (uint32_t)T + 1, kStFills)) return e;
-    PF_CUDA(launch_bin_paths(b, true, slots32, st));
-    record(c, 3);
-    PF_CUDA(launch_propagate(b, c->n_cols, st));
-    record(c, 4);
-    record(c, 5);
-    PF_CUDA(launch_composite(b, st));
-    record(c, 6);
-    if (int e = read_status(c)) return e;
-    const uint32_t err = c->h_status[kStErr];
-    if (err & (kErrOverflowLeaf | kErrOverflowFill)) {
-        // a prediction was too small: redo the frame exactly
+    // the spill pool's lines listed by path, so each path's CTA finds them
+    PF_CUDA(cudaMemsetAsync(c->pool_cnt.p, 0, (size_t(N) + 2) * 4, st));
+    b.pool_cnt = c->pool_cnt.as<uint32_t>() + 1;
+    PF_CUDA(launch_pool_lists(b, false, st));
+    if (int e = scan(c, b.pool_cnt, N + 1, kStPoolListed)) return e;
+    PF_CUDA(launch_pool_lists(b, true, st));
+    if (int e = bin_and_composite(c, b, true)) return e;
+    if (c->h_status[kStErr] & kErrOverflowLeaf) {
+        // a path overran its leaf region and the pool: redo the frame exactly
         const int e = render_exact(c, first, count, stats);
         if (stats) stats->overflow = 1;
         return e;
     }
     c->n_leaves = c->h_status[kStLeafCount];
-    c->n_fills = c->h_status[kStFills];
     c->last_paths_over = c->h_status[kStPathsOver];
     c->last_pool_used = c->h_status[kStPoolUsed];
     const int e = finish_frame(c, first, count, launches0, stats);
@@ -693,10 +704,12 @@ int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
         h.tile_first[p] = tf[p] - t0;
         h.col_first[p] = cf[p] - k0;
     }
-    // after the fill write pass the fills of tile t are [tile_fills[t - 1], tile_fills[t])
-    std::vector<uint32_t> tend;
+    // every path's fills are one block from path_fill[p], grouped by tile; tile_fills[t] is one
+    // past the last fill of tile t
+    std::vector<uint32_t> tend, pfill;
     std::vector<uint16_t> state;
-    if (int e = d2h(c, tend, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0) + 1)) return e;
+    if (int e = d2h(c, tend, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0))) return e;
+    if (int e = d2h(c, pfill, c->path_fill.as<uint32_t>() + p0, np)) return e;
     if (int e = d2h(c, state, c->tile_state.as<uint16_t>() + t0, t1 - t0)) return e;
     if (int e = d2h(c, h.col_backdrop, c->col_final.as<int32_t>() + k0, k1 - k0)) return e;
     if (int e = d2h(c, h.z, c->z.as<int32_t>() + fb0, size_t(S.fbw) * S.fbh)) return e;
@@ -704,12 +717,30 @@ int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
     if (int e = d2h(c, fbc, c->fb_count.as<uint32_t>() + fb0, size_t(S.fbw) * S.fbh + 1)) return e;
     PF_CUDA(cudaStreamSynchronize(c->stream));
     const size_t nt = t1 - t0;
-    const uint32_t f0 = tend[0], f1 = tend[nt];  // tend[k] = tile_fills[t0 - 1 + k]
-    std::vector<uint2> fl;
-    if (int e = d2h(c, fl, c->fills.as<uint2>() + f0, f1 - f0)) return e;
+    // gather the paths' blocks in path order (one copy per run of blocks adjacent on the device)
+    std::vector<uint64_t> blk(np + 1, 0);
+    for (uint32_t p = 0; p < np; p++) {
+        const uint32_t a = tf[p] - t0, e = tf[p + 1] - t0;
+        blk[p + 1] = blk[p] + (e > a ? tend[e - 1] - pfill[p] : 0u);
+    }
+    std::vector<uint2> fl(blk[np]);
+    for (uint32_t p = 0; p < np;) {
+        uint32_t q = p + 1;
+        while (q < np && pfill[q] == pfill[q - 1] + (blk[q] - blk[q - 1])) q++;
+        if (blk[q] > blk[p])
+            PF_CUDA(cudaMemcpyAsync(fl.data() + blk[p], c->fills.as<uint2>() + pfill[p], (blk[q] - blk[p]) * 8,
+                                    cudaMemcpyDeviceToHost, c->stream));
+        p = q;
+    }
     const uint32_t l0 = fbc[0], l1 = fbc[size_t(S.fbw) * S.fbh];
     if (int e = d2h(c, h.list, c->list.as<uint32_t>() + l0, l1 - l0)) return e;
     PF_CUDA(cudaStreamSynchronize(c->stream));
+    // tile t's fills in the gathered numbering: [begin[t], begin[t + 1])
+    std::vector<uint64_t> begin(nt + 1);
+    for (uint32_t p = 0; p < np; p++)
+        for (uint32_t t = tf[p] - t0; t < tf[p + 1] - t0; t++)
+            begin[t + 1] = blk[p] + (tend[t] - pfill[p]);
+    const uint64_t f0 = 0, f1 = blk[np];
 
     h.alpha.resize(nt);
     h.backdrop.resize(nt);
@@ -717,7 +748,7 @@ int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
     h.fills.resize(size_t(f1 - f0) * 4);
     std::vector<uint64_t> keys;
     for (size_t t = 0; t < nt; t++) {
-        const uint32_t a = tend[t] - f0, e = tend[t + 1] - f0;
+        const uint64_t a = begin[t] - f0, e = begin[t + 1] - f0;
         h.fill_count[t] = e - a;
         h.alpha[t] = (state[t] >> 8) & 1;
         h.backdrop[t] = (int8_t)(state[t] & 0xff);
@@ -860,8 +891,9 @@ int pf_ctx_destroy(void *ctx) {
                       &c->points, &c->pflags, &c->cstart, &c->pstart, &c->fill_rule, &c->color, &c->scenes,
                       &c->scene_path_first, &c->scene_contour_first, &c->scene_fb_first, &c->contour_point_first,
                       &c->contour_path, &c->paths, &c->path_tiles, &c->path_cols, &c->contour_segs,
-                      &c->path_contours, &c->segs, &c->seg_leaves, &c->leaves, &c->leaf_path, &c->tile_fills,
-                      &c->tile_delta, &c->tile_state, &c->col_above, &c->col_final, &c->fills, &c->row_first,
+                      &c->path_contours, &c->segs, &c->seg_leaves, &c->leaves, &c->pool_path, &c->pool_cnt,
+                      &c->pool_idx, &c->tile_fills, &c->path_fill, &c->path_cls, &c->tile_state, &c->col_above,
+                      &c->col_final, &c->fills, &c->row_first,
                       &c->row_paths, &c->scene_row_first, &c->z, &c->fb_count, &c->list, &c->image,
                       &c->status, &c->scan_temp};
     for (DevBuf *b : bufs) b->release();

@@ -113,15 +113,21 @@ struct Batch {
     uint32_t seg_cap;
     uint32_t *seg_leaves;                // [segs + 1] -> scanned
     float4 *leaves;
-    uint32_t *leaf_path;
     uint32_t leaf_cap;
+    // learned frame: the spill pool's lines listed by path.  pool_cnt points one past the start
+    // of its allocation (pool_cnt[-1] == 0); once listed, path p's pooled lines are
+    // pool_idx[pool_cnt[p - 1] .. pool_cnt[p]).  Null in an exact frame.
+    uint32_t *pool_path;                 // [pool cap] path of each pooled line
+    uint32_t *pool_cnt;                  // [-1 .. n_paths]
+    uint32_t *pool_idx;                  // [pool cap]
 
-    // tiles.  tile_fills points one past the start of its allocation, so tile_fills[-1] == 0:
-    // fill counts -> (scan) first fill of each tile -> (write pass, used as the cursor) one
-    // past the last fill; after the write pass the fills of tile t are
-    // [tile_fills[t - 1], tile_fills[t]).
-    uint32_t *tile_fills;                // [-1 .. tiles]
-    int32_t *tile_delta;                 // [tiles] summed backdrop deltas (bin)
+    // tiles.  Each path's fills are one block starting at path_fill[p], grouped by tile in the
+    // path's row-major tile order; tile_fills[t] is one past the last fill of tile t, so the
+    // fills of tile t are [t == the path's first tile ? path_fill[p] : tile_fills[t - 1],
+    // tile_fills[t]).  (Class-3 paths use tile_fills as counters, then cursors, on the way.)
+    uint32_t *tile_fills;                // [tiles]
+    uint32_t *path_fill;                 // [n_paths] first fill of each path
+    uint8_t *path_cls;                   // [n_paths] binning class (0xff: no columns)
     uint16_t *tile_state;                // [tiles] propagated int8 backdrop | alpha << 8
     int32_t *col_above;                  // [cols] deltas landing above the rect
     int32_t *col_final;                  // [cols]
@@ -143,7 +149,7 @@ struct Batch {
     uint32_t *list;
 
     uint8_t *image;                      // batch image buffer
-    uint32_t *status;                    // [16] error bits and totals
+    uint32_t *status;                    // [kStCount] error bits and totals
     uint32_t counters;                   // nonzero: the composite adds its work counters to status
 };
 
@@ -154,7 +160,7 @@ enum : int {
     kStTiles = 2,
     kStCols = 3,
     kStLeaves = 4,
-    kStFills = 5,
+    // slot 5 is unused (fills are counted in the 64-bit kStFill64)
     kStList = 6,
     kStListFills = 7,  // fills of the alpha tiles that made it into composite lists
     kStRows = 8,       // entries of the per-row path lists
@@ -165,7 +171,9 @@ enum : int {
     kStPoolUsed = 13,  // learned frame: leaf slots taken from the spill pool
     kStPathsOver = 14, // learned frame: paths that overran their leaf budget
     kStWalkChunks = 15,// composite: 32-candidate chunks walked (all framebuffer tiles)
-    kStCount = 16,
+    kStFill64 = 16,    // two words: fills reserved by the frame's paths (64-bit)
+    kStPoolListed = 18,// learned frame: pooled lines listed by path
+    kStCount = 20,
 };
 
 // Kernels launched by this library (host-side counter, all contexts).
@@ -183,8 +191,6 @@ cudaError_t launch_path_setup(const Batch &b, const uint2 *path_contours, cudaSt
 cudaError_t launch_path_offsets(const Batch &b, cudaStream_t st);
 cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st);
-cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream_t st);
-cudaError_t launch_propagate(const Batch &b, uint32_t n_cols, cudaStream_t st);
 cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_composite(const Batch &b, cudaStream_t st);
 cudaError_t launch_list_dump(const Batch &b, bool write, cudaStream_t st);
@@ -197,10 +203,12 @@ cudaError_t launch_budgets(const Batch &b, const float *pred, float mul, float a
 cudaError_t launch_path_counts(const Batch &b, const uint2 *path_contours, uint32_t *leaves, uint32_t *fills,
                                cudaStream_t st);
 cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t st);
-// Binning by path: classify (leaf ranges, size classes), then count or write.  `pool` is
-// true in a learned frame (leaves past the per-path regions are binned by the global pass).
+// Binning by path: classify (leaf ranges, size classes), then bin every path (counts,
+// backdrops, fill offsets, fills).  A learned frame first lists its pooled lines by path:
+// count, scan pool_cnt, scatter.
 cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st);
-cudaError_t launch_bin_paths(const Batch &b, bool write, uint32_t n_leaf_slots, cudaStream_t st);
+cudaError_t launch_bin_paths(const Batch &b, cudaStream_t st);
+cudaError_t launch_pool_lists(const Batch &b, bool scatter, cudaStream_t st);
 cudaError_t launch_mlp_predict(const __nv_bfloat16 *w, const float *feat, uint32_t n, float *out, cudaStream_t st);
 cudaError_t launch_mlp_grad(const __nv_bfloat16 *w, const float *feat, const float *target, const uint32_t *index,
                             uint32_t n, float *grad, float *loss, cudaStream_t st);

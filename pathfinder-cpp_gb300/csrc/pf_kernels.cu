@@ -5,9 +5,11 @@
 //   BuiltPath / round_rect_out_to_tile_bounds -> k_path_setup
 //   dice.comp (here: the d3d9 recursive bisection, tiler.cpp:284-315)  -> k_flatten<count|write>
 //   bin.comp (here: the d3d9 tile walk + add_fill, tiler.cpp:131-279,
-//             object_builder.cpp:19-114)        -> k_bin<count|write>
-//   bound.comp (tile records)                  -> memsets + per-tile counting sort (no linked lists)
-//   propagate.comp / Tiler::prepare_tiles       -> k_propagate
+//             object_builder.cpp:19-114),
+//   bound.comp (tile records), propagate.comp / Tiler::prepare_tiles
+//                                              -> k_bin_fused (one CTA per path: counts, backdrops,
+//                                                 offsets, fills grouped by tile; no linked lists);
+//                                                 k_bin_large* for rects too big for a CTA
 //   sort.comp                                  -> k_list_count / k_list_write / k_list_sort
 //   fill.comp + tile.comp                      -> k_composite (coverage never leaves the SM)
 //
@@ -355,10 +357,7 @@ __global__ void __launch_bounds__(kThreads) k_flatten(Batch b, uint32_t n_segs) 
     uint32_t out = kWrite ? b.seg_leaves[i] : 0u;
     uint32_t count = 0;
     auto emit = [&](float x0, float y0, float x1, float y1) {
-        if (kWrite) {
-            b.leaves[out + count] = make_float4(x0, y0, x1, y1);
-            b.leaf_path[out + count] = sg.path;
-        }
+        if (kWrite) b.leaves[out + count] = make_float4(x0, y0, x1, y1);
         count++;
     };
     const float2 p0 = b.points[sg.a];
@@ -523,50 +522,6 @@ __device__ void walk_line(const WalkCtx &w, float x0, float y0, float x1, float 
     }
 }
 
-__device__ __forceinline__ int path_class(const PathDev &P);
-
-template <bool kWrite>
-__global__ void __launch_bounds__(kThreads) k_bin(Batch b, uint32_t n_leaves) {
-    const uint32_t i = global_tid();
-    if (i >= n_leaves || i >= b.status[kStLeaves]) return;
-    if (kWrite && b.status[kStFills] > b.fill_cap) {
-        if (i == 0) atomicOr(&b.status[kStErr], kErrOverflowFill);
-        return;
-    }
-    const uint32_t p = b.leaf_path[i];
-    if (p == kNone) return;  // unused slot of a learned frame's leaf region
-    const PathDev P = b.paths[p];
-    // paths that fit a CTA are binned by k_bin_paths, except leaves in the spill pool
-    if (i < b.leaf_pool_first && path_class(P) < 3) return;
-    const float4 L = b.leaves[i];
-    const SceneDev &S = b.scenes[P.scene];
-    WalkCtx w;
-    w.rx0 = P.rx0;
-    w.ry0 = P.ry0;
-    w.rx1 = P.rx1;
-    w.ry1 = P.ry1;
-    w.rw = max(P.rx1 - P.rx0, 0);
-    w.rh = max(P.ry1 - P.ry0, 0);
-    w.vb_right = S.vb_right;
-    w.vb_bottom = S.vb_bottom;
-    const uint32_t tb = P.tile_first, cb = P.col_first;
-    if (kWrite) {
-        // tile_fills[t] holds the next free slot of tile t (counting sort, second pass)
-        walk_line(
-            w, L.x, L.y, L.z, L.w,
-            [&](int32_t local, uint2 q) { b.fills[atomicAdd(&b.tile_fills[tb + (uint32_t)local], 1u)] = q; },
-            [&](int32_t, int) {}, &b.status[kStErr]);
-    } else {
-        walk_line(
-            w, L.x, L.y, L.z, L.w, [&](int32_t local, uint2) { atomicAdd(&b.tile_fills[tb + (uint32_t)local], 1u); },
-            [&](int32_t where, int d) {
-                if (where >= 0) atomicAdd(&b.tile_delta[tb + (uint32_t)where], d);
-                else atomicAdd(&b.col_above[cb + (uint32_t)(-1 - where)], d);
-            },
-            &b.status[kStErr]);
-    }
-}
-
 // Learned frame: flatten one segment and store its leaf lines in the path's leaf region,
 // laid out from the sizer's budget (slots reserved eight at a time); lines past the budget
 // spill into the shared pool.  An exhausted pool sets the overflow bit and the frame is
@@ -585,10 +540,7 @@ __global__ void __launch_bounds__(kThreads) k_flatten_budget(Batch b, uint32_t n
         if (!npend) return;
         const uint32_t slot = atomicAdd(&b.path_leaf_cursor[sg.path], (uint32_t)npend);
         const uint32_t in_region = slot >= budget ? 0u : min((uint32_t)npend, budget - slot);
-        for (uint32_t k = 0; k < in_region; k++) {
-            b.leaves[region + slot + k] = pend[k];
-            b.leaf_path[region + slot + k] = sg.path;
-        }
+        for (uint32_t k = 0; k < in_region; k++) b.leaves[region + slot + k] = pend[k];
         if (in_region < (uint32_t)npend) {
             const uint32_t extra = (uint32_t)npend - in_region;
             if (slot <= budget && slot + npend > budget) atomicAdd(&b.status[kStPathsOver], 1u);
@@ -596,7 +548,7 @@ __global__ void __launch_bounds__(kThreads) k_flatten_budget(Batch b, uint32_t n
             for (uint32_t k = 0; k < extra; k++) {
                 if (q + k < b.leaf_pool_cap) {
                     b.leaves[b.leaf_pool_first + q + k] = pend[in_region + k];
-                    b.leaf_path[b.leaf_pool_first + q + k] = sg.path;
+                    b.pool_path[q + k] = sg.path;
                 } else {
                     atomicOr(&b.status[kStErr], kErrOverflowLeaf);
                 }
@@ -635,42 +587,106 @@ __global__ void __launch_bounds__(kThreads) k_flatten_budget(Batch b, uint32_t n
 }
 
 // ---------------------------------------------------------------------------
-// Binning by path.  A path's tiles belong to it alone, so one CTA can bin all of a path's
-// leaf lines with shared-memory counters (count pass) and shared-memory cursors (write pass)
-// and write its tiles' counts / deltas / end offsets out densely: no global atomics and no
-// memsets for those tiles.  Paths are bucketed by tile count; each class has its own CTA
-// shape; paths above the largest class, and leaves in a learned frame's spill pool, go
-// through the per-leaf global-atomic k_bin.
+// Binning by path (the d3d9 Tiler::process_line_segment walk and Tiler::prepare_tiles,
+// tiler.cpp:131-279 / 369-439, which the reference's GPU frame runs as bin.comp and
+// propagate.comp).  A path's tiles belong to it alone, so one CTA bins all of a path's leaf
+// lines in shared memory: it counts fills and backdrop deltas per tile, propagates the
+// backdrops down each column, scans the counts into fill offsets (reserving the path's block
+// of fills with one atomic), and walks the lines again to write the fills grouped by tile.
+// No tile needs clearing, there is no frame-wide scan over tiles and no global atomic per
+// fill.  Paths too large for a CTA (class 3) take global passes: counts with atomics, a CTA
+// per path for backdrops and offsets, then the writes with atomics.
 
-// Classes 0 and 1 are binned by CTAs; a CTA for larger rects would need so much shared memory
-// that too few fit on an SM, so class 2 and above use the per-leaf global pass.
-__host__ __device__ constexpr uint32_t class_tiles(int c) { return c == 0 ? 1024u : 4096u; }
-__host__ __device__ constexpr int class_threads(int) { return 256; }
-constexpr uint32_t kMaxCols = 4096;  // widest tile rect (65536 px canvas)
-static_assert(class_tiles(1) <= 4096, "a class-1 rect fits the column buffer");
-// bin_ctl slots
-enum : int { kCtlCount = 0, kCtlTicketCount = 4, kCtlTicketWrite = 8, kCtlTicketZero = 12 };
+// Size classes by shared-memory words: one per tile (fill count in bits 0-23, the int8 sum of
+// backdrop deltas in bits 24-31, later the tile's write cursor) and one per column (deltas
+// landing above the rect, summed as int32).
+constexpr int kCtaClasses = 3;
+__host__ __device__ constexpr uint32_t class_words(int c) { return c == 0 ? 1088u : c == 1 ? 4352u : 16896u; }
+__host__ __device__ constexpr int class_threads(int c) { return c == 2 ? 512 : 256; }
+// One line gives a tile at most two fills (the walk visits a tile once, with at most one
+// extra fill for a vertical crossing), so with at most 2^22 lines per CTA-binned path the
+// 24-bit counters cannot carry into the delta byte.
+constexpr uint32_t kCtaMaxLeaves = 1u << 22;
+// bin_ctl slots: paths per CTA class, work tickets per CTA class, tickets of the class-3
+// zeroing and set-up passes, and at slot 12 a 64-bit word: class-3 paths << 40 | their lines.
+enum : int { kCtlCount = 0, kCtlTicket = 4, kCtlTicketZero = 8, kCtlTicketPrep = 9, kCtl3 = 12 };
+constexpr uint64_t kLow40 = (1ull << 40) - 1;
 
-__device__ __forceinline__ int size_class(uint32_t tiles) {
-    return tiles <= class_tiles(0) ? 0 : tiles <= class_tiles(1) ? 1 : 3;
+__device__ __forceinline__ unsigned long long *ctl3_word(const Batch &b) {
+    return reinterpret_cast<unsigned long long *>(b.bin_ctl + kCtl3);
+}
+__device__ __forceinline__ unsigned long long *fill_total(const Batch &b) {
+    return reinterpret_cast<unsigned long long *>(b.status + kStFill64);
 }
 
-// -1: no columns (nothing to bin); 3: binned by the global pass (too many tiles for a CTA, or
-// columns but no tile rows, where only deltas above the rect can land)
-__device__ __forceinline__ int path_class(const PathDev &P) {
+// -1: no columns (nothing can land); 0-2: CTA classes; 3: global passes
+__device__ __forceinline__ int path_class(const PathDev &P, uint32_t leaves) {
     const int32_t rw = max(P.rx1 - P.rx0, 0), rh = max(P.ry1 - P.ry0, 0);
     if (rw == 0) return -1;
-    if (rh == 0) return 3;
-    return size_class((uint32_t)rw * (uint32_t)rh);
+    if (leaves > kCtaMaxLeaves) return 3;
+    const uint32_t words = (uint32_t)rw * (uint32_t)rh + (uint32_t)rw;
+    return words <= class_words(0) ? 0 : words <= class_words(1) ? 1 : words <= class_words(2) ? 2 : 3;
 }
 
+// The leaf lines of one path: its region of the leaf buffer, then (learned frame) its lines
+// in the spill pool, listed by k_pool_scatter.
+struct PathLeaves {
+    uint32_t first, nreg, pool0, n;
+    __device__ __forceinline__ uint32_t index(const Batch &b, uint32_t k) const {
+        return k < nreg ? first + k : b.leaf_pool_first + b.pool_idx[pool0 + (k - nreg)];
+    }
+};
+
+__device__ __forceinline__ PathLeaves path_leaves(const Batch &b, uint32_t p) {
+    const uint2 r = b.path_leaf_range[p];
+    PathLeaves L{r.x, r.y - r.x, 0u, r.y - r.x};
+    if (b.pool_cnt) {
+        L.pool0 = b.pool_cnt[(int64_t)p - 1];
+        L.n += b.pool_cnt[p] - L.pool0;
+    }
+    return L;
+}
+
+__device__ __forceinline__ WalkCtx walk_ctx(const Batch &b, const PathDev &P) {
+    const SceneDev &S = b.scenes[P.scene];
+    WalkCtx w;
+    w.rx0 = P.rx0;
+    w.ry0 = P.ry0;
+    w.rx1 = P.rx1;
+    w.ry1 = P.ry1;
+    w.rw = max(P.rx1 - P.rx0, 0);
+    w.rh = max(P.ry1 - P.ry0, 0);
+    w.vb_right = S.vb_right;
+    w.vb_bottom = S.vb_bottom;
+    return w;
+}
+
+// Adds an int8 delta to the low byte of a 16-bit tile state (class-3 count pass; the high
+// byte is still zero).  A compare-and-swap on the enclosing word: every failed round means
+// another thread's update went in, and the loop is bounded all the same.
+__device__ __forceinline__ void add_delta_u16(uint16_t *a, int d, uint32_t *status) {
+    uint32_t *word = reinterpret_cast<uint32_t *>(reinterpret_cast<uintptr_t>(a) & ~uintptr_t(3));
+    const int sh = (reinterpret_cast<uintptr_t>(a) & 2) ? 16 : 0;
+    uint32_t old = *word;
+    for (int it = 0; it < (1 << 20); it++) {
+        const uint32_t byte = ((old >> sh) + (uint32_t)d) & 0xffu;
+        const uint32_t want = (old & ~(0xffu << sh)) | (byte << sh);
+        const uint32_t seen = atomicCAS(word, old, want);
+        if (seen == old) return;
+        old = seen;
+    }
+    atomicOr(status, kErrWalk);
+}
+
+// Leaf ranges of every path and the size classes.  Classes 0-2 are listed with one atomic per
+// warp and class; class-3 paths take a 64-bit atomic that also hands out their offsets in the
+// class-3 line numbering the global passes stride over.
 __global__ void k_bin_classify(Batch b, bool learned) {
     const uint32_t p = global_tid();
     const int lane = threadIdx.x & 31;
     int cls = -1;
     if (p < b.n_paths) {
         const PathDev P = b.paths[p];
-        const uint32_t tiles = (uint32_t)max(P.rx1 - P.rx0, 0) * (uint32_t)max(P.ry1 - P.ry0, 0);
         uint2 range;
         if (learned) {
             const uint32_t f = b.path_leaf_first[p];
@@ -680,11 +696,20 @@ __global__ void k_bin_classify(Batch b, bool learned) {
             range = make_uint2(b.seg_leaves[b.contour_segs[pc.x]], b.seg_leaves[b.contour_segs[pc.y]]);
         }
         b.path_leaf_range[p] = range;
-        (void)tiles;
-        cls = path_class(P);
+        uint32_t n = range.y - range.x;
+        if (b.pool_cnt) n += b.pool_cnt[p] - b.pool_cnt[(int64_t)p - 1];
+        cls = path_class(P, n);
+        b.path_cls[p] = (uint8_t)cls;
+        if (cls < 0) b.path_fill[p] = 0;
+        if (cls == 3) {
+            const unsigned long long old = atomicAdd(ctl3_word(b), (1ull << 40) | (unsigned long long)n);
+            const uint32_t item = (uint32_t)(old >> 40);
+            b.bin_list[(size_t)3 * b.n_paths + item] = p;
+            b.bin_list[(size_t)4 * b.n_paths + item] = (uint32_t)(old & kLow40);
+        }
     }
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
+    for (int c = 0; c < kCtaClasses; c++) {
         const uint32_t m = __ballot_sync(0xffffffffu, cls == c);
         if (!m) continue;
         const int leader = __ffs(m) - 1;
@@ -695,122 +720,269 @@ __global__ void k_bin_classify(Batch b, bool learned) {
     }
 }
 
-template <bool kWrite, int kCls>
-__global__ void __launch_bounds__(class_threads(kCls)) k_bin_paths(Batch b) {
+template <int kCls>
+__global__ void __launch_bounds__(class_threads(kCls)) k_bin_fused(Batch b) {
+    constexpr int kThr = class_threads(kCls), kWarps = kThr / 32;
     extern __shared__ uint32_t sm[];
-    constexpr uint32_t kT = class_tiles(kCls);
-    constexpr uint32_t kCols = kT < kMaxCols ? kT : kMaxCols;
-    uint32_t *cnt = sm;                                           // counts, then cursors
-    int32_t *dlt = reinterpret_cast<int32_t *>(sm + kT);          // backdrop deltas
-    int32_t *above = reinterpret_cast<int32_t *>(sm + 2 * kT);    // deltas above the rect
-    __shared__ uint32_t s_item;
-    if (kWrite && b.status[kStFills] > b.fill_cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&b.status[kStErr], kErrOverflowFill);
-        return;
-    }
+    __shared__ uint32_t s_item, s_base, s_write;
+    __shared__ int32_t s_seg[kThr];
+    __shared__ uint32_t s_warp[kWarps];
+    __shared__ unsigned long long s_wsum[kWarps];
+    const uint32_t tid = threadIdx.x;
+    const int lane = (int)(tid & 31), warp = (int)(tid >> 5);
     const uint32_t *list = b.bin_list + (size_t)kCls * b.n_paths;
     const uint32_t n_items = b.bin_ctl[kCtlCount + kCls];
-    uint32_t *ticket = &b.bin_ctl[(kWrite ? kCtlTicketWrite : kCtlTicketCount) + kCls];
+    uint32_t *const err = &b.status[kStErr];
     for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(ticket, 1u);
+        if (tid == 0) s_item = atomicAdd(&b.bin_ctl[kCtlTicket + kCls], 1u);
         __syncthreads();
         const uint32_t item = s_item;
-        __syncthreads();
         if (item >= n_items) return;
         const uint32_t p = list[item];
         const PathDev P = b.paths[p];
-        const SceneDev &S = b.scenes[P.scene];
-        WalkCtx w;
-        w.rx0 = P.rx0;
-        w.ry0 = P.ry0;
-        w.rx1 = P.rx1;
-        w.ry1 = P.ry1;
-        w.rw = P.rx1 - P.rx0;
-        w.rh = P.ry1 - P.ry0;
-        w.vb_right = S.vb_right;
-        w.vb_bottom = S.vb_bottom;
-        const uint32_t T = (uint32_t)(w.rw * w.rh), tb = P.tile_first, cb = P.col_first;
-        const uint2 range = b.path_leaf_range[p];
-        if (!kWrite) {
-            for (uint32_t t = threadIdx.x; t < T; t += blockDim.x) {
-                cnt[t] = 0;
-                dlt[t] = 0;
-            }
-            for (uint32_t x = threadIdx.x; x < (uint32_t)w.rw; x += blockDim.x) above[x] = 0;
-        } else {
-            for (uint32_t t = threadIdx.x; t < T; t += blockDim.x) cnt[t] = b.tile_fills[tb + t];
+        const WalkCtx w = walk_ctx(b, P);
+        const uint32_t rw = (uint32_t)w.rw, rh = (uint32_t)w.rh, T = rw * rh, tb = P.tile_first, cb = P.col_first;
+        uint32_t *cnt = sm;                                   // per tile: count | delta << 24, then cursor
+        int32_t *above = reinterpret_cast<int32_t *>(sm + T);  // per column
+        const PathLeaves L = path_leaves(b, p);
+        for (uint32_t t = tid; t < T + rw; t += kThr) sm[t] = 0;
+        __syncthreads();
+
+        // 1. fill counts and backdrop deltas
+        for (uint32_t k = tid; k < L.n; k += kThr) {
+            const float4 f = b.leaves[L.index(b, k)];
+            walk_line(
+                w, f.x, f.y, f.z, f.w, [&](int32_t local, uint2) { atomicAdd(&cnt[local], 1u); },
+                [&](int32_t where, int d) {
+                    if (where >= 0) atomicAdd(&cnt[where], (uint32_t)d << 24);
+                    else atomicAdd(&above[-1 - where], d);
+                },
+                err);
         }
         __syncthreads();
-        for (uint32_t i = range.x + threadIdx.x; i < range.y; i += blockDim.x) {
-            const float4 L = b.leaves[i];
-            if (kWrite) {
-                walk_line(
-                    w, L.x, L.y, L.z, L.w, [&](int32_t local, uint2 q) { b.fills[atomicAdd(&cnt[local], 1u)] = q; },
-                    [&](int32_t, int) {}, &b.status[kStErr]);
-            } else {
-                walk_line(
-                    w, L.x, L.y, L.z, L.w, [&](int32_t local, uint2) { atomicAdd(&cnt[local], 1u); },
-                    [&](int32_t where, int d) {
-                        if (where >= 0) atomicAdd(&dlt[where], d);
-                        else atomicAdd(&above[-1 - where], d);
-                    },
-                    &b.status[kStErr]);
+
+        // 2. backdrops down each column (tile backdrop = int8 of the running column sum before
+        //    the tile's own delta); columns are cut into segments of rows so every thread has
+        //    work: segment sums first, then each segment's walk from its starting sum.
+        const uint32_t segs = rw >= (uint32_t)kThr ? 1u : (uint32_t)kThr / rw;
+        const uint32_t seg_rows = (rh + segs - 1) / segs;
+        if (segs > 1) {
+            if (tid < rw * segs) {
+                const uint32_t x = tid % rw, s = tid / rw;
+                const uint32_t y0 = min(rh, s * seg_rows), y1 = min(rh, y0 + seg_rows);
+                int32_t sum = 0;
+                for (uint32_t y = y0; y < y1; y++) sum += (int8_t)(cnt[y * rw + x] >> 24);
+                s_seg[tid] = sum;
             }
+            __syncthreads();
+        }
+        for (uint32_t u = tid; u < rw * segs; u += kThr) {
+            const uint32_t x = u % rw, s = u / rw;
+            int32_t run = above[x];
+            for (uint32_t k = 0; k < s; k++) run += s_seg[k * rw + x];
+            const uint32_t y0 = min(rh, s * seg_rows), y1 = min(rh, y0 + seg_rows);
+            for (uint32_t y = y0; y < y1; y++) {
+                const uint32_t t = y * rw + x, c = cnt[t];
+                b.tile_state[tb + t] = (uint16_t)((uint32_t)(uint8_t)(int8_t)run | ((c & 0xffffffu) ? 0x100u : 0u));
+                run += (int8_t)(c >> 24);
+            }
+            if (s == segs - 1) b.col_final[cb + x] = run;
         }
         __syncthreads();
-        for (uint32_t t = threadIdx.x; t < T; t += blockDim.x) {
-            b.tile_fills[tb + t] = cnt[t];
-            if (!kWrite) b.tile_delta[tb + t] = dlt[t];
+
+        // 3. fill offsets: one atomic reserves the path's block of fills; each warp scans a
+        //    contiguous chunk of tiles into write cursors (shared) and end offsets (global)
+        const uint32_t chunk = ((T + kWarps - 1) / kWarps + 31u) & ~31u;
+        const uint32_t c0 = min(T, (uint32_t)warp * chunk), c1 = min(T, c0 + chunk);
+        unsigned long long wsum = 0;  // 64-bit: a path's fills need not fit 32 bits (it then overflows)
+        for (uint32_t t = c0 + lane; t < c1; t += 32) wsum += cnt[t] & 0xffffffu;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) wsum += __shfl_down_sync(0xffffffffu, wsum, o);
+        if (lane == 0) s_wsum[warp] = wsum;
+        __syncthreads();
+        if (tid == 0) {
+            unsigned long long run = 0;
+            for (int k = 0; k < kWarps; k++) {
+                const unsigned long long v = s_wsum[k];
+                s_warp[k] = (uint32_t)run;
+                run += v;
+            }
+            const unsigned long long base = atomicAdd(fill_total(b), run);
+            const bool fits = base + run <= (unsigned long long)b.fill_cap;
+            if (!fits) atomicOr(err, kErrOverflowFill);
+            b.path_fill[p] = (uint32_t)base;
+            s_base = (uint32_t)base;
+            s_write = fits && run > 0;
         }
-        if (!kWrite)
-            for (uint32_t x = threadIdx.x; x < (uint32_t)w.rw; x += blockDim.x) b.col_above[cb + x] = above[x];
-        (void)kCols;
+        __syncthreads();
+        uint32_t carry = s_base + s_warp[warp];
+        for (uint32_t t0 = c0; t0 < c1; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            const uint32_t v = t < c1 ? (cnt[t] & 0xffffffu) : 0u;
+            uint32_t incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t n = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += n;
+            }
+            if (t < c1) {
+                cnt[t] = carry + incl - v;
+                b.tile_fills[tb + t] = carry + incl;
+            }
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        __syncthreads();
+
+        // 4. the fills, grouped by tile
+        if (s_write) {
+            for (uint32_t k = tid; k < L.n; k += kThr) {
+                const float4 f = b.leaves[L.index(b, k)];
+                walk_line(
+                    w, f.x, f.y, f.z, f.w,
+                    [&](int32_t local, uint2 q) { b.fills[atomicAdd(&cnt[local], 1u)] = q; },
+                    [&](int32_t, int) {}, err);
+            }
+        }
         __syncthreads();
     }
 }
 
-// Zero the tile counters of the paths too large for a CTA (the global pass adds into them).
+// Class 3: clear the counters, deltas and column sums of the paths' tiles.
 __global__ void k_bin_zero_large(Batch b) {
     __shared__ uint32_t s_item;
-    const uint32_t *list = b.bin_list + (size_t)3 * b.n_paths;
-    const uint32_t n_items = b.bin_ctl[kCtlCount + 3];
+    const uint32_t n3 = (uint32_t)(*ctl3_word(b) >> 40);
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(&b.bin_ctl[kCtlTicketZero], 1u);
         __syncthreads();
         const uint32_t item = s_item;
         __syncthreads();
-        if (item >= n_items) return;
-        const PathDev P = b.paths[list[item]];
-        const uint32_t rw = (uint32_t)(P.rx1 - P.rx0), T = rw * (uint32_t)(P.ry1 - P.ry0);
+        if (item >= n3) return;
+        const PathDev P = b.paths[b.bin_list[(size_t)3 * b.n_paths + item]];
+        const uint32_t rw = (uint32_t)(P.rx1 - P.rx0), T = rw * (uint32_t)max(P.ry1 - P.ry0, 0);
         for (uint32_t t = threadIdx.x; t < T; t += blockDim.x) {
             b.tile_fills[P.tile_first + t] = 0;
-            b.tile_delta[P.tile_first + t] = 0;
+            b.tile_state[P.tile_first + t] = 0;
         }
         for (uint32_t x = threadIdx.x; x < rw; x += blockDim.x) b.col_above[P.col_first + x] = 0;
     }
 }
 
-// ---------------------------------------------------------------------------
-// Backdrop propagation down each tile column (Tiler::prepare_tiles, tiler.cpp:369-439:
-// tile backdrop = int8(running int32 column sum), running += int8 tile delta).  Every tile
-// gets a 2-byte state: its propagated backdrop and whether it holds fills (alpha tile).
-
-__global__ void __launch_bounds__(kThreads) k_propagate(Batch b, uint32_t n_cols) {
-    const uint32_t gc = global_tid();
-    if (gc >= n_cols || gc >= b.status[kStCols]) return;
-    const uint32_t p = upper_bound(b.path_cols, b.n_paths + 1, gc) - 1;
-    const PathDev P = b.paths[p];
-    const int32_t rw = P.rx1 - P.rx0, rh = P.ry1 - P.ry0;
-    const int32_t x = (int32_t)(gc - P.col_first);
-    int32_t run = b.col_above[gc];
-    for (int32_t y = 0; y < rh; y++) {
-        const uint32_t gt = P.tile_first + (uint32_t)(y * rw + x);
-        const int8_t delta = (int8_t)(b.tile_delta[gt] & 0xff);
-        const bool alpha = b.tile_fills[gt] != b.tile_fills[(int64_t)gt - 1];
-        b.tile_state[gt] = (uint16_t)((uint8_t)(int8_t)run) | (alpha ? 0x100u : 0u);
-        run += delta;
+// Class 3, per line (strided over the class-3 numbering of lines): count (global atomics on
+// the tile counters, deltas into the low byte of the tile state) or write (the counters have
+// become cursors).
+template <bool kWrite>
+__global__ void __launch_bounds__(kThreads) k_bin_large(Batch b) {
+    const unsigned long long c3 = *ctl3_word(b);
+    const uint32_t n3 = (uint32_t)(c3 >> 40), total = (uint32_t)(c3 & kLow40);
+    if (n3 == 0) return;
+    if (kWrite && (b.status[kStErr] & kErrOverflowFill)) return;
+    const uint32_t *list = b.bin_list + (size_t)3 * b.n_paths, *first = b.bin_list + (size_t)4 * b.n_paths;
+    for (uint32_t j = global_tid(); j < total; j += gridDim.x * blockDim.x) {
+        const uint32_t item = upper_bound(first, n3, j) - 1;
+        const uint32_t p = list[item];
+        const PathDev P = b.paths[p];
+        const PathLeaves L = path_leaves(b, p);
+        const float4 f = b.leaves[L.index(b, j - first[item])];
+        const WalkCtx w = walk_ctx(b, P);
+        const uint32_t tb = P.tile_first, cb = P.col_first;
+        if (kWrite) {
+            walk_line(
+                w, f.x, f.y, f.z, f.w,
+                [&](int32_t local, uint2 q) { b.fills[atomicAdd(&b.tile_fills[tb + (uint32_t)local], 1u)] = q; },
+                [&](int32_t, int) {}, &b.status[kStErr]);
+        } else {
+            walk_line(
+                w, f.x, f.y, f.z, f.w, [&](int32_t local, uint2) { atomicAdd(&b.tile_fills[tb + (uint32_t)local], 1u); },
+                [&](int32_t where, int d) {
+                    if (where >= 0) add_delta_u16(&b.tile_state[tb + (uint32_t)where], d, &b.status[kStErr]);
+                    else atomicAdd(&b.col_above[cb + (uint32_t)(-1 - where)], d);
+                },
+                &b.status[kStErr]);
+        }
     }
-    b.col_final[gc] = run;
+}
+
+// Class 3, one CTA per path: backdrops down each column, then the path's block of fills and
+// the counts scanned into write cursors.
+constexpr int kPrepThreads = 256;
+
+__global__ void __launch_bounds__(kPrepThreads) k_bin_large_prep(Batch b) {
+    constexpr int kWarps = kPrepThreads / 32;
+    __shared__ uint32_t s_item, s_base;
+    __shared__ unsigned long long s_red[kWarps];
+    __shared__ uint32_t s_warp[kWarps];
+    const uint32_t tid = threadIdx.x;
+    const int lane = (int)(tid & 31), warp = (int)(tid >> 5);
+    const uint32_t n3 = (uint32_t)(*ctl3_word(b) >> 40);
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(&b.bin_ctl[kCtlTicketPrep], 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        if (item >= n3) return;
+        const uint32_t p = b.bin_list[(size_t)3 * b.n_paths + item];
+        const PathDev P = b.paths[p];
+        const uint32_t rw = (uint32_t)max(P.rx1 - P.rx0, 0), rh = (uint32_t)max(P.ry1 - P.ry0, 0), T = rw * rh;
+        const uint32_t tb = P.tile_first, cb = P.col_first;
+        unsigned long long sum = 0;
+        for (uint32_t x = tid; x < rw; x += kPrepThreads) {
+            int32_t run = b.col_above[cb + x];
+            for (uint32_t y = 0; y < rh; y++) {
+                const uint32_t t = tb + y * rw + x, c = b.tile_fills[t];
+                const int8_t delta = (int8_t)(b.tile_state[t] & 0xffu);
+                b.tile_state[t] = (uint16_t)((uint32_t)(uint8_t)(int8_t)run | (c ? 0x100u : 0u));
+                run += delta;
+                sum += c;
+            }
+            b.col_final[cb + x] = run;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+        if (lane == 0) s_red[warp] = sum;
+        __syncthreads();
+        if (tid == 0) {
+            unsigned long long total = 0;
+            for (int k = 0; k < kWarps; k++) total += s_red[k];
+            const unsigned long long base = atomicAdd(fill_total(b), total);
+            if (base + total > (unsigned long long)b.fill_cap) atomicOr(&b.status[kStErr], kErrOverflowFill);
+            b.path_fill[p] = (uint32_t)base;
+            s_base = (uint32_t)base;
+        }
+        __syncthreads();
+        uint32_t carry = s_base;
+        for (uint32_t t0 = 0; t0 < T; t0 += kPrepThreads) {
+            const uint32_t t = t0 + tid;
+            const uint32_t v = t < T ? b.tile_fills[tb + t] : 0u;
+            uint32_t incl = v;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t n = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += n;
+            }
+            if (lane == 31) s_warp[warp] = incl;
+            __syncthreads();
+            uint32_t before = 0, chunk_total = 0;
+            for (int k = 0; k < kWarps; k++) {
+                if (k < warp) before += s_warp[k];
+                chunk_total += s_warp[k];
+            }
+            if (t < T) b.tile_fills[tb + t] = carry + before + incl - v;
+            carry += chunk_total;
+            __syncthreads();
+        }
+    }
+}
+
+// Learned frame: list the spill pool's lines by path (count, scan, scatter), so each path's
+// CTA finds its pooled lines.
+__global__ void k_pool_count(Batch b) {
+    const uint32_t n = min(b.status[kStPoolUsed], b.leaf_pool_cap);
+    for (uint32_t j = global_tid(); j < n; j += gridDim.x * blockDim.x) atomicAdd(&b.pool_cnt[b.pool_path[j]], 1u);
+}
+
+__global__ void k_pool_scatter(Batch b) {
+    const uint32_t n = min(b.status[kStPoolUsed], b.leaf_pool_cap);
+    for (uint32_t j = global_tid(); j < n; j += gridDim.x * blockDim.x)
+        b.pool_idx[atomicAdd(&b.pool_cnt[b.pool_path[j]], 1u)] = j;
 }
 
 // ---------------------------------------------------------------------------
@@ -1043,9 +1215,17 @@ __device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint3
 
 __device__ __forceinline__ bool solid_hidden(bool eo, int8_t bd) { return eo && ((bd < 0 ? -bd : bd) & 1) == 0; }
 
+// First fill of tile gt of path p: the path's block starts at path_fill[p]; every other tile
+// starts where the tile before it ends.
+__device__ __forceinline__ uint32_t fill_begin(const Batch &b, uint32_t p, uint32_t gt) {
+    return gt == b.path_tiles[p] ? b.path_fill[p] : b.tile_fills[gt - 1];
+}
+
 __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
     __shared__ int cells[kCompWarps][kCovCells];
     __shared__ FillPrep prep[kCompWarps][32];
+    // a frame whose leaf lines or fills overran their buffers is redone; nothing to read here
+    if (b.status[kStErr] & (kErrOverflowLeaf | kErrOverflowFill)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int *D = cells[warp];
     const int col = lane & 15, h = lane >> 4;
@@ -1078,7 +1258,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
                 for (int k = 0; k < 8; k++) cov[k] = 1.0f;
                 stop = (flags & 2u) != 0;
             } else {
-                const uint32_t f0 = b.tile_fills[(int64_t)gt - 1], f1 = b.tile_fills[gt];
+                const uint32_t f0 = fill_begin(b, p, gt), f1 = b.tile_fills[gt];
                 comp_fills += f1 - f0;
                 zero_cells(D);
                 alpha_coverage(b, f0, f1, bd, eo, D, prep[warp], cov);
@@ -1184,7 +1364,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_coverage_dump(Batch b, cons
     const uint32_t p = upper_bound(b.path_tiles, b.n_paths + 1, gt) - 1;
     zero_cells(D);
     float cov[8];
-    alpha_coverage(b, b.tile_fills[(int64_t)gt - 1], b.tile_fills[gt], (int8_t)(b.tile_state[gt] & 0xffu),
+    alpha_coverage(b, fill_begin(b, p, gt), b.tile_fills[gt], (int8_t)(b.tile_state[gt] & 0xffu),
                    (b.paths[p].flags & 1u) != 0, D, prep[warp], cov);
     const int col = lane & 15, h = lane >> 4;
 #pragma unroll
@@ -1236,13 +1416,6 @@ cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStre
     return cudaGetLastError();
 }
 
-cudaError_t launch_bin(const Batch &b, uint32_t n_leaves, bool write, cudaStream_t st) {
-    if (!n_leaves) return cudaSuccess;
-    if (write) PF_LAUNCH(k_bin<true><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves));
-    else PF_LAUNCH(k_bin<false><<<grid_for(n_leaves), kThreads, 0, st>>>(b, n_leaves));
-    return cudaGetLastError();
-}
-
 cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t st) {
     if (n_segs) PF_LAUNCH(k_flatten_budget<<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
     return cudaGetLastError();
@@ -1253,43 +1426,48 @@ cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-template <bool kWrite, int kCls>
-static cudaError_t launch_class(const Batch &b, int sms, cudaStream_t st) {
-    const size_t smem = (2 * size_t(class_tiles(kCls)) + std::min<uint32_t>(class_tiles(kCls), kMaxCols)) * 4;
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_bin_paths<kWrite, kCls>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+template <int kCls>
+static cudaError_t launch_fused(const Batch &b, int sms, cudaStream_t st) {
+    const size_t smem = size_t(class_words(kCls)) * 4;
+    static int configured_device = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (configured_device != dev) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_bin_fused<kCls>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        configured = true;
+        configured_device = dev;
     }
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin_paths<kWrite, kCls>, class_threads(kCls), smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin_fused<kCls>, class_threads(kCls), smem);
     const unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)sms;
-    PF_LAUNCH(k_bin_paths<kWrite, kCls><<<grid, class_threads(kCls), smem, st>>>(b));
+    PF_LAUNCH(k_bin_fused<kCls><<<grid, class_threads(kCls), smem, st>>>(b));
     return cudaGetLastError();
 }
 
-// Count pass: per-path CTAs, zero the large paths, then the global pass (large paths, pool).
-// Write pass: per-path CTAs, then the global pass.
-cudaError_t launch_bin_paths(const Batch &b, bool write, uint32_t n_leaf_slots, cudaStream_t st) {
+// Class 3 (zero, count, backdrops and offsets, write; each returns at once when the class is
+// empty), then the CTA classes, largest rects first.
+cudaError_t launch_bin_paths(const Batch &b, cudaStream_t st) {
+    if (!b.n_paths) return cudaSuccess;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    PF_LAUNCH(k_bin_zero_large<<<sms * 2, 256, 0, st>>>(b));
+    PF_LAUNCH(k_bin_large<false><<<sms * 8, kThreads, 0, st>>>(b));
+    PF_LAUNCH(k_bin_large_prep<<<sms * 2, kPrepThreads, 0, st>>>(b));
+    PF_LAUNCH(k_bin_large<true><<<sms * 8, kThreads, 0, st>>>(b));
     cudaError_t e;
-    if (!write) {
-        if ((e = launch_class<false, 0>(b, sms, st)) != cudaSuccess) return e;
-        if ((e = launch_class<false, 1>(b, sms, st)) != cudaSuccess) return e;
-        PF_LAUNCH(k_bin_zero_large<<<sms * 4, 256, 0, st>>>(b));
-    } else {
-        if ((e = launch_class<true, 0>(b, sms, st)) != cudaSuccess) return e;
-        if ((e = launch_class<true, 1>(b, sms, st)) != cudaSuccess) return e;
-    }
-    return launch_bin(b, n_leaf_slots, write, st);
+    if ((e = launch_fused<2>(b, sms, st)) != cudaSuccess) return e;
+    if ((e = launch_fused<1>(b, sms, st)) != cudaSuccess) return e;
+    return launch_fused<0>(b, sms, st);
 }
 
-cudaError_t launch_propagate(const Batch &b, uint32_t n_cols, cudaStream_t st) {
-    if (n_cols) PF_LAUNCH(k_propagate<<<grid_for(n_cols), kThreads, 0, st>>>(b, n_cols));
+cudaError_t launch_pool_lists(const Batch &b, bool scatter, cudaStream_t st) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (scatter) PF_LAUNCH(k_pool_scatter<<<sms * 2, kThreads, 0, st>>>(b));
+    else PF_LAUNCH(k_pool_count<<<sms * 2, kThreads, 0, st>>>(b));
     return cudaGetLastError();
 }
 

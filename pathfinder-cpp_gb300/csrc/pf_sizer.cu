@@ -110,7 +110,7 @@ __global__ void k_path_counts(Batch b, const uint2 *path_contours, uint32_t *lea
     const uint32_t s0 = b.contour_segs[cr.x], s1 = b.contour_segs[cr.y];
     leaves[p] = b.seg_leaves[s1] - b.seg_leaves[s0];
     const uint32_t t0 = b.path_tiles[p], t1 = b.path_tiles[p + 1];
-    fills[p] = b.tile_fills[(int64_t)t1 - 1] - b.tile_fills[(int64_t)t0 - 1];
+    fills[p] = t1 > t0 ? b.tile_fills[t1 - 1] - b.path_fill[p] : 0u;
 }
 
 // ---------------------------------------------------------------------------

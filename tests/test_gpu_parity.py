@@ -122,3 +122,25 @@ def test_invalid_scenes_are_rejected(renderer, pf):
     # the context stays usable
     _, got, _ = render(renderer, sc)
     assert got["path_rect"].shape == (4, 4)
+
+
+def test_fill_buffer_grows_and_frame_is_redone(pf, oracle_mod):
+    # Long straight edges give many fills per line: a fresh context's first frame overruns its
+    # starting fills capacity (about three per line), is counted, and binned again.
+    pts = np.array([[3.5, 5.25], [2040.0, 7.0], [2043.5, 2041.0], [9.0, 2039.5],
+                    [100.0, 100.0], [1900.0, 130.0], [1000.0, 1950.0]], np.float32)
+    sc = S.Scene(points=pts, flags=np.zeros(7, np.uint8),
+                 contour_start=np.array([0, 4, 7], np.uint32), path_start=np.array([0, 1, 2], np.uint32),
+                 fill_rule=np.array([0, 1], np.uint8),
+                 color=np.array([0xff2040c0, 0x80c02010], np.uint32), width=2048.0, height=2048.0)
+    with pf.Renderer(device=0) as r:
+        stats, got, img = render(r, sc)
+        assert stats["fills"] > 3 * stats["microlines"]
+        want = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D11, threads=4)
+        assert_canon(got, want, TILE_KEYS + LIST_KEYS)
+        ref_img, _ = oracle_mod.render(sc, threads=8)
+        assert np.abs(img.astype(np.int32) - ref_img.astype(np.int32)).max() <= PIXEL_TOL
+        # the context keeps the larger buffer: the next frame needs no second binning
+        stats2, got2, _ = render(r, sc)
+        assert stats2["host_syncs"] < stats["host_syncs"]
+        assert_canon(got2, want, TILE_KEYS + LIST_KEYS)
