@@ -305,6 +305,7 @@ def main():
     st = dict(st)
     st["composite_entries"] = st_c["composite_entries"]
     st["composited_fills"] = st_c["composited_fills"]
+    st["walk_chunks"] = int(r.debug_counters()[15])  # 32-candidate chunks the composite's z-walks read
 
     # roofline of the composite kernel (fused coverage + src-over)
     pixels = sum(int(np.ceil(s.width)) * int(np.ceil(s.height)) for s in scenes_list)
@@ -345,7 +346,8 @@ def main():
             "stages_ms": {k: st[k] for k in ("ms_setup", "ms_flatten", "ms_bin", "ms_propagate", "ms_lists",
                                              "ms_composite", "ms_total")},
             "counts": {k: st[k] for k in ("paths", "segments", "microlines", "tiles", "fills", "composite_entries",
-                                          "composited_fills", "framebuffer_tiles", "host_syncs")},
+                                          "composited_fills", "framebuffer_tiles", "walk_chunks",
+                                          "host_syncs")},
             "roofline": {"kernel": "k_composite", "bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
                          "peak_source": peak_src, "algorithmic_bytes": comp_bytes},

@@ -90,7 +90,7 @@ struct Ctx {
     float sz_mul = 1.25f, sz_add = 8.0f, sz_pool = 0.10f;
     uint32_t last_paths_over = 0, last_pool_used = 0;
     DevBuf segs, seg_leaves, leaves, pool_path, pool_cnt, pool_idx;
-    DevBuf tile_fills, tile_state, col_above, col_final, fills, path_fill, path_cls;
+    DevBuf tile_fills, tile_state, col_above, col_final, fills, path_fill, path_cls, bin_stage;
     DevBuf row_first, row_paths, scene_row_first;
     DevBuf z, fb_count, list, image, status, scan_temp;
     uint32_t *h_status = nullptr;  // pinned
@@ -340,6 +340,7 @@ Batch make_batch(Ctx *c) {
     b.col_final = c->col_final.as<int32_t>();
     b.fills = c->fills.as<uint2>();
     b.fill_cap = (uint32_t)std::min<size_t>(c->fills.cap / 8, 0xffffffffu);
+    b.stage = c->bin_stage.as<uint2>();
     b.row_first = c->row_first.as<uint32_t>();
     b.row_paths = c->row_paths.as<uint4>();
     b.row_cap = (uint32_t)std::min<size_t>(c->row_paths.cap / 16, 0xffffffffu);
@@ -422,6 +423,9 @@ int begin_frame(Ctx *c, uint32_t first, uint32_t count) {
     PF_CUDA(c->row_first.ensure((size_t(c->r_rows) + 1) * 4));
     PF_CUDA(c->bin_list.ensure(size_t(N) * 20 + 16));
     PF_CUDA(c->path_fill.ensure(size_t(N) * 4 + 16));
+    size_t stage_bytes = 0;
+    PF_CUDA(bin_stage_bytes(&stage_bytes));
+    PF_CUDA(c->bin_stage.ensure(stage_bytes));
     PF_CUDA(c->path_cls.ensure(size_t(N) + 16));
     PF_CUDA(c->bin_ctl.ensure(64));
     PF_CUDA(c->path_leaf_range.ensure(size_t(N) * 8 + 16));
@@ -893,7 +897,7 @@ int pf_ctx_destroy(void *ctx) {
                       &c->contour_path, &c->paths, &c->path_tiles, &c->path_cols, &c->contour_segs,
                       &c->path_contours, &c->segs, &c->seg_leaves, &c->leaves, &c->pool_path, &c->pool_cnt,
                       &c->pool_idx, &c->tile_fills, &c->path_fill, &c->path_cls, &c->tile_state, &c->col_above,
-                      &c->col_final, &c->fills, &c->row_first,
+                      &c->col_final, &c->fills, &c->bin_stage, &c->row_first,
                       &c->row_paths, &c->scene_row_first, &c->z, &c->fb_count, &c->list, &c->image,
                       &c->status, &c->scan_temp};
     for (DevBuf *b : bufs) b->release();

@@ -133,6 +133,7 @@ struct Batch {
     int32_t *col_final;                  // [cols]
     uint2 *fills;                        // [fills] packed u16 x4
     uint32_t fill_cap;
+    uint2 *stage;                        // per binning CTA: fills staged during its count walk
 
     // per framebuffer-tile row of each scene: the paths whose tile rect spans the row,
     // in path order
@@ -209,6 +210,8 @@ cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t 
 cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st);
 cudaError_t launch_bin_paths(const Batch &b, cudaStream_t st);
 cudaError_t launch_pool_lists(const Batch &b, bool scatter, cudaStream_t st);
+// Bytes of the binning CTAs' fill stage on the current device.
+cudaError_t bin_stage_bytes(size_t *bytes);
 cudaError_t launch_mlp_predict(const __nv_bfloat16 *w, const float *feat, uint32_t n, float *out, cudaStream_t st);
 cudaError_t launch_mlp_grad(const __nv_bfloat16 *w, const float *feat, const float *target, const uint32_t *index,
                             uint32_t n, float *grad, float *loss, cudaStream_t st);

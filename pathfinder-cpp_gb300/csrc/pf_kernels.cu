@@ -248,11 +248,19 @@ __device__ __forceinline__ bool flat_quad(const float bb[4], const float cc[2]) 
 
 __device__ __forceinline__ float half_lerp(float a, float b) { return fadd(a, fmul(0.5f, fsub(b, a))); }
 
+// The stack of pending second halves is kept small, as it lives in local memory: an entry
+// holds a half's start point and control points only.  A half ends where the half pushed
+// before it (the entry below) begins, or at the segment's end for the bottom entry, because
+// each split pushes the second half of the current piece, whose end is the current piece's.
+// Depths need no slot either: the path from the root has at most one pending half per depth,
+// so a bit mask of pending depths gives the top entry's depth (its highest bit).
+
 template <class Emit>
 __device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, float c1, float c2, float c3,
                               Emit &&emit, uint32_t *status) {
-    float stk[kMaxDepth][8];
-    int dstk[kMaxDepth];
+    float4 sa[kMaxDepth];  // start x, y, first control x, y
+    float2 sb[kMaxDepth];  // second control x, y
+    uint32_t pending = 0;
     int sp = 0;
     float bb[4] = {b0, b1, b2, b3}, cc[4] = {c0, c1, c2, c3};
     int depth = 0;
@@ -262,12 +270,24 @@ __device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, 
             emit(bb[0], bb[1], bb[2], bb[3]);
             if (sp == 0) return;
             sp--;
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                bb[k] = stk[sp][k];
-                cc[k] = stk[sp][4 + k];
+            const float4 a = sa[sp];
+            const float2 c = sb[sp];
+            bb[0] = a.x;
+            bb[1] = a.y;
+            cc[0] = a.z;
+            cc[1] = a.w;
+            cc[2] = c.x;
+            cc[3] = c.y;
+            if (sp > 0) {
+                const float4 below = sa[sp - 1];
+                bb[2] = below.x;
+                bb[3] = below.y;
+            } else {
+                bb[2] = b2;
+                bb[3] = b3;
             }
-            depth = dstk[sp];
+            depth = 31 - __clz(pending);
+            pending &= ~(1u << depth);
             continue;
         }
         float p01[2], p12[2], p23[2], p012[2], p123[2], p0123[2];
@@ -281,31 +301,25 @@ __device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, 
             p0123[k] = half_lerp(p012[k], p123[k]);
         }
         // push the second half, continue with the first
-        stk[sp][0] = p0123[0];
-        stk[sp][1] = p0123[1];
-        stk[sp][2] = bb[2];
-        stk[sp][3] = bb[3];
-        stk[sp][4] = p123[0];
-        stk[sp][5] = p123[1];
-        stk[sp][6] = p23[0];
-        stk[sp][7] = p23[1];
-        dstk[sp] = depth + 1;
+        sa[sp] = make_float4(p0123[0], p0123[1], p123[0], p123[1]);
+        sb[sp] = make_float2(p23[0], p23[1]);
         sp++;
+        depth++;
+        pending |= 1u << depth;
         bb[2] = p0123[0];
         bb[3] = p0123[1];
         cc[0] = p01[0];
         cc[1] = p01[1];
         cc[2] = p012[0];
         cc[3] = p012[1];
-        depth++;
     }
 }
 
 template <class Emit>
 __device__ void flatten_quad(float b0, float b1, float b2, float b3, float c0, float c1, Emit &&emit,
                              uint32_t *status) {
-    float stk[kMaxDepth][6];
-    int dstk[kMaxDepth];
+    float4 sa[kMaxDepth];  // start x, y, control x, y
+    uint32_t pending = 0;
     int sp = 0;
     float bb[4] = {b0, b1, b2, b3}, cc[2] = {c0, c1};
     int depth = 0;
@@ -315,11 +329,21 @@ __device__ void flatten_quad(float b0, float b1, float b2, float b3, float c0, f
             emit(bb[0], bb[1], bb[2], bb[3]);
             if (sp == 0) return;
             sp--;
-#pragma unroll
-            for (int k = 0; k < 4; k++) bb[k] = stk[sp][k];
-            cc[0] = stk[sp][4];
-            cc[1] = stk[sp][5];
-            depth = dstk[sp];
+            const float4 a = sa[sp];
+            bb[0] = a.x;
+            bb[1] = a.y;
+            cc[0] = a.z;
+            cc[1] = a.w;
+            if (sp > 0) {
+                const float4 below = sa[sp - 1];
+                bb[2] = below.x;
+                bb[3] = below.y;
+            } else {
+                bb[2] = b2;
+                bb[3] = b3;
+            }
+            depth = 31 - __clz(pending);
+            pending &= ~(1u << depth);
             continue;
         }
         float a[2], q[2], m[2];
@@ -329,19 +353,14 @@ __device__ void flatten_quad(float b0, float b1, float b2, float b3, float c0, f
             q[k] = fadd(cc[k], fmul(fsub(bb[2 + k], cc[k]), 0.5f));
             m[k] = fadd(a[k], fmul(fsub(q[k], a[k]), 0.5f));
         }
-        stk[sp][0] = m[0];
-        stk[sp][1] = m[1];
-        stk[sp][2] = bb[2];
-        stk[sp][3] = bb[3];
-        stk[sp][4] = q[0];
-        stk[sp][5] = q[1];
-        dstk[sp] = depth + 1;
+        sa[sp] = make_float4(m[0], m[1], q[0], q[1]);
         sp++;
+        depth++;
+        pending |= 1u << depth;
         bb[2] = m[0];
         bb[3] = m[1];
         cc[0] = a[0];
         cc[1] = a[1];
-        depth++;
     }
 }
 
@@ -603,6 +622,12 @@ __global__ void __launch_bounds__(kThreads) k_flatten_budget(Batch b, uint32_t n
 constexpr int kCtaClasses = 3;
 __host__ __device__ constexpr uint32_t class_words(int c) { return c == 0 ? 1088u : c == 1 ? 4352u : 16896u; }
 __host__ __device__ constexpr int class_threads(int c) { return c == 2 ? 512 : 256; }
+// CTAs per SM the register budget is set for (shared memory allows 3 of class 2, 12 of class 1)
+__host__ __device__ constexpr int class_min_ctas(int c) { return c == 2 ? 3 : 6; }
+// Fills a CTA stages during its count walk (8 bytes each, in its own slice of a global buffer
+// that stays in L2): the fills are then placed without walking the lines again.  A path with
+// more fills than this walks its lines twice.
+__host__ __device__ constexpr uint32_t class_stage(int c) { return c == 0 ? 3072u : c == 1 ? 6144u : 12288u; }
 // One line gives a tile at most two fills (the walk visits a tile once, with at most one
 // extra fill for a vertical crossing), so with at most 2^22 lines per CTA-binned path the
 // 24-bit counters cannot carry into the delta byte.
@@ -720,11 +745,25 @@ __global__ void k_bin_classify(Batch b, bool learned) {
     }
 }
 
+// A staged fill: the four 12-bit coordinates of the packed u16 fill and the tile (< 2^16).
+__device__ __forceinline__ uint2 stage_pack(uint2 q, uint32_t local) {
+    const uint32_t x0 = q.x & 0xfffu, y0 = q.x >> 16, x1 = q.y & 0xfffu, y1 = q.y >> 16;
+    return make_uint2(x0 | y0 << 12 | (x1 & 0xffu) << 24, x1 >> 8 | y1 << 4 | local << 16);
+}
+__device__ __forceinline__ uint2 stage_fill(uint2 v) {
+    const uint32_t x0 = v.x & 0xfffu, y0 = (v.x >> 12) & 0xfffu, x1 = v.x >> 24 | (v.y & 0xfu) << 8,
+                   y1 = (v.y >> 4) & 0xfffu;
+    return make_uint2(x0 | y0 << 16, x1 | y1 << 16);
+}
+
 template <int kCls>
-__global__ void __launch_bounds__(class_threads(kCls)) k_bin_fused(Batch b) {
+__global__ void __launch_bounds__(class_threads(kCls), class_min_ctas(kCls)) k_bin_fused(Batch b) {
     constexpr int kThr = class_threads(kCls), kWarps = kThr / 32;
+    constexpr uint32_t kStage = class_stage(kCls);
+    static_assert(class_words(kCls) <= 65536u, "a staged fill holds its tile in 16 bits");
     extern __shared__ uint32_t sm[];
-    __shared__ uint32_t s_item, s_base, s_write;
+    __shared__ uint32_t s_item, s_base, s_write, s_next, s_nstage;
+    uint2 *const stage = b.stage ? b.stage + (size_t)blockIdx.x * kStage : nullptr;
     __shared__ int32_t s_seg[kThr];
     __shared__ uint32_t s_warp[kWarps];
     __shared__ unsigned long long s_wsum[kWarps];
@@ -746,13 +785,29 @@ __global__ void __launch_bounds__(class_threads(kCls)) k_bin_fused(Batch b) {
         int32_t *above = reinterpret_cast<int32_t *>(sm + T);  // per column
         const PathLeaves L = path_leaves(b, p);
         for (uint32_t t = tid; t < T + rw; t += kThr) sm[t] = 0;
+        if (tid == 0) {
+            s_next = 0;
+            s_nstage = 0;
+        }
         __syncthreads();
 
-        // 1. fill counts and backdrop deltas
-        for (uint32_t k = tid; k < L.n; k += kThr) {
+        // 1. fill counts and backdrop deltas, the fills staged with their tiles.  Warps take
+        //    the lines 32 at a time, so a warp that drew short lines takes more.
+        for (;;) {
+            uint32_t k0 = 0;
+            if (lane == 0) k0 = atomicAdd(&s_next, 32u);
+            k0 = __shfl_sync(0xffffffffu, k0, 0);
+            if (k0 >= L.n) break;
+            const uint32_t k = k0 + (uint32_t)lane;
+            if (k >= L.n) continue;
             const float4 f = b.leaves[L.index(b, k)];
             walk_line(
-                w, f.x, f.y, f.z, f.w, [&](int32_t local, uint2) { atomicAdd(&cnt[local], 1u); },
+                w, f.x, f.y, f.z, f.w,
+                [&](int32_t local, uint2 q) {
+                    atomicAdd(&cnt[local], 1u);
+                    const uint32_t slot = atomicAdd(&s_nstage, 1u);
+                    if (stage && slot < kStage) stage[slot] = stage_pack(q, (uint32_t)local);
+                },
                 [&](int32_t where, int d) {
                     if (where >= 0) atomicAdd(&cnt[where], (uint32_t)d << 24);
                     else atomicAdd(&above[-1 - where], d);
@@ -761,7 +816,27 @@ __global__ void __launch_bounds__(class_threads(kCls)) k_bin_fused(Batch b) {
         }
         __syncthreads();
 
-        // 2. backdrops down each column (tile backdrop = int8 of the running column sum before
+        // 2. the count of each warp's chunk of tiles; thread 0 reserves the path's block of
+        //    fills with one atomic whose result it reads only after the column pass
+        const uint32_t chunk = ((T + kWarps - 1) / kWarps + 31u) & ~31u;
+        const uint32_t c0 = min(T, (uint32_t)warp * chunk), c1 = min(T, c0 + chunk);
+        unsigned long long wsum = 0;  // 64-bit: a path's fills need not fit 32 bits (it then overflows)
+        for (uint32_t t = c0 + lane; t < c1; t += 32) wsum += cnt[t] & 0xffffffu;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) wsum += __shfl_down_sync(0xffffffffu, wsum, o);
+        if (lane == 0) s_wsum[warp] = wsum;
+        __syncthreads();
+        unsigned long long base = 0, total = 0;
+        if (tid == 0) {
+            for (int k = 0; k < kWarps; k++) {
+                const unsigned long long v = s_wsum[k];
+                s_warp[k] = (uint32_t)total;
+                total += v;
+            }
+            base = atomicAdd(fill_total(b), total);
+        }
+
+        // 3. backdrops down each column (tile backdrop = int8 of the running column sum before
         //    the tile's own delta); columns are cut into segments of rows so every thread has
         //    work: segment sums first, then each segment's walk from its starting sum.
         const uint32_t segs = rw >= (uint32_t)kThr ? 1u : (uint32_t)kThr / rw;
@@ -788,33 +863,16 @@ __global__ void __launch_bounds__(class_threads(kCls)) k_bin_fused(Batch b) {
             }
             if (s == segs - 1) b.col_final[cb + x] = run;
         }
-        __syncthreads();
-
-        // 3. fill offsets: one atomic reserves the path's block of fills; each warp scans a
-        //    contiguous chunk of tiles into write cursors (shared) and end offsets (global)
-        const uint32_t chunk = ((T + kWarps - 1) / kWarps + 31u) & ~31u;
-        const uint32_t c0 = min(T, (uint32_t)warp * chunk), c1 = min(T, c0 + chunk);
-        unsigned long long wsum = 0;  // 64-bit: a path's fills need not fit 32 bits (it then overflows)
-        for (uint32_t t = c0 + lane; t < c1; t += 32) wsum += cnt[t] & 0xffffffu;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) wsum += __shfl_down_sync(0xffffffffu, wsum, o);
-        if (lane == 0) s_wsum[warp] = wsum;
-        __syncthreads();
         if (tid == 0) {
-            unsigned long long run = 0;
-            for (int k = 0; k < kWarps; k++) {
-                const unsigned long long v = s_wsum[k];
-                s_warp[k] = (uint32_t)run;
-                run += v;
-            }
-            const unsigned long long base = atomicAdd(fill_total(b), run);
-            const bool fits = base + run <= (unsigned long long)b.fill_cap;
+            const bool fits = base + total <= (unsigned long long)b.fill_cap;
             if (!fits) atomicOr(err, kErrOverflowFill);
             b.path_fill[p] = (uint32_t)base;
             s_base = (uint32_t)base;
-            s_write = fits && run > 0;
+            s_write = fits && total > 0;
         }
         __syncthreads();
+
+        // 4. each warp scans its chunk into write cursors (shared) and end offsets (global)
         uint32_t carry = s_base + s_warp[warp];
         for (uint32_t t0 = c0; t0 < c1; t0 += 32) {
             const uint32_t t = t0 + lane;
@@ -833,8 +891,20 @@ __global__ void __launch_bounds__(class_threads(kCls)) k_bin_fused(Batch b) {
         }
         __syncthreads();
 
-        // 4. the fills, grouped by tile
-        if (s_write) {
+        // 5. the fills, grouped by tile: from the stage (four loads in flight per thread), or by
+        //    walking the lines again
+        const uint32_t nstage = s_nstage;
+        if (s_write && stage && nstage <= kStage) {
+            for (uint32_t k = tid; k < nstage; k += 4 * kThr) {
+                uint2 v[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (k + j * kThr < nstage) v[j] = stage[k + j * kThr];
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (k + j * kThr < nstage) b.fills[atomicAdd(&cnt[v[j].y >> 16], 1u)] = stage_fill(v[j]);
+            }
+        } else if (s_write) {
             for (uint32_t k = tid; k < L.n; k += kThr) {
                 const float4 f = b.leaves[L.index(b, k)];
                 walk_line(
@@ -1031,9 +1101,10 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(Batch b) {
             // adding fx >= rx0 brings it back into range)
             const uint32_t row_tile = b.paths[p].tile_first + (uint32_t)(y - rect.y) * (uint32_t)(rect.z - rect.x) -
                                       (uint32_t)rect.x;
+            // flags: bit 0 even-odd, bit 1 occludes, bit 2 this row is the rect's first row
             if (out + rank < b.row_cap)
                 b.row_paths[out + rank] = make_uint4(p, (uint32_t)rect.x | ((uint32_t)rect.z << 16), row_tile,
-                                                     b.paths[p].flags);
+                                                     b.paths[p].flags | (y == rect.y ? 4u : 0u));
         }
         out += chunk_total;
         total += chunk_total;
@@ -1180,35 +1251,58 @@ constexpr int kCompWarps = 4;
 // walk ends at the first occluding tile - a solid, opaque tile whose fill rule covers it
 // (the d3d11 z-buffer rule, propagate.comp:190-205) - so the tiles visited are exactly the
 // framebuffer tile's composite list after z-culling (sort.comp:49-83), in reverse order.
-// visit(p, gt, state) returns true to stop the walk.
-template <class Visit>
-__device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint32_t fx, uint32_t fy, Visit &&visit,
+// With kFetch, every visible candidate also loads its colour and (alpha tiles) its fill
+// range in parallel before the visits, so a visit waits on its fills alone.
+// visit(candidate) returns true to stop the walk.
+struct Cand {
+    uint32_t p, gt, st, flags;
+    uint32_t f0, f1, color;  // kFetch only
+};
+
+template <bool kFetch, class Visit>
+__device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint32_t fx, Visit &&visit,
                                              uint32_t &chunks) {
     const int lane = threadIdx.x & 31;
     const uint32_t k_lo = b.row_first[row], k_hi = b.row_first[row + 1];
     for (uint32_t top = k_hi; top > k_lo; top = top > k_lo + 32 ? top - 32 : k_lo) {
         chunks++;
         const int64_t k = (int64_t)top - 1 - lane;
-        uint4 e = make_uint4(0, 0, 0, 0);
-        uint32_t gt = 0, st = 0;
+        Cand c{0, 0, 0, 0, 0, 0, 0};
         bool vis = false;
         if (k >= (int64_t)k_lo) {
-            e = b.row_paths[k];
+            const uint4 e = b.row_paths[k];
             if (fx >= (e.y & 0xffffu) && fx < (e.y >> 16)) {
-                gt = e.z + fx;
-                st = b.tile_state[gt];
-                vis = st != 0;
+                c.p = e.x;
+                c.flags = e.w;
+                c.gt = e.z + fx;
+                c.st = b.tile_state[c.gt];
+                vis = c.st != 0;
+                if (kFetch && vis) {
+                    c.color = b.color[b.path_base + c.p];
+                    if (c.st & 0x100u) {
+                        // the first tile of a path starts the path's block of fills
+                        const bool first = (c.flags & 4u) && fx == (e.y & 0xffffu);
+                        c.f0 = first ? b.path_fill[c.p] : b.tile_fills[c.gt - 1];
+                        c.f1 = b.tile_fills[c.gt];
+                    }
+                }
             }
         }
         uint32_t mask = __ballot_sync(0xffffffffu, vis);
         while (mask) {
             const int l = __ffs(mask) - 1;
             mask &= mask - 1;
-            const uint32_t pl = __shfl_sync(0xffffffffu, e.x, l);
-            const uint32_t gtl = __shfl_sync(0xffffffffu, gt, l);
-            const uint32_t stl = __shfl_sync(0xffffffffu, st, l);
-            const uint32_t fl = __shfl_sync(0xffffffffu, e.w, l);
-            if (visit(pl, gtl, stl, fl)) return;
+            Cand v;
+            v.p = __shfl_sync(0xffffffffu, c.p, l);
+            v.gt = __shfl_sync(0xffffffffu, c.gt, l);
+            v.st = __shfl_sync(0xffffffffu, c.st, l);
+            v.flags = __shfl_sync(0xffffffffu, c.flags, l);
+            if (kFetch) {
+                v.f0 = __shfl_sync(0xffffffffu, c.f0, l);
+                v.f1 = __shfl_sync(0xffffffffu, c.f1, l);
+                v.color = __shfl_sync(0xffffffffu, c.color, l);
+            }
+            if (visit(v)) return;
         }
     }
 }
@@ -1221,7 +1315,7 @@ __device__ __forceinline__ uint32_t fill_begin(const Batch &b, uint32_t p, uint3
     return gt == b.path_tiles[p] ? b.path_fill[p] : b.tile_fills[gt - 1];
 }
 
-__global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
+__global__ void __launch_bounds__(kCompWarps * 32, 8) k_composite(Batch b) {
     __shared__ int cells[kCompWarps][kCovCells];
     __shared__ FillPrep prep[kCompWarps][32];
     // a frame whose leaf lines or fills overran their buffers is redone; nothing to read here
@@ -1238,33 +1332,32 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
         const SceneDev &S = b.scenes[s];
         const uint32_t local = fbg - S.fb_first;
         const uint32_t fx = local % S.fbw, fy = local / S.fbw;
-        // front to back: acc = sum of T * premultiplied source, T = product of (1 - a) above
-        float ar[8], ag[8], ab[8], aa[8], tr[8];
+        // front to back: acc = sum of T * premultiplied source, T = product of (1 - a) above;
+        // the accumulated alpha is 1 - T
+        float ar[8], ag[8], ab[8], tr[8];
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            ar[k] = ag[k] = ab[k] = aa[k] = 0.0f;
+            ar[k] = ag[k] = ab[k] = 0.0f;
             tr[k] = 1.0f;
         }
-        walk_fb_tile(b, S.row_first - b.row_base + fy, fx, fy,
-                     [&](uint32_t p, uint32_t gt, uint32_t st, uint32_t flags) -> bool {
-            const bool eo = (flags & 1u) != 0;
-            const int8_t bd = (int8_t)(st & 0xffu);
+        walk_fb_tile<true>(b, S.row_first - b.row_base + fy, fx, [&](const Cand &v) -> bool {
+            const bool eo = (v.flags & 1u) != 0;
+            const int8_t bd = (int8_t)(v.st & 0xffu);
             float cov[8];
             bool stop = false;
             entries++;
-            if (!(st & 0x100u)) {
+            if (!(v.st & 0x100u)) {
                 if (solid_hidden(eo, bd)) return false;
 #pragma unroll
                 for (int k = 0; k < 8; k++) cov[k] = 1.0f;
-                stop = (flags & 2u) != 0;
+                stop = (v.flags & 2u) != 0;
             } else {
-                const uint32_t f0 = fill_begin(b, p, gt), f1 = b.tile_fills[gt];
-                comp_fills += f1 - f0;
+                comp_fills += v.f1 - v.f0;
                 zero_cells(D);
-                alpha_coverage(b, f0, f1, bd, eo, D, prep[warp], cov);
+                alpha_coverage(b, v.f0, v.f1, bd, eo, D, prep[warp], cov);
                 __syncwarp();
             }
-            const uint32_t color = b.color[b.path_base + p];
+            const uint32_t color = v.color;
             const float pr = (float)(color & 0xffu) * inv255, pg = (float)((color >> 8) & 0xffu) * inv255,
                         pb = (float)((color >> 16) & 0xffu) * inv255, pa = (float)(color >> 24) * inv255;
             bool opaque = true;
@@ -1274,7 +1367,6 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
                 ar[k] += w * pr;
                 ag[k] += w * pg;
                 ab[k] += w * pb;
-                aa[k] += w;
                 tr[k] *= 1.0f - a;
                 opaque &= tr[k] == 0.0f;
             }
@@ -1293,7 +1385,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(Batch b) {
                         make_uchar4((unsigned char)__float2uint_rn(__saturatef(ar[k] + tr[k] * cr) * 255.0f),
                                     (unsigned char)__float2uint_rn(__saturatef(ag[k] + tr[k] * cg) * 255.0f),
                                     (unsigned char)__float2uint_rn(__saturatef(ab[k] + tr[k] * cb) * 255.0f),
-                                    (unsigned char)__float2uint_rn(__saturatef(aa[k] + tr[k] * ca) * 255.0f));
+                                    (unsigned char)__float2uint_rn(__saturatef(1.0f - tr[k] + tr[k] * ca) * 255.0f));
                 }
             }
         }
@@ -1334,13 +1426,12 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_list_dump(Batch b) {
         first = b.fb_count[fb];
         count = b.fb_count[fb + 1] - first;
     }
-    walk_fb_tile(b, S.row_first - b.row_base + fy, fx, fy,
-                 [&](uint32_t p, uint32_t gt, uint32_t st, uint32_t flags) -> bool {
-        if (kWrite && lane == 0) b.list[first + count - 1 - n] = gt;
+    walk_fb_tile<false>(b, S.row_first - b.row_base + fy, fx, [&](const Cand &v) -> bool {
+        if (kWrite && lane == 0) b.list[first + count - 1 - n] = v.gt;
         n++;
-        const int8_t bd = (int8_t)(st & 0xffu);
-        if (!(st & 0x100u) && (flags & 2u) && !solid_hidden((flags & 1u) != 0, bd)) {
-            z = (int32_t)p;
+        const int8_t bd = (int8_t)(v.st & 0xffu);
+        if (!(v.st & 0x100u) && (v.flags & 2u) && !solid_hidden((v.flags & 1u) != 0, bd)) {
+            z = (int32_t)v.p;
             return true;
         }
         return false;
@@ -1426,12 +1517,14 @@ cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Grid of a CTA class: as many CTAs as fit on every SM (they take paths by ticket).
 template <int kCls>
-static cudaError_t launch_fused(const Batch &b, int sms, cudaStream_t st) {
+static cudaError_t fused_grid(unsigned *grid) {
     const size_t smem = size_t(class_words(kCls)) * 4;
     static int configured_device = -1;
-    int dev = 0;
+    int dev = 0, sms = 152;
     cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (configured_device != dev) {
         const cudaError_t e =
             cudaFuncSetAttribute(k_bin_fused<kCls>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1439,10 +1532,30 @@ static cudaError_t launch_fused(const Batch &b, int sms, cudaStream_t st) {
         configured_device = dev;
     }
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin_fused<kCls>, class_threads(kCls), smem);
-    const unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)sms;
-    PF_LAUNCH(k_bin_fused<kCls><<<grid, class_threads(kCls), smem, st>>>(b));
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin_fused<kCls>, class_threads(kCls), smem);
+    if (e != cudaSuccess) return e;
+    *grid = (unsigned)std::max(1, per_sm) * (unsigned)sms;
+    return cudaSuccess;
+}
+
+template <int kCls>
+static cudaError_t launch_fused(const Batch &b, cudaStream_t st) {
+    unsigned grid = 0;
+    const cudaError_t e = fused_grid<kCls>(&grid);
+    if (e != cudaSuccess) return e;
+    PF_LAUNCH(k_bin_fused<kCls><<<grid, class_threads(kCls), size_t(class_words(kCls)) * 4, st>>>(b));
     return cudaGetLastError();
+}
+
+cudaError_t bin_stage_bytes(size_t *bytes) {
+    unsigned g0 = 0, g1 = 0, g2 = 0;
+    cudaError_t e;
+    if ((e = fused_grid<0>(&g0)) != cudaSuccess) return e;
+    if ((e = fused_grid<1>(&g1)) != cudaSuccess) return e;
+    if ((e = fused_grid<2>(&g2)) != cudaSuccess) return e;
+    *bytes = 8 * std::max({size_t(g0) * class_stage(0), size_t(g1) * class_stage(1), size_t(g2) * class_stage(2)});
+    return cudaSuccess;
 }
 
 // Class 3 (zero, count, backdrops and offsets, write; each returns at once when the class is
@@ -1457,9 +1570,9 @@ cudaError_t launch_bin_paths(const Batch &b, cudaStream_t st) {
     PF_LAUNCH(k_bin_large_prep<<<sms * 2, kPrepThreads, 0, st>>>(b));
     PF_LAUNCH(k_bin_large<true><<<sms * 8, kThreads, 0, st>>>(b));
     cudaError_t e;
-    if ((e = launch_fused<2>(b, sms, st)) != cudaSuccess) return e;
-    if ((e = launch_fused<1>(b, sms, st)) != cudaSuccess) return e;
-    return launch_fused<0>(b, sms, st);
+    if ((e = launch_fused<2>(b, st)) != cudaSuccess) return e;
+    if ((e = launch_fused<1>(b, st)) != cudaSuccess) return e;
+    return launch_fused<0>(b, st);
 }
 
 cudaError_t launch_pool_lists(const Batch &b, bool scatter, cudaStream_t st) {
