@@ -34,6 +34,8 @@ PKG = os.path.join(ROOT, "pathfinder-cpp_gb300")
 sys.path.insert(0, PKG)
 
 METRIC = "frame ms & scenes/s: batched+learned vs plain CUDA pipeline, 1 GB300, exact tiles"
+# From profiles/bin_fused_batched32.md: DRAM bytes of k_bin_fused<0..2> / their algorithmic bytes.
+BIN_TRAFFIC_PER_ALGORITHMIC_BYTE = 1.04
 UNIT = "scenes/s"
 
 
@@ -288,7 +290,11 @@ def main():
     plain_pass()
     ms_plain, launches_plain = timed(plain_pass, max(1, min(args.steps, 3)))
 
-    # 4. end to end through the C-ABI: pinned H2D upload, frame, D2H of every image
+    # 4. end to end through the C-ABI: pinned H2D upload, frame, every image delivered to
+    #    pinned host memory.  The composite writes the images straight into the host buffer
+    #    over NVLink-C2C (pf_set_host_image), so they cross while it runs.
+    r.set_host_image(img_host.data_ptr(), img_bytes)
+
     def e2e_step():
         r.upload_views(views)
         s = frame()
@@ -297,6 +303,7 @@ def main():
     for _ in range(max(1, args.warmup // 2)):
         e2e_step()
     ms_e2e, _ = timed(e2e_step, args.steps)
+    r.set_host_image(None)
 
     # one more (untimed) frame with the composite's work counters on, for the roofline's bytes
     r.set_flags(stage_timing=True, counters=True)
@@ -307,17 +314,30 @@ def main():
     st["composited_fills"] = st_c["composited_fills"]
     st["walk_chunks"] = int(r.debug_counters()[15])  # 32-candidate chunks the composite's z-walks read
 
-    # roofline of the composite kernel (fused coverage + src-over)
-    pixels = sum(int(np.ceil(s.width)) * int(np.ceil(s.height)) for s in scenes_list)
-    comp_bytes = (8 * st["composited_fills"] + 13 * st["composite_entries"]
-                  + 8 * (st["framebuffer_tiles"] + 1) + 4 * pixels)
-    comp_ms = st["ms_composite"]
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, peak_src = 6800.0, "fallback 6.8 TB/s"
     if os.path.exists(peaks_path):
         with open(peaks_path) as f:
             peak = float(json.load(f)["hbm_gbs"])
         peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+
+    # roofline of the dominant kernel: binning (k_bin_fused, the three CTA classes, with the
+    # classification and the class-3 passes that run empty here), timed by the library's
+    # stage events on the frame's stream over the timed steps.  Algorithmic bytes: every leaf
+    # line read once (16 B), every fill written (8 B), every tile's state and end offset
+    # written (2 + 4 B), every path record read and its fill block written (32 + 4 B).
+    bin_ms = sum(x["ms_bin"] for x in stats_b) / len(stats_b)
+    bin_bytes = 16 * st["microlines"] + 8 * st["fills"] + 6 * st["tiles"] + 36 * st["paths"]
+    bin_achieved = bin_bytes / (bin_ms * 1e-3) / 1e9 if bin_ms > 0 else None
+    # DRAM bytes per algorithmic byte of the binning kernels in the ncu capture of the
+    # 32-scene batch (dram__bytes_read.sum + dram__bytes_write.sum over k_bin_fused<0..2>)
+    bin_traffic_ratio = BIN_TRAFFIC_PER_ALGORITHMIC_BYTE
+
+    # roofline of the composite kernel (fused coverage + src-over)
+    pixels = sum(int(np.ceil(s.width)) * int(np.ceil(s.height)) for s in scenes_list)
+    comp_bytes = (8 * st["composited_fills"] + 13 * st["composite_entries"]
+                  + 8 * (st["framebuffer_tiles"] + 1) + 4 * pixels)
+    comp_ms = sum(x["ms_composite"] for x in stats_b) / len(stats_b)
     achieved = comp_bytes / (comp_ms * 1e-3) / 1e9 if comp_ms > 0 else None
 
     cpu = None
@@ -342,15 +362,22 @@ def main():
             "speedup_vs_plain": ms_plain / ms_batched,
             "sizer": sizer,
             "e2e": {"value": world * n_scenes / (ms_e2e * 1e-3), "unit": UNIT, "ms_per_step": ms_e2e,
-                    "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": img_bytes},
+                    "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": img_bytes,
+                    "images": "composited into pinned host memory (pf_set_host_image)"},
             "stages_ms": {k: st[k] for k in ("ms_setup", "ms_flatten", "ms_bin", "ms_propagate", "ms_lists",
                                              "ms_composite", "ms_total")},
             "counts": {k: st[k] for k in ("paths", "segments", "microlines", "tiles", "fills", "composite_entries",
                                           "composited_fills", "framebuffer_tiles", "walk_chunks",
                                           "host_syncs")},
-            "roofline": {"kernel": "k_composite", "bound": "hbm", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
-                         "peak_source": peak_src, "algorithmic_bytes": comp_bytes},
+            "roofline": {"kernel": "k_bin_fused (binning stage)", "bound": "hbm", "achieved": bin_achieved,
+                         "peak": peak, "unit": "GB/s", "frac": (bin_achieved / peak) if bin_achieved else None,
+                         "traffic": bin_traffic_ratio * bin_bytes / 1e9, "traffic_unit": "GB per launch",
+                         "algorithmic_bytes": bin_bytes, "ms": bin_ms, "peak_source": peak_src,
+                         "note": "latency/compute bound: the exact-IEEE tile walk per line; DRAM traffic is "
+                                 "the algorithmic minimum"},
+            "roofline_composite": {"kernel": "k_composite", "bound": "hbm", "achieved": achieved, "peak": peak,
+                                   "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                                   "traffic": None, "algorithmic_bytes": comp_bytes, "ms": comp_ms},
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": int(st["kernel_launches"]) * args.steps,

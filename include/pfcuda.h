@@ -207,6 +207,17 @@ int pf_sizer_last_frame(void *ctx, uint32_t *paths_over_budget, uint32_t *pool_s
 int pf_sizer_predict(void *ctx, const float *features, uint32_t n, float *out);
 
 /*
+ * Composite every later frame straight into host memory: `host` (at least pf_image_bytes bytes;
+ * scene i's image at pf_image_offset(i)) receives the RGBA8 images over the GPU's coherent
+ * link while the composite runs, so no copy follows the frame and pf_read_images into the same
+ * buffer returns at once.  The buffer is pinned and mapped here (cudaHostRegister) unless the
+ * caller pinned it already; NULL restores device-resident images.  No counterpart in the
+ * reference (its destination is a GPU texture, Renderer::get_dest_texture,
+ * pathfinder/core/renderer.h:82).
+ */
+int pf_set_host_image(void *ctx, void *host, size_t bytes);
+
+/*
  * pf_sizer_predict without any device allocation, for callers that cannot call cudaMalloc
  * (a render loop that must not stall the device, a CUDA-graph capture in progress, or GPU
  * memory owned by another allocator).  No counterpart in the reference.  Features and

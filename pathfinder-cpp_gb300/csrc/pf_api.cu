@@ -93,6 +93,11 @@ struct Ctx {
     DevBuf tile_fills, tile_state, col_above, col_final, fills, path_fill, path_cls, bin_stage;
     DevBuf row_first, row_paths, scene_row_first;
     DevBuf z, fb_count, list, image, status, scan_temp;
+    // host image target (pf_set_host_image): frames composite straight into this host buffer
+    uint8_t *host_img = nullptr;      // host address
+    uint8_t *host_img_dev = nullptr;  // the same memory as the device addresses it
+    size_t host_img_bytes = 0;
+    bool host_img_registered = false; // pinned by this context (unpinned when replaced)
     uint32_t *h_status = nullptr;  // pinned
 
     // the scene range of the last frame and its totals
@@ -349,7 +354,7 @@ Batch make_batch(Ctx *c) {
     b.z = c->z.as<int32_t>();
     b.fb_count = c->fb_count.as<uint32_t>();
     b.list = c->list.as<uint32_t>();
-    b.image = c->image.as<uint8_t>();
+    b.image = c->host_img_dev ? c->host_img_dev : c->image.as<uint8_t>();
     b.status = c->status.as<uint32_t>();
     b.counters = (c->flags & PF_CONFIG_FRAME_COUNTERS) ? 1u : 0u;
     return b;
@@ -402,6 +407,8 @@ void set_range(Ctx *c, uint32_t first, uint32_t count) {
 
 int begin_frame(Ctx *c, uint32_t first, uint32_t count) {
     if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
+    if (c->host_img && c->host_img_bytes < c->image_bytes)
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "the host image buffer is smaller than the batch's images");
     if (count == 0 || first >= c->n_scenes || count > c->n_scenes - first)
         return fail(c, PF_ERR_INVALID_ARGUMENT, "scene range out of bounds");
     c->rendered = false;
@@ -803,9 +810,23 @@ int read_image(Ctx *c, uint32_t si, uint8_t *rgba, size_t cap) {
     const SceneDev &S = c->h_scenes[si];
     const size_t bytes = size_t(S.img_w) * S.img_h * 4;
     if (!rgba || cap < bytes) return fail(c, PF_ERR_INVALID_ARGUMENT, "image buffer too small");
+    if (c->host_img) {
+        // the frame already wrote the image into host memory
+        if (rgba != c->host_img + S.img_offset) std::memcpy(rgba, c->host_img + S.img_offset, bytes);
+        return PF_OK;
+    }
     PF_CUDA(cudaMemcpyAsync(rgba, c->image.as<uint8_t>() + S.img_offset, bytes, cudaMemcpyDeviceToHost, c->stream));
     PF_CUDA(cudaStreamSynchronize(c->stream));
     return PF_OK;
+}
+
+// Unpin a host image target this context pinned.
+void drop_host_image(Ctx *c) {
+    if (c->host_img_registered) cudaHostUnregister(c->host_img);
+    c->host_img = nullptr;
+    c->host_img_dev = nullptr;
+    c->host_img_bytes = 0;
+    c->host_img_registered = false;
 }
 
 Ctx *as_ctx(void *p) { return static_cast<Ctx *>(p); }
@@ -833,14 +854,57 @@ extern "C" int pf_read_images(void *ctx, uint8_t *dst, size_t capacity_bytes) {
     if (!c || !dst) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
     if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
     if (capacity_bytes < c->image_bytes) return fail(c, PF_ERR_INVALID_ARGUMENT, "image buffer too small");
+    if (c->host_img) {
+        if (dst != c->host_img) std::memcpy(dst, c->host_img, c->image_bytes);
+        return PF_OK;
+    }
     PF_CUDA(cudaMemcpyAsync(dst, c->image.p, c->image_bytes, cudaMemcpyDeviceToHost, c->stream));
     PF_CUDA(cudaStreamSynchronize(c->stream));
     return PF_OK;
 }
 
-namespace {
-
-}  // namespace
+// Frames composite straight into host memory over the GPU's coherent link (NVLink-C2C on
+// GB300): the pixels cross to the host while the composite runs, and no copy follows the
+// frame.  The buffer is pinned and mapped here unless the caller pinned it already (then it
+// stays the caller's to unpin).  NULL restores device-resident images.
+extern "C" int pf_set_host_image(void *ctx, void *host, size_t bytes) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    cudaSetDevice(c->device);
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    drop_host_image(c);
+    c->rendered = false;
+    if (!host) return PF_OK;
+    if (bytes == 0) return fail(c, PF_ERR_INVALID_ARGUMENT, "empty host image buffer");
+    bool registered = false;
+    cudaPointerAttributes attr{};
+    cudaError_t e = cudaPointerGetAttributes(&attr, host);
+    if (e != cudaSuccess) cudaGetLastError();
+    if (e != cudaSuccess || attr.type != cudaMemoryTypeHost) {
+        // pageable memory: pin and map it here
+        e = cudaHostRegister(host, bytes, cudaHostRegisterMapped);
+        if (e == cudaSuccess) {
+            registered = true;
+        } else if (e == cudaErrorHostMemoryAlreadyRegistered) {
+            cudaGetLastError();
+        } else {
+            cudaGetLastError();
+            return cuda_fail(c, e, "cudaHostRegister(host image)");
+        }
+    }
+    void *dev = nullptr;
+    e = cudaHostGetDevicePointer(&dev, host, 0);
+    if (e != cudaSuccess) {
+        if (registered) cudaHostUnregister(host);
+        cudaGetLastError();
+        return cuda_fail(c, e, "cudaHostGetDevicePointer(host image)");
+    }
+    c->host_img = static_cast<uint8_t *>(host);
+    c->host_img_dev = static_cast<uint8_t *>(dev);
+    c->host_img_bytes = bytes;
+    c->host_img_registered = registered;
+    return PF_OK;
+}
 
 extern "C" {
 
@@ -888,6 +952,7 @@ int pf_ctx_destroy(void *ctx) {
     if (!c) return PF_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_host_image(c);
     DevBuf *bufs[] = {&c->sz_w, &c->sz_master, &c->sz_m, &c->sz_v, &c->sz_grad, &c->sz_loss, &c->sz_feat,
                       &c->sz_target, &c->sz_index, &c->sz_pred, &c->path_feat, &c->path_pred, &c->path_leaf_first,
                       &c->path_leaf_budget, &c->path_leaf_cursor, &c->path_fill_budget, &c->path_bounds,
@@ -958,7 +1023,7 @@ int pf_image_device_ptr(void *ctx, void **rgba, uint32_t *width_px, uint32_t *he
     Ctx *c = as_ctx(ctx);
     if (!c || !rgba) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
     if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
-    *rgba = c->image.as<uint8_t>() + c->h_scenes[c->r_first].img_offset;
+    *rgba = (c->host_img_dev ? c->host_img_dev : c->image.as<uint8_t>()) + c->h_scenes[c->r_first].img_offset;
     if (width_px) *width_px = c->h_scenes[c->r_first].img_w;
     if (height_px) *height_px = c->h_scenes[c->r_first].img_h;
     return PF_OK;

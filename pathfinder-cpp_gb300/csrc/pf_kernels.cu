@@ -488,6 +488,16 @@ __device__ void walk_line(const WalkCtx &w, float x0, float y0, float x1, float 
     const int32_t fx = (int32_t)floorf(fmul(x0, inv)), fy = (int32_t)floorf(fmul(y0, inv));
     const int32_t ex = (int32_t)floorf(fmul(x1, inv)), ey = (int32_t)floorf(fmul(y1, inv));
     const float vx = fsub(x1, x0), vy = fsub(y1, y0);
+    if (fx == ex && fy == ey) {
+        // A line inside one tile: the walk below would stop at its first step with t = 1
+        // (the next tile boundary in each direction lies beyond the end point, so both
+        // crossing parameters are >= 1 or infinite), add the one fill from (x0, y0) to
+        // (x0 + vx * 1, y0 + vy * 1), and neither an extra fill nor a backdrop delta.
+        uint2 q;
+        if (quantise(w, x0, y0, fadd(x0, vx), fadd(y0, vy), fx, fy, q))
+            on_fill((fy - w.ry0) * w.rw + (fx - w.rx0), q);
+        return;
+    }
     const int32_t sx = vx < 0.0f ? -1 : 1, sy = vy < 0.0f ? -1 : 1;
     const float cx = fmul(fadd((float)fx, vx >= 0.0f ? 1.0f : 0.0f), 16.0f);
     const float cy = fmul(fadd((float)fy, vy >= 0.0f ? 1.0f : 0.0f), 16.0f);
@@ -547,7 +557,7 @@ __device__ void walk_line(const WalkCtx &w, float x0, float y0, float x1, float 
 // redone by the exact two-pass method.
 constexpr int kLeafBatch = 8;
 
-__global__ void __launch_bounds__(kThreads) k_flatten_budget(Batch b, uint32_t n_segs) {
+__global__ void __launch_bounds__(kThreads, 8) k_flatten_budget(Batch b, uint32_t n_segs) {
     const uint32_t i = global_tid();
     if (i >= n_segs || i >= b.status[kStSegs]) return;
     const SegDev sg = b.segs[i];

@@ -30,6 +30,7 @@ EXPORTS = [
     "pf_sizer_init", "pf_sizer_set_params", "pf_sizer_get_params", "pf_sizer_set_margin", "pf_sizer_predict",
     "pf_sizer_gradient", "pf_sizer_train", "pf_sizer_save", "pf_sizer_load", "pf_path_features", "pf_path_counts",
     "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags", "pf_sizer_predict_noalloc",
+    "pf_set_host_image",
 ]
 
 N_FEATURES = 12
@@ -221,6 +222,11 @@ class Renderer:
     def read_images(self, dst_ptr: int, capacity: int) -> None:
         """Copy every image of the batch into host memory at dst_ptr (one transfer)."""
         self._check(self.lib.pf_read_images(self.ctx, C.c_void_p(dst_ptr), C.c_size_t(capacity)), self.ctx)
+
+    def set_host_image(self, host_ptr: Optional[int], capacity: int = 0) -> None:
+        """Composite later frames straight into host memory at host_ptr (None: device images)."""
+        self._check(self.lib.pf_set_host_image(self.ctx, C.c_void_p(host_ptr or 0), C.c_size_t(capacity)),
+                    self.ctx)
 
     def upload_views(self, views) -> None:
         """Upload a batch described by ready-made SceneView structs (host pointers)."""
