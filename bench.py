@@ -39,6 +39,21 @@ BIN_TRAFFIC_PER_ALGORITHMIC_BYTE = 1.04
 UNIT = "scenes/s"
 
 
+def replica_first_seed(rank: int) -> int:
+    """First scene seed of a rank's batch: replicas render disjoint batches (no collective)."""
+    return 1000 + 100000 * rank
+
+
+def max_over_ranks(ms: float, dist, device: str) -> float:
+    """The slowest rank's time (the whole job's step time); dist None for one process."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -222,7 +237,7 @@ def main():
             dist.barrier()
 
     # replicas: every rank renders its own batch (seeds offset by rank); no data-path collective
-    scenes_list = S.batched(n_scenes=args.scenes, first_seed=1000 + 100000 * rank)
+    scenes_list = S.batched(n_scenes=args.scenes, first_seed=replica_first_seed(rank))
     bufs, views, h2d_bytes = pack_pinned(scenes_list)
     stream = torch.cuda.Stream()
     r = pfcuda.Renderer(device=local_rank, stream=stream.cuda_stream, stage_timing=True)
@@ -241,11 +256,7 @@ def main():
         torch.cuda.synchronize()
         barrier()
         ms = e0.elapsed_time(e1) / steps
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms, out
+        return max_over_ranks(ms, dist, "cuda"), out
 
     learned = os.path.exists(pfcuda.DEFAULT_WEIGHTS)
     if learned:

@@ -89,7 +89,7 @@ struct Ctx {
     bool sz_ready = false;
     float sz_mul = 1.25f, sz_add = 8.0f, sz_pool = 0.10f;
     uint32_t last_paths_over = 0, last_pool_used = 0;
-    DevBuf segs, seg_leaves, leaves, pool_path, pool_cnt, pool_idx;
+    DevBuf segs, seg_leaves, seg_order, seg_ctl, leaves, pool_path, pool_cnt, pool_idx;
     DevBuf tile_fills, tile_state, col_above, col_final, fills, path_fill, path_cls, bin_stage;
     DevBuf row_first, row_paths, scene_row_first;
     DevBuf z, fb_count, list, image, status, scan_temp;
@@ -332,6 +332,7 @@ Batch make_batch(Ctx *c) {
     b.segs = c->segs.as<SegDev>();
     b.seg_cap = (uint32_t)std::min<size_t>(c->segs.cap / sizeof(SegDev), 0xffffffffu);
     b.seg_leaves = c->seg_leaves.as<uint32_t>();
+    b.seg_order = c->seg_order.as<uint32_t>();
     b.leaves = c->leaves.as<float4>();
     b.leaf_cap = (uint32_t)std::min<size_t>(c->leaves.cap / 16, 0xffffffffu);
     b.pool_path = nullptr;  // set by a learned frame
@@ -486,6 +487,8 @@ int stage_setup(Ctx *c, bool learned) {
     c->n_row_entries = c->h_status[kStRows];
     PF_CUDA(c->segs.ensure(size_t(c->n_segs) * sizeof(SegDev) + 16));
     PF_CUDA(c->seg_leaves.ensure((size_t(c->n_segs) + 1) * 4));
+    PF_CUDA(c->seg_order.ensure(size_t(c->n_segs) * 4 + 16));
+    PF_CUDA(c->seg_ctl.ensure(256));
     PF_CUDA(c->row_paths.ensure(size_t(c->n_row_entries) * 16 + 16));
     const size_t T = c->n_tiles, K = c->n_cols;
     PF_CUDA(c->tile_fills.ensure(T * 4 + 16));
@@ -581,6 +584,7 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     Batch b = make_batch(c);
     PF_CUDA(launch_contour_segments(b, true, st));
     PF_CUDA(launch_rows(b, true, st));
+    PF_CUDA(launch_seg_order(b, c->n_segs, c->seg_ctl.as<uint32_t>(), st));
     PF_CUDA(cudaMemsetAsync(b.seg_leaves + c->n_segs, 0, 4, st));
     PF_CUDA(launch_flatten(b, c->n_segs, false, st));
     if (int e = scan(c, b.seg_leaves, c->n_segs + 1, kStLeaves)) return e;
@@ -633,6 +637,7 @@ int render_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats
     b.pool_idx = c->pool_idx.as<uint32_t>();
     PF_CUDA(launch_contour_segments(b, true, st));
     PF_CUDA(launch_rows(b, true, st));
+    PF_CUDA(launch_seg_order(b, c->n_segs, c->seg_ctl.as<uint32_t>(), st));
     PF_CUDA(launch_flatten_budget(b, c->n_segs, st));
     record(c, 2);
     // the spill pool's lines listed by path, so each path's CTA finds them
@@ -960,7 +965,7 @@ int pf_ctx_destroy(void *ctx) {
                       &c->points, &c->pflags, &c->cstart, &c->pstart, &c->fill_rule, &c->color, &c->scenes,
                       &c->scene_path_first, &c->scene_contour_first, &c->scene_fb_first, &c->contour_point_first,
                       &c->contour_path, &c->paths, &c->path_tiles, &c->path_cols, &c->contour_segs,
-                      &c->path_contours, &c->segs, &c->seg_leaves, &c->leaves, &c->pool_path, &c->pool_cnt,
+                      &c->path_contours, &c->segs, &c->seg_leaves, &c->seg_order, &c->seg_ctl, &c->leaves, &c->pool_path, &c->pool_cnt,
                       &c->pool_idx, &c->tile_fills, &c->path_fill, &c->path_cls, &c->tile_state, &c->col_above,
                       &c->col_final, &c->fills, &c->bin_stage, &c->row_first,
                       &c->row_paths, &c->scene_row_first, &c->z, &c->fb_count, &c->list, &c->image,

@@ -111,6 +111,7 @@ struct Batch {
     // segments / leaves
     SegDev *segs;
     uint32_t seg_cap;
+    uint32_t *seg_order;                 // [segs] the order the flattening kernels take them in
     uint32_t *seg_leaves;                // [segs + 1] -> scanned
     float4 *leaves;
     uint32_t leaf_cap;
@@ -204,6 +205,8 @@ cudaError_t launch_budgets(const Batch &b, const float *pred, float mul, float a
 cudaError_t launch_path_counts(const Batch &b, const uint2 *path_contours, uint32_t *leaves, uint32_t *fills,
                                cudaStream_t st);
 cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t st);
+// Orders the segments by estimated subdivision depth (seg_order); ctl holds 32 words.
+cudaError_t launch_seg_order(const Batch &b, uint32_t n_segs, uint32_t *ctl, cudaStream_t st);
 // Binning by path: classify (leaf ranges, size classes), then bin every path (counts,
 // backdrops, fill offsets, fills).  A learned frame first lists its pooled lines by path:
 // count, scan pool_cnt, scatter.

@@ -364,14 +364,67 @@ __device__ void flatten_quad(float b0, float b1, float b2, float b3, float c0, f
     }
 }
 
+// Segment order for the flattening kernels.  A warp's lanes flatten 32 segments in step, so
+// its time is its largest segment's.  Segments are bucketed by the depth a uniform bisection
+// would need, ceil(log16 of the root's flatness value) - the value shrinks about 16-fold per
+// level - and the kernels take them bucket by bucket, deepest first, so a warp's segments have
+// like leaf counts.  The order changes no output: every segment writes its own leaf range
+// (exact frame) or reserves slots in its path's region (learned frame).
+constexpr int kSegBuckets = 16;
+
+__device__ __forceinline__ int seg_bucket(const Batch &b, const SegDev &sg) {
+    if (sg.kind == kSegLine || sg.kind == kSegClose) return 0;
+    const float2 p0 = b.points[sg.a], c0 = b.points[sg.a + 1], c1 = b.points[sg.a + 2];
+    float m;
+    if (sg.kind == kSegQuad) {
+        const float dx = c0.x - 0.5f * (p0.x + c1.x), dy = c0.y - 0.5f * (p0.y + c1.y);
+        m = 4.0f * (dx * dx + dy * dy);
+    } else {
+        const float2 p3 = b.points[sg.a + 3];
+        const float ux = 3.0f * c0.x - 2.0f * p0.x - p3.x, uy = 3.0f * c0.y - 2.0f * p0.y - p3.y;
+        const float vx = 3.0f * c1.x - 2.0f * p3.x - p0.x, vy = 3.0f * c1.y - 2.0f * p3.y - p0.y;
+        m = fmaxf(ux * ux, vx * vx) + fmaxf(uy * uy, vy * vy);
+    }
+    if (!(m > 1.0f)) return 0;  // also NaN
+    const int d = (int)ceilf(__log2f(m) * 0.25f);
+    return d < kSegBuckets - 1 ? d : kSegBuckets - 1;
+}
+
+// ctl[0..15]: segments per bucket, then (scatter) ctl[16..31]: next slot per bucket
+template <bool kScatter>
+__global__ void __launch_bounds__(kThreads) k_seg_buckets(Batch b, uint32_t *ctl) {
+    const uint32_t i = global_tid();
+    const uint32_t n = b.status[kStSegs];
+    const int lane = threadIdx.x & 31;
+    const int bk = i < n ? seg_bucket(b, b.segs[i]) : -1;
+    const unsigned group = __match_any_sync(0xffffffffu, bk);
+    if (bk < 0) return;
+    const int leader = __ffs(group) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&ctl[(kScatter ? kSegBuckets : 0) + bk], (uint32_t)__popc(group));
+    base = __shfl_sync(group, base, leader);
+    if (kScatter) b.seg_order[base + __popc(group & ((1u << lane) - 1u))] = i;
+}
+
+// Bucket starts, deepest bucket first.
+__global__ void k_seg_bucket_starts(uint32_t *ctl) {
+    if (threadIdx.x != 0) return;
+    uint32_t run = 0;
+    for (int bk = kSegBuckets - 1; bk >= 0; bk--) {
+        ctl[kSegBuckets + bk] = run;
+        run += ctl[bk];
+    }
+}
+
 template <bool kWrite>
 __global__ void __launch_bounds__(kThreads) k_flatten(Batch b, uint32_t n_segs) {
-    const uint32_t i = global_tid();
-    if (i >= n_segs || i >= b.status[kStSegs]) return;
+    const uint32_t t = global_tid();
+    if (t >= n_segs || t >= b.status[kStSegs]) return;
     if (kWrite && b.status[kStLeaves] > b.leaf_cap) {
-        if (i == 0) atomicOr(&b.status[kStErr], kErrOverflowLeaf);
+        if (t == 0) atomicOr(&b.status[kStErr], kErrOverflowLeaf);
         return;
     }
+    const uint32_t i = b.seg_order ? b.seg_order[t] : t;
     const SegDev sg = b.segs[i];
     uint32_t out = kWrite ? b.seg_leaves[i] : 0u;
     uint32_t count = 0;
@@ -558,8 +611,9 @@ __device__ void walk_line(const WalkCtx &w, float x0, float y0, float x1, float 
 constexpr int kLeafBatch = 8;
 
 __global__ void __launch_bounds__(kThreads, 8) k_flatten_budget(Batch b, uint32_t n_segs) {
-    const uint32_t i = global_tid();
-    if (i >= n_segs || i >= b.status[kStSegs]) return;
+    const uint32_t t = global_tid();
+    if (t >= n_segs || t >= b.status[kStSegs]) return;
+    const uint32_t i = b.seg_order ? b.seg_order[t] : t;
     const SegDev sg = b.segs[i];
     const uint32_t region = b.path_leaf_first[sg.path], budget = b.path_leaf_budget[sg.path];
     float4 pend[kLeafBatch];
@@ -1514,6 +1568,16 @@ cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStre
     if (!n_segs) return cudaSuccess;
     if (write) PF_LAUNCH(k_flatten<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
     else PF_LAUNCH(k_flatten<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_seg_order(const Batch &b, uint32_t n_segs, uint32_t *ctl, cudaStream_t st) {
+    if (!n_segs) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(ctl, 0, 2 * kSegBuckets * 4, st);
+    if (e != cudaSuccess) return e;
+    PF_LAUNCH(k_seg_buckets<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, ctl));
+    PF_LAUNCH(k_seg_bucket_starts<<<1, 32, 0, st>>>(ctl));
+    PF_LAUNCH(k_seg_buckets<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, ctl));
     return cudaGetLastError();
 }
 
