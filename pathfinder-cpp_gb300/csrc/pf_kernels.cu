@@ -530,77 +530,170 @@ __device__ __forceinline__ bool quantise(const WalkCtx &w, float x0, float y0, f
     return true;
 }
 
-// Walk one line; on_fill(local_tile, packed) for every fill kept; on_delta(local_tile or
-// -1 - column, delta) for every backdrop change that lands in the rect or above it.
-template <class OnFill, class OnDelta>
-__device__ void walk_line(const WalkCtx &w, float x0, float y0, float x1, float y1, OnFill &&on_fill,
-                          OnDelta &&on_delta, uint32_t *status) {
-    if (!(isfinite(x0) && isfinite(y0) && isfinite(x1) && isfinite(y1))) return;
-    if (!clip_line(w, x0, y0, x1, y1, status)) return;
+// Walk of one line, split into a set-up and steps.  A step has a decision - which tile
+// boundary the line crosses next and at which parameter (crossing parameters accumulate, so
+// decisions are sequential) - and an emission: the fill(s) and backdrop delta of the tile,
+// which depend only on that step's decision and the one before.  on_fill(local_tile, packed)
+// for every fill kept; on_delta(local_tile or -1 - column, delta) for every backdrop change
+// that lands in the rect or above it.
+struct WalkState {
+    float x0, y0, vx, vy, tmx, tmy, tdx, tdy, curx, cury;
+    int32_t tcx, tcy, ex, ey, sx, sy;
+    int last;  // 0 none, 1 x, 2 y
+    uint32_t it;
+};
+
+struct WalkStep {
+    float curx, cury, nt;
+    int32_t tcx, tcy;
+    int last, next;
+};
+
+// False when nothing is left to step: a non-finite or clipped-away line, or a line inside one
+// tile, whose single fill is emitted here.
+template <class OnFill>
+__device__ __forceinline__ bool walk_begin(const WalkCtx &w, float x0, float y0, float x1, float y1, WalkState &s,
+                                           OnFill &&on_fill, uint32_t *status) {
+    if (!(isfinite(x0) && isfinite(y0) && isfinite(x1) && isfinite(y1))) return false;
+    if (!clip_line(w, x0, y0, x1, y1, status)) return false;
     const float inv = 1.0f / kTile;
     const int32_t fx = (int32_t)floorf(fmul(x0, inv)), fy = (int32_t)floorf(fmul(y0, inv));
     const int32_t ex = (int32_t)floorf(fmul(x1, inv)), ey = (int32_t)floorf(fmul(y1, inv));
     const float vx = fsub(x1, x0), vy = fsub(y1, y0);
     if (fx == ex && fy == ey) {
-        // A line inside one tile: the walk below would stop at its first step with t = 1
-        // (the next tile boundary in each direction lies beyond the end point, so both
-        // crossing parameters are >= 1 or infinite), add the one fill from (x0, y0) to
+        // A line inside one tile: the walk would stop at its first step with t = 1 (the next
+        // tile boundary in each direction lies beyond the end point, so both crossing
+        // parameters are >= 1 or infinite), add the one fill from (x0, y0) to
         // (x0 + vx * 1, y0 + vy * 1), and neither an extra fill nor a backdrop delta.
         uint2 q;
         if (quantise(w, x0, y0, fadd(x0, vx), fadd(y0, vy), fx, fy, q))
             on_fill((fy - w.ry0) * w.rw + (fx - w.rx0), q);
-        return;
+        return false;
     }
-    const int32_t sx = vx < 0.0f ? -1 : 1, sy = vy < 0.0f ? -1 : 1;
+    s.x0 = x0;
+    s.y0 = y0;
+    s.vx = vx;
+    s.vy = vy;
+    s.sx = vx < 0.0f ? -1 : 1;
+    s.sy = vy < 0.0f ? -1 : 1;
     const float cx = fmul(fadd((float)fx, vx >= 0.0f ? 1.0f : 0.0f), 16.0f);
     const float cy = fmul(fadd((float)fy, vy >= 0.0f ? 1.0f : 0.0f), 16.0f);
-    float tmx = fdiv(fsub(cx, x0), vx), tmy = fdiv(fsub(cy, y0), vy);
-    const float tdx = fabsf(fdiv(16.0f, vx)), tdy = fabsf(fdiv(16.0f, vy));
-    float curx = x0, cury = y0;
-    int32_t tcx = fx, tcy = fy;
-    int last = 0;  // 0 none, 1 x, 2 y
-    for (uint32_t it = 0;; it++) {
-        if (it >= kMaxWalk) {
-            atomicOr(status, kErrWalk);
-            return;
+    s.tmx = fdiv(fsub(cx, x0), vx);
+    s.tmy = fdiv(fsub(cy, y0), vy);
+    s.tdx = fabsf(fdiv(16.0f, vx));
+    s.tdy = fabsf(fdiv(16.0f, vy));
+    s.curx = x0;
+    s.cury = y0;
+    s.tcx = fx;
+    s.tcy = fy;
+    s.ex = ex;
+    s.ey = ey;
+    s.last = 0;
+    s.it = 0;
+    return true;
+}
+
+// The decision of the next step, which it records, and the walk state advanced past it;
+// false once the line is done (or the step bound is hit).
+__device__ __forceinline__ bool walk_decide(WalkState &s, WalkStep &r, uint32_t *status) {
+    if (s.it >= kMaxWalk) {
+        atomicOr(status, kErrWalk);
+        r.next = -1;  // nothing to emit
+        return false;
+    }
+    s.it++;
+    int next;
+    if (s.tmx < s.tmy) next = 1;
+    else if (s.tmx > s.tmy) next = 2;
+    else next = s.sx > 0 ? 1 : 2;
+    float nt = next == 1 ? s.tmx : s.tmy;
+    nt = (1.0f < nt) ? 1.0f : nt;
+    if (s.tcx == s.ex && s.tcy == s.ey) next = 0;
+    r.curx = s.curx;
+    r.cury = s.cury;
+    r.nt = nt;
+    r.tcx = s.tcx;
+    r.tcy = s.tcy;
+    r.last = s.last;
+    r.next = next;
+    if (next == 1) {
+        s.tmx = fadd(s.tmx, s.tdx);
+        s.tcx += s.sx;
+    } else if (next == 2) {
+        s.tmy = fadd(s.tmy, s.tdy);
+        s.tcy += s.sy;
+    } else {
+        return false;
+    }
+    s.curx = fadd(s.x0, fmul(s.vx, nt));
+    s.cury = fadd(s.y0, fmul(s.vy, nt));
+    s.last = next;
+    return true;
+}
+
+// The fills and backdrop delta of one decided step.
+template <class OnFill, class OnDelta>
+__device__ __forceinline__ void walk_emit(const WalkCtx &w, const WalkState &s, const WalkStep &r, OnFill &&on_fill,
+                                          OnDelta &&on_delta) {
+    const float npx = fadd(s.x0, fmul(s.vx, r.nt)), npy = fadd(s.y0, fmul(s.vy, r.nt));
+    const int32_t lx = r.tcx - w.rx0, ly = r.tcy - w.ry0;
+    uint2 q;
+    if (quantise(w, r.curx, r.cury, npx, npy, r.tcx, r.tcy, q)) on_fill(ly * w.rw + lx, q);
+    if (s.sy < 0 && r.next == 2) {
+        if (quantise(w, npx, npy, fmul((float)r.tcx, 16.0f), fmul((float)r.tcy, 16.0f), r.tcx, r.tcy, q))
+            on_fill(ly * w.rw + lx, q);
+    } else if (s.sy > 0 && r.last == 2) {
+        if (quantise(w, fmul((float)r.tcx, 16.0f), fmul((float)r.tcy, 16.0f), r.curx, r.cury, r.tcx, r.tcy, q))
+            on_fill(ly * w.rw + lx, q);
+    }
+    int delta = 0;
+    if (s.sx < 0 && r.last == 1) delta = 1;
+    else if (s.sx > 0 && r.next == 1) delta = -1;
+    if (delta != 0 && lx >= 0 && lx < w.rw && ly < w.rh) {
+        if (ly < 0) on_delta(-1 - lx, delta);
+        else on_delta(ly * w.rw + lx, delta);
+    }
+}
+
+// One lane walks one line.
+template <class OnFill, class OnDelta>
+__device__ void walk_line(const WalkCtx &w, float x0, float y0, float x1, float y1, OnFill &&on_fill,
+                          OnDelta &&on_delta, uint32_t *status) {
+    WalkState s;
+    if (!walk_begin(w, x0, y0, x1, y1, s, on_fill, status)) return;
+    for (;;) {
+        WalkStep r;
+        const bool more = walk_decide(s, r, status);
+        if (r.next >= 0) walk_emit(w, s, r, on_fill, on_delta);
+        if (!more) return;
+    }
+}
+
+// The whole warp walks one (long) line: every lane runs the same sequence of decisions, lane
+// j % 32 keeps step j, and the lanes emit their steps together, 32 steps per round.  The
+// decisions are a few instructions each, the emissions (clip, quantise, fills) the bulk.
+template <class OnFill, class OnDelta>
+__device__ void walk_line_warp(const WalkCtx &w, float4 f, OnFill &&on_fill, OnDelta &&on_delta, uint32_t *status) {
+    const int lane = threadIdx.x & 31;
+    WalkState s;
+    if (!walk_begin(w, f.x, f.y, f.z, f.w, s,
+                    [&](int32_t local, uint2 q) {
+                        if (lane == 0) on_fill(local, q);
+                    },
+                    status))
+        return;
+    bool more = true;
+    while (more) {
+        WalkStep mine;
+        mine.next = -1;
+#pragma unroll 1
+        for (int j = 0; j < 32 && more; j++) {
+            WalkStep r;
+            more = walk_decide(s, r, status);
+            if (j == lane) mine = r;
         }
-        int next;
-        if (tmx < tmy) next = 1;
-        else if (tmx > tmy) next = 2;
-        else next = sx > 0 ? 1 : 2;
-        float nt = next == 1 ? tmx : tmy;
-        nt = (1.0f < nt) ? 1.0f : nt;
-        if (tcx == ex && tcy == ey) next = 0;
-        const float npx = fadd(x0, fmul(vx, nt)), npy = fadd(y0, fmul(vy, nt));
-        const int32_t lx = tcx - w.rx0, ly = tcy - w.ry0;
-        uint2 q;
-        if (quantise(w, curx, cury, npx, npy, tcx, tcy, q)) on_fill(ly * w.rw + lx, q);
-        if (sy < 0 && next == 2) {
-            if (quantise(w, npx, npy, fmul((float)tcx, 16.0f), fmul((float)tcy, 16.0f), tcx, tcy, q))
-                on_fill(ly * w.rw + lx, q);
-        } else if (sy > 0 && last == 2) {
-            if (quantise(w, fmul((float)tcx, 16.0f), fmul((float)tcy, 16.0f), curx, cury, tcx, tcy, q))
-                on_fill(ly * w.rw + lx, q);
-        }
-        int delta = 0;
-        if (sx < 0 && last == 1) delta = 1;
-        else if (sx > 0 && next == 1) delta = -1;
-        if (delta != 0 && lx >= 0 && lx < w.rw && ly < w.rh) {
-            if (ly < 0) on_delta(-1 - lx, delta);
-            else on_delta(ly * w.rw + lx, delta);
-        }
-        if (next == 1) {
-            tmx = fadd(tmx, tdx);
-            tcx += sx;
-        } else if (next == 2) {
-            tmy = fadd(tmy, tdy);
-            tcy += sy;
-        } else {
-            break;
-        }
-        curx = npx;
-        cury = npy;
-        last = next;
+        if (mine.next >= 0) walk_emit(w, s, mine, on_fill, on_delta);
+        __syncwarp();
     }
 }
 
@@ -809,6 +902,14 @@ __global__ void k_bin_classify(Batch b, bool learned) {
     }
 }
 
+// Tiles a line's walk visits at most (its end points' tile distance, before clipping, plus one):
+// lines above kLongLine are walked by a whole warp.
+constexpr float kLongLine = 8.0f;
+__device__ __forceinline__ float line_span(const float4 &f) {
+    return fabsf(floorf(f.z * 0.0625f) - floorf(f.x * 0.0625f)) + fabsf(floorf(f.w * 0.0625f) - floorf(f.y * 0.0625f)) +
+           1.0f;
+}
+
 // A staged fill: the four 12-bit coordinates of the packed u16 fill and the tile (< 2^16).
 __device__ __forceinline__ uint2 stage_pack(uint2 q, uint32_t local) {
     const uint32_t x0 = q.x & 0xfffu, y0 = q.x >> 16, x1 = q.y & 0xfffu, y1 = q.y >> 16;
@@ -857,26 +958,37 @@ __global__ void __launch_bounds__(class_threads(kCls), class_min_ctas(kCls)) k_b
 
         // 1. fill counts and backdrop deltas, the fills staged with their tiles.  Warps take
         //    the lines 32 at a time, so a warp that drew short lines takes more.
+        //    A line of many tiles (a contour's closing line spans the canvas) would hold its
+        //    warp, and at the barrier its CTA, for tens of steps: such lines are walked by the
+        //    whole warp after its short lines.
+        auto on_fill = [&](int32_t local, uint2 q) {
+            atomicAdd(&cnt[local], 1u);
+            const uint32_t slot = atomicAdd(&s_nstage, 1u);
+            if (stage && slot < kStage) stage[slot] = stage_pack(q, (uint32_t)local);
+        };
+        auto on_delta = [&](int32_t where, int d) {
+            if (where >= 0) atomicAdd(&cnt[where], (uint32_t)d << 24);
+            else atomicAdd(&above[-1 - where], d);
+        };
         for (;;) {
             uint32_t k0 = 0;
             if (lane == 0) k0 = atomicAdd(&s_next, 32u);
             k0 = __shfl_sync(0xffffffffu, k0, 0);
             if (k0 >= L.n) break;
             const uint32_t k = k0 + (uint32_t)lane;
-            if (k >= L.n) continue;
-            const float4 f = b.leaves[L.index(b, k)];
-            walk_line(
-                w, f.x, f.y, f.z, f.w,
-                [&](int32_t local, uint2 q) {
-                    atomicAdd(&cnt[local], 1u);
-                    const uint32_t slot = atomicAdd(&s_nstage, 1u);
-                    if (stage && slot < kStage) stage[slot] = stage_pack(q, (uint32_t)local);
-                },
-                [&](int32_t where, int d) {
-                    if (where >= 0) atomicAdd(&cnt[where], (uint32_t)d << 24);
-                    else atomicAdd(&above[-1 - where], d);
-                },
-                err);
+            float4 f = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            bool along = false;
+            if (k < L.n) {
+                f = b.leaves[L.index(b, k)];
+                along = line_span(f) > kLongLine;
+                if (!along) walk_line(w, f.x, f.y, f.z, f.w, on_fill, on_delta, err);
+            }
+            for (unsigned m = __ballot_sync(0xffffffffu, along); m; m &= m - 1) {
+                const int l = __ffs(m) - 1;
+                const float4 g = make_float4(__shfl_sync(0xffffffffu, f.x, l), __shfl_sync(0xffffffffu, f.y, l),
+                                             __shfl_sync(0xffffffffu, f.z, l), __shfl_sync(0xffffffffu, f.w, l));
+                walk_line_warp(w, g, on_fill, on_delta, err);
+            }
         }
         __syncthreads();
 
