@@ -186,6 +186,9 @@ int pf_render_scenes(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_fram
  * set-up instead of the exact method's count-then-allocate passes).  Output is identical
  * to pf_render_scenes.  If a prediction is too small the frame is redone by the exact
  * method and stats->overflow is set.  Needs sizer weights (pf_sizer_load / _init).
+ * Once such a frame has run, it is recorded as a CUDA graph; the next learned frames over
+ * the same scene range replay it (one launch, one synchronisation: stats->host_syncs == 1)
+ * until the scenes, the sizer, the flags, the host image target or a buffer changes.
  */
 int pf_render_learned(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats);
 

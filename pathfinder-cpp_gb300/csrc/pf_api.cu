@@ -112,9 +112,21 @@ struct Ctx {
 
     HostCanon canon;
     cudaEvent_t ev[8] = {};
+
+    // The learned frame captured as a CUDA graph once it has run with its buffers sized: later
+    // frames over the same scenes replay it (one launch, one synchronisation) while the
+    // uploaded scenes, the sizer, the flags, the image target and every buffer stay the same.
+    cudaGraphExec_t lg_exec = nullptr;
+    uint32_t lg_first = 0, lg_count = 0, lg_flags = 0, lg_launches = 0;
+    uint32_t lg_status[kStCount] = {};  // the totals the captured frame was sized for
+    std::vector<void *> lg_ptrs;        // the buffers it uses, by address
+    bool capturing = false;             // recording the graph: no host synchronisation
+    bool learned_done = false;          // the last learned frame ran the learned path to the end
 };
 
 thread_local std::string g_last_error;
+
+void drop_graph(Ctx *c);
 
 int fail(Ctx *c, int code, const std::string &msg) {
     if (c) c->err = msg;
@@ -195,6 +207,7 @@ struct CopyPlan {
 
 int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     if (!scenes || n == 0) return fail(c, PF_ERR_INVALID_ARGUMENT, "no scenes");
+    drop_graph(c);
     uint64_t P = 0, C = 0, N = 0, fb = 0, img = 0, cs = 0, ps = 0;
     c->h_scenes.assign(n, SceneDev{});
     c->h_scene_fb_first.assign(n + 1, 0);
@@ -362,6 +375,7 @@ Batch make_batch(Ctx *c) {
 }
 
 int read_status(Ctx *c) {
+    if (c->capturing) return PF_OK;  // the captured frame's totals are already in h_status
     PF_CUDA(cudaMemcpyAsync(c->h_status, c->status.p, kStCount * 4, cudaMemcpyDeviceToHost, c->stream));
     PF_CUDA(cudaStreamSynchronize(c->stream));
     c->syncs++;
@@ -389,7 +403,10 @@ int scan(Ctx *c, uint32_t *arr, uint32_t n, int slot) {
 }
 
 void record(Ctx *c, int i) {
-    if (c->flags & PF_CONFIG_STAGE_TIMING) cudaEventRecord(c->ev[i], c->stream);
+    if (!(c->flags & PF_CONFIG_STAGE_TIMING)) return;
+    // while a graph is recorded, an external record makes the event a node the replay records
+    if (c->capturing) cudaEventRecordWithFlags(c->ev[i], c->stream, cudaEventRecordExternal);
+    else cudaEventRecord(c->ev[i], c->stream);
 }
 
 void set_range(Ctx *c, uint32_t first, uint32_t count) {
@@ -556,7 +573,7 @@ int finish_frame(Ctx *c, uint32_t first, uint32_t count, uint64_t launches0, pf_
         stats->alpha_tiles = 0;
         stats->kernel_launches = (uint32_t)(launches() - launches0);
         stats->host_syncs = c->syncs;
-        if (c->flags & PF_CONFIG_STAGE_TIMING) {
+        if ((c->flags & PF_CONFIG_STAGE_TIMING) && !c->capturing) {
             float ms[6] = {};
             for (int i = 0; i < 6; i++) cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]);
             stats->ms_setup = ms[0];
@@ -609,8 +626,8 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
 // same kernel) and the frame synchronises only after set-up.  If a path overruns its leaf
 // budget or the fills overrun the capacity, the frame is redone by the exact two-pass method
 // (the reference's own recovery, renderer.cpp:540-577, made exact).
-int render_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
-    if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights loaded");
+int render_learned_frame(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
+    c->learned_done = false;
     if (int e = begin_frame(c, first, count)) return e;
     const uint64_t launches0 = launches();
     cudaStream_t st = c->stream;
@@ -661,6 +678,115 @@ int render_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats
         stats->microlines = c->n_leaves;
         stats->overflow = 0;
     }
+    c->learned_done = e == PF_OK;
+    return e;
+}
+
+// The buffers a learned frame uses, by address (a reallocated one invalidates the graph).
+std::vector<void *> frame_buffers(const Ctx *c) {
+    const DevBuf *bufs[] = {&c->status, &c->contour_point_first, &c->contour_path, &c->paths, &c->path_tiles,
+                            &c->path_cols, &c->path_contours, &c->path_bounds, &c->row_first, &c->bin_list,
+                            &c->bin_ctl, &c->path_leaf_range, &c->path_fill, &c->path_cls, &c->bin_stage,
+                            &c->path_feat, &c->path_pred, &c->path_leaf_first, &c->path_leaf_budget,
+                            &c->path_leaf_cursor, &c->path_fill_budget, &c->segs, &c->seg_leaves, &c->seg_order,
+                            &c->seg_ctl, &c->row_paths, &c->tile_fills, &c->tile_state, &c->col_above,
+                            &c->col_final, &c->leaves, &c->pool_path, &c->pool_idx, &c->pool_cnt, &c->fills,
+                            &c->scan_temp, &c->image, &c->sz_w};
+    std::vector<void *> v;
+    for (const DevBuf *d : bufs) v.push_back(d->p);
+    v.push_back(c->host_img_dev);
+    return v;
+}
+
+void drop_graph(Ctx *c) {
+    if (c->lg_exec) cudaGraphExecDestroy(c->lg_exec);
+    c->lg_exec = nullptr;
+}
+
+// Records the learned frame over [first, first + count) as a graph, right after the same frame
+// ran with the same buffers.  A failure leaves the plain path in use.
+void capture_learned(Ctx *c, uint32_t first, uint32_t count) {
+    drop_graph(c);
+    uint32_t saved[kStCount];
+    std::memcpy(saved, c->h_status, sizeof saved);
+    const bool rendered = c->rendered, dumped = c->lists_dumped;
+    const uint32_t syncs = c->syncs;
+    const uint64_t l0 = launches();
+    cudaGraph_t g = nullptr;
+    c->capturing = true;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
+    int r = PF_ERR_CUDA;
+    if (e == cudaSuccess) {
+        pf_frame_stats scratch;
+        r = render_learned_frame(c, first, count, &scratch);
+        e = cudaStreamEndCapture(c->stream, &g);
+    }
+    c->capturing = false;
+    std::memcpy(c->h_status, saved, sizeof saved);
+    c->rendered = rendered;
+    c->lists_dumped = dumped;
+    c->syncs = syncs;
+    if (e == cudaSuccess && r == PF_OK && g) e = cudaGraphInstantiate(&c->lg_exec, g, 0);
+    else e = cudaErrorUnknown;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (e != cudaSuccess) {
+        c->lg_exec = nullptr;
+        return;
+    }
+    c->lg_first = first;
+    c->lg_count = count;
+    c->lg_flags = c->flags;
+    c->lg_launches = (uint32_t)(launches() - l0);
+    std::memcpy(c->lg_status, saved, sizeof saved);
+    c->lg_ptrs = frame_buffers(c);
+}
+
+constexpr int kReplayMiss = -1;
+
+// Replays the captured learned frame; kReplayMiss when it does not apply (or its frame came out
+// different from the one it was sized for), and the caller runs the plain frame.
+int replay_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
+    if (!c->lg_exec || c->lg_first != first || c->lg_count != count || c->lg_flags != c->flags ||
+        c->lg_ptrs != frame_buffers(c)) {
+        drop_graph(c);
+        return kReplayMiss;
+    }
+    c->rendered = false;
+    c->lists_dumped = false;
+    set_range(c, first, count);
+    c->syncs = 0;
+    const uint64_t l0 = launches();
+    PF_CUDA(cudaGraphLaunch(c->lg_exec, c->stream));
+    if (int e = read_status(c)) return e;
+    const uint32_t *h = c->h_status, *want = c->lg_status;
+    if (h[kStErr] != 0 || h[kStSegs] != want[kStSegs] || h[kStTiles] != want[kStTiles] ||
+        h[kStCols] != want[kStCols] || h[kStRows] != want[kStRows] || h[kStLeafBudget] != want[kStLeafBudget] ||
+        h[kStFillBudget] != want[kStFillBudget]) {
+        drop_graph(c);
+        return kReplayMiss;
+    }
+    c->n_leaves = h[kStLeafCount];
+    c->n_fills = uint64_t(h[kStFill64]) | uint64_t(h[kStFill64 + 1]) << 32;
+    c->last_paths_over = h[kStPathsOver];
+    c->last_pool_used = h[kStPoolUsed];
+    const int e = finish_frame(c, first, count, l0, stats);
+    if (stats) {
+        stats->microlines = c->n_leaves;
+        stats->overflow = 0;
+        stats->kernel_launches = c->lg_launches;
+    }
+    return e;
+}
+
+int render_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
+    if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights loaded");
+    const int r = replay_learned(c, first, count, stats);
+    if (r != kReplayMiss) return r;
+    pf_frame_stats local;
+    pf_frame_stats *st = stats ? stats : &local;
+    const int e = render_learned_frame(c, first, count, st);
+    if (e == PF_OK && c->learned_done) capture_learned(c, first, count);
     return e;
 }
 
@@ -957,6 +1083,7 @@ int pf_ctx_destroy(void *ctx) {
     if (!c) return PF_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    drop_graph(c);
     drop_host_image(c);
     DevBuf *bufs[] = {&c->sz_w, &c->sz_master, &c->sz_m, &c->sz_v, &c->sz_grad, &c->sz_loss, &c->sz_feat,
                       &c->sz_target, &c->sz_index, &c->sz_pred, &c->path_feat, &c->path_pred, &c->path_leaf_first,
@@ -1148,6 +1275,7 @@ extern "C" {
 int pf_sizer_init(void *ctx, uint64_t seed) {
     Ctx *c = as_ctx(ctx);
     if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    drop_graph(c);
     cudaSetDevice(c->device);
     // He-uniform initialisation from a splitmix64 stream
     std::vector<float> w(kSizerParams, 0.0f);
@@ -1173,6 +1301,7 @@ int pf_sizer_param_count(void) { return kSizerParams; }
 int pf_sizer_set_params(void *ctx, const float *params, size_t n) {
     Ctx *c = as_ctx(ctx);
     if (!c || !params || n != (size_t)kSizerParams) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad sizer parameters");
+    drop_graph(c);
     cudaSetDevice(c->device);
     return sizer_upload(c, params);
 }
@@ -1189,6 +1318,7 @@ int pf_sizer_get_params(void *ctx, float *params, size_t n) {
 int pf_sizer_set_margin(void *ctx, float mul, float add, float pool) {
     Ctx *c = as_ctx(ctx);
     if (!c || !(mul > 0.0f) || !(add >= 0.0f) || !(pool >= 0.0f)) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad margin");
+    drop_graph(c);
     c->sz_mul = mul;
     c->sz_add = add;
     c->sz_pool = pool;
@@ -1247,6 +1377,7 @@ int pf_sizer_train(void *ctx, const float *feat, const float *target, uint32_t n
     Ctx *c = as_ctx(ctx);
     if (!c || !feat || !target || n == 0 || batch == 0) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad arguments");
     if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights");
+    drop_graph(c);
     cudaSetDevice(c->device);
     if (int e = upload_dataset(c, feat, target, n)) return e;
     PF_CUDA(c->sz_index.ensure(size_t(n) * 4 + 16));
@@ -1313,6 +1444,7 @@ int pf_sizer_save(void *ctx, const char *path) {
 int pf_sizer_load(void *ctx, const char *path) {
     Ctx *c = as_ctx(ctx);
     if (!c || !path) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    drop_graph(c);
     cudaSetDevice(c->device);
     FILE *f = std::fopen(path, "rb");
     if (!f) return fail(c, PF_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);

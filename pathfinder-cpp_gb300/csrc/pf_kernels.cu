@@ -778,7 +778,7 @@ __global__ void __launch_bounds__(kThreads, 8) k_flatten_budget(Batch b, uint32_
 // landing above the rect, summed as int32).
 constexpr int kCtaClasses = 3;
 __host__ __device__ constexpr uint32_t class_words(int c) { return c == 0 ? 1088u : c == 1 ? 4352u : 16896u; }
-__host__ __device__ constexpr int class_threads(int c) { return c == 2 ? 512 : 256; }
+__host__ __device__ constexpr int class_threads(int c) { return c == 2 ? 384 : 256; }
 // CTAs per SM the register budget is set for (shared memory allows 3 of class 2, 12 of class 1)
 __host__ __device__ constexpr int class_min_ctas(int c) { return c == 2 ? 3 : 6; }
 // Fills a CTA stages during its count walk (8 bytes each, in its own slice of a global buffer
