@@ -698,33 +698,40 @@ __device__ void walk_line_warp(const WalkCtx &w, float4 f, OnFill &&on_fill, OnD
 }
 
 // Learned frame: flatten one segment and store its leaf lines in the path's leaf region,
-// laid out from the sizer's budget (slots reserved eight at a time); lines past the budget
+// laid out from the sizer's budget (slots reserved four at a time); lines past the budget
 // spill into the shared pool.  An exhausted pool sets the overflow bit and the frame is
 // redone by the exact two-pass method.
-constexpr int kLeafBatch = 8;
+constexpr int kLeafBatch = 4;
 
-__global__ void __launch_bounds__(kThreads, 8) k_flatten_budget(Batch b, uint32_t n_segs) {
+__global__ void __launch_bounds__(kThreads, 5) k_flatten_budget(Batch b, uint32_t n_segs) {
     const uint32_t t = global_tid();
     if (t >= n_segs || t >= b.status[kStSegs]) return;
     const uint32_t i = b.seg_order ? b.seg_order[t] : t;
     const SegDev sg = b.segs[i];
     const uint32_t region = b.path_leaf_first[sg.path], budget = b.path_leaf_budget[sg.path];
-    float4 pend[kLeafBatch];
-    int npend = 0;
+    // pending leaves, in registers (an indexed array would live in local memory)
+    float4 q0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), q1 = q0, q2 = q0, q3 = q0;
+    uint32_t npend = 0;
     uint32_t produced = 0;
     auto flush = [&]() {
         if (!npend) return;
-        const uint32_t slot = atomicAdd(&b.path_leaf_cursor[sg.path], (uint32_t)npend);
-        const uint32_t in_region = slot >= budget ? 0u : min((uint32_t)npend, budget - slot);
-        for (uint32_t k = 0; k < in_region; k++) b.leaves[region + slot + k] = pend[k];
-        if (in_region < (uint32_t)npend) {
-            const uint32_t extra = (uint32_t)npend - in_region;
+        const uint32_t slot = atomicAdd(&b.path_leaf_cursor[sg.path], npend);
+        const uint32_t in_region = slot >= budget ? 0u : min(npend, budget - slot);
+        uint32_t q = 0;
+        if (in_region < npend) {
             if (slot <= budget && slot + npend > budget) atomicAdd(&b.status[kStPathsOver], 1u);
-            const uint32_t q = atomicAdd(&b.status[kStPoolUsed], extra);
-            for (uint32_t k = 0; k < extra; k++) {
-                if (q + k < b.leaf_pool_cap) {
-                    b.leaves[b.leaf_pool_first + q + k] = pend[in_region + k];
-                    b.pool_path[q + k] = sg.path;
+            q = atomicAdd(&b.status[kStPoolUsed], npend - in_region);
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < (uint32_t)kLeafBatch; k++) {
+            const float4 v = k == 0 ? q0 : k == 1 ? q1 : k == 2 ? q2 : q3;
+            if (k < in_region) {
+                b.leaves[region + slot + k] = v;
+            } else if (k < npend) {
+                const uint32_t j = q + (k - in_region);
+                if (j < b.leaf_pool_cap) {
+                    b.leaves[b.leaf_pool_first + j] = v;
+                    b.pool_path[j] = sg.path;
                 } else {
                     atomicOr(&b.status[kStErr], kErrOverflowLeaf);
                 }
@@ -733,8 +740,12 @@ __global__ void __launch_bounds__(kThreads, 8) k_flatten_budget(Batch b, uint32_
         npend = 0;
     };
     auto emit = [&](float x0, float y0, float x1, float y1) {
-        pend[npend++] = make_float4(x0, y0, x1, y1);
-        if (npend == kLeafBatch) flush();
+        const float4 v = make_float4(x0, y0, x1, y1);
+        if (npend == 0) q0 = v;
+        else if (npend == 1) q1 = v;
+        else if (npend == 2) q2 = v;
+        else q3 = v;
+        if (++npend == (uint32_t)kLeafBatch) flush();
         produced++;
     };
     const float2 p0 = b.points[sg.a];
@@ -994,7 +1005,7 @@ __global__ void __launch_bounds__(class_threads(kCls), class_min_ctas(kCls)) k_b
 
         // 2. the count of each warp's chunk of tiles; thread 0 reserves the path's block of
         //    fills with one atomic whose result it reads only after the column pass
-        const uint32_t chunk = ((T + kWarps - 1) / kWarps + 31u) & ~31u;
+        const uint32_t chunk = ((T + kWarps - 1) / kWarps + 127u) & ~127u;
         const uint32_t c0 = min(T, (uint32_t)warp * chunk), c1 = min(T, c0 + chunk);
         unsigned long long wsum = 0;  // 64-bit: a path's fills need not fit 32 bits (it then overflows)
         for (uint32_t t = c0 + lane; t < c1; t += 32) wsum += cnt[t] & 0xffffffu;
@@ -1048,21 +1059,44 @@ __global__ void __launch_bounds__(class_threads(kCls), class_min_ctas(kCls)) k_b
         }
         __syncthreads();
 
-        // 4. each warp scans its chunk into write cursors (shared) and end offsets (global)
+        // 4. each warp scans its chunk into write cursors (shared) and end offsets (global): a
+        //    lane takes four consecutive tiles (one 16-byte shared load; chunks start on
+        //    multiples of 128 tiles), and one warp scan covers 128 tiles
         uint32_t carry = s_base + s_warp[warp];
-        for (uint32_t t0 = c0; t0 < c1; t0 += 32) {
-            const uint32_t t = t0 + lane;
-            const uint32_t v = t < c1 ? (cnt[t] & 0xffffffu) : 0u;
-            uint32_t incl = v;
+        for (uint32_t t0 = c0; t0 < c1; t0 += 128) {
+            const uint32_t t = t0 + 4 * (uint32_t)lane;
+            uint32_t v[4];
+            if (t + 4 <= c1) {
+                const uint4 q = *reinterpret_cast<const uint4 *>(&cnt[t]);
+                v[0] = q.x & 0xffffffu;
+                v[1] = q.y & 0xffffffu;
+                v[2] = q.z & 0xffffffu;
+                v[3] = q.w & 0xffffffu;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) v[j] = t + j < c1 ? (cnt[t + j] & 0xffffffu) : 0u;
+            }
+            const uint32_t own = v[0] + v[1] + v[2] + v[3];
+            uint32_t incl = own;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t n = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += n;
             }
-            if (t < c1) {
-                cnt[t] = carry + incl - v;
-                b.tile_fills[tb + t] = carry + incl;
+            uint32_t e[5];
+            e[0] = carry + incl - own;
+#pragma unroll
+            for (int j = 0; j < 4; j++) e[j + 1] = e[j] + v[j];
+            if (t + 4 <= c1) {
+                *reinterpret_cast<uint4 *>(&cnt[t]) = make_uint4(e[0], e[1], e[2], e[3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    if (t + j < c1) cnt[t + j] = e[j];
             }
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (t + j < c1) b.tile_fills[tb + t + j] = e[j + 1];
             carry += __shfl_sync(0xffffffffu, incl, 31);
         }
         __syncthreads();
@@ -1419,7 +1453,7 @@ __device__ __forceinline__ void zero_cells(int *D) {
     __syncwarp();
 }
 
-constexpr int kCompWarps = 4;
+constexpr int kCompWarps = 1;
 
 // One framebuffer tile: walk the paths spanning its row from the topmost down, test 32
 // candidates at a time (one per lane), and visit the visible tiles in order.  A visible tile
@@ -1491,7 +1525,7 @@ __device__ __forceinline__ uint32_t fill_begin(const Batch &b, uint32_t p, uint3
     return gt == b.path_tiles[p] ? b.path_fill[p] : b.tile_fills[gt - 1];
 }
 
-__global__ void __launch_bounds__(kCompWarps * 32, 8) k_composite(Batch b) {
+__global__ void __launch_bounds__(kCompWarps * 32, 32 / kCompWarps) k_composite(Batch b) {
     __shared__ int cells[kCompWarps][kCovCells];
     __shared__ FillPrep prep[kCompWarps][32];
     // a frame whose leaf lines or fills overran their buffers is redone; nothing to read here
