@@ -35,7 +35,7 @@ sys.path.insert(0, PKG)
 
 METRIC = "frame ms & scenes/s: batched+learned vs plain CUDA pipeline, 1 GB300, exact tiles"
 # From profiles/kernels_full_batched32.md: DRAM bytes of k_bin_fused<0..2> / their algorithmic bytes.
-BIN_TRAFFIC_PER_ALGORITHMIC_BYTE = 1.36
+BIN_TRAFFIC_PER_ALGORITHMIC_BYTE = 1.16
 UNIT = "scenes/s"
 
 
