@@ -10,8 +10,14 @@
 //                                              -> k_bin_fused (one CTA per path: counts, backdrops,
 //                                                 offsets, fills grouped by tile; no linked lists);
 //                                                 k_bin_large* for rects too big for a CTA
-//   sort.comp                                  -> k_list_count / k_list_write / k_list_sort
+//   sort.comp (z-culled per-framebuffer-tile lists)
+//                                              -> k_rows (per framebuffer row: the spanning paths in
+//                                                 path order) + the front-to-back walk of k_composite,
+//                                                 which stops at the first occluder; k_list_dump
+//                                                 writes the lists out for the canonical read-back
 //   fill.comp + tile.comp                      -> k_composite (coverage never leaves the SM)
+//   (learned frame) per-path budgets            -> pf_sizer.cu: k_features, k_mlp_predict, k_budgets;
+//                                                 here k_flatten_budget and the spill-pool lists
 //
 // Integer outputs follow the reference's d3d9 CPU tiler bit for bit, so every float
 // operation on that path is written with __f*_rn intrinsics (no FMA contraction), in the
