@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define PF_ABI_VERSION 1
+#define PF_ABI_VERSION 2
 
 typedef enum pf_status {
     PF_OK = 0,
@@ -43,6 +43,9 @@ typedef enum pf_status {
 /* Fill rules (pathfinder/core/data/data.h:136-141). */
 #define PF_FILL_NONZERO 0u
 #define PF_FILL_EVEN_ODD 1u
+
+/* No clip path (pf_scene_view::path_clip). */
+#define PF_NO_CLIP 0xffffffffu
 
 /* Point flags (pathfinder/core/data/data.h:120-129). */
 #define PF_POINT_ON_CURVE 0u
@@ -67,6 +70,16 @@ typedef enum pf_status {
  *                 its right edge is rounded up to a multiple of 16 as in
  *                 Scene::set_view_box, pathfinder/core/scene.cpp:170-179)
  *   clear_color   RGBA8 colour the destination is cleared to
+ *   path_clip     [n_paths] or NULL: the scene-local index of the clip path of each path, or
+ *                 PF_NO_CLIP (DrawPath::clip_path, pathfinder/core/data/path.h:36)
+ *   path_is_clip  [n_paths] or NULL: 1 for a clip path (Scene::clip_paths, ClipPath,
+ *                 pathfinder/core/data/path.h:45-57): tiled like the others, never drawn, and
+ *                 not clipped itself.  Clip paths follow all draw paths.  A clipped draw tile
+ *                 follows Tiler::prepare_tiles (pathfinder/core/d3d9/tiler.cpp:386-431): culled
+ *                 outside the clip's rect or over a blank clip tile, drawn with the clip's mask
+ *                 when it is solid and the clip tile is an alpha tile, and drawn with the two
+ *                 masks combined (tile_clip_combine.frag: min of |mask + backdrop|) when both
+ *                 are alpha tiles.
  */
 typedef struct pf_scene_view {
     const float *points;
@@ -81,6 +94,8 @@ typedef struct pf_scene_view {
     float width;
     float height;
     uint32_t clear_color;
+    const uint32_t *path_clip;   /* ABI 2 */
+    const uint8_t *path_is_clip; /* ABI 2 */
 } pf_scene_view;
 
 /* Context configuration.  Zero-initialise and set what you need. */
@@ -141,6 +156,12 @@ typedef struct pf_canon {
     const uint64_t *fb_list_first;     /* [fb tiles + 1]                        */
     uint64_t n_list;
     const uint32_t *fb_list;           /* global tile indices, back to front    */
+    /* clipped draw tiles (ABI 2): 0 own mask, 1 the clip tile's mask (the draw tile was
+     * solid), 2 own mask combined with the clip tile's; the clip tile (global index, or
+     * UINT64_MAX) and, for 2, the draw tile's backdrop before it was zeroed */
+    const uint8_t *tile_mask;          /* [n_tiles] */
+    const uint64_t *tile_clip;         /* [n_tiles] */
+    const int8_t *tile_dest_backdrop;  /* [n_tiles] */
 } pf_canon;
 
 /* Library and device queries. */
@@ -271,6 +292,7 @@ int pf_read_canon_scene(void *ctx, uint32_t scene, pf_canon *out);
  * Coverage after the fill rule of every alpha tile of scene 0 of the last frame,
  * in tile order: *n_alpha x 256 floats (row-major 16x16).  With out == NULL only
  * *n_alpha is set.  A test and debugging aid (the frame itself never stores coverage).
+ * A clipped tile is listed with its own mask, before the clip is applied.
  */
 int pf_read_coverage(void *ctx, float *out, size_t capacity_floats, uint64_t *n_alpha);
 

@@ -34,6 +34,7 @@ class SceneView(C.Structure):
         ("path_start", C.c_void_p), ("fill_rule", C.c_void_p), ("color", C.c_void_p),
         ("n_points", C.c_uint32), ("n_contours", C.c_uint32), ("n_paths", C.c_uint32),
         ("width", C.c_float), ("height", C.c_float), ("clear_color", C.c_uint32),
+        ("path_clip", C.c_void_p), ("path_is_clip", C.c_void_p),
     ]
 
 
@@ -46,6 +47,7 @@ class Result(C.Structure):
         ("fb_tiles_x", C.c_uint32), ("fb_tiles_y", C.c_uint32), ("z", C.c_void_p),
         ("fb_list_first", C.c_void_p), ("n_list", C.c_uint64), ("fb_list", C.c_void_p),
         ("n_microlines", C.c_uint64), ("path_microlines", C.c_void_p), ("path_fills", C.c_void_p),
+        ("tile_mask", C.c_void_p), ("tile_clip", C.c_void_p), ("tile_dest_backdrop", C.c_void_p),
     ]
 
 
@@ -57,6 +59,11 @@ def scene_view(scene) -> "tuple[SceneView, list]":
             np.ascontiguousarray(scene.fill_rule, np.uint8), np.ascontiguousarray(scene.color, np.uint32)]
     v = SceneView(*(a.ctypes.data for a in arrs), scene.n_points, scene.n_contours, scene.n_paths,
                   scene.width, scene.height, scene.clear)
+    if getattr(scene, "path_clip", None) is not None:
+        clip = np.ascontiguousarray(scene.path_clip, np.uint32)
+        is_clip = np.ascontiguousarray(scene.path_is_clip, np.uint8)
+        v.path_clip, v.path_is_clip = clip.ctypes.data, is_clip.ctypes.data
+        arrs += [clip, is_clip]
     return v, arrs
 
 
@@ -82,6 +89,9 @@ def result_to_dict(r: Result) -> Dict[str, np.ndarray]:
         "z": _arr(r.z, nfb, np.int32),
         "fb_list_first": _arr(r.fb_list_first, nfb + 1, np.uint64),
         "fb_list": _arr(r.fb_list, r.n_list, np.uint32),
+        "tile_mask": _arr(r.tile_mask, r.n_tiles, np.uint8),
+        "tile_clip": _arr(r.tile_clip, r.n_tiles, np.uint64),
+        "tile_dest_backdrop": _arr(r.tile_dest_backdrop, r.n_tiles, np.int8),
     }
     if r.path_fills:
         d["path_fills"] = _arr(r.path_fills, r.n_paths, np.uint32)
@@ -179,7 +189,7 @@ def compare(a: Dict[str, np.ndarray], b: Dict[str, np.ndarray], keys=None) -> li
     """Names of canonical arrays that differ between two results."""
     keys = keys or ["path_rect", "path_tile_first", "path_column_first", "tile_alpha",
                     "tile_backdrop", "tile_fill_count", "fills", "column_backdrop", "fb_tiles",
-                    "fb_list_first", "fb_list"]
+                    "fb_list_first", "fb_list", "tile_mask", "tile_clip", "tile_dest_backdrop"]
     bad = []
     for k in keys:
         if a[k].shape != b[k].shape or not np.array_equal(a[k], b[k]):

@@ -451,8 +451,25 @@ static int validate(const pf_scene_view *s) {
     for (uint32_t c = 0; c < s->n_contours; c++)
         if (s->contour_start[c] > s->contour_start[c + 1]) return 1;
     if (!(s->width > 0.0f) || !(s->height > 0.0f)) return 1;
+    if (s->path_clip || s->path_is_clip) {
+        /* clip paths follow the draw paths, are not clipped, and draw paths name clip paths */
+        if (!s->path_clip || !s->path_is_clip) return 1;
+        int seen_clip = 0;
+        for (uint32_t p = 0; p < s->n_paths; p++) {
+            const uint32_t c = s->path_clip[p];
+            if (s->path_is_clip[p]) {
+                seen_clip = 1;
+                if (c != PF_NO_CLIP) return 1;
+            } else {
+                if (seen_clip) return 1;
+                if (c != PF_NO_CLIP && (c >= s->n_paths || !s->path_is_clip[c])) return 1;
+            }
+        }
+    }
     return 0;
 }
+
+static int is_clip_path(const pf_scene_view *s, uint32_t p) { return s->path_is_clip && s->path_is_clip[p]; }
 
 int pfo_tile_scene_mt(const pf_scene_view *s, int z_rule, int threads, pfo_result *out) {
     if (!out) return 1;
@@ -558,7 +575,53 @@ int pfo_tile_scene_mt(const pf_scene_view *s, int z_rule, int threads, pfo_resul
     }
     free(keys);
 
-    /* z-buffer and composite lists (scene_builder.cpp:18-95; propagate.comp:190-205; sort.comp) */
+    /* clipped draw tiles: Tiler::prepare_tiles (tiler.cpp:386-431) against the clip path's
+     * tile at the same coordinates, which is not clipped itself */
+    {
+        const uint64_t nt = out->n_tiles ? out->n_tiles : 1;
+        out->tile_mask = (uint8_t *)calloc(nt, 1);
+        out->tile_clip = (uint64_t *)malloc(sizeof(uint64_t) * nt);
+        out->tile_dest_backdrop = (int8_t *)calloc(nt, 1);
+        for (uint64_t t = 0; t < out->n_tiles; t++) out->tile_clip[t] = UINT64_MAX;
+        for (uint32_t p = 0; s->path_clip && p < n; p++) {
+            const uint32_t c = s->path_clip[p];
+            if (c == PF_NO_CLIP) continue;
+            const path_ctx *pc = &pcs[p], *cc = &pcs[c];
+            const uint64_t tb = out->path_tile_first[p], cb = out->path_tile_first[c];
+            for (int32_t y = 0; y < pc->rh; y++)
+                for (int32_t x = 0; x < pc->rw; x++) {
+                    const uint64_t g = tb + (uint64_t)y * pc->rw + x;
+                    const int32_t tx = pc->rx0 + x, ty = pc->ry0 + y;
+                    const uint8_t da = out->tile_alpha[g];
+                    const int8_t dbd = out->tile_backdrop[g];
+                    if (tx < cc->rx0 || tx >= cc->rx1 || ty < cc->ry0 || ty >= cc->ry1) {
+                        out->tile_alpha[g] = 0;  /* outside the clip's rect: culled */
+                        out->tile_backdrop[g] = 0;
+                        continue;
+                    }
+                    const uint64_t gc = cb + (uint64_t)(ty - cc->ry0) * cc->rw + (uint64_t)(tx - cc->rx0);
+                    const uint8_t ca = out->tile_alpha[gc];
+                    const int8_t cbd = out->tile_backdrop[gc];
+                    if (ca && da) {
+                        out->tile_mask[g] = 2;  /* both masks, combined */
+                        out->tile_clip[g] = gc;
+                        out->tile_dest_backdrop[g] = dbd;
+                        out->tile_backdrop[g] = 0;
+                    } else if (ca && !da && dbd != 0) {
+                        out->tile_mask[g] = 1;  /* a solid tile takes the clip's mask */
+                        out->tile_clip[g] = gc;
+                        out->tile_alpha[g] = 1;
+                        out->tile_backdrop[g] = cbd;
+                    } else if (!ca && cbd == 0) {
+                        out->tile_alpha[g] = 0;  /* blank clip tile: culled */
+                        out->tile_backdrop[g] = 0;
+                    }
+                }
+        }
+    }
+
+    /* z-buffer and composite lists (scene_builder.cpp:18-95; propagate.comp:190-205; sort.comp);
+     * clip paths are not drawn */
     const float vbr = view_box_right(s->width);
     const uint32_t fbw = (uint32_t)ceilf(vbr / (float)TILE);
     const uint32_t fbh = (uint32_t)ceilf(s->height / (float)TILE);
@@ -569,7 +632,7 @@ int pfo_tile_scene_mt(const pf_scene_view *s, int z_rule, int threads, pfo_resul
     for (size_t i = 0; i < nfb; i++) out->z[i] = -1;
     for (uint32_t p = 0; p < n; p++) {
         const int occludes = ((s->color[p] >> 24) & 0xffu) == 0xffu;
-        if (!occludes) continue;
+        if (!occludes || is_clip_path(s, p)) continue;
         const path_ctx *pc = &pcs[p];
         const uint64_t tb = out->path_tile_first[p];
         for (int32_t y = 0; y < pc->rh; y++)
@@ -593,6 +656,7 @@ int pfo_tile_scene_mt(const pf_scene_view *s, int z_rule, int threads, pfo_resul
             memcpy(cur, out->fb_list_first, sizeof(uint64_t) * nfb);
         }
         for (uint32_t p = 0; p < n; p++) {
+            if (is_clip_path(s, p)) continue;
             const path_ctx *pc = &pcs[p];
             const uint64_t tb = out->path_tile_first[p];
             for (int32_t y = 0; y < pc->rh; y++)
@@ -637,6 +701,9 @@ void pfo_free(pfo_result *r) {
     free(r->fb_list);
     free(r->path_microlines);
     free(r->path_fills);
+    free(r->tile_mask);
+    free(r->tile_clip);
+    free(r->tile_dest_backdrop);
     memset(r, 0, sizeof(*r));
 }
 
@@ -690,17 +757,37 @@ static double apply_rule(double c, int even_odd) {
     return v < 0.0 ? 0.0 : (v > 1.0 ? 1.0 : v);
 }
 
-/* coverage after the fill rule of alpha tile g into cov[256] (row-major 16x16) */
-static void alpha_tile_coverage(const pfo_result *r, const uint64_t *fill_first, uint64_t g, int8_t bd, int eo,
-                                double cov[256]) {
-    for (int k = 0; k < 256; k++) cov[k] = (double)bd;
+/* backdrop + signed areas of the fills of tile g, before the fill rule, into raw[256] */
+static void tile_raw(const pfo_result *r, const uint64_t *fill_first, uint64_t g, int8_t bd, double raw[256]) {
+    for (int k = 0; k < 256; k++) raw[k] = (double)bd;
     for (uint64_t f = fill_first[g]; f < fill_first[g + 1]; f++) {
         const uint16_t *q = r->fills + 4 * f;
         const double x0 = q[0] / 256.0, y0 = q[1] / 256.0, x1 = q[2] / 256.0, y1 = q[3] / 256.0;
         const int i0 = (int)floor(x0 < x1 ? x0 : x1), i1 = (int)ceil(x0 < x1 ? x1 : x0);
         for (int i = i0; i < i1 && i < 16; i++) {
             if (i < 0) continue;
-            for (int jj = 0; jj < 16; jj++) cov[jj * 16 + i] += fill_area(x0, y0, x1, y1, i, jj);
+            for (int jj = 0; jj < 16; jj++) raw[jj * 16 + i] += fill_area(x0, y0, x1, y1, i, jj);
+        }
+    }
+}
+
+/* coverage of a visible alpha tile g after the fill rule, into cov[256]: its own mask, the
+ * clip tile's mask (d3d9 tile.frag sampleMask with the draw path's rule), or both combined as
+ * tile_clip_combine.frag does (min of |mask + backdrop|, then the draw path's rule) */
+static void tile_coverage(const pfo_result *r, const uint64_t *fill_first, uint64_t g, int eo, double cov[256]) {
+    const uint8_t mode = r->tile_mask ? r->tile_mask[g] : 0;
+    if (mode == 0) {
+        tile_raw(r, fill_first, g, r->tile_backdrop[g], cov);
+    } else if (mode == 1) {
+        tile_raw(r, fill_first, r->tile_clip[g], r->tile_backdrop[g], cov);
+    } else {
+        double clip[256];
+        tile_raw(r, fill_first, g, r->tile_dest_backdrop[g], cov);
+        const uint64_t gc = r->tile_clip[g];
+        tile_raw(r, fill_first, gc, r->tile_backdrop[gc], clip);
+        for (int k = 0; k < 256; k++) {
+            const double a = fabs(cov[k]), b = fabs(clip[k]);
+            cov[k] = a < b ? a : b;
         }
     }
     for (int k = 0; k < 256; k++) cov[k] = apply_rule(cov[k], eo);
@@ -740,7 +827,7 @@ static void *render_worker(void *arg) {
             const int eo = j->s->fill_rule[p] == PF_FILL_EVEN_ODD;
             const int8_t bd = r->tile_backdrop[g];
             if (r->tile_alpha[g]) {
-                alpha_tile_coverage(r, j->fill_first, g, bd, eo, cov);
+                tile_coverage(r, j->fill_first, g, eo, cov);
             } else {
                 if (eo && (abs((int)bd) % 2) == 0) continue;
                 for (int k = 0; k < 256; k++) cov[k] = 1.0;
@@ -781,7 +868,7 @@ static void *coverage_worker(void *arg) {
     for (uint64_t g = j->first; g < r->n_tiles; g += j->step) {
         if (!r->tile_alpha[g]) continue;
         const uint32_t p = j->tile_path[g];
-        alpha_tile_coverage(r, j->fill_first, g, r->tile_backdrop[g], j->s->fill_rule[p] == PF_FILL_EVEN_ODD, cov);
+        tile_coverage(r, j->fill_first, g, j->s->fill_rule[p] == PF_FILL_EVEN_ODD, cov);
         for (int k = 0; k < 256; k++) j->cov_out[(size_t)g * 256 + k] = (float)cov[k];
     }
     return NULL;

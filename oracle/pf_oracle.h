@@ -51,6 +51,12 @@ typedef struct pfo_result {
     uint64_t n_microlines;       /* flattened leaf lines that reached the tile walk */
     uint32_t *path_microlines;   /* [n_paths] leaf lines per path */
     uint32_t *path_fills;        /* [n_paths] fills per path */
+    /* clipped draw tiles (Tiler::prepare_tiles, tiler.cpp:386-431): 0 own mask, 1 the clip
+     * tile's mask, 2 own mask combined with the clip tile's; the clip tile (global index or
+     * UINT64_MAX); for 2, the draw tile's backdrop before it was zeroed */
+    uint8_t *tile_mask;
+    uint64_t *tile_clip;
+    int8_t *tile_dest_backdrop;
 } pfo_result;
 
 /* Restated tiler: flatten, bin, propagate, z-buffer, composite lists.  The _mt

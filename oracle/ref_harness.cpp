@@ -13,6 +13,7 @@
 //     (visible tiles in path order and the z-buffer).
 // SceneBuilderD3D9::build itself is bypassed because it needs a GPU Renderer for the palette.
 #include <algorithm>
+#include <climits>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -61,7 +62,35 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
     builder.attach(&scene);
 
     const uint32_t n_paths = sv->n_paths;
-    std::vector<BuiltDrawPath> built(n_paths);
+    // clip paths follow the draw paths; each is tiled on its own (build_clip_path_on_cpu,
+    // pathfinder/core/d3d9/scene_builder.cpp:200-223) before the draw paths that use it
+    uint32_t n_draw = n_paths;
+    std::vector<uint32_t> clip_index(n_paths, 0xffffffffu);  // path -> index among the clip paths
+    std::vector<BuiltPath> built_clips;
+    if (sv->path_is_clip) {
+        for (uint32_t p = 0; p < n_paths; p++)
+            if (sv->path_is_clip[p]) {
+                if (n_draw == n_paths) n_draw = p;
+                clip_index[p] = uint32_t(built_clips.size());
+                built_clips.emplace_back();
+            } else if (n_draw != n_paths) {
+                return 4;  // a draw path after a clip path
+            }
+    }
+    std::vector<BuiltDrawPath> built(n_draw);
+    // clip paths' alpha tile ids -> (clip path, tile in its rect); draw tiles that name one are
+    // resolved to global tile indices once every path's first tile is known
+    std::map<uint32_t, std::pair<uint32_t, uint64_t>> alpha_clip;
+    struct ClipRef {
+        uint64_t g;           // draw tile (global)
+        uint32_t clip_path;
+        uint64_t clip_tile;   // in the clip path's rect
+        int src_backdrop;     // clip job's source backdrop, or INT32_MIN
+    };
+    std::vector<ClipRef> clip_refs;
+    std::vector<uint8_t> tile_mask;
+    std::vector<uint64_t> tile_clip;
+    std::vector<int8_t> tile_dest_backdrop;
     std::vector<int32_t> rect(4 * n_paths);
     std::vector<uint64_t> tile_first(n_paths + 1, 0), col_first(n_paths + 1, 0);
     std::vector<uint8_t> tile_alpha;
@@ -70,6 +99,33 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
     std::vector<uint16_t> fills;
     std::vector<int32_t> col_backdrop;
     std::vector<uint32_t> path_fills(n_paths, 0);
+
+    auto make_outline = [&](uint32_t p) {
+        Outline outline;
+        for (uint32_t c = sv->path_start[p]; c < sv->path_start[p + 1]; c++) {
+            Contour contour;
+            for (uint32_t i = sv->contour_start[c]; i < sv->contour_start[c + 1]; i++) {
+                contour.push_point(Vec2F(sv->points[2 * i], sv->points[2 * i + 1]),
+                                   static_cast<PointFlag>(sv->point_flags[i]), true);
+            }
+            contour.closed = true;
+            outline.push_contour(contour);
+        }
+        return outline;
+    };
+    std::vector<std::vector<Fill>> clip_fills(built_clips.size());
+    for (uint32_t p = n_draw; p < n_paths; p++) {
+        const FillRule rule = sv->fill_rule[p] ? FillRule::EvenOdd : FillRule::Winding;
+        TilingPathInfo info{};
+        info.type = TilingPathInfo::Type::Clip;
+        Tiler tiler(builder, clip_index[p], make_outline(p), rule, view_box, nullptr, {}, info);
+        tiler.generate_tiles();
+        built_clips[clip_index[p]] = tiler.object_builder.built_path;
+        clip_fills[clip_index[p]] = tiler.object_builder.fills;
+        const auto &tiles = built_clips[clip_index[p]].data.tiles.data;
+        for (uint64_t t = 0; t < tiles.size(); t++)
+            if (tiles[t].alpha_tile_id.is_valid()) alpha_clip[tiles[t].alpha_tile_id.value] = {p, t};
+    }
 
     for (uint32_t p = 0; p < n_paths; p++) {
         Outline outline;
@@ -84,16 +140,49 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
         }
 
         const FillRule rule = sv->fill_rule[p] ? FillRule::EvenOdd : FillRule::Winding;
-        TilingPathInfo info{};
-        info.type = TilingPathInfo::Type::Draw;
-        info.info.paint_id = 0;
-        info.info.blend_mode = BlendMode::SrcOver;
-        info.info.fill_rule = rule;
-
-        Tiler tiler(builder, p, outline, rule, view_box, nullptr, {}, info);
-        tiler.generate_tiles();
-
-        const BuiltPath &bp = tiler.object_builder.built_path;
+        const bool is_clip = p >= n_draw;
+        BuiltPath bp;
+        std::vector<Fill> own_fills;
+        std::vector<uint64_t> fill_tile;  // clipped draw paths: the tile of each fill
+        if (is_clip) {
+            bp = built_clips[clip_index[p]];
+            own_fills = clip_fills[clip_index[p]];
+        } else {
+            TilingPathInfo info{};
+            info.type = TilingPathInfo::Type::Draw;
+            info.info.paint_id = 0;
+            info.info.blend_mode = BlendMode::SrcOver;
+            info.info.fill_rule = rule;
+            std::shared_ptr<uint32_t> clip_id;
+            if (sv->path_clip && sv->path_clip[p] != PF_NO_CLIP) {
+                const uint32_t c = sv->path_clip[p];
+                if (c >= n_paths || clip_index[c] == 0xffffffffu) return 5;
+                clip_id = std::make_shared<uint32_t>(clip_index[c]);
+            }
+            Tiler tiler(builder, p, outline, rule, view_box, clip_id, built_clips, info);
+            tiler.generate_tiles();
+            bp = tiler.object_builder.built_path;
+            own_fills = tiler.object_builder.fills;
+            if (clip_id) {
+                // prepare_tiles takes the alpha tile id off a culled tile, while its fills keep
+                // linking to it: the fills' tiles come from the same path tiled without the clip,
+                // whose fills are the same sequence
+                Tiler plain(builder, p, outline, rule, view_box, nullptr, {}, info);
+                plain.generate_tiles();
+                const auto &ptiles = plain.object_builder.built_path.data.tiles.data;
+                std::map<uint32_t, uint64_t> plain_tile;
+                for (uint64_t t = 0; t < ptiles.size(); t++)
+                    if (ptiles[t].alpha_tile_id.is_valid()) plain_tile[ptiles[t].alpha_tile_id.value] = t;
+                const auto &pf = plain.object_builder.fills;
+                if (pf.size() != own_fills.size()) return 9;
+                fill_tile.assign(pf.size(), 0);
+                for (size_t k = 0; k < pf.size(); k++) {
+                    auto it = plain_tile.find(pf[k].link);
+                    if (it == plain_tile.end()) return 9;
+                    fill_tile[k] = it->second;
+                }
+            }
+        }
         const RectI tb = bp.tile_bounds;
         rect[4 * p + 0] = tb.left;
         rect[4 * p + 1] = tb.top;
@@ -104,26 +193,62 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
         tile_first[p + 1] = base + ntiles;
         col_first[p + 1] = col_first[p] + bp.data.backdrops.size();
 
+        // the path's own fills link to its own alpha tiles; a clipped solid tile may now name the
+        // clip's alpha tile (mask 1), found through the clip paths' ids
         std::map<uint32_t, uint64_t> alpha_to_tile;
+        if (fill_tile.empty())
+            for (const Fill &f : own_fills) alpha_to_tile[f.link] = UINT64_MAX;
         for (uint64_t t = 0; t < ntiles; t++) {
             const auto &tile = bp.data.tiles.data[t];
             tile_alpha.push_back(tile.alpha_tile_id.is_valid() ? 1 : 0);
             tile_backdrop.push_back(tile.backdrop);
             tile_fill_count.push_back(0);
-            if (tile.alpha_tile_id.is_valid()) alpha_to_tile[tile.alpha_tile_id.value] = t;
+            tile_mask.push_back(0);
+            tile_clip.push_back(UINT64_MAX);
+            tile_dest_backdrop.push_back(0);
+            if (!tile.alpha_tile_id.is_valid()) continue;
+            auto own = alpha_to_tile.find(tile.alpha_tile_id.value);
+            if (own != alpha_to_tile.end()) {
+                own->second = t;
+            } else if (!fill_tile.empty() && alpha_clip.find(tile.alpha_tile_id.value) == alpha_clip.end()) {
+                alpha_to_tile[tile.alpha_tile_id.value] = t;  // a clipped path's own alpha tile
+            } else {
+                auto ct = alpha_clip.find(tile.alpha_tile_id.value);
+                if (ct == alpha_clip.end()) return 6;  // an alpha tile with neither own fills nor a clip's
+                tile_mask.back() = 1;
+                clip_refs.push_back({base + t, ct->second.first, ct->second.second, INT32_MIN});
+            }
+        }
+        if (bp.data.clip_tiles) {
+            for (const auto &job : bp.data.clip_tiles->data) {
+                if (!(job.dest_tile_id.is_valid() && job.src_tile_id.is_valid())) continue;
+                auto d = alpha_to_tile.find(job.dest_tile_id.value);
+                auto c = alpha_clip.find(job.src_tile_id.value);
+                if (d == alpha_to_tile.end() || d->second == UINT64_MAX || c == alpha_clip.end()) return 7;
+                tile_mask[base + d->second] = 2;
+                tile_dest_backdrop[base + d->second] = int8_t(job.dest_backdrop);
+                clip_refs.push_back({base + d->second, c->second.first, c->second.second, int(job.src_backdrop)});
+            }
         }
         for (int32_t b : bp.data.backdrops) col_backdrop.push_back(b);
 
         // group this path's fills by tile, canonical order inside a tile
         std::vector<std::vector<uint64_t>> per_tile(ntiles);
-        for (const Fill &f : tiler.object_builder.fills) {
-            auto it = alpha_to_tile.find(f.link);
-            if (it == alpha_to_tile.end()) return 2;  // fill without its alpha tile: should not happen
+        for (size_t k = 0; k < own_fills.size(); k++) {
+            const Fill &f = own_fills[k];
+            uint64_t tile = 0;
+            if (!fill_tile.empty()) {
+                tile = fill_tile[k];
+            } else {
+                auto it = alpha_to_tile.find(f.link);
+                if (it == alpha_to_tile.end() || it->second == UINT64_MAX) return 2;  // fill without its alpha tile
+                tile = it->second;
+            }
             const uint64_t key = (uint64_t(f.line_segment.from_x) << 48) | (uint64_t(f.line_segment.from_y) << 32) |
                                  (uint64_t(f.line_segment.to_x) << 16) | uint64_t(f.line_segment.to_y);
-            per_tile[it->second].push_back(key);
+            per_tile[tile].push_back(key);
         }
-        path_fills[p] = tiler.object_builder.fills.size();
+        path_fills[p] = own_fills.size();
         for (uint64_t t = 0; t < ntiles; t++) {
             auto &v = per_tile[t];
             std::sort(v.begin(), v.end());
@@ -136,6 +261,7 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
             }
         }
 
+        if (is_clip) continue;
         BuiltDrawPath bdp;
         bdp.path = bp;
         bdp.occludes = ((sv->color[p] >> 24) & 0xffu) == 0xffu;
@@ -143,7 +269,13 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
         built[p] = bdp;
     }
 
-    auto batches = build_tile_batches_for_draw_path_display_item(scene, built, Range(0, n_paths));
+    for (const ClipRef &c : clip_refs) {
+        const uint64_t gc = tile_first[c.clip_path] + c.clip_tile;
+        tile_clip[c.g] = gc;
+        if (c.src_backdrop != INT32_MIN && int8_t(c.src_backdrop) != tile_backdrop[gc]) return 8;
+    }
+
+    auto batches = build_tile_batches_for_draw_path_display_item(scene, built, Range(0, n_draw));
     const RectI fb_rect = round_rect_out_to_tile_bounds(view_box);
     const uint32_t fbw = fb_rect.width(), fbh = fb_rect.height();
     std::vector<int32_t> z(size_t(fbw) * fbh, -1);
@@ -153,7 +285,7 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
         const auto &batch = batches[0];
         // the reference z-buffer starts at 0 and takes max(path id); -1 marks "no occluder" here
         std::vector<uint8_t> occluded(size_t(fbw) * fbh, 0);
-        for (uint32_t p = 0; p < n_paths; p++) {
+        for (uint32_t p = 0; p < n_draw; p++) {
             if (!built[p].occludes) continue;
             for (const auto &tile : built[p].path.data.tiles.data) {
                 if (tile.alpha_tile_id.is_valid() || tile.backdrop == 0) continue;
@@ -199,6 +331,9 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
     out->fb_list = dup(flat);
     out->path_fills = dup(path_fills);
     out->path_microlines = nullptr;
+    out->tile_mask = dup(tile_mask);
+    out->tile_clip = dup(tile_clip);
+    out->tile_dest_backdrop = dup(tile_dest_backdrop);
     return 0;
 }
 
@@ -217,5 +352,8 @@ extern "C" void pfref_free(pfo_result *r) {
     std::free(r->fb_list);
     std::free(r->path_fills);
     std::free(r->path_microlines);
+    std::free(r->tile_mask);
+    std::free(r->tile_clip);
+    std::free(r->tile_dest_backdrop);
     std::memset(r, 0, sizeof(*r));
 }

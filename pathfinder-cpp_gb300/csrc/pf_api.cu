@@ -61,6 +61,9 @@ struct HostCanon {
     std::vector<int32_t> z;
     std::vector<uint64_t> list_first;
     std::vector<uint32_t> list;
+    std::vector<uint8_t> mask;
+    std::vector<uint64_t> clip;
+    std::vector<int8_t> dest_backdrop;
 };
 
 struct Ctx {
@@ -75,6 +78,11 @@ struct Ctx {
         scene_fb_first;
     std::vector<SceneDev> h_scenes;
     std::vector<uint32_t> h_scene_fb_first;
+    // clip paths: per uploaded path its scene-local clip path (PF_NO_CLIP) and whether it is one;
+    // empty when no scene of the batch has clip paths
+    DevBuf path_clip, path_is_clip, path_clip_rel;
+    std::vector<uint32_t> h_path_clip;
+    std::vector<uint8_t> h_path_is_clip;
     uint32_t n_scenes = 0, n_paths = 0, n_contours = 0, n_points = 0, n_fb = 0;
     uint64_t image_bytes = 0;
     bool uploaded = false, rendered = false;
@@ -174,6 +182,24 @@ int validate_scene(Ctx *c, const pf_scene_view *s) {
     for (uint32_t k = 0; k < s->n_contours; k++)
         if (s->contour_start[k] > s->contour_start[k + 1])
             return fail(c, PF_ERR_INVALID_ARGUMENT, "contour_start must be non-decreasing");
+    if (s->path_clip || s->path_is_clip) {
+        // Scene::push_draw_path / push_clip_path: clip paths come after every draw path, are not
+        // clipped themselves, and a draw path names a clip path or none
+        if (!s->path_clip || !s->path_is_clip)
+            return fail(c, PF_ERR_INVALID_ARGUMENT, "path_clip and path_is_clip go together");
+        bool seen_clip = false;
+        for (uint32_t p = 0; p < s->n_paths; p++) {
+            const uint32_t k = s->path_clip[p];
+            if (s->path_is_clip[p]) {
+                seen_clip = true;
+                if (k != PF_NO_CLIP) return fail(c, PF_ERR_INVALID_ARGUMENT, "a clip path is not clipped");
+            } else {
+                if (seen_clip) return fail(c, PF_ERR_INVALID_ARGUMENT, "clip paths follow all draw paths");
+                if (k != PF_NO_CLIP && (k >= s->n_paths || !s->path_is_clip[k]))
+                    return fail(c, PF_ERR_INVALID_ARGUMENT, "path_clip must name a clip path of the scene");
+            }
+        }
+    }
     return PF_OK;
 }
 
@@ -276,6 +302,25 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     PF_CUDA(c->scene_fb_first.ensure((n + 1) * 4));
     PF_CUDA(c->scene_row_first.ensure((n + 1) * 4));
     PF_CUDA(c->image.ensure(img + 256));
+    bool clips = false;
+    for (uint32_t i = 0; i < n; i++) clips |= scenes[i].path_clip != nullptr;
+    c->h_path_clip.clear();
+    c->h_path_is_clip.clear();
+    if (clips) {
+        c->h_path_clip.assign(N, PF_NO_CLIP);
+        c->h_path_is_clip.assign(N, 0);
+        for (uint32_t i = 0; i < n; i++) {
+            const pf_scene_view &s = scenes[i];
+            if (!s.path_clip) continue;
+            const uint32_t b = c->h_scenes[i].path_first;
+            std::memcpy(c->h_path_clip.data() + b, s.path_clip, size_t(s.n_paths) * 4);
+            std::memcpy(c->h_path_is_clip.data() + b, s.path_is_clip, s.n_paths);
+        }
+        PF_CUDA(c->path_clip.ensure(N * 4 + 16));
+        PF_CUDA(c->path_is_clip.ensure(N + 16));
+        PF_CUDA(cudaMemcpyAsync(c->path_clip.p, c->h_path_clip.data(), N * 4, cudaMemcpyHostToDevice, c->stream));
+        PF_CUDA(cudaMemcpyAsync(c->path_is_clip.p, c->h_path_is_clip.data(), N, cudaMemcpyHostToDevice, c->stream));
+    }
 
     CopyPlan pts, fl, csp, psp, fr, col;
     for (uint32_t i = 0; i < n; i++) {
@@ -317,6 +362,10 @@ Batch make_batch(Ctx *c) {
     b.scene_contour_first = c->scene_contour_first.as<uint32_t>();
     b.scene_fb_first = c->scene_fb_first.as<uint32_t>();
     b.scene_row_first = c->scene_row_first.as<uint32_t>();
+    const bool clips = !c->h_path_clip.empty();
+    b.path_clip_cat = clips ? c->path_clip.as<uint32_t>() : nullptr;
+    b.path_is_clip_cat = clips ? c->path_is_clip.as<uint8_t>() : nullptr;
+    b.path_clip_rel = clips ? c->path_clip_rel.as<uint32_t>() : nullptr;
     b.n_scenes_all = c->n_scenes;
     b.scene_base = c->r_first;
     b.n_scenes = c->r_count;
@@ -454,6 +503,7 @@ int begin_frame(Ctx *c, uint32_t first, uint32_t count) {
     PF_CUDA(c->path_cls.ensure(size_t(N) + 16));
     PF_CUDA(c->bin_ctl.ensure(64));
     PF_CUDA(c->path_leaf_range.ensure(size_t(N) * 8 + 16));
+    if (!c->h_path_clip.empty()) PF_CUDA(c->path_clip_rel.ensure(size_t(N) * 4 + 16));
     return PF_OK;
 }
 
@@ -691,7 +741,7 @@ std::vector<void *> frame_buffers(const Ctx *c) {
                             &c->path_leaf_cursor, &c->path_fill_budget, &c->segs, &c->seg_leaves, &c->seg_order,
                             &c->seg_ctl, &c->row_paths, &c->tile_fills, &c->tile_state, &c->col_above,
                             &c->col_final, &c->leaves, &c->pool_path, &c->pool_idx, &c->pool_cnt, &c->fills,
-                            &c->scan_temp, &c->image, &c->sz_w};
+                            &c->scan_temp, &c->image, &c->sz_w, &c->path_clip_rel};
     std::vector<void *> v;
     for (const DevBuf *d : bufs) v.push_back(d->p);
     v.push_back(c->host_img_dev);
@@ -907,6 +957,43 @@ int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
             d[3] = uint16_t(keys[k]);
         }
     }
+    // clipped draw tiles (Tiler::prepare_tiles, pathfinder/core/d3d9/tiler.cpp:386-431), as the
+    // kernels apply them on the fly; clip paths are not clipped, so their tiles read as stored
+    h.mask.assign(nt, 0);
+    h.clip.assign(nt, UINT64_MAX);
+    h.dest_backdrop.assign(nt, 0);
+    for (uint32_t p = 0; !c->h_path_clip.empty() && p < np; p++) {
+        const uint32_t k = c->h_path_clip[S.path_first + p];
+        if (k == PF_NO_CLIP) continue;
+        const int32_t *R = &h.rect[4 * p], *CR = &h.rect[4 * k];
+        const int32_t w = R[2] - R[0], cw = CR[2] - CR[0];
+        for (int32_t y = R[1]; y < R[3]; y++)
+            for (int32_t x = R[0]; x < R[2]; x++) {
+                const uint64_t g = h.tile_first[p] + uint64_t(y - R[1]) * w + uint64_t(x - R[0]);
+                if (x < CR[0] || x >= CR[2] || y < CR[1] || y >= CR[3]) {
+                    h.alpha[g] = 0;
+                    h.backdrop[g] = 0;
+                    continue;
+                }
+                const uint64_t gc = h.tile_first[k] + uint64_t(y - CR[1]) * cw + uint64_t(x - CR[0]);
+                const bool ca = h.alpha[gc] != 0, da = h.alpha[g] != 0;
+                const int8_t cbd = h.backdrop[gc], dbd = h.backdrop[g];
+                if (ca && da) {
+                    h.mask[g] = 2;
+                    h.clip[g] = gc;
+                    h.dest_backdrop[g] = dbd;
+                    h.backdrop[g] = 0;
+                } else if (ca && dbd != 0) {
+                    h.mask[g] = 1;
+                    h.clip[g] = gc;
+                    h.alpha[g] = 1;
+                    h.backdrop[g] = cbd;
+                } else if (!ca && cbd == 0) {
+                    h.alpha[g] = 0;
+                    h.backdrop[g] = 0;
+                }
+            }
+    }
     for (auto &z : h.z)
         if (z >= 0) z -= (int32_t)p0;
     h.list_first.resize(fbc.size());
@@ -932,6 +1019,9 @@ int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
     out->fb_list_first = h.list_first.data();
     out->n_list = l1 - l0;
     out->fb_list = h.list.data();
+    out->tile_mask = h.mask.data();
+    out->tile_clip = h.clip.data();
+    out->tile_dest_backdrop = h.dest_backdrop.data();
     return PF_OK;
 }
 
@@ -1096,7 +1186,7 @@ int pf_ctx_destroy(void *ctx) {
                       &c->pool_idx, &c->tile_fills, &c->path_fill, &c->path_cls, &c->tile_state, &c->col_above,
                       &c->col_final, &c->fills, &c->bin_stage, &c->row_first,
                       &c->row_paths, &c->scene_row_first, &c->z, &c->fb_count, &c->list, &c->image,
-                      &c->status, &c->scan_temp};
+                      &c->status, &c->scan_temp, &c->path_clip, &c->path_is_clip, &c->path_clip_rel};
     for (DevBuf *b : bufs) b->release();
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);

@@ -13,7 +13,8 @@ constexpr int kTile = 16;
 constexpr int kCovShift = 20;
 constexpr int kMaxDepth = 32;              // flattening recursion bound (depth of the d3d9 bisection)
 constexpr uint32_t kMaxWalk = 1u << 20;    // tile-walk step bound per line
-constexpr uint32_t kNone = 0xffffffffu;
+constexpr uint32_t kNone = 0xffffffffu;       // also the scene format's "no clip path"
+constexpr uint32_t kPathIsClip = 8u;           // PathDev::flags: a clip path (tiled, never drawn)
 
 // Learned sizer: per-path features -> 64 -> 64 -> (log1p leaf lines, log1p fills).
 constexpr int kSizerIn = 12, kSizerHidden = 64, kSizerOut = 2;
@@ -55,7 +56,7 @@ struct PathDev {
     uint32_t tile_first;         // first global tile
     uint32_t col_first;          // first global column
     uint32_t scene;
-    uint32_t flags;              // bit0 even-odd, bit1 occludes (opaque src-over)
+    uint32_t flags;              // bit0 even-odd, bit1 occludes (opaque src-over), bit3 clip path
 };
 
 // Segment record: points index a, kind, and the second point for closing lines.
@@ -76,6 +77,10 @@ struct Batch {
     const uint32_t *path_start_cat;      // per scene n_paths+1 entries, scene-local
     const uint8_t *fill_rule;
     const uint32_t *color;
+    const uint32_t *path_clip_cat;       // per uploaded path: scene-local clip path, kNone (or null:
+                                         // no clip paths in the batch)
+    const uint8_t *path_is_clip_cat;     // per uploaded path: 1 for a clip path
+    uint32_t *path_clip_rel;             // [n_paths] the clip path within the frame, kNone
     const SceneDev *scenes;
     const uint32_t *scene_path_first;    // [n_scenes_all + 1]
     const uint32_t *scene_contour_first; // [n_scenes_all + 1]

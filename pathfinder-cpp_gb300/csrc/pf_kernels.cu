@@ -84,6 +84,13 @@ __global__ void k_normalize_paths(Batch b, uint2 *path_contours) {
     PathDev P{};
     P.scene = s;
     P.flags = (b.fill_rule[pg] ? 1u : 0u) | (((b.color[pg] >> 24) == 0xffu) ? 2u : 0u);
+    if (b.path_clip_cat) {
+        // clip paths are tiled like the others but never drawn; a clipped path's clip is in its
+        // scene, addressed here within the frame
+        if (b.path_is_clip_cat[pg]) P.flags |= kPathIsClip;
+        const uint32_t lc = b.path_clip_cat[pg];
+        b.path_clip_rel[p] = lc == kNone ? kNone : S.path_first - b.path_base + lc;
+    }
     b.paths[p] = P;
 }
 
@@ -1276,6 +1283,9 @@ __global__ void k_pool_scatter(Batch b) {
 // in path order (one block per row; a block scan keeps the order, no sort is needed).
 
 constexpr int kRowThreads = 256;
+// Row-entry flag of a clipped path; mask sources of a clipped tile.
+constexpr uint32_t kRowClipped = 16u;
+enum : uint32_t { kMaskOwn = 0, kMaskClip = 1, kMaskBoth = 2 };
 
 template <bool kWrite>
 __global__ void __launch_bounds__(kRowThreads) k_rows(Batch b) {
@@ -1296,7 +1306,7 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(Batch b) {
         int4 rect = make_int4(0, 0, 0, 0);
         if (p < p1) {
             rect = *reinterpret_cast<const int4 *>(&b.paths[p].rx0);
-            spans = rect.y <= y && y < rect.w && rect.x < rect.z;
+            spans = rect.y <= y && y < rect.w && rect.x < rect.z && !(b.paths[p].flags & kPathIsClip);
         }
         const uint32_t ballot = __ballot_sync(0xffffffffu, spans);
         if (lane == 0) warp_counts[warp] = __popc(ballot);
@@ -1317,10 +1327,13 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(Batch b) {
             // adding fx >= rx0 brings it back into range)
             const uint32_t row_tile = b.paths[p].tile_first + (uint32_t)(y - rect.y) * (uint32_t)(rect.z - rect.x) -
                                       (uint32_t)rect.x;
-            // flags: bit 0 even-odd, bit 1 occludes, bit 2 this row is the rect's first row
+            // flags: bit 0 even-odd, bit 1 occludes, bit 2 this row is the rect's first row,
+            // bit 4 the path is clipped
+            const bool clipped = b.path_clip_cat && b.path_clip_rel[p] != kNone;
             if (out + rank < b.row_cap)
                 b.row_paths[out + rank] = make_uint4(p, (uint32_t)rect.x | ((uint32_t)rect.z << 16), row_tile,
-                                                     b.paths[p].flags | (y == rect.y ? 4u : 0u));
+                                                     b.paths[p].flags | (y == rect.y ? 4u : 0u) |
+                                                         (clipped ? kRowClipped : 0u));
         }
         out += chunk_total;
         total += chunk_total;
@@ -1387,8 +1400,9 @@ __device__ __forceinline__ void raster_column(const FillPrep &fp, int i, int *D)
 // (lane>>4)*8 .. +7) of an alpha tile; D must be zeroed on entry and is left dirty.
 // Fills are rasterised as (fill, pixel column) work items spread over the lanes, 32 fills
 // at a time, so a tile of a few wide fills still keeps the warp busy.
-__device__ __forceinline__ void alpha_coverage(const Batch &b, uint32_t f0, uint32_t f1, int8_t bd, bool eo, int *D,
-                                               FillPrep *prep, float cov[8]) {
+// backdrop + the fills' area sums (fixed point) of the warp's 8 pixels per lane, before the fill rule
+__device__ __forceinline__ void coverage_raw(const Batch &b, uint32_t f0, uint32_t f1, int8_t bd, int *D,
+                                             FillPrep *prep, int raw[8]) {
     const int lane = threadIdx.x & 31;
     for (uint32_t base = f0; base < f1; base += 32) {
         const uint32_t f = base + lane;
@@ -1440,10 +1454,16 @@ __device__ __forceinline__ void alpha_coverage(const Batch &b, uint32_t f0, uint
     }
     const int upper = __shfl_sync(0xffffffffu, run, col);  // rows 0..7 total of this column
     const int base = (h ? upper : 0) + ((int)bd << kCovShift);
+#pragma unroll
+    for (int k = 0; k < 8; k++) raw[k] = base + acc[k];
+}
+
+// The fill rule (fill.comp:133-140): nonzero min(|c|, 1), even-odd 1 - |1 - (c mod 2)|.
+__device__ __forceinline__ void coverage_rule(const int raw[8], bool eo, float cov[8]) {
     const float scale = 1.0f / (float)(1 << kCovShift);
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-        const int c = base + acc[k];
+        const int c = raw[k];
         if (!eo) {
             cov[k] = fminf(fabsf((float)c) * scale, 1.0f);
         } else {
@@ -1451,6 +1471,13 @@ __device__ __forceinline__ void alpha_coverage(const Batch &b, uint32_t f0, uint
             cov[k] = __saturatef(1.0f - fabsf(1.0f - t));
         }
     }
+}
+
+__device__ __forceinline__ void alpha_coverage(const Batch &b, uint32_t f0, uint32_t f1, int8_t bd, bool eo, int *D,
+                                               FillPrep *prep, float cov[8]) {
+    int raw[8];
+    coverage_raw(b, f0, f1, bd, D, prep, raw);
+    coverage_rule(raw, eo, cov);
 }
 
 __device__ __forceinline__ void zero_cells(int *D) {
@@ -1471,19 +1498,51 @@ constexpr int kCompWarps = 1;
 // range in parallel before the visits, so a visit waits on its fills alone.
 // visit(candidate) returns true to stop the walk.
 struct Cand {
-    uint32_t p, gt, st, flags;
-    uint32_t f0, f1, color;  // kFetch only
+    uint32_t p, gt, st, flags;  // st: the tile state, with a clipped tile's mask source in bits 9-10
+                                // and (kMaskBoth) the draw tile's own backdrop in bits 16-23
+    uint32_t f0, f1, color;     // kFetch only (kMaskClip: the clip tile's fills)
+    uint32_t gc;                // kMaskBoth: the clip tile
 };
 
-template <bool kFetch, class Visit>
-__device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint32_t fx, Visit &&visit,
+__device__ __forceinline__ uint32_t mask_mode(uint32_t st) { return (st >> 9) & 3u; }
+
+// A clipped draw tile against the clip path's tile at the same coordinates
+// (Tiler::prepare_tiles, pathfinder/core/d3d9/tiler.cpp:386-431): culled outside the clip's
+// rect or over a blank clip tile; a solid tile over a clip alpha tile takes the clip's mask and
+// backdrop; an alpha tile over a clip alpha tile keeps its mask, to be combined with the clip's,
+// and its backdrop is zeroed; otherwise unchanged.  Updates c.st (and c.f0/f1, c.gc).
+__device__ __forceinline__ void apply_clip(const Batch &b, uint32_t p, int32_t tx, int32_t ty, Cand &c) {
+    const uint32_t cp = b.path_clip_rel[p];
+    const PathDev C = b.paths[cp];
+    if (tx < C.rx0 || tx >= C.rx1 || ty < C.ry0 || ty >= C.ry1) {
+        c.st = 0;
+        return;
+    }
+    const uint32_t gc = C.tile_first + (uint32_t)((ty - C.ry0) * (C.rx1 - C.rx0) + (tx - C.rx0));
+    const uint32_t cs = b.tile_state[gc];
+    const bool ca = (cs & 0x100u) != 0, da = (c.st & 0x100u) != 0;
+    const int8_t cbd = (int8_t)(cs & 0xffu), dbd = (int8_t)(c.st & 0xffu);
+    if (ca && da) {
+        c.st = 0x100u | kMaskBoth << 9 | (uint32_t)(uint8_t)dbd << 16;
+        c.gc = gc;
+    } else if (ca && dbd != 0) {
+        c.st = 0x100u | kMaskClip << 9 | (uint32_t)(uint8_t)cbd;
+        c.f0 = gc == C.tile_first ? b.path_fill[cp] : b.tile_fills[gc - 1];
+        c.f1 = b.tile_fills[gc];
+    } else if (!ca && cbd == 0) {
+        c.st = 0;
+    }
+}
+
+template <bool kFetch, bool kClip, class Visit>
+__device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint32_t fx, uint32_t fy, Visit &&visit,
                                              uint32_t &chunks) {
     const int lane = threadIdx.x & 31;
     const uint32_t k_lo = b.row_first[row], k_hi = b.row_first[row + 1];
     for (uint32_t top = k_hi; top > k_lo; top = top > k_lo + 32 ? top - 32 : k_lo) {
         chunks++;
         const int64_t k = (int64_t)top - 1 - lane;
-        Cand c{0, 0, 0, 0, 0, 0, 0};
+        Cand c{0, 0, 0, 0, 0, 0, 0, 0};
         bool vis = false;
         if (k >= (int64_t)k_lo) {
             const uint4 e = b.row_paths[k];
@@ -1492,10 +1551,11 @@ __device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint3
                 c.flags = e.w;
                 c.gt = e.z + fx;
                 c.st = b.tile_state[c.gt];
+                if (kClip && (c.flags & kRowClipped)) apply_clip(b, c.p, (int32_t)fx, (int32_t)fy, c);
                 vis = c.st != 0;
                 if (kFetch && vis) {
                     c.color = b.color[b.path_base + c.p];
-                    if (c.st & 0x100u) {
+                    if ((c.st & 0x100u) && mask_mode(c.st) != kMaskClip) {
                         // the first tile of a path starts the path's block of fills
                         const bool first = (c.flags & 4u) && fx == (e.y & 0xffffu);
                         c.f0 = first ? b.path_fill[c.p] : b.tile_fills[c.gt - 1];
@@ -1517,6 +1577,7 @@ __device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint3
                 v.f0 = __shfl_sync(0xffffffffu, c.f0, l);
                 v.f1 = __shfl_sync(0xffffffffu, c.f1, l);
                 v.color = __shfl_sync(0xffffffffu, c.color, l);
+                if (kClip) v.gc = __shfl_sync(0xffffffffu, c.gc, l);
             }
             if (visit(v)) return;
         }
@@ -1531,9 +1592,13 @@ __device__ __forceinline__ uint32_t fill_begin(const Batch &b, uint32_t p, uint3
     return gt == b.path_tiles[p] ? b.path_fill[p] : b.tile_fills[gt - 1];
 }
 
-__global__ void __launch_bounds__(kCompWarps * 32, 32 / kCompWarps) k_composite(Batch b) {
+// kClip: the batch has clip paths (a variant of its own, so that the clip code's registers
+// cost batches without clips nothing)
+template <bool kClip>
+__global__ void __launch_bounds__(kCompWarps * 32, (kClip ? 24 : 32) / kCompWarps) k_composite(Batch b) {
     __shared__ int cells[kCompWarps][kCovCells];
     __shared__ FillPrep prep[kCompWarps][32];
+    __shared__ int park[kCompWarps][8][32];  // kMaskBoth: the clip tile's |coverage|
     // a frame whose leaf lines or fills overran their buffers is redone; nothing to read here
     if (b.status[kStErr] & (kErrOverflowLeaf | kErrOverflowFill)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1556,7 +1621,7 @@ __global__ void __launch_bounds__(kCompWarps * 32, 32 / kCompWarps) k_composite(
             ar[k] = ag[k] = ab[k] = 0.0f;
             tr[k] = 1.0f;
         }
-        walk_fb_tile<true>(b, S.row_first - b.row_base + fy, fx, [&](const Cand &v) -> bool {
+        walk_fb_tile<true, kClip>(b, S.row_first - b.row_base + fy, fx, fy, [&](const Cand &v) -> bool {
             const bool eo = (v.flags & 1u) != 0;
             const int8_t bd = (int8_t)(v.st & 0xffu);
             float cov[8];
@@ -1568,10 +1633,39 @@ __global__ void __launch_bounds__(kCompWarps * 32, 32 / kCompWarps) k_composite(
                 for (int k = 0; k < 8; k++) cov[k] = 1.0f;
                 stop = (v.flags & 2u) != 0;
             } else {
-                comp_fills += v.f1 - v.f0;
-                zero_cells(D);
-                alpha_coverage(b, v.f0, v.f1, bd, eo, D, prep[warp], cov);
-                __syncwarp();
+                // the tile's own mask; kMaskClip (a solid tile over a clip alpha tile): the clip's;
+                // kMaskBoth: the clip's mask first, parked, then the tile's own, combined as
+                // tile_clip_combine.frag does - min(|draw + its backdrop|, |clip + its backdrop|) -
+                // before the draw path's fill rule
+                bool both = kClip && mask_mode(v.st) == kMaskBoth, combined = false;
+                uint32_t f0 = v.f0, f1 = v.f1;
+                int8_t tbd = bd;
+                if (both) {
+                    const uint32_t cp = b.path_clip_rel[v.p];
+                    f0 = fill_begin(b, cp, v.gc);
+                    f1 = b.tile_fills[v.gc];
+                    tbd = (int8_t)(b.tile_state[v.gc] & 0xffu);
+                }
+                int raw[8];
+                for (;;) {
+                    comp_fills += f1 - f0;
+                    zero_cells(D);
+                    coverage_raw(b, f0, f1, tbd, D, prep[warp], raw);
+                    __syncwarp();
+                    if (!both) break;
+#pragma unroll
+                    for (int k = 0; k < 8; k++) park[warp][k][lane] = abs(raw[k]);
+                    both = false;
+                    combined = true;
+                    f0 = v.f0;
+                    f1 = v.f1;
+                    tbd = (int8_t)(v.st >> 16);
+                }
+                if (combined) {
+#pragma unroll
+                    for (int k = 0; k < 8; k++) raw[k] = min(abs(raw[k]), park[warp][k][lane]);
+                }
+                coverage_rule(raw, eo, cov);
             }
             const uint32_t color = v.color;
             const float pr = (float)(color & 0xffu) * inv255, pg = (float)((color >> 8) & 0xffu) * inv255,
@@ -1642,7 +1736,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_list_dump(Batch b) {
         first = b.fb_count[fb];
         count = b.fb_count[fb + 1] - first;
     }
-    walk_fb_tile<false>(b, S.row_first - b.row_base + fy, fx, [&](const Cand &v) -> bool {
+    walk_fb_tile<false, true>(b, S.row_first - b.row_base + fy, fx, fy, [&](const Cand &v) -> bool {
         if (kWrite && lane == 0) b.list[first + count - 1 - n] = v.gt;
         n++;
         const int8_t bd = (int8_t)(v.st & 0xffu);
@@ -1818,7 +1912,12 @@ cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st) {
 }
 
 cudaError_t launch_composite(const Batch &b, cudaStream_t st) {
-    if (b.n_fb) PF_LAUNCH(k_composite<<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
+    if (b.n_fb) {
+        if (b.path_clip_cat)
+            PF_LAUNCH(k_composite<true><<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
+        else
+            PF_LAUNCH(k_composite<false><<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
+    }
     return cudaGetLastError();
 }
 

@@ -44,6 +44,7 @@ class SceneView(C.Structure):
         ("path_start", C.c_void_p), ("fill_rule", C.c_void_p), ("color", C.c_void_p),
         ("n_points", C.c_uint32), ("n_contours", C.c_uint32), ("n_paths", C.c_uint32),
         ("width", C.c_float), ("height", C.c_float), ("clear_color", C.c_uint32),
+        ("path_clip", C.c_void_p), ("path_is_clip", C.c_void_p),
     ]
 
 
@@ -73,6 +74,7 @@ class Canon(C.Structure):
         ("fills", C.c_void_p), ("n_columns", C.c_uint64), ("column_backdrop", C.c_void_p),
         ("fb_tiles_x", C.c_uint32), ("fb_tiles_y", C.c_uint32), ("z", C.c_void_p),
         ("fb_list_first", C.c_void_p), ("n_list", C.c_uint64), ("fb_list", C.c_void_p),
+        ("tile_mask", C.c_void_p), ("tile_clip", C.c_void_p), ("tile_dest_backdrop", C.c_void_p),
     ]
 
 
@@ -109,6 +111,15 @@ def scene_view(scene) -> "tuple[SceneView, list]":
             np.ascontiguousarray(scene.fill_rule, np.uint8), np.ascontiguousarray(scene.color, np.uint32)]
     v = SceneView(*(a.ctypes.data for a in arrs), scene.n_points, scene.n_contours, scene.n_paths,
                   scene.width, scene.height, scene.clear)
+    # the clip arrays go in as given (the library checks that they come together)
+    if getattr(scene, "path_clip", None) is not None:
+        clip = np.ascontiguousarray(scene.path_clip, np.uint32)
+        v.path_clip = clip.ctypes.data
+        arrs.append(clip)
+    if getattr(scene, "path_is_clip", None) is not None:
+        is_clip = np.ascontiguousarray(scene.path_is_clip, np.uint8)
+        v.path_is_clip = is_clip.ctypes.data
+        arrs.append(is_clip)
     return v, arrs
 
 
@@ -198,6 +209,9 @@ class Renderer:
             "z": _arr(r.z, nfb, np.int32),
             "fb_list_first": _arr(r.fb_list_first, nfb + 1, np.uint64),
             "fb_list": _arr(r.fb_list, r.n_list, np.uint32),
+            "tile_mask": _arr(r.tile_mask, r.n_tiles, np.uint8),
+            "tile_clip": _arr(r.tile_clip, r.n_tiles, np.uint64),
+            "tile_dest_backdrop": _arr(r.tile_dest_backdrop, r.n_tiles, np.int8),
         }
 
     def set_flags(self, stage_timing: bool = False, counters: bool = False) -> None:

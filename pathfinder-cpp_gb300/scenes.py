@@ -27,7 +27,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
-from typing import List
+from typing import List, Optional
 
 import numpy as np
 
@@ -92,6 +92,8 @@ class Scene:
     width: float
     height: float
     clear: int = 0              # RGBA8 clear colour, red in the low byte
+    path_clip: Optional[np.ndarray] = None     # uint32 [N] clip path of each path, or NO_CLIP
+    path_is_clip: Optional[np.ndarray] = None  # uint8 [N] 1 for clip paths (after the draw paths)
 
     @property
     def n_paths(self) -> int:
@@ -319,6 +321,40 @@ def concat(parts: List[Scene], width: float, height: float, clear: int = 0) -> S
                  contour_start=np.concatenate(cs), path_start=np.concatenate(ps),
                  fill_rule=np.concatenate(fr), color=np.concatenate(col),
                  width=float(width), height=float(height), clear=int(clear))
+
+
+NO_CLIP = 0xFFFFFFFF
+
+
+def with_clips(draw: Scene, clips: Scene, assign: np.ndarray) -> Scene:
+    """`draw`'s paths followed by `clips`'s paths as clip paths; draw path i is clipped by
+    clip path assign[i] (an index into `clips`, or -1 for none)."""
+    out = concat([draw, clips], draw.width, draw.height, draw.clear)
+    n_draw, n_clip = draw.n_paths, clips.n_paths
+    pc = np.full(n_draw + n_clip, NO_CLIP, np.uint32)
+    a = np.asarray(assign, np.int64)
+    pc[:n_draw] = np.where(a >= 0, a + n_draw, NO_CLIP).astype(np.uint32)
+    out.path_clip = pc
+    out.path_is_clip = np.concatenate([np.zeros(n_draw, np.uint8), np.ones(n_clip, np.uint8)])
+    return out
+
+
+def clipped(seed: int = 0, n_paths: int = 240, side: int = 1024, n_clips: int = 8,
+            clip_share: float = 0.6) -> Scene:
+    """The 240-path cubic scene with clip paths: n_clips closed cubic shapes, each a quarter to
+    a whole of the canvas wide, alternately nonzero and even-odd; each draw path is clipped by a
+    random one with probability clip_share; 30 % of the draw paths translucent."""
+    rng = Rng(seed, 6)
+    draw = plain_small(seed=seed, n_paths=n_paths, side=side)
+    alpha = np.where(rng.uniform(n_paths) < 0.3, (rng.uniform(n_paths) * 180 + 40).astype(np.uint32), 255)
+    draw.color = (draw.color & np.uint32(0x00FFFFFF)) | (alpha.astype(np.uint32) << np.uint32(24))
+    size = side * (0.25 + 0.75 * rng.uniform(n_clips))
+    lo = rng.uniform(2 * n_clips).reshape(n_clips, 2) * (side - size)[:, None]
+    cpts, cfl = _cubic_paths(rng, n_clips, lo, np.asarray(size, np.float64), 3, 8)
+    clips = _assemble(cpts, cfl, np.ones(n_clips, np.int64), (np.arange(n_clips) % 2).astype(np.uint8),
+                      np.full(n_clips, 0xFFFFFFFF, np.uint32), side, side)
+    assign = np.where(rng.uniform(n_paths) < clip_share, rng.integers(0, n_clips - 1, n_paths), -1)
+    return with_clips(draw, clips, assign)
 
 
 def mixed(seed: int = 7, n_paths: int = 8192, side: int = 4096) -> Scene:

@@ -13,9 +13,10 @@ for p in (os.path.join(ROOT, "oracle"), PKG, ROOT):
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 CANON_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha", "tile_backdrop",
-              "tile_fill_count", "fills", "column_backdrop", "fb_tiles", "z", "fb_list_first", "fb_list"]
+              "tile_fill_count", "fills", "column_backdrop", "fb_tiles", "z", "fb_list_first", "fb_list",
+              "tile_mask", "tile_clip", "tile_dest_backdrop"]
 TILE_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha", "tile_backdrop",
-             "tile_fill_count", "fills", "column_backdrop"]
+             "tile_fill_count", "fills", "column_backdrop", "tile_mask", "tile_clip", "tile_dest_backdrop"]
 
 
 def pytest_configure(config):
@@ -32,7 +33,9 @@ def load_golden(name):
     w, h, clear = d["meta"]
     sc = S.Scene(points=d["points"], flags=d["flags"], contour_start=d["contour_start"],
                  path_start=d["path_start"], fill_rule=d["fill_rule"], color=d["color"],
-                 width=float(w), height=float(h), clear=int(clear))
+                 width=float(w), height=float(h), clear=int(clear),
+                 path_clip=d["path_clip"] if "path_clip" in d else None,
+                 path_is_clip=d["path_is_clip"] if "path_is_clip" in d else None)
     ref = {k: d["ref_" + k] for k in CANON_KEYS}
     return sc, ref
 

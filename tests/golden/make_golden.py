@@ -33,8 +33,10 @@ import oracle  # noqa: E402
 import scenes as S  # noqa: E402
 
 CANON_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha", "tile_backdrop",
-              "tile_fill_count", "fills", "column_backdrop", "fb_tiles", "z", "fb_list_first", "fb_list"]
+              "tile_fill_count", "fills", "column_backdrop", "fb_tiles", "z", "fb_list_first", "fb_list",
+              "tile_mask", "tile_clip", "tile_dest_backdrop"]
 INPUT_KEYS = ["points", "flags", "contour_start", "path_start", "fill_rule", "color"]
+CLIP_KEYS = ["path_clip", "path_is_clip"]  # stored when the scene has clip paths
 
 
 def build_scene(paths, width, height, clear=0) -> S.Scene:
@@ -137,6 +139,41 @@ def edge_scenes():
     return out
 
 
+def clip_scenes():
+    """Clip paths: every case of Tiler::prepare_tiles (tiler.cpp:386-431)."""
+    red, blue, half = (255, 0, 0, 255), (0, 0, 255, 255), (20, 40, 200, 128)
+    white = (255, 255, 255, 255)
+    out = {}
+    # a square clipped by a smaller diamond: alpha over alpha (combined masks), solid inside
+    # (unchanged), solid over the diamond's edge tiles (the clip's mask), outside its rect (culled)
+    diamond = poly(48, 8, 88, 48, 48, 88, 8, 48)
+    sq = poly(2, 2, 94, 2, 94, 94, 2, 94)
+    out["clip_diamond"] = S.with_clips(
+        build_scene([([sq], 0, red), ([poly(30, 30, 66, 30, 66, 66, 30, 66)], 0, half)], 96, 96),
+        build_scene([([diamond], 0, white)], 96, 96), np.array([0, -1]))
+    # a clip with a hole: blank clip tiles inside its rect cull the draw path's solid tiles there
+    outer = poly(4, 4, 92, 4, 92, 92, 4, 92)
+    inner = poly(28, 28, 28, 68, 68, 68, 68, 28)
+    out["clip_hole"] = S.with_clips(
+        build_scene([([poly(0, 0, 96, 0, 96, 96, 0, 96)], 0, blue), ([poly(10, 40, 86, 44, 48, 90)], 1, half)],
+                    96, 96),
+        build_scene([([outer, inner], 0, white)], 96, 96), np.array([0, 0]))
+    # an even-odd star as the clip of an even-odd star and of a translucent quadratic blob
+    star = poly(50, 5, 79, 95, 2, 40, 98, 40, 21, 95)
+    blob = (np.asarray([[10, 50], [50, -10], [90, 50], [50, 110], [10, 50]], np.float32),
+            np.asarray([0, 1, 0, 1, 0], np.uint8))
+    out["clip_even_odd"] = S.with_clips(
+        build_scene([([poly(*(np.asarray(star[0]).ravel() + 2))], 1, red), ([blob], 0, half)], 100, 100),
+        build_scene([([star], 1, white)], 100, 100), np.array([0, 0]))
+    # two clips, one partly outside the view box, one path clipped by a clip of an empty rect
+    out["clip_two"] = S.with_clips(
+        build_scene([([poly(0, 0, 80, 0, 80, 80, 0, 80)], 0, red), ([poly(20, 10, 70, 60, 5, 70)], 0, blue),
+                     ([poly(40, 40, 60, 40, 50, 60)], 0, half)], 80, 80),
+        build_scene([([poly(-20, 30, 50, -10, 70, 70)], 0, white), ([poly(200, 200, 240, 200, 220, 240)], 0, white)],
+                    80, 80), np.array([0, 0, 1]))
+    return out
+
+
 def generator_scenes():
     return {
         "gen_plain_small_s1": S.plain_small(seed=1, n_paths=24, side=256),
@@ -144,6 +181,7 @@ def generator_scenes():
         "gen_glyphs_s3": S.glyphs(seed=3, n_paths=400, side=256),
         "gen_mixed_s4": S.mixed(seed=4, n_paths=96, side=512),
         "gen_batched_scene_s5": S.batched(n_scenes=3, first_seed=5, hi_paths=64)[2],
+        "gen_clipped_s6": S.clipped(seed=6, n_paths=60, side=256, n_clips=4),
     }
 
 
@@ -169,10 +207,13 @@ def main() -> None:
     if not oracle.have_reference():
         raise SystemExit("the reference tiler could not be built (is the reference tree present?)")
     small = dict(edge_scenes())
+    small.update(clip_scenes())
     small.update(generator_scenes())
     for name, sc in small.items():
         ref = oracle.reference_tile_scene(sc)
         arrays = {k: getattr(sc, k) for k in INPUT_KEYS}
+        if sc.path_clip is not None:
+            arrays.update({k: getattr(sc, k) for k in CLIP_KEYS})
         arrays["meta"] = np.asarray([sc.width, sc.height, sc.clear], np.float64)
         for k in CANON_KEYS:
             arrays["ref_" + k] = ref[k]

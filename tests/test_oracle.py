@@ -66,6 +66,39 @@ def test_restated_tiler_matches_live_reference(oracle_mod, seed):
         assert oracle_mod.compare(ref, ours, CANON_KEYS) == []
 
 
+@pytest.mark.parametrize("seed", [21, 22, 23])
+def test_restated_clipping_matches_live_reference(oracle_mod, seed):
+    if not os.path.isdir(os.path.join(oracle_mod.REF_ROOT, "pathfinder")):
+        pytest.skip("reference tree not present")
+    oracle_mod.build(reference=True)
+    import scenes as S
+    sc = S.clipped(seed=seed, n_paths=80, side=384, n_clips=5)
+    ref = oracle_mod.reference_tile_scene(sc)
+    ours = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D9)
+    assert oracle_mod.compare(ref, ours, CANON_KEYS) == []
+    assert set(np.unique(ours["tile_mask"])) == {0, 1, 2}  # every clip case occurs
+
+
+def test_clip_pixel_known_answers(oracle_mod):
+    # an opaque square over [0, 64)^2 clipped by a pixel-aligned rectangle [16, 48) x [8, 40):
+    # the intersection is covered, everything else shows the clear colour.  As for any path,
+    # add_fill's clamp to 4095/256 px (object_builder.cpp:33-35) leaves the last pixel column of
+    # a tile 1/256 off: 254 inside, and at most 1 code of leak below the clip's bottom edge.
+    import sys
+    import scenes as S
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_golden import build_scene, poly
+    draw = build_scene([([poly(0, 0, 64, 0, 64, 64, 0, 64)], 0, (255, 0, 0, 255))], 64, 64)
+    clip = build_scene([([poly(16, 8, 48, 8, 48, 40, 16, 40)], 0, (255, 255, 255, 255))], 64, 64)
+    sc = S.with_clips(draw, clip, np.array([0]))
+    img, _ = oracle_mod.render(sc)
+    inside = img[8:40, 16:48]
+    assert (inside[..., 0] >= 254).all() and (inside[..., 3] >= 254).all()
+    outside = img.copy()
+    outside[8:40, 16:48] = 0
+    assert (outside <= 1).all() and (outside[:8] == 0).all() and (outside[:, :16] == 0).all()
+
+
 def test_z_rules_differ_only_on_even_odd_even_backdrop(oracle_mod):
     sc, _ = load_golden("int8_wrap")
     d9 = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D9)
