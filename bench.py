@@ -62,6 +62,9 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--cpu-sample-every", type=int, default=32)
+    ap.add_argument("--clips", type=int, default=0,
+                    help="clip paths per scene (0: none): the batched scenes with that many clip shapes "
+                         "each, 60%% of the draw paths clipped")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-frames", action="store_true",
                     help="only the batched exact and learned frames (warm-up + steps each), a short summary "
@@ -69,11 +72,22 @@ def parse_args():
     return ap.parse_args()
 
 
-def workload_config(n_scenes, scenes_list):
+def make_scenes(args, first_seed):
+    import scenes as S
+    if args.clips > 0:
+        return S.batched_clipped(n_scenes=args.scenes, first_seed=first_seed, n_clips=args.clips)
+    return S.batched(n_scenes=args.scenes, first_seed=first_seed)
+
+
+def workload_config(n_scenes, scenes_list, clips=0):
     import numpy as np
+    desc = ("batched: %d scenes, paths/scene log-uniform 16-4096 (cubic 8-24 seg, control points "
+            "uniform over the canvas), canvas side in {256,512,1024,2048}, seeds 1000+i" % n_scenes)
+    if clips:
+        desc += "; %d clip paths per scene (cubic 3-8 seg, a quarter to a whole canvas wide), 60%% of the " \
+                "draw paths clipped" % clips
     return {
-        "workload": "batched: %d scenes, paths/scene log-uniform 16-4096 (cubic 8-24 seg, control points "
-                    "uniform over the canvas), canvas side in {256,512,1024,2048}, seeds 1000+i" % n_scenes,
+        "workload": desc,
         "scenes": n_scenes,
         "paths": int(sum(s.n_paths for s in scenes_list)),
         "points": int(sum(s.n_points for s in scenes_list)),
@@ -144,9 +158,17 @@ def pack_pinned(scenes_list):
     import pfcuda
     keys = [("points", np.float32, 8), ("flags", np.uint8, 1), ("contour_start", np.uint32, 4),
             ("path_start", np.uint32, 4), ("fill_rule", np.uint8, 1), ("color", np.uint32, 4)]
+    if any(getattr(s, "path_clip", None) is not None for s in scenes_list):
+        keys += [("path_clip", np.uint32, 4), ("path_is_clip", np.uint8, 1)]
+    def field(s, k):
+        a = getattr(s, k)
+        if a is None:  # a scene without clip paths in a batch with some
+            a = np.full(s.n_paths, 0xFFFFFFFF, np.uint32) if k == "path_clip" else np.zeros(s.n_paths, np.uint8)
+        return a
+
     bufs = {}
     for k, dt, _ in keys:
-        total = sum(getattr(s, k).nbytes for s in scenes_list)
+        total = sum(field(s, k).nbytes for s in scenes_list)
         t = torch.empty(max(total, 16), dtype=torch.uint8, pin_memory=True)
         bufs[k] = t
     offs = {k: 0 for k, _, _ in keys}
@@ -154,12 +176,15 @@ def pack_pinned(scenes_list):
     for s in scenes_list:
         ptrs = []
         for k, dt, _ in keys:
-            a = np.ascontiguousarray(getattr(s, k), dt)
+            a = np.ascontiguousarray(field(s, k), dt)
             dst = bufs[k].numpy()[offs[k]:offs[k] + a.nbytes]
             dst[:] = a.view(np.uint8).reshape(-1)
             ptrs.append(bufs[k].data_ptr() + offs[k])
             offs[k] += a.nbytes
-        views.append(pfcuda.SceneView(*ptrs, s.n_points, s.n_contours, s.n_paths, s.width, s.height, s.clear))
+        v = pfcuda.SceneView(*ptrs[:6], s.n_points, s.n_contours, s.n_paths, s.width, s.height, s.clear)
+        if len(ptrs) > 6:
+            v.path_clip, v.path_is_clip = ptrs[6], ptrs[7]
+        views.append(v)
     h2d = sum(offs.values())
     return bufs, views, h2d
 
@@ -198,7 +223,7 @@ def run_reference(args, scenes_list):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 tiling, f64 coverage",
-        "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list),
+        "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list, args.clips),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -215,7 +240,7 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
 
     if args.impl == "reference":
-        scenes_list = S.batched(n_scenes=args.scenes)
+        scenes_list = make_scenes(args, 1000)
         run_reference(args, scenes_list)
         return
 
@@ -237,7 +262,7 @@ def main():
             dist.barrier()
 
     # replicas: every rank renders its own batch (seeds offset by rank); no data-path collective
-    scenes_list = S.batched(n_scenes=args.scenes, first_seed=replica_first_seed(rank))
+    scenes_list = make_scenes(args, replica_first_seed(rank))
     bufs, views, h2d_bytes = pack_pinned(scenes_list)
     stream = torch.cuda.Stream()
     r = pfcuda.Renderer(device=local_rank, stream=stream.cuda_stream, stage_timing=True)
@@ -365,7 +390,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_batched, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (exact-IEEE tiling), int32 fixed-point coverage", "data": "synthetic",
-            "config": workload_config(n_scenes, scenes_list) | {"parallelism": f"replicas x{world}"},
+            "config": workload_config(n_scenes, scenes_list, args.clips) | {"parallelism": f"replicas x{world}"},
             "frame": "batched learned one-pass" if learned else "batched exact two-pass",
             "batched_exact": {"value": world * n_scenes / (ms_exact * 1e-3), "unit": UNIT, "ms_per_step": ms_exact},
             "plain": {"value": world * n_scenes / (ms_plain * 1e-3), "unit": UNIT, "ms_per_step": ms_plain,

@@ -17,8 +17,10 @@ void SceneBuilderCuda::build(Scene *scene, Renderer *renderer) {
     path_start_.assign(1, 0);
     color_.clear();
     fill_rule_.clear();
-    for (const DrawPath &path : scene->draw_paths) {
-        for (const Contour &contour : path.outline.contours) {
+    path_clip_.clear();
+    path_is_clip_.clear();
+    auto push_outline = [&](const Outline &outline) {
+        for (const Contour &contour : outline.contours) {
             for (size_t i = 0; i < contour.points.size(); i++) {
                 points_.push_back(contour.points[i].x);
                 points_.push_back(contour.points[i].y);
@@ -27,9 +29,26 @@ void SceneBuilderCuda::build(Scene *scene, Renderer *renderer) {
             contour_start_.push_back(static_cast<uint32_t>(flags_.size()));
         }
         path_start_.push_back(static_cast<uint32_t>(contour_start_.size() - 1));
+    };
+    // draw paths, then the clip paths (Scene::clip_paths) after them; a draw path's clip
+    // (DrawPath::clip_path) names its clip path by its index among all paths
+    const uint32_t n_draw = static_cast<uint32_t>(scene->draw_paths.size());
+    for (const DrawPath &path : scene->draw_paths) {
+        push_outline(path.outline);
         const ColorU c = scene->get_paint(path.paint).get_base_color();
         color_.push_back(uint32_t(c.r_) | uint32_t(c.g_) << 8 | uint32_t(c.b_) << 16 | uint32_t(c.a_) << 24);
         fill_rule_.push_back(path.fill_rule == FillRule::EvenOdd ? PF_FILL_EVEN_ODD : PF_FILL_NONZERO);
+        path_clip_.push_back(path.clip_path ? n_draw + *path.clip_path : PF_NO_CLIP);
+        path_is_clip_.push_back(0);
+    }
+    for (const ClipPath &clip : scene->clip_paths) {
+        push_outline(clip.outline);
+        color_.push_back(0xffffffffu);  // never drawn
+        fill_rule_.push_back(clip.fill_rule == FillRule::EvenOdd ? PF_FILL_EVEN_ODD : PF_FILL_NONZERO);
+        // a clipped clip path (nested clips) is not supported by the d3d9 tiler either; the
+        // upload rejects it
+        path_clip_.push_back(clip.clip_path ? n_draw + *clip.clip_path : PF_NO_CLIP);
+        path_is_clip_.push_back(1);
     }
     const RectF vb = scene->get_view_box();
     view_ = pf_scene_view{};
@@ -42,6 +61,10 @@ void SceneBuilderCuda::build(Scene *scene, Renderer *renderer) {
     view_.n_points = static_cast<uint32_t>(flags_.size());
     view_.n_contours = static_cast<uint32_t>(contour_start_.size() - 1);
     view_.n_paths = static_cast<uint32_t>(color_.size());
+    if (!scene->clip_paths.empty()) {
+        view_.path_clip = path_clip_.data();
+        view_.path_is_clip = path_is_clip_.data();
+    }
     view_.width = vb.width();
     view_.height = vb.height();
     view_.clear_color = 0;

@@ -23,7 +23,7 @@
 
 namespace Pathfinder {
 
-/// Packs the scene's draw paths into the C-ABI's outline arrays
+/// Packs the scene's draw paths and clip paths into the C-ABI's outline arrays
 /// (SceneBuilder::build, pathfinder/core/scene_builder.h:16-27).  Replaces
 /// SceneBuilderD3D11::build's segment packing (pathfinder/core/d3d11/scene_builder.cpp:209-223):
 /// segments, bounds and tile rects are derived on the GPU.
@@ -39,8 +39,8 @@ public:
 private:
     std::vector<float> points_;
     std::vector<uint8_t> flags_;
-    std::vector<uint32_t> contour_start_, path_start_, color_;
-    std::vector<uint8_t> fill_rule_;
+    std::vector<uint32_t> contour_start_, path_start_, color_, path_clip_;
+    std::vector<uint8_t> fill_rule_, path_is_clip_;
     pf_scene_view view_{};
 };
 

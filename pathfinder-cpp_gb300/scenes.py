@@ -357,6 +357,29 @@ def clipped(seed: int = 0, n_paths: int = 240, side: int = 1024, n_clips: int = 
     return with_clips(draw, clips, assign)
 
 
+def add_clips(draw: Scene, seed: int, n_clips: int = 8, clip_share: float = 0.6) -> Scene:
+    """`draw` with n_clips clip paths appended: closed cubic shapes a quarter to a whole of the
+    canvas wide, alternately nonzero and even-odd; each draw path is clipped by a random one
+    with probability clip_share."""
+    rng = Rng(seed, 7)
+    side = float(min(draw.width, draw.height))
+    size = side * (0.25 + 0.75 * rng.uniform(n_clips))
+    lo = rng.uniform(2 * n_clips).reshape(n_clips, 2) * (side - size)[:, None]
+    cpts, cfl = _cubic_paths(rng, n_clips, lo, np.asarray(size, np.float64), 3, 8)
+    clips = _assemble(cpts, cfl, np.ones(n_clips, np.int64), (np.arange(n_clips) % 2).astype(np.uint8),
+                      np.full(n_clips, 0xFFFFFFFF, np.uint32), draw.width, draw.height)
+    n = draw.n_paths
+    assign = np.where(rng.uniform(n) < clip_share, rng.integers(0, n_clips - 1, n), -1)
+    return with_clips(draw, clips, assign)
+
+
+def batched_clipped(n_scenes: int = 512, first_seed: int = 1000, n_clips: int = 8, clip_share: float = 0.6,
+                    **kw) -> List[Scene]:
+    """The batched scenes, each with n_clips clip paths (add_clips, seeded by the scene's seed)."""
+    return [add_clips(sc, first_seed + i, n_clips, clip_share)
+            for i, sc in enumerate(batched(n_scenes=n_scenes, first_seed=first_seed, **kw))]
+
+
 def mixed(seed: int = 7, n_paths: int = 8192, side: int = 4096) -> Scene:
     """A mixture of the three path families on one canvas (held-out evaluation scene)."""
     rng = Rng(seed, 5)

@@ -1,7 +1,7 @@
-// Builds a scene through the reference's own API (Path2d, Paint, Scene::push_draw_path), packs
-// it with the drop-in SceneBuilderCuda, and tiles the packed scene with both the reference's
-// d3d9 tiler (through the harness) and the restated oracle.  Prints "OK <fills>" when the two
-// agree and the packed colours / fill rules are the ones the scene holds.
+// Builds a scene through the reference's own API (Path2d, Paint, Scene::push_draw_path and
+// push_clip_path), packs it with the drop-in SceneBuilderCuda, and tiles the packed scene with
+// both the reference's d3d9 tiler (through the harness) and the restated oracle.  Prints "OK <fills>" when the two
+// agree and the packed colours / fill rules / clip assignments are the ones the scene holds.
 #include <cstdio>
 #include <cstring>
 
@@ -14,6 +14,31 @@ using namespace Pathfinder;
 
 int main() {
     Scene scene(0, RectF({0.f, 0.f}, {300.f, 200.f}));
+    // two clip paths (Scene::push_clip_path): a diamond and an even-odd ring
+    uint32_t clip_ids[2];
+    {
+        Path2d c;
+        c.move_to(150.f, 5.f);
+        c.line_to(290.f, 100.f);
+        c.line_to(150.f, 195.f);
+        c.line_to(10.f, 100.f);
+        c.close_path();
+        ClipPath cp;
+        cp.outline = c.into_outline();
+        clip_ids[0] = scene.push_clip_path(cp);
+        Path2d r;
+        r.move_to(40.f, 30.f);
+        r.cubic_to(260.f, 10.f, 280.f, 190.f, 60.f, 170.f);
+        r.close_path();
+        r.move_to(90.f, 70.f);
+        r.line_to(180.f, 75.f);
+        r.line_to(150.f, 130.f);
+        r.close_path();
+        ClipPath cr;
+        cr.outline = r.into_outline();
+        cr.fill_rule = FillRule::EvenOdd;
+        clip_ids[1] = scene.push_clip_path(cr);
+    }
     for (int i = 0; i < 8; i++) {
         Path2d p;
         const float o = 7.f * i;
@@ -32,13 +57,18 @@ int main() {
         dp.outline = p.into_outline();
         dp.paint = scene.push_paint(Paint::from_color(ColorU(20 * i, 255 - 20 * i, 100, i % 2 ? 160 : 255)));
         dp.fill_rule = i % 2 ? FillRule::EvenOdd : FillRule::Winding;
+        if (i % 4 != 3) dp.clip_path = std::make_shared<uint32_t>(clip_ids[i % 2]);
         scene.push_draw_path(dp);
     }
     SceneBuilderCuda builder;
     builder.build(&scene, nullptr);
     const pf_scene_view &v = builder.view();
-    if (v.n_paths != 8) return std::printf("FAIL paths %u\n", v.n_paths), 1;
-    for (uint32_t i = 0; i < v.n_paths; i++) {
+    if (v.n_paths != 10 || !v.path_clip || !v.path_is_clip) return std::printf("FAIL paths %u\n", v.n_paths), 1;
+    for (uint32_t i = 0; i < 10; i++) {
+        const uint32_t want = i >= 8 ? PF_NO_CLIP : i % 4 == 3 ? PF_NO_CLIP : 8 + clip_ids[i % 2];
+        if (v.path_clip[i] != want || v.path_is_clip[i] != (i >= 8)) return std::printf("FAIL clip %u\n", i), 1;
+    }
+    for (uint32_t i = 0; i < 8; i++) {
         const uint32_t want = uint32_t(20 * i) | uint32_t(255 - 20 * i) << 8 | 100u << 16 | uint32_t(i % 2 ? 160 : 255) << 24;
         if (v.color[i] != want || v.fill_rule[i] != (i % 2)) return std::printf("FAIL paint %u\n", i), 1;
     }
@@ -47,7 +77,12 @@ int main() {
     bool same = a.n_tiles == b.n_tiles && a.n_fills == b.n_fills && a.n_list == b.n_list &&
                 !std::memcmp(a.tile_backdrop, b.tile_backdrop, a.n_tiles) &&
                 !std::memcmp(a.tile_alpha, b.tile_alpha, a.n_tiles) &&
-                !std::memcmp(a.fills, b.fills, a.n_fills * 8) && !std::memcmp(a.fb_list, b.fb_list, a.n_list * 4);
+                !std::memcmp(a.fills, b.fills, a.n_fills * 8) && !std::memcmp(a.fb_list, b.fb_list, a.n_list * 4) &&
+                !std::memcmp(a.tile_mask, b.tile_mask, a.n_tiles) &&
+                !std::memcmp(a.tile_clip, b.tile_clip, a.n_tiles * 8);
+    uint64_t clipped = 0;
+    for (uint64_t t = 0; t < a.n_tiles; t++) clipped += a.tile_mask[t] != 0;
+    same = same && clipped > 0;
     std::printf("%s %llu\n", same ? "OK" : "FAIL", (unsigned long long)a.n_fills);
     return same ? 0 : 1;
 }
