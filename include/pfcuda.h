@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define PF_ABI_VERSION 2
+#define PF_ABI_VERSION 3
 
 typedef enum pf_status {
     PF_OK = 0,
@@ -46,6 +46,32 @@ typedef enum pf_status {
 
 /* No clip path (pf_scene_view::path_clip). */
 #define PF_NO_CLIP 0xffffffffu
+
+/* Line caps and joins (LineCap, LineJoin, pathfinder/core/data/data.h:73-96). */
+#define PF_CAP_BUTT 0u
+#define PF_CAP_SQUARE 1u
+#define PF_CAP_ROUND 2u
+#define PF_JOIN_MITER 0u
+#define PF_JOIN_BEVEL 1u
+#define PF_JOIN_ROUND 2u
+
+/*
+ * How a path is stroked: StrokeStyle (pathfinder/core/stroke.h:14-27) and the canvas's line
+ * dash (Canvas::stroke_path, pathfinder/core/canvas.cpp:270-300).  A stroked path's outline is
+ * dashed (OutlineDash, pathfinder/core/dash.cpp) when it has a pattern, then converted to its
+ * stroke outline (OutlineStrokeToFill, pathfinder/core/stroke.cpp) on the GPU when the scene is
+ * uploaded; the stroke outline is filled with the nonzero rule, as the canvas does.
+ */
+typedef struct pf_stroke {
+    float line_width;    /* > 0: the path is stroked with this width; 0: it is filled      */
+    float miter_limit;   /* PF_JOIN_MITER: the miter limit ratio                            */
+    uint8_t line_cap;    /* PF_CAP_*                                                       */
+    uint8_t line_join;   /* PF_JOIN_*                                                      */
+    uint16_t reserved;
+    uint32_t dash_first; /* the dash pattern: dashes[dash_first, dash_first + dash_count) */
+    uint32_t dash_count; /* 0: a solid stroke                                              */
+    float dash_offset;   /* the pattern's phase (the canvas passes 0)                      */
+} pf_stroke;
 
 /* Point flags (pathfinder/core/data/data.h:120-129). */
 #define PF_POINT_ON_CURVE 0u
@@ -80,6 +106,12 @@ typedef enum pf_status {
  *                 when it is solid and the clip tile is an alpha tile, and drawn with the two
  *                 masks combined (tile_clip_combine.frag: min of |mask + backdrop|) when both
  *                 are alpha tiles.
+ *   path_stroke   [n_paths] or NULL: how each path is stroked (line_width 0: filled)
+ *   contour_closed [n_contours] or NULL (every contour open): Contour::closed
+ *                 (pathfinder/core/data/contour.h:27), which decides between caps and a
+ *                 closing join when the contour is stroked; fills close every contour
+ *   dashes        [n_dashes]: the dash patterns the strokes refer to; finite, >= 0, and each
+ *                 pattern's total > 0
  */
 typedef struct pf_scene_view {
     const float *points;
@@ -96,6 +128,10 @@ typedef struct pf_scene_view {
     uint32_t clear_color;
     const uint32_t *path_clip;   /* ABI 2 */
     const uint8_t *path_is_clip; /* ABI 2 */
+    const pf_stroke *path_stroke;   /* ABI 3 */
+    const uint8_t *contour_closed;  /* ABI 3 */
+    const float *dashes;            /* ABI 3 */
+    uint32_t n_dashes;              /* ABI 3 */
 } pf_scene_view;
 
 /* Context configuration.  Zero-initialise and set what you need. */

@@ -35,6 +35,16 @@ class SceneView(C.Structure):
         ("n_points", C.c_uint32), ("n_contours", C.c_uint32), ("n_paths", C.c_uint32),
         ("width", C.c_float), ("height", C.c_float), ("clear_color", C.c_uint32),
         ("path_clip", C.c_void_p), ("path_is_clip", C.c_void_p),
+        ("path_stroke", C.c_void_p), ("contour_closed", C.c_void_p), ("dashes", C.c_void_p),
+        ("n_dashes", C.c_uint32),
+    ]
+
+
+class Outline(C.Structure):
+    _fields_ = [
+        ("n_points", C.c_uint32), ("n_contours", C.c_uint32), ("n_paths", C.c_uint32),
+        ("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_start", C.c_void_p),
+        ("path_start", C.c_void_p), ("fill_rule", C.c_void_p),
     ]
 
 
@@ -64,6 +74,19 @@ def scene_view(scene) -> "tuple[SceneView, list]":
         is_clip = np.ascontiguousarray(scene.path_is_clip, np.uint8)
         v.path_clip, v.path_is_clip = clip.ctypes.data, is_clip.ctypes.data
         arrs += [clip, is_clip]
+    if getattr(scene, "path_stroke", None) is not None:
+        st = np.ascontiguousarray(scene.path_stroke)
+        assert st.dtype.itemsize == 24
+        v.path_stroke = st.ctypes.data
+        arrs.append(st)
+        if getattr(scene, "contour_closed", None) is not None:
+            cc = np.ascontiguousarray(scene.contour_closed, np.uint8)
+            v.contour_closed = cc.ctypes.data
+            arrs.append(cc)
+        if getattr(scene, "dashes", None) is not None:
+            d = np.ascontiguousarray(scene.dashes, np.float32)
+            v.dashes, v.n_dashes = d.ctypes.data, len(d)
+            arrs.append(d)
     return v, arrs
 
 
@@ -124,9 +147,47 @@ def have_reference() -> bool:
     return os.path.exists(LIB_REF)
 
 
+def _outline_scene(scene, o: Outline):
+    import dataclasses
+    pts = _arr(o.points, 2 * o.n_points, np.float32).reshape(-1, 2)
+    return dataclasses.replace(
+        scene, points=pts, flags=_arr(o.point_flags, o.n_points, np.uint8),
+        contour_start=_arr(o.contour_start, o.n_contours + 1, np.uint32),
+        path_start=_arr(o.path_start, o.n_paths + 1, np.uint32),
+        fill_rule=_arr(o.fill_rule, o.n_paths, np.uint8), path_stroke=None, contour_closed=None, dashes=None)
+
+
+def stroke_scene(scene, reference: bool = False):
+    """The scene's fill outline: stroked paths dashed and converted to stroke outlines
+    (pf_stroke.c, or with reference=True the reference's own OutlineDash/OutlineStrokeToFill)."""
+    lib = _lib(LIB_REF if reference else LIB_ORACLE)
+    v, keep = scene_view(scene)
+    o = Outline()
+    st = (lib.pfref_stroke_scene if reference else lib.pfo_stroke_scene)(C.byref(v), C.byref(o))
+    if st != 0:
+        raise RuntimeError(f"stroke_scene failed with status {st}")
+    try:
+        return _outline_scene(scene, o)
+    finally:
+        if reference:
+            for name in ("points", "point_flags", "contour_start", "path_start", "fill_rule"):
+                C.CDLL(None).free(C.c_void_p(getattr(o, name)))
+        else:
+            lib.pfo_outline_free(C.byref(o))
+
+
+def fill_scene(scene):
+    """A scene with strokes turned into fills (the oracle's stroker); others unchanged."""
+    st = getattr(scene, "path_stroke", None)
+    if st is None or not np.any(st["line_width"] > 0):
+        return scene
+    return stroke_scene(scene)
+
+
 def tile_scene(scene, z_rule: int = Z_D3D11, threads: int = 1) -> Dict[str, np.ndarray]:
     """Restated d3d9 tiler over a scene: canonical integer outputs."""
     lib = _lib(LIB_ORACLE)
+    scene = fill_scene(scene)
     v, keep = scene_view(scene)
     r = Result()
     st = lib.pfo_tile_scene_mt(C.byref(v), C.c_int(z_rule), C.c_int(threads), C.byref(r))
@@ -141,8 +202,12 @@ def tile_scene(scene, z_rule: int = Z_D3D11, threads: int = 1) -> Dict[str, np.n
 
 
 def reference_tile_scene(scene) -> Dict[str, np.ndarray]:
-    """The reference's own tiler (z rule D3D9) over a scene."""
+    """The reference's own tiler (z rule D3D9) over a scene (strokes through the reference's own
+    stroker first)."""
     lib = _lib(LIB_REF)
+    st = getattr(scene, "path_stroke", None)
+    if st is not None and np.any(st["line_width"] > 0):
+        scene = stroke_scene(scene, reference=True)
     v, keep = scene_view(scene)
     r = Result()
     st = lib.pfref_tile_scene(C.byref(v), C.byref(r))
@@ -158,6 +223,7 @@ def render(scene, z_rule: int = Z_D3D11, threads: int = 1, coverage: bool = Fals
            tiled: Optional[Dict[str, np.ndarray]] = None):
     """FP64 analytic-area coverage + src-over composite; returns (rgba u8 [H,W,4], coverage|None)."""
     lib = _lib(LIB_ORACLE)
+    scene = fill_scene(scene)
     v, keep = scene_view(scene)
     r = Result()
     st = lib.pfo_tile_scene_mt(C.byref(v), C.c_int(z_rule), C.c_int(threads), C.byref(r))

@@ -77,8 +77,30 @@ int pfo_render(const pf_scene_view *scene, const pfo_result *tiled, uint8_t *rgb
 
 void pfo_free(pfo_result *r);
 
+/*
+ * Stroke-to-fill and dashing (pf_stroke.c): the scene's fill outline, every stroked path
+ * (pf_stroke::line_width > 0) replaced by its stroke outline (OutlineDash, then
+ * OutlineStrokeToFill, as Canvas::stroke_path does) and filled nonzero; other paths copied.
+ */
+typedef struct pfo_outline {
+    uint32_t n_points, n_contours, n_paths;
+    float *points;           /* [n_points][2] */
+    uint8_t *point_flags;    /* [n_points] */
+    uint32_t *contour_start; /* [n_contours + 1] */
+    uint32_t *path_start;    /* [n_paths + 1] */
+    uint8_t *fill_rule;      /* [n_paths] */
+} pfo_outline;
+
+/* 0 ok; 1 invalid stroke data; 3 out of memory; 4 too large; 5 a dash pattern needs more than
+ * 2^22 steps on one path */
+int pfo_stroke_scene(const pf_scene_view *scene, pfo_outline *out);
+int pfo_stroke_check(const pf_scene_view *scene);
+void pfo_outline_free(pfo_outline *o);
+
 /* Reference harness (oracle/_ref/libpfref.so): same output, z rule D3D9. */
 int pfref_tile_scene(const pf_scene_view *scene, pfo_result *out);
+/* The reference's own OutlineDash + OutlineStrokeToFill over the same scene. */
+int pfref_stroke_scene(const pf_scene_view *scene, pfo_outline *out);
 void pfref_free(pfo_result *r);
 
 #ifdef __cplusplus

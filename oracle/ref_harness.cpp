@@ -21,7 +21,9 @@
 
 #include "core/d3d9/scene_builder.h"
 #include "core/d3d9/tiler.h"
+#include "core/dash.h"
 #include "core/scene.h"
+#include "core/stroke.h"
 
 #include "pf_oracle.h"
 
@@ -334,6 +336,82 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
     out->tile_mask = dup(tile_mask);
     out->tile_clip = dup(tile_clip);
     out->tile_dest_backdrop = dup(tile_dest_backdrop);
+    return 0;
+}
+
+// Canvas::stroke_path (pathfinder/core/canvas.cpp:270-300) minus the canvas: each stroked
+// path's outline (contours as Path2d::into_outline makes them: empty ones dropped) is dashed
+// with OutlineDash when it has a pattern, then converted with OutlineStrokeToFill; other paths
+// are copied.
+extern "C" int pfref_stroke_scene(const pf_scene_view *sv, pfo_outline *out) {
+    std::memset(out, 0, sizeof(*out));
+    // the reference loops forever on an all-zero dash pattern: only well-formed patterns
+    for (uint32_t p = 0; sv->path_stroke && p < sv->n_paths; p++) {
+        const pf_stroke &st = sv->path_stroke[p];
+        if (!(st.line_width > 0.0f) || !st.dash_count) continue;
+        if (uint64_t(st.dash_first) + st.dash_count > sv->n_dashes) return 1;
+        float total = 0;
+        for (uint32_t i = 0; i < st.dash_count; i++) total += sv->dashes[st.dash_first + i];
+        if (!(total > 0.0f)) return 1;
+    }
+    std::vector<float> pts;
+    std::vector<uint8_t> flags, rule(sv->n_paths);
+    std::vector<uint32_t> cstart{0}, pstart{0};
+    auto emit = [&](const Contour &c) {
+        for (size_t i = 0; i < c.points.size(); i++) {
+            pts.push_back(c.points[i].x);
+            pts.push_back(c.points[i].y);
+            flags.push_back(static_cast<uint8_t>(c.flags[i]));
+        }
+        cstart.push_back(static_cast<uint32_t>(flags.size()));
+    };
+    for (uint32_t p = 0; p < sv->n_paths; p++) {
+        const pf_stroke *st = sv->path_stroke ? &sv->path_stroke[p] : nullptr;
+        rule[p] = sv->fill_rule[p];
+        if (!st || !(st->line_width > 0.0f)) {
+            for (uint32_t k = sv->path_start[p]; k < sv->path_start[p + 1]; k++) {
+                Contour c;
+                for (uint32_t i = sv->contour_start[k]; i < sv->contour_start[k + 1]; i++)
+                    c.push_point(Vec2F(sv->points[2 * i], sv->points[2 * i + 1]),
+                                 static_cast<PointFlag>(sv->point_flags[i]), false);
+                emit(c);
+            }
+        } else {
+            rule[p] = PF_FILL_NONZERO;
+            Outline outline;
+            for (uint32_t k = sv->path_start[p]; k < sv->path_start[p + 1]; k++) {
+                Contour c;
+                for (uint32_t i = sv->contour_start[k]; i < sv->contour_start[k + 1]; i++)
+                    c.push_point(Vec2F(sv->points[2 * i], sv->points[2 * i + 1]),
+                                 static_cast<PointFlag>(sv->point_flags[i]), true);
+                c.closed = sv->contour_closed && sv->contour_closed[k];
+                outline.push_contour(c);
+            }
+            if (st->dash_count) {
+                std::vector<float> dashes(sv->dashes + st->dash_first, sv->dashes + st->dash_first + st->dash_count);
+                OutlineDash dasher(outline, dashes, st->dash_offset);
+                dasher.dash();
+                outline = dasher.into_outline();
+            }
+            StrokeStyle style;
+            style.line_width = st->line_width;
+            style.miter_limit = st->miter_limit;
+            style.line_cap = static_cast<LineCap>(st->line_cap);
+            style.line_join = static_cast<LineJoin>(st->line_join);
+            OutlineStrokeToFill stroker(outline, style);
+            stroker.offset();
+            for (const Contour &c : stroker.into_outline().contours) emit(c);
+        }
+        pstart.push_back(static_cast<uint32_t>(cstart.size() - 1));
+    }
+    out->n_points = static_cast<uint32_t>(flags.size());
+    out->n_contours = static_cast<uint32_t>(cstart.size() - 1);
+    out->n_paths = sv->n_paths;
+    out->points = dup(pts);
+    out->point_flags = dup(flags);
+    out->contour_start = dup(cstart);
+    out->path_start = dup(pstart);
+    out->fill_rule = dup(rule);
     return 0;
 }
 

@@ -182,6 +182,9 @@ int validate_scene(Ctx *c, const pf_scene_view *s) {
     for (uint32_t k = 0; k < s->n_contours; k++)
         if (s->contour_start[k] > s->contour_start[k + 1])
             return fail(c, PF_ERR_INVALID_ARGUMENT, "contour_start must be non-decreasing");
+    for (uint32_t p = 0; s->path_stroke && p < s->n_paths; p++)
+        if (s->path_stroke[p].line_width != 0.0f)
+            return fail(c, PF_ERR_INVALID_ARGUMENT, "stroked paths are not supported by this build");
     if (s->path_clip || s->path_is_clip) {
         // Scene::push_draw_path / push_clip_path: clip paths come after every draw path, are not
         // clipped themselves, and a draw path names a clip path or none

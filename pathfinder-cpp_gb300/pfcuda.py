@@ -38,6 +38,13 @@ N_OUTPUTS = 2
 DEFAULT_WEIGHTS = os.path.join(HERE, "weights", "sizer.bin")
 
 
+class Stroke(C.Structure):
+    """pf_stroke (the numpy layout is scenes.STROKE_DTYPE)."""
+    _fields_ = [("line_width", C.c_float), ("miter_limit", C.c_float), ("line_cap", C.c_uint8),
+                ("line_join", C.c_uint8), ("reserved", C.c_uint16), ("dash_first", C.c_uint32),
+                ("dash_count", C.c_uint32), ("dash_offset", C.c_float)]
+
+
 class SceneView(C.Structure):
     _fields_ = [
         ("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_start", C.c_void_p),
@@ -45,6 +52,8 @@ class SceneView(C.Structure):
         ("n_points", C.c_uint32), ("n_contours", C.c_uint32), ("n_paths", C.c_uint32),
         ("width", C.c_float), ("height", C.c_float), ("clear_color", C.c_uint32),
         ("path_clip", C.c_void_p), ("path_is_clip", C.c_void_p),
+        ("path_stroke", C.c_void_p), ("contour_closed", C.c_void_p), ("dashes", C.c_void_p),
+        ("n_dashes", C.c_uint32),
     ]
 
 
@@ -120,6 +129,20 @@ def scene_view(scene) -> "tuple[SceneView, list]":
         is_clip = np.ascontiguousarray(scene.path_is_clip, np.uint8)
         v.path_is_clip = is_clip.ctypes.data
         arrs.append(is_clip)
+    if getattr(scene, "path_stroke", None) is not None:
+        st = np.ascontiguousarray(scene.path_stroke)
+        if st.dtype.itemsize != C.sizeof(Stroke):
+            raise ValueError("path_stroke must use scenes.STROKE_DTYPE (pf_stroke)")
+        v.path_stroke = st.ctypes.data
+        arrs.append(st)
+    if getattr(scene, "contour_closed", None) is not None:
+        cc = np.ascontiguousarray(scene.contour_closed, np.uint8)
+        v.contour_closed = cc.ctypes.data
+        arrs.append(cc)
+    if getattr(scene, "dashes", None) is not None:
+        d = np.ascontiguousarray(scene.dashes, np.float32)
+        v.dashes, v.n_dashes = d.ctypes.data, len(d)
+        arrs.append(d)
     return v, arrs
 
 

@@ -31,6 +31,13 @@ from typing import List, Optional
 
 import numpy as np
 
+# pf_stroke (include/pfcuda.h): StrokeStyle plus the canvas's line dash
+STROKE_DTYPE = np.dtype([("line_width", "<f4"), ("miter_limit", "<f4"), ("line_cap", "u1"),
+                         ("line_join", "u1"), ("reserved", "<u2"), ("dash_first", "<u4"),
+                         ("dash_count", "<u4"), ("dash_offset", "<f4")])
+CAP_BUTT, CAP_SQUARE, CAP_ROUND = 0, 1, 2
+JOIN_MITER, JOIN_BEVEL, JOIN_ROUND = 0, 1, 2
+
 _GOLDEN = np.uint64(0x9E3779B97F4A7C15)
 _M1 = np.uint64(0xBF58476D1CE4E5B9)
 _M2 = np.uint64(0x94D049BB133111EB)
@@ -94,6 +101,9 @@ class Scene:
     clear: int = 0              # RGBA8 clear colour, red in the low byte
     path_clip: Optional[np.ndarray] = None     # uint32 [N] clip path of each path, or NO_CLIP
     path_is_clip: Optional[np.ndarray] = None  # uint8 [N] 1 for clip paths (after the draw paths)
+    path_stroke: Optional[np.ndarray] = None   # STROKE_DTYPE [N]: how each path is stroked
+    contour_closed: Optional[np.ndarray] = None  # uint8 [C] Contour::closed (strokes only)
+    dashes: Optional[np.ndarray] = None        # float32 [D] dash patterns of the strokes
 
     @property
     def n_paths(self) -> int:
@@ -378,6 +388,67 @@ def batched_clipped(n_scenes: int = 512, first_seed: int = 1000, n_clips: int = 
     """The batched scenes, each with n_clips clip paths (add_clips, seeded by the scene's seed)."""
     return [add_clips(sc, first_seed + i, n_clips, clip_share)
             for i, sc in enumerate(batched(n_scenes=n_scenes, first_seed=first_seed, **kw))]
+
+
+def stroked(seed: int = 0, n_paths: int = 200, side: int = 1024, dash_share: float = 0.3,
+            fill_share: float = 0.0) -> Scene:
+    """Stroked paths (Canvas::stroke_path): 1-3 contours each, a random walk of 1-12 segments
+    (lines, quadratic and cubic curves), 40 % of the contours closed; line width log-uniform
+    0.5-24 px; caps, joins and miter limits (1-12) uniform; dash_share of the paths dashed with
+    a 2- or 4-entry pattern of 1-40 px (a third of them with a phase); fill_share of the paths
+    filled instead.  Colours are translucent or opaque, nonzero rule."""
+    rng = Rng(seed, 8)
+    pts, fl, cstart, pstart, closed = [], [], [0], [0], []
+    n = n_paths
+    n_contours = rng.integers(1, 3, n)
+    width = _log_uniform(rng, 0.5, 24.0, n)
+    caps = rng.integers(0, 2, n)
+    joins = rng.integers(0, 2, n)
+    miter = 1.0 + 11.0 * rng.uniform(n)
+    dashed = rng.uniform(n) < dash_share
+    filled = rng.uniform(n) < fill_share
+    dashes: list = []
+    st = np.zeros(n, STROKE_DTYPE)
+    for p in range(n):
+        box = float(_log_uniform(rng, 16.0, float(side), 1)[0])
+        origin = rng.uniform(2) * (side - box)
+        for _ in range(int(n_contours[p])):
+            nseg = int(rng.integers(1, 12, 1)[0])
+            kinds = rng.integers(0, 2, nseg)
+            cur = origin + rng.uniform(2) * box
+            cp, cf = [cur], [0]
+            for k in kinds:
+                for _ in range(int(k)):  # control points
+                    cp.append(origin + rng.uniform(2) * box)
+                    cf.append(1 if len(cf) == 0 or cf[-1] == 0 else 2)
+                cp.append(origin + rng.uniform(2) * box)
+                cf.append(0)
+            pts.append(np.array(cp, np.float64))
+            fl.append(np.array(cf, np.uint8))
+            cstart.append(cstart[-1] + len(cp))
+            closed.append(1 if rng.uniform(1)[0] < 0.4 else 0)
+        pstart.append(len(cstart) - 1)
+        st[p]["line_width"] = 0.0 if filled[p] else width[p]
+        st[p]["miter_limit"] = miter[p]
+        st[p]["line_cap"] = caps[p]
+        st[p]["line_join"] = joins[p]
+        if dashed[p] and not filled[p]:
+            m = 2 if rng.uniform(1)[0] < 0.5 else 4
+            pat = 1.0 + 39.0 * rng.uniform(m)
+            st[p]["dash_first"] = len(dashes)
+            st[p]["dash_count"] = m
+            st[p]["dash_offset"] = float(rng.uniform(1)[0] * pat.sum()) if rng.uniform(1)[0] < 0.33 else 0.0
+            dashes.extend(pat.tolist())
+    rgb = rng.integers(0, 0xFFFFFF, n).astype(np.uint32)
+    alpha = np.where(rng.uniform(n) < 0.4, (rng.uniform(n) * 180 + 60).astype(np.uint32), 255)
+    sc = Scene(points=np.concatenate(pts).astype(np.float32), flags=np.concatenate(fl),
+               contour_start=np.asarray(cstart, np.uint32), path_start=np.asarray(pstart, np.uint32),
+               fill_rule=np.zeros(n, np.uint8), color=rgb | (alpha.astype(np.uint32) << np.uint32(24)),
+               width=float(side), height=float(side))
+    sc.path_stroke = st
+    sc.contour_closed = np.asarray(closed, np.uint8)
+    sc.dashes = np.asarray(dashes if dashes else [1.0], np.float32)
+    return sc
 
 
 def mixed(seed: int = 7, n_paths: int = 8192, side: int = 4096) -> Scene:

@@ -15,6 +15,8 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 CANON_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha", "tile_backdrop",
               "tile_fill_count", "fills", "column_backdrop", "fb_tiles", "z", "fb_list_first", "fb_list",
               "tile_mask", "tile_clip", "tile_dest_backdrop"]
+# the stroke outline stored with stroked fixtures (out_<key>)
+OUTLINE_KEYS = ["points", "flags", "contour_start", "path_start", "fill_rule"]
 TILE_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha", "tile_backdrop",
              "tile_fill_count", "fills", "column_backdrop", "tile_mask", "tile_clip", "tile_dest_backdrop"]
 
@@ -35,8 +37,14 @@ def load_golden(name):
                  path_start=d["path_start"], fill_rule=d["fill_rule"], color=d["color"],
                  width=float(w), height=float(h), clear=int(clear),
                  path_clip=d["path_clip"] if "path_clip" in d else None,
-                 path_is_clip=d["path_is_clip"] if "path_is_clip" in d else None)
+                 path_is_clip=d["path_is_clip"] if "path_is_clip" in d else None,
+                 path_stroke=d["path_stroke"] if "path_stroke" in d else None,
+                 contour_closed=d["contour_closed"] if "contour_closed" in d else None,
+                 dashes=d["dashes"] if "dashes" in d else None)
     ref = {k: d["ref_" + k] for k in CANON_KEYS}
+    for k in OUTLINE_KEYS:
+        if "out_" + k in d:
+            ref["out_" + k] = d["out_" + k]
     return sc, ref
 
 

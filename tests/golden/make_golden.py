@@ -37,6 +37,9 @@ CANON_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha",
               "tile_mask", "tile_clip", "tile_dest_backdrop"]
 INPUT_KEYS = ["points", "flags", "contour_start", "path_start", "fill_rule", "color"]
 CLIP_KEYS = ["path_clip", "path_is_clip"]  # stored when the scene has clip paths
+STROKE_KEYS = ["path_stroke", "contour_closed", "dashes"]  # stored when the scene has strokes
+# the reference's stroke outline (OutlineDash + OutlineStrokeToFill), stored as out_<key>
+OUTLINE_KEYS = ["points", "flags", "contour_start", "path_start", "fill_rule"]
 
 
 def build_scene(paths, width, height, clear=0) -> S.Scene:
@@ -174,6 +177,88 @@ def clip_scenes():
     return out
 
 
+def stroke(width, cap=S.CAP_BUTT, join=S.JOIN_MITER, miter=10.0, dash=None, offset=0.0):
+    return (width, cap, join, miter, dash, offset)
+
+
+def with_strokes(sc: S.Scene, styles, closed) -> S.Scene:
+    """styles: per path a stroke(...) tuple or None (filled); closed: per contour 0/1."""
+    st = np.zeros(sc.n_paths, S.STROKE_DTYPE)
+    dashes = []
+    for p, style in enumerate(styles):
+        if style is None:
+            continue
+        width, cap, join, miter, dash, offset = style
+        st[p] = (width, miter, cap, join, 0, len(dashes), len(dash) if dash else 0, offset)
+        if dash:
+            dashes.extend(dash)
+    sc.path_stroke = st
+    sc.contour_closed = np.asarray(closed, np.uint8)
+    sc.dashes = np.asarray(dashes if dashes else [1.0], np.float32)
+    return sc
+
+
+def curve(*items):
+    """A contour from (x, y, flag) triples."""
+    a = np.asarray(items, np.float32).reshape(-1, 3)
+    return a[:, :2].copy(), a[:, 2].astype(np.uint8)
+
+
+def stroke_scenes():
+    """Stroke-to-fill and dashing (core/stroke.cpp, core/dash.cpp): caps, joins, curves,
+    degenerate input and dash patterns."""
+    red, green, blue = (255, 0, 0, 255), (0, 160, 0, 255), (0, 0, 255, 255)
+    half = (20, 40, 200, 128)
+    out = {}
+    v = poly(10, 80, 40, 20, 70, 80)
+    out["stroke_caps"] = with_strokes(build_scene(
+        [([v], 0, red), ([poly(10, 100, 40, 40, 70, 100)], 0, half), ([poly(10, 60, 40, 5, 70, 60)], 0, blue),
+         ([poly(85, 10, 85, 110)], 0, green)], 100, 120),
+        [stroke(6, S.CAP_BUTT), stroke(10, S.CAP_SQUARE, S.JOIN_BEVEL), stroke(14, S.CAP_ROUND, S.JOIN_ROUND),
+         stroke(5, S.CAP_ROUND)], [0, 0, 0, 0])
+    tri = poly(20, 20, 100, 30, 40, 90)
+    sharp = poly(10, 110, 118, 100, 10, 104)
+    ring = poly(70, 70, 110, 70, 110, 110, 70, 110, 70, 70)   # last point repeats the first
+    out["stroke_joins"] = with_strokes(build_scene(
+        [([tri], 0, red), ([poly(60, 10, 120, 50, 80, 60)], 0, half), ([sharp], 0, blue), ([ring], 0, green),
+         ([poly(5, 60, 30, 40, 55, 60)], 0, half)], 128, 128),
+        [stroke(8, join=S.JOIN_MITER), stroke(6, join=S.JOIN_BEVEL), stroke(4, join=S.JOIN_MITER, miter=1.5),
+         stroke(7, join=S.JOIN_ROUND), stroke(9, S.CAP_SQUARE, S.JOIN_ROUND)], [1, 1, 1, 1, 0])
+    quad = curve(10, 100, 0, 50, -20, 1, 90, 100, 0)
+    cub = curve(10, 20, 0, 10, 20, 1, 60, 90, 2, 110, 20, 0)             # ctrl0 == from
+    cub2 = curve(10, 60, 0, 50, 0, 1, 110, 60, 2, 110, 60, 0)            # ctrl1 == to
+    loop = curve(20, 110, 0, 120, 40, 1, 0, 40, 2, 100, 110, 0)          # a cubic with a loop
+    tight = curve(60, 60, 0, 64, 50, 1, 68, 50, 2, 72, 60, 0)            # wide stroke, tight curve
+    out["stroke_curves"] = with_strokes(build_scene(
+        [([quad], 0, red), ([cub], 0, half), ([cub2], 0, blue), ([loop], 0, green), ([tight], 0, half)],
+        128, 128),
+        [stroke(5, S.CAP_ROUND, S.JOIN_ROUND), stroke(3), stroke(4, S.CAP_SQUARE, S.JOIN_BEVEL),
+         stroke(6, S.CAP_BUTT, S.JOIN_MITER, 4.0), stroke(30, S.CAP_ROUND, S.JOIN_ROUND)], [0, 1, 0, 0, 0])
+    out["stroke_degenerate"] = with_strokes(build_scene(
+        [([poly(30, 30)], 0, red),                                   # one point
+         ([poly(50, 50, 50, 50)], 0, red),                           # two equal points
+         ([poly(10, 80, 40, 80, 40, 80, 70, 60)], 0, blue),          # a zero-length line inside
+         ([poly(80, 10, 80.05, 10.02, 80.09, 10.01, 110, 40)], 0, half),  # segments under 0.1 px
+         ([poly(20, 110, 100, 110, 40, 110)], 0, green),             # a 180-degree turn
+         ([poly(60, 60, 70, 65)], 0, half),                          # a huge width
+         ([poly(5, 5, 20, 5, 20, 20)], 0, red)],                     # width under a pixel
+        128, 128),
+        [stroke(6, S.CAP_ROUND, S.JOIN_ROUND), stroke(6, S.CAP_SQUARE), stroke(5, S.CAP_SQUARE, S.JOIN_MITER),
+         stroke(4, S.CAP_ROUND, S.JOIN_ROUND), stroke(6, S.CAP_BUTT, S.JOIN_MITER), stroke(200, S.CAP_ROUND),
+         stroke(0.5, S.CAP_BUTT, S.JOIN_BEVEL)], [0, 1, 0, 0, 0, 0, 1])
+    wave = curve(10, 40, 0, 40, 0, 1, 60, 80, 2, 90, 40, 0, 100, 30, 0)
+    out["stroke_dashes"] = with_strokes(build_scene(
+        [([poly(10, 10, 110, 10), poly(10, 20, 110, 20)], 0, red),   # the pattern runs on across contours
+         ([wave], 0, blue),
+         ([poly(20, 60, 100, 60, 100, 110, 20, 110)], 0, half),     # a closed contour dashed
+         ([poly(10, 120, 118, 120)], 0, green)],                     # a zero entry in the pattern
+        128, 128),
+        [stroke(4, S.CAP_BUTT, dash=[7, 5]), stroke(5, S.CAP_ROUND, S.JOIN_ROUND, dash=[12, 4, 3, 4], offset=9.5),
+         stroke(6, S.CAP_SQUARE, S.JOIN_MITER, dash=[20, 10], offset=25.0),
+         stroke(3, S.CAP_ROUND, dash=[0, 8, 6, 4])], [0, 0, 0, 1, 0])
+    return out
+
+
 def generator_scenes():
     return {
         "gen_plain_small_s1": S.plain_small(seed=1, n_paths=24, side=256),
@@ -182,6 +267,7 @@ def generator_scenes():
         "gen_mixed_s4": S.mixed(seed=4, n_paths=96, side=512),
         "gen_batched_scene_s5": S.batched(n_scenes=3, first_seed=5, hi_paths=64)[2],
         "gen_clipped_s6": S.clipped(seed=6, n_paths=60, side=256, n_clips=4),
+        "gen_stroked_s7": S.stroked(seed=7, n_paths=40, side=256, dash_share=0.4, fill_share=0.2),
     }
 
 
@@ -208,12 +294,17 @@ def main() -> None:
         raise SystemExit("the reference tiler could not be built (is the reference tree present?)")
     small = dict(edge_scenes())
     small.update(clip_scenes())
+    small.update(stroke_scenes())
     small.update(generator_scenes())
     for name, sc in small.items():
         ref = oracle.reference_tile_scene(sc)
         arrays = {k: getattr(sc, k) for k in INPUT_KEYS}
         if sc.path_clip is not None:
             arrays.update({k: getattr(sc, k) for k in CLIP_KEYS})
+        if sc.path_stroke is not None:
+            arrays.update({k: getattr(sc, k) for k in STROKE_KEYS})
+            outline = oracle.stroke_scene(sc, reference=True)
+            arrays.update({"out_" + k: getattr(outline, k) for k in OUTLINE_KEYS})
         arrays["meta"] = np.asarray([sc.width, sc.height, sc.clear], np.float64)
         for k in CANON_KEYS:
             arrays["ref_" + k] = ref[k]

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import CANON_KEYS, GOLDEN, golden_names, load_golden
+from conftest import CANON_KEYS, GOLDEN, OUTLINE_KEYS, golden_names, load_golden
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -16,6 +16,45 @@ def test_restated_tiler_matches_reference_golden(oracle_mod, name):
     for k in CANON_KEYS:
         assert ours[k].shape == ref[k].shape, k
         assert np.array_equal(ours[k], ref[k]), k
+
+
+STROKED = [n for n in golden_names() if n.startswith("stroke_") or n.startswith("gen_stroked")]
+
+
+@pytest.mark.parametrize("name", STROKED)
+def test_restated_stroker_matches_reference_golden(oracle_mod, name):
+    """The restated OutlineDash + OutlineStrokeToFill against the reference's own output, bit for
+    bit (points compared as bit patterns)."""
+    sc, ref = load_golden(name)
+    ours = oracle_mod.stroke_scene(sc)
+    for k in OUTLINE_KEYS:
+        a, b = getattr(ours, k), ref["out_" + k]
+        assert a.shape == b.shape, k
+        assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), k
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13, 14])
+def test_restated_stroker_matches_live_reference(oracle_mod, seed):
+    import scenes as S
+    if not oracle_mod.have_reference():
+        pytest.skip("reference harness not built")
+    sc = S.stroked(seed=seed, n_paths=80, side=512, dash_share=0.5, fill_share=0.1)
+    a, b = oracle_mod.stroke_scene(sc), oracle_mod.stroke_scene(sc, reference=True)
+    for k in OUTLINE_KEYS:
+        assert np.array_equal(getattr(a, k).view(np.uint8), getattr(b, k).view(np.uint8)), k
+    assert oracle_mod.compare(oracle_mod.tile_scene(sc, oracle_mod.Z_D3D9), oracle_mod.reference_tile_scene(sc)) == []
+
+
+def test_stroke_layout_checks(oracle_mod):
+    import scenes as S
+    sc = S.stroked(seed=3, n_paths=6, side=128, dash_share=1.0)
+    bad = S.Scene(**{**sc.__dict__, "dashes": np.zeros_like(sc.dashes)})  # patterns of total 0
+    with pytest.raises(RuntimeError):
+        oracle_mod.stroke_scene(bad)
+    st = sc.path_stroke.copy()
+    st["line_cap"][0] = 7
+    with pytest.raises(RuntimeError):
+        oracle_mod.stroke_scene(S.Scene(**{**sc.__dict__, "path_stroke": st}))
 
 
 def _digest(a):
