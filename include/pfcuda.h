@@ -320,6 +320,21 @@ int pf_read_images(void *ctx, uint8_t *dst, size_t capacity_bytes);
  * render on this context). */
 int pf_image_device_ptr(void *ctx, void **rgba, uint32_t *width_px, uint32_t *height_px);
 
+/*
+ * The fill outline of an uploaded scene, as the frames tile it: stroked paths replaced by
+ * their stroke outlines (OutlineDash + OutlineStrokeToFill), other paths as uploaded.  Host
+ * arrays owned by the context, valid until the next call on it (synchronises).
+ */
+typedef struct pf_outline {
+    uint32_t n_points, n_contours, n_paths;
+    const float *points;            /* [n_points][2] */
+    const uint8_t *point_flags;     /* [n_points] */
+    const uint32_t *contour_start;  /* [n_contours + 1] */
+    const uint32_t *path_start;     /* [n_paths + 1] */
+    const uint8_t *fill_rule;       /* [n_paths] (stroke outlines: PF_FILL_NONZERO) */
+} pf_outline;
+int pf_read_outline(void *ctx, uint32_t scene, pf_outline *out);
+
 /* Canonical integer output of the last rendered scene (synchronises). */
 int pf_read_canon(void *ctx, pf_canon *out);
 int pf_read_canon_scene(void *ctx, uint32_t scene, pf_canon *out);

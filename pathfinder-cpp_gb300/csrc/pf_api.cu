@@ -83,6 +83,10 @@ struct Ctx {
     DevBuf path_clip, path_is_clip, path_clip_rel;
     std::vector<uint32_t> h_path_clip;
     std::vector<uint8_t> h_path_is_clip;
+    // stroked paths: the uploaded outline and what the upload's stroke pass works in
+    DevBuf in_points, in_pflags, in_cstart, in_pstart, st_stroke, st_closed, st_dashes, st_scenes, st_cfirst;
+    DevBuf dash_pts, dash_cnt, dash_end, dash_points, dash_flags, job_first, jobs, job_pts, st_bounds;
+    uint32_t stroke_jobs = 0, stroke_dash_points = 0;  // of the last upload with strokes
     uint32_t n_scenes = 0, n_paths = 0, n_contours = 0, n_points = 0, n_fb = 0;
     uint64_t image_bytes = 0;
     bool uploaded = false, rendered = false;
@@ -119,6 +123,11 @@ struct Ctx {
     uint32_t syncs = 0;
 
     HostCanon canon;
+    struct {
+        std::vector<float2> points;
+        std::vector<uint8_t> flags, rule;
+        std::vector<uint32_t> cstart, pstart;
+    } outline;  // pf_read_outline's arrays
     cudaEvent_t ev[8] = {};
 
     // The learned frame captured as a CUDA graph once it has run with its buffers sized: later
@@ -182,9 +191,32 @@ int validate_scene(Ctx *c, const pf_scene_view *s) {
     for (uint32_t k = 0; k < s->n_contours; k++)
         if (s->contour_start[k] > s->contour_start[k + 1])
             return fail(c, PF_ERR_INVALID_ARGUMENT, "contour_start must be non-decreasing");
-    for (uint32_t p = 0; s->path_stroke && p < s->n_paths; p++)
-        if (s->path_stroke[p].line_width != 0.0f)
-            return fail(c, PF_ERR_INVALID_ARGUMENT, "stroked paths are not supported by this build");
+    for (uint32_t p = 0; s->path_stroke && p < s->n_paths; p++) {
+        // StrokeStyle (core/stroke.h:14-27) and the canvas's dash pattern
+        const pf_stroke &st = s->path_stroke[p];
+        if (!(st.line_width >= 0.0f) || !std::isfinite(st.line_width) || !std::isfinite(st.miter_limit) ||
+            st.line_cap > PF_CAP_ROUND || st.line_join > PF_JOIN_ROUND)
+            return fail(c, PF_ERR_INVALID_ARGUMENT, "stroke styles need a finite width >= 0, a finite miter "
+                                                    "limit and a known cap and join");
+        if (st.line_width == 0.0f) continue;
+        for (uint32_t i = s->contour_start[s->path_start[p]]; i < s->contour_start[s->path_start[p + 1]]; i++)
+            if (!std::isfinite(s->points[2 * i]) || !std::isfinite(s->points[2 * i + 1]))
+                return fail(c, PF_ERR_INVALID_ARGUMENT, "a stroked path has a non-finite point");
+        if (st.dash_count) {
+            if (!s->dashes || uint64_t(st.dash_first) + st.dash_count > s->n_dashes)
+                return fail(c, PF_ERR_INVALID_ARGUMENT, "a dash pattern lies outside the dashes array");
+            float total = 0.0f;
+            for (uint32_t i = 0; i < st.dash_count; i++) {
+                const float d = s->dashes[st.dash_first + i];
+                if (!(d >= 0.0f) || !std::isfinite(d))
+                    return fail(c, PF_ERR_INVALID_ARGUMENT, "dash lengths must be finite and >= 0");
+                total += d;
+            }
+            // an all-zero pattern never advances (the reference loops forever on it)
+            if (!(total > 0.0f) || !std::isfinite(total) || !std::isfinite(st.dash_offset))
+                return fail(c, PF_ERR_INVALID_ARGUMENT, "a dash pattern needs a finite positive total and phase");
+        }
+    }
     if (s->path_clip || s->path_is_clip) {
         // Scene::push_draw_path / push_clip_path: clip paths come after every draw path, are not
         // clipped themselves, and a draw path names a clip path or none
@@ -233,6 +265,160 @@ struct CopyPlan {
         return cudaSuccess;
     }
 };
+
+template <class T>
+int d2h_wait(Ctx *c, T *host, const void *dev, size_t count) {
+    PF_CUDA(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+// Stroke-to-fill and dashing of the uploaded scenes (pf_stroke.cu): reads the outline staged
+// in the in_* buffers with the input layout in c->h_scenes, writes the fill outline into the
+// buffers the frames read and rewrites the scene table for it.  scf: the input's first contour
+// per scene.
+int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::vector<uint32_t> &scf) {
+    cudaStream_t st = c->stream;
+    const uint32_t N = c->n_paths, C = c->n_contours;
+    std::vector<pf_stroke> hs(N);
+    std::vector<uint8_t> hc(C, 0);
+    std::vector<float> hd;
+    bool dashed = false;
+    std::memset(hs.data(), 0, hs.size() * sizeof(pf_stroke));
+    for (uint32_t i = 0; i < n; i++) {
+        const pf_scene_view &s = scenes[i];
+        const SceneDev &S = c->h_scenes[i];
+        const uint32_t base = (uint32_t)hd.size();
+        if (s.path_stroke)
+            for (uint32_t p = 0; p < s.n_paths; p++) {
+                pf_stroke x = s.path_stroke[p];
+                if (!(x.line_width > 0.0f)) x.dash_count = 0;
+                x.dash_first += base;
+                dashed |= x.line_width > 0.0f && x.dash_count != 0;
+                hs[S.path_first + p] = x;
+            }
+        if (s.dashes && s.n_dashes) hd.insert(hd.end(), s.dashes, s.dashes + s.n_dashes);
+        if (s.contour_closed && s.n_contours) std::memcpy(hc.data() + S.contour_first, s.contour_closed, s.n_contours);
+    }
+    if (hd.empty()) hd.push_back(0.0f);
+    PF_CUDA(c->st_stroke.ensure(size_t(N) * sizeof(pf_stroke) + 16));
+    PF_CUDA(c->st_closed.ensure(size_t(C) + 16));
+    PF_CUDA(c->st_dashes.ensure(hd.size() * 4));
+    PF_CUDA(c->st_scenes.ensure(size_t(n) * sizeof(SceneDev)));
+    PF_CUDA(c->st_cfirst.ensure((size_t(n) + 1) * 4));
+    PF_CUDA(cudaMemcpyAsync(c->st_stroke.p, hs.data(), size_t(N) * sizeof(pf_stroke), cudaMemcpyHostToDevice, st));
+    PF_CUDA(cudaMemcpyAsync(c->st_closed.p, hc.data(), C, cudaMemcpyHostToDevice, st));
+    PF_CUDA(cudaMemcpyAsync(c->st_dashes.p, hd.data(), hd.size() * 4, cudaMemcpyHostToDevice, st));
+    PF_CUDA(cudaMemcpyAsync(c->st_scenes.p, c->h_scenes.data(), size_t(n) * sizeof(SceneDev), cudaMemcpyHostToDevice, st));
+    PF_CUDA(cudaMemcpyAsync(c->st_cfirst.p, scf.data(), (size_t(n) + 1) * 4, cudaMemcpyHostToDevice, st));
+    PF_CUDA(c->status.ensure(kStCount * 4));
+    PF_CUDA(cudaMemsetAsync(c->status.p, 0, kStCount * 4, st));
+    uint32_t *status = c->status.as<uint32_t>();
+
+    StrokeIn in{};
+    in.n_paths = N;
+    in.n_scenes = n;
+    in.scenes = c->st_scenes.as<SceneDev>();
+    in.scene_path_first = c->scene_path_first.as<uint32_t>();
+    in.scene_contour_first = c->st_cfirst.as<uint32_t>();
+    in.cstart = c->in_cstart.as<uint32_t>();
+    in.pstart = c->in_pstart.as<uint32_t>();
+    in.points = c->in_points.as<float2>();
+    in.flags = c->in_pflags.as<uint8_t>();
+    in.closed = c->st_closed.as<uint8_t>();
+    in.stroke = c->st_stroke.as<pf_stroke>();
+    in.dashes = c->st_dashes.as<float>();
+    PF_CUDA(c->dash_pts.ensure((size_t(N) + 1) * 4));
+    PF_CUDA(c->dash_cnt.ensure((size_t(N) + 1) * 4));
+    PF_CUDA(c->job_first.ensure((size_t(N) + 1) * 4));
+    in.dash_pts = c->dash_pts.as<uint32_t>();
+    in.dash_cnt = c->dash_cnt.as<uint32_t>();
+    in.job_first = c->job_first.as<uint32_t>();
+    PF_CUDA(c->scan_temp.ensure(scan_temp_bytes(N + 1)));
+
+    // dashing: counts, offsets, the dashed contours
+    if (dashed) {
+        PF_CUDA(launch_dash(in, false, status, st));
+        PF_CUDA(scan_exclusive_u32(in.dash_pts, in.dash_pts, N, in.dash_pts + N, c->scan_temp.p, st, status));
+        PF_CUDA(scan_exclusive_u32(in.dash_cnt, in.dash_cnt, N, in.dash_cnt + N, c->scan_temp.p, st, status));
+        uint32_t tot[3];
+        uint64_t wide = 0;  // the 64-bit total of the dash points (slots 16-17)
+        PF_CUDA(cudaMemcpyAsync(&tot[0], in.dash_pts + N, 4, cudaMemcpyDeviceToHost, st));
+        PF_CUDA(cudaMemcpyAsync(&tot[1], in.dash_cnt + N, 4, cudaMemcpyDeviceToHost, st));
+        PF_CUDA(cudaMemcpyAsync(&wide, status + kStFill64, 8, cudaMemcpyDeviceToHost, st));
+        if (int e = d2h_wait(c, &tot[2], status + kStErr, 1)) return e;
+        if (tot[2] & kErrStroke)
+            return fail(c, PF_ERR_KERNEL_LIMIT, "a dash pattern needs more than 2^22 steps on one path");
+        if (tot[2]) return fail(c, PF_ERR_CUDA, "dash pass failed");
+        if (wide >= (1ull << 31)) return fail(c, PF_ERR_OVERFLOW, "dashed outline too large (2^31 points)");
+        c->stroke_dash_points = tot[0];
+        PF_CUDA(c->dash_points.ensure(size_t(tot[0]) * 8 + 16));
+        PF_CUDA(c->dash_flags.ensure(size_t(tot[0]) + 16));
+        PF_CUDA(c->dash_end.ensure(size_t(tot[1]) * 4 + 16));
+        in.dash_points = c->dash_points.as<float2>();
+        in.dash_flags = c->dash_flags.as<uint8_t>();
+        in.dash_end = c->dash_end.as<uint32_t>();
+        PF_CUDA(launch_dash(in, true, status, st));
+    }
+    // one job per output contour
+    PF_CUDA(launch_stroke_jobs(in, false, st));
+    PF_CUDA(scan_exclusive_u32(in.job_first, in.job_first, N, in.job_first + N, c->scan_temp.p, st, status));
+    uint32_t J = 0;
+    if (int e = d2h_wait(c, &J, in.job_first + N, 1)) return e;
+    if (J >= (1u << 31)) return fail(c, PF_ERR_OVERFLOW, "stroked outline too large (2^31 contours)");
+    PF_CUDA(c->jobs.ensure(size_t(J) * 16 + 16));
+    PF_CUDA(c->job_pts.ensure((size_t(J) + 1) * 4));
+    PF_CUDA(c->scan_temp.ensure(scan_temp_bytes(J + 1)));
+    in.n_jobs = J;
+    in.jobs = c->jobs.as<uint4>();
+    in.job_pts = c->job_pts.as<uint32_t>();
+    c->stroke_jobs = J;
+    PF_CUDA(launch_stroke_jobs(in, true, st));
+    PF_CUDA(launch_stroke(in, false, status, st));
+    PF_CUDA(scan_exclusive_u32(in.job_pts, in.job_pts, J, in.job_pts + J, c->scan_temp.p, st, status));
+    uint32_t tot[2];
+    uint64_t wide = 0;  // the 64-bit total of the output points (slots 18-19)
+    PF_CUDA(cudaMemcpyAsync(&tot[0], in.job_pts + J, 4, cudaMemcpyDeviceToHost, st));
+    PF_CUDA(cudaMemcpyAsync(&wide, status + kStFill64 + 2, 8, cudaMemcpyDeviceToHost, st));
+    if (int e = d2h_wait(c, &tot[1], status + kStErr, 1)) return e;
+    if (wide >= (1ull << 31)) return fail(c, PF_ERR_OVERFLOW, "stroked outline too large (2^31 points)");
+    if (tot[1] & kErrStroke)
+        return fail(c, PF_ERR_KERNEL_LIMIT, "stroking hit a limit (a dash pattern over 2^22 steps on one path, "
+                                            "or a cap searching back past 64 points)");
+    if (tot[1]) return fail(c, PF_ERR_CUDA, "stroke pass failed");
+    const uint32_t P = tot[0];
+    if (P >= (1u << 31)) return fail(c, PF_ERR_OVERFLOW, "stroked outline too large (2^31 points)");
+    PF_CUDA(c->points.ensure(size_t(P) * 8 + 16));
+    PF_CUDA(c->pflags.ensure(size_t(P) + 16));
+    in.out_points = c->points.as<float2>();
+    in.out_flags = c->pflags.as<uint8_t>();
+    in.n_out_points = P;
+    PF_CUDA(launch_stroke(in, true, status, st));
+    // the new layout: per scene its first contour and point
+    PF_CUDA(c->st_bounds.ensure((size_t(n) + 1) * 8));
+    PF_CUDA(launch_scene_bounds(in, c->st_bounds.as<uint32_t>(), st));
+    std::vector<uint32_t> bounds(2 * (size_t(n) + 1));
+    if (int e = d2h_wait(c, bounds.data(), c->st_bounds.p, bounds.size())) return e;
+    std::vector<uint32_t> ocf(n + 1);
+    for (uint32_t i = 0; i < n; i++) {
+        SceneDev &S = c->h_scenes[i];
+        S.contour_first = bounds[2 * i];
+        S.contour_end = bounds[2 * i + 2];
+        S.point_first = bounds[2 * i + 1];
+        S.point_end = bounds[2 * i + 3];
+        S.cstart_base = S.contour_first + i;
+        ocf[i] = S.contour_first;
+    }
+    ocf[n] = J;
+    c->n_points = P;
+    c->n_contours = J;
+    PF_CUDA(c->cstart.ensure((size_t(J) + n) * 4 + 16));
+    PF_CUDA(cudaMemcpyAsync(c->scenes.p, c->h_scenes.data(), size_t(n) * sizeof(SceneDev), cudaMemcpyHostToDevice, st));
+    PF_CUDA(cudaMemcpyAsync(c->scene_contour_first.p, ocf.data(), (size_t(n) + 1) * 4, cudaMemcpyHostToDevice, st));
+    PF_CUDA(launch_outline_starts(in, c->scenes.as<SceneDev>(), c->cstart.as<uint32_t>(), c->pstart.as<uint32_t>(),
+                                  st));
+    return PF_OK;
+}
 
 int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     if (!scenes || n == 0) return fail(c, PF_ERR_INVALID_ARGUMENT, "no scenes");
@@ -293,10 +479,22 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     c->n_fb = (uint32_t)fb;
     c->image_bytes = img;
 
-    PF_CUDA(c->points.ensure(P * 8 + 16));
-    PF_CUDA(c->pflags.ensure(P + 16));
-    PF_CUDA(c->cstart.ensure(cs * 4 + 16));
+    bool strokes = false;
+    for (uint32_t i = 0; i < n && !strokes; i++)
+        for (uint32_t p = 0; scenes[i].path_stroke && p < scenes[i].n_paths; p++)
+            if (scenes[i].path_stroke[p].line_width > 0.0f) {
+                strokes = true;
+                break;
+            }
+    // With stroked paths the uploaded outline lands in the in_* buffers and the stroke pass
+    // writes the outline the frames read.
+    DevBuf &d_points = strokes ? c->in_points : c->points, &d_pflags = strokes ? c->in_pflags : c->pflags;
+    DevBuf &d_cstart = strokes ? c->in_cstart : c->cstart;
+    PF_CUDA(d_points.ensure(P * 8 + 16));
+    PF_CUDA(d_pflags.ensure(P + 16));
+    PF_CUDA(d_cstart.ensure(cs * 4 + 16));
     PF_CUDA(c->pstart.ensure(ps * 4 + 16));
+    if (strokes) PF_CUDA(c->in_pstart.ensure(ps * 4 + 16));
     PF_CUDA(c->fill_rule.ensure(N + 16));
     PF_CUDA(c->color.ensure(N * 4 + 16));
     PF_CUDA(c->scenes.ensure(n * sizeof(SceneDev)));
@@ -325,26 +523,48 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
         PF_CUDA(cudaMemcpyAsync(c->path_is_clip.p, c->h_path_is_clip.data(), N, cudaMemcpyHostToDevice, c->stream));
     }
 
+    // stroke outlines are filled nonzero (Canvas::stroke_path)
+    std::vector<uint8_t> rules;
+    if (strokes) {
+        rules.resize(N);
+        for (uint32_t i = 0; i < n; i++) {
+            const pf_scene_view &s = scenes[i];
+            for (uint32_t p = 0; p < s.n_paths; p++)
+                rules[c->h_scenes[i].path_first + p] =
+                    s.path_stroke && s.path_stroke[p].line_width > 0.0f ? uint8_t(PF_FILL_NONZERO) : s.fill_rule[p];
+        }
+    }
+    DevBuf &d_pstart = strokes ? c->in_pstart : c->pstart;
     CopyPlan pts, fl, csp, psp, fr, col;
     for (uint32_t i = 0; i < n; i++) {
         const pf_scene_view &s = scenes[i];
         const SceneDev &S = c->h_scenes[i];
-        pts.add(c->points.as<char>() + uint64_t(S.point_first) * 8, s.points, uint64_t(s.n_points) * 8);
-        fl.add(c->pflags.as<char>() + S.point_first, s.point_flags, s.n_points);
-        csp.add(c->cstart.as<char>() + uint64_t(S.cstart_base) * 4, s.contour_start, uint64_t(s.n_contours + 1) * 4);
-        psp.add(c->pstart.as<char>() + uint64_t(S.pstart_base) * 4, s.path_start, uint64_t(s.n_paths + 1) * 4);
-        fr.add(c->fill_rule.as<char>() + S.path_first, s.fill_rule, s.n_paths);
+        pts.add(d_points.as<char>() + uint64_t(S.point_first) * 8, s.points, uint64_t(s.n_points) * 8);
+        fl.add(d_pflags.as<char>() + S.point_first, s.point_flags, s.n_points);
+        csp.add(d_cstart.as<char>() + uint64_t(S.cstart_base) * 4, s.contour_start, uint64_t(s.n_contours + 1) * 4);
+        psp.add(d_pstart.as<char>() + uint64_t(S.pstart_base) * 4, s.path_start, uint64_t(s.n_paths + 1) * 4);
+        fr.add(c->fill_rule.as<char>() + S.path_first, strokes ? rules.data() + S.path_first : s.fill_rule,
+               s.n_paths);
         col.add(c->color.as<char>() + uint64_t(S.path_first) * 4, s.color, uint64_t(s.n_paths) * 4);
     }
     for (CopyPlan *cp : {&pts, &fl, &csp, &psp, &fr, &col}) PF_CUDA(cp->run(c->stream));
-    PF_CUDA(cudaMemcpyAsync(c->scenes.p, c->h_scenes.data(), n * sizeof(SceneDev), cudaMemcpyHostToDevice,
-                            c->stream));
     PF_CUDA(cudaMemcpyAsync(c->scene_path_first.p, spf.data(), (n + 1) * 4, cudaMemcpyHostToDevice, c->stream));
-    PF_CUDA(cudaMemcpyAsync(c->scene_contour_first.p, scf.data(), (n + 1) * 4, cudaMemcpyHostToDevice, c->stream));
     PF_CUDA(cudaMemcpyAsync(c->scene_fb_first.p, c->h_scene_fb_first.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
                             c->stream));
     PF_CUDA(cudaMemcpyAsync(c->scene_row_first.p, c->h_scene_row_first.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
                             c->stream));
+    if (strokes) {
+        if (int e = stroke_upload(c, scenes, n, scf)) {
+            cudaStreamSynchronize(c->stream);
+            c->uploaded = false;
+            return e;
+        }
+    } else {
+        PF_CUDA(cudaMemcpyAsync(c->scenes.p, c->h_scenes.data(), n * sizeof(SceneDev), cudaMemcpyHostToDevice,
+                                c->stream));
+        PF_CUDA(cudaMemcpyAsync(c->scene_contour_first.p, scf.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
+                                c->stream));
+    }
     // the host arrays are borrowed only for this call
     PF_CUDA(cudaStreamSynchronize(c->stream));
     c->uploaded = true;
@@ -1189,7 +1409,10 @@ int pf_ctx_destroy(void *ctx) {
                       &c->pool_idx, &c->tile_fills, &c->path_fill, &c->path_cls, &c->tile_state, &c->col_above,
                       &c->col_final, &c->fills, &c->bin_stage, &c->row_first,
                       &c->row_paths, &c->scene_row_first, &c->z, &c->fb_count, &c->list, &c->image,
-                      &c->status, &c->scan_temp, &c->path_clip, &c->path_is_clip, &c->path_clip_rel};
+                      &c->status, &c->scan_temp, &c->path_clip, &c->path_is_clip, &c->path_clip_rel,
+                      &c->in_points, &c->in_pflags, &c->in_cstart, &c->in_pstart, &c->st_stroke, &c->st_closed,
+                      &c->st_dashes, &c->st_scenes, &c->st_cfirst, &c->dash_pts, &c->dash_cnt, &c->dash_end,
+                      &c->dash_points, &c->dash_flags, &c->job_first, &c->jobs, &c->job_pts, &c->st_bounds};
     for (DevBuf *b : bufs) b->release();
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -1258,6 +1481,32 @@ int pf_read_canon(void *ctx, pf_canon *out) {
     Ctx *c = as_ctx(ctx);
     if (!c || !out) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
     return read_canon(c, 0, out);
+}
+
+int pf_read_outline(void *ctx, uint32_t scene, pf_outline *out) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !out) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
+    if (scene >= c->n_scenes) return fail(c, PF_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const SceneDev &S = c->h_scenes[scene];
+    const uint32_t np = S.path_end - S.path_first, nc = S.contour_end - S.contour_first,
+                   npt = S.point_end - S.point_first;
+    auto &o = c->outline;
+    if (int e = d2h(c, o.points, c->points.as<float2>() + S.point_first, npt)) return e;
+    if (int e = d2h(c, o.flags, c->pflags.as<uint8_t>() + S.point_first, npt)) return e;
+    if (int e = d2h(c, o.cstart, c->cstart.as<uint32_t>() + S.cstart_base, size_t(nc) + 1)) return e;
+    if (int e = d2h(c, o.pstart, c->pstart.as<uint32_t>() + S.pstart_base, size_t(np) + 1)) return e;
+    if (int e = d2h(c, o.rule, c->fill_rule.as<uint8_t>() + S.path_first, np)) return e;
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    out->n_points = npt;
+    out->n_contours = nc;
+    out->n_paths = np;
+    out->points = reinterpret_cast<const float *>(o.points.data());
+    out->point_flags = o.flags.data();
+    out->contour_start = o.cstart.data();
+    out->path_start = o.pstart.data();
+    out->fill_rule = o.rule.data();
+    return PF_OK;
 }
 
 int pf_read_canon_scene(void *ctx, uint32_t scene, pf_canon *out) {

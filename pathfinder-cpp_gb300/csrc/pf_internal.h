@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "pfcuda.h"
+
 namespace pfc {
 
 constexpr int kTile = 16;
@@ -28,6 +30,7 @@ enum : uint32_t {
     kErrClip = 1u << 2,     // Cohen-Sutherland clipping did not settle
     kErrNonFinite = 1u << 3,// a point is NaN or infinite
     kErrScanWait = 1u << 4, // a scan's look-back wait hit its bound
+    kErrStroke = 1u << 5,   // a dash pattern ran past its step bound or a cap search past its ring
     kErrOverflowSeg = 1u << 8,
     kErrOverflowLeaf = 1u << 9,
     kErrOverflowFill = 1u << 10,
@@ -191,6 +194,37 @@ void count_launches(uint32_t n);
 size_t scan_temp_bytes(uint32_t n);
 cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t *total, void *temp,
                                cudaStream_t st, uint32_t *err);
+
+// Stroke-to-fill and dashing at upload (pf_stroke.cu).  Inputs: the uploaded outline in the
+// upload's per-scene layout; outputs: the dashed contours, one job per output contour, and the
+// new outline.
+struct StrokeIn {
+    uint32_t n_paths, n_scenes, n_jobs, n_out_points;
+    const SceneDev *scenes;             // the input layout's scene table
+    const uint32_t *scene_path_first;   // [n_scenes + 1]
+    const uint32_t *scene_contour_first;
+    const uint32_t *cstart, *pstart;    // scene-local offset arrays
+    const float2 *points;
+    const uint8_t *flags;
+    const uint8_t *closed;              // [contours] or null
+    const pf_stroke *stroke;            // [n_paths] (dash_first rebased into dashes)
+    const float *dashes;
+    uint32_t *dash_pts, *dash_cnt;      // [n_paths + 1] counts -> scanned
+    uint32_t *dash_end;                 // [dash contours] one past each contour's last point
+    float2 *dash_points;
+    uint8_t *dash_flags;
+    uint32_t *job_first;                // [n_paths + 1] counts -> scanned
+    uint4 *jobs;                        // [n_jobs]
+    uint32_t *job_pts;                  // [n_jobs + 1] counts -> scanned
+    float2 *out_points;
+    uint8_t *out_flags;
+};
+cudaError_t launch_dash(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);
+cudaError_t launch_stroke_jobs(const StrokeIn &in, bool fill, cudaStream_t st);
+cudaError_t launch_stroke(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);
+cudaError_t launch_outline_starts(const StrokeIn &in, const SceneDev *out_scenes, uint32_t *cstart,
+                                  uint32_t *pstart, cudaStream_t st);
+cudaError_t launch_scene_bounds(const StrokeIn &in, uint32_t *out, cudaStream_t st);
 
 // Stage launchers (all asynchronous on the given stream).
 cudaError_t launch_normalize(const Batch &b, uint2 *path_contours, cudaStream_t st);

@@ -30,7 +30,7 @@ EXPORTS = [
     "pf_sizer_init", "pf_sizer_set_params", "pf_sizer_get_params", "pf_sizer_set_margin", "pf_sizer_predict",
     "pf_sizer_gradient", "pf_sizer_train", "pf_sizer_save", "pf_sizer_load", "pf_path_features", "pf_path_counts",
     "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags", "pf_sizer_predict_noalloc",
-    "pf_set_host_image",
+    "pf_set_host_image", "pf_read_outline",
 ]
 
 N_FEATURES = 12
@@ -84,6 +84,14 @@ class Canon(C.Structure):
         ("fb_tiles_x", C.c_uint32), ("fb_tiles_y", C.c_uint32), ("z", C.c_void_p),
         ("fb_list_first", C.c_void_p), ("n_list", C.c_uint64), ("fb_list", C.c_void_p),
         ("tile_mask", C.c_void_p), ("tile_clip", C.c_void_p), ("tile_dest_backdrop", C.c_void_p),
+    ]
+
+
+class OutlineOut(C.Structure):
+    _fields_ = [
+        ("n_points", C.c_uint32), ("n_contours", C.c_uint32), ("n_paths", C.c_uint32),
+        ("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_start", C.c_void_p),
+        ("path_start", C.c_void_p), ("fill_rule", C.c_void_p),
     ]
 
 
@@ -214,6 +222,18 @@ class Renderer:
         self._check(self.lib.pf_read_image_scene(self.ctx, scene, C.c_void_p(out.ctypes.data), out.nbytes),
                     self.ctx)
         return out
+
+    def outline(self, scene: int = 0) -> Dict[str, np.ndarray]:
+        """The scene's fill outline as the frames tile it (strokes converted)."""
+        r = OutlineOut()
+        self._check(self.lib.pf_read_outline(self.ctx, scene, C.byref(r)), self.ctx)
+        return {
+            "points": _arr(r.points, 2 * r.n_points, np.float32).reshape(-1, 2),
+            "flags": _arr(r.point_flags, r.n_points, np.uint8),
+            "contour_start": _arr(r.contour_start, r.n_contours + 1, np.uint32),
+            "path_start": _arr(r.path_start, r.n_paths + 1, np.uint32),
+            "fill_rule": _arr(r.fill_rule, r.n_paths, np.uint8),
+        }
 
     def canon(self, scene: int = 0) -> Dict[str, np.ndarray]:
         r = Canon()
