@@ -62,6 +62,9 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--scenes", type=int, default=512)
     ap.add_argument("--cpu-sample-every", type=int, default=32)
+    ap.add_argument("--strokes", action="store_true",
+                    help="the batched scenes as stroked paths (scenes.batched_stroked: 30%% dashed); the upload "
+                         "strokes them on the GPU, and the line reports that stage too")
     ap.add_argument("--clips", type=int, default=0,
                     help="clip paths per scene (0: none): the batched scenes with that many clip shapes "
                          "each, 60%% of the draw paths clipped")
@@ -74,15 +77,22 @@ def parse_args():
 
 def make_scenes(args, first_seed):
     import scenes as S
+    if args.strokes:
+        return S.batched_stroked(n_scenes=args.scenes, first_seed=first_seed)
     if args.clips > 0:
         return S.batched_clipped(n_scenes=args.scenes, first_seed=first_seed, n_clips=args.clips)
     return S.batched(n_scenes=args.scenes, first_seed=first_seed)
 
 
-def workload_config(n_scenes, scenes_list, clips=0):
+def workload_config(n_scenes, scenes_list, clips=0, strokes=False):
     import numpy as np
     desc = ("batched: %d scenes, paths/scene log-uniform 16-4096 (cubic 8-24 seg, control points "
             "uniform over the canvas), canvas side in {256,512,1024,2048}, seeds 1000+i" % n_scenes)
+    if strokes:
+        desc = ("batched stroked: %d scenes, paths/scene log-uniform 16-4096, canvas side in "
+                "{256,512,1024,2048}, seeds 1000+i; every path stroked (1-3 contours of 1-12 line/quad/cubic "
+                "segments in a log-uniform box, 40%% closed, width 0.5-24 px, caps/joins uniform), 30%% "
+                "dashed" % n_scenes)
     if clips:
         desc += "; %d clip paths per scene (cubic 3-8 seg, a quarter to a whole canvas wide), 60%% of the " \
                 "draw paths clipped" % clips
@@ -156,34 +166,45 @@ def pack_pinned(scenes_list):
     import numpy as np
     import torch
     import pfcuda
-    keys = [("points", np.float32, 8), ("flags", np.uint8, 1), ("contour_start", np.uint32, 4),
-            ("path_start", np.uint32, 4), ("fill_rule", np.uint8, 1), ("color", np.uint32, 4)]
-    if any(getattr(s, "path_clip", None) is not None for s in scenes_list):
-        keys += [("path_clip", np.uint32, 4), ("path_is_clip", np.uint8, 1)]
+    import scenes as S
+    keys = [("points", np.float32), ("flags", np.uint8), ("contour_start", np.uint32),
+            ("path_start", np.uint32), ("fill_rule", np.uint8), ("color", np.uint32)]
+    has = lambda k: any(getattr(s, k, None) is not None for s in scenes_list)  # noqa: E731
+    if has("path_clip"):
+        keys += [("path_clip", np.uint32), ("path_is_clip", np.uint8)]
+    if has("path_stroke"):
+        keys += [("path_stroke", S.STROKE_DTYPE), ("contour_closed", np.uint8), ("dashes", np.float32)]
+
     def field(s, k):
         a = getattr(s, k)
-        if a is None:  # a scene without clip paths in a batch with some
-            a = np.full(s.n_paths, 0xFFFFFFFF, np.uint32) if k == "path_clip" else np.zeros(s.n_paths, np.uint8)
+        if a is None:  # a scene without clips or strokes in a batch with some
+            defaults = {"path_clip": np.full(s.n_paths, 0xFFFFFFFF, np.uint32),
+                        "path_stroke": np.zeros(s.n_paths, S.STROKE_DTYPE),
+                        "contour_closed": np.zeros(s.n_contours, np.uint8), "dashes": np.zeros(0, np.float32)}
+            a = defaults.get(k, np.zeros(s.n_paths, np.uint8))
         return a
 
     bufs = {}
-    for k, dt, _ in keys:
+    for k, dt in keys:
         total = sum(field(s, k).nbytes for s in scenes_list)
-        t = torch.empty(max(total, 16), dtype=torch.uint8, pin_memory=True)
-        bufs[k] = t
-    offs = {k: 0 for k, _, _ in keys}
+        bufs[k] = torch.empty(max(total, 16), dtype=torch.uint8, pin_memory=True)
+    offs = {k: 0 for k, _ in keys}
     views = []
     for s in scenes_list:
-        ptrs = []
-        for k, dt, _ in keys:
+        ptrs = {}
+        for k, dt in keys:
             a = np.ascontiguousarray(field(s, k), dt)
             dst = bufs[k].numpy()[offs[k]:offs[k] + a.nbytes]
             dst[:] = a.view(np.uint8).reshape(-1)
-            ptrs.append(bufs[k].data_ptr() + offs[k])
+            ptrs[k] = bufs[k].data_ptr() + offs[k]
             offs[k] += a.nbytes
-        v = pfcuda.SceneView(*ptrs[:6], s.n_points, s.n_contours, s.n_paths, s.width, s.height, s.clear)
-        if len(ptrs) > 6:
-            v.path_clip, v.path_is_clip = ptrs[6], ptrs[7]
+        v = pfcuda.SceneView(*(ptrs[k] for k, _ in keys[:6]), s.n_points, s.n_contours, s.n_paths,
+                             s.width, s.height, s.clear)
+        if "path_clip" in ptrs:
+            v.path_clip, v.path_is_clip = ptrs["path_clip"], ptrs["path_is_clip"]
+        if "path_stroke" in ptrs:
+            v.path_stroke, v.contour_closed, v.dashes = ptrs["path_stroke"], ptrs["contour_closed"], ptrs["dashes"]
+            v.n_dashes = len(field(s, "dashes"))
         views.append(v)
     h2d = sum(offs.values())
     return bufs, views, h2d
@@ -223,7 +244,7 @@ def run_reference(args, scenes_list):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 tiling, f64 coverage",
-        "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list, args.clips),
+        "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list, args.clips, args.strokes),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -357,6 +378,59 @@ def main():
             peak = float(json.load(f)["hbm_gbs"])
         peak_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
 
+    # the stroke pass of the upload (--strokes): uploads from pinned host memory, timed on the
+    # host clock (H2D copies, dashing, stroking and the pass's three synchronisations), and
+    # the dash / stroke kernels' device time from the library's events
+    stroke_stage = None
+    if args.strokes:
+        ups, ust = [], []
+        for _ in range(args.warmup):
+            r.upload_views(views)
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r.upload_views(views)
+            ups.append((time.perf_counter() - t0) * 1e3)
+            ust.append(r.upload_stats())
+        us = ust[-1]
+        ms_dash = sum(x["ms_dash"] for x in ust) / len(ust)
+        ms_stroke = sum(x["ms_stroke"] for x in ust) / len(ust)
+        stroked_in = 0
+        for sc in scenes_list:
+            w = sc.path_stroke["line_width"] > 0
+            plain = w & (sc.path_stroke["dash_count"] == 0)
+            pts_per_path = np.diff(sc.contour_start.astype(np.int64)[sc.path_start.astype(np.int64)])
+            stroked_in += int(pts_per_path[plain].sum())
+        stroked_in += us["dash_points"]
+        # each pass (count, write) reads every stroked input point twice (forward and backward
+        # offsets; 8 B + 1 B flag) and the write pass stores every outline point (9 B)
+        s_bytes = 2 * 2 * 9 * stroked_in + 9 * us["n_points"]
+        s_ach = s_bytes / (ms_stroke * 1e-3) / 1e9 if ms_stroke > 0 else None
+        stroke_stage = {
+            "upload_ms": sum(ups) / len(ups), "ms_dash": ms_dash, "ms_stroke": ms_stroke,
+            "stroked_paths": us["stroked_paths"], "dashed_paths": us["dashed_paths"],
+            "dash_points": us["dash_points"], "stroke_input_points": stroked_in,
+            "outline_points": us["n_points"], "outline_contours": us["n_contours"],
+            "roofline": {"kernel": "k_stroke (count + write passes)", "bound": "hbm", "achieved": s_ach,
+                         "peak": peak, "unit": "GB/s", "frac": s_ach / peak if s_ach else None, "traffic": None,
+                         "algorithmic_bytes": s_bytes,
+                         "note": "compute bound: exact-IEEE offset curves (divisions, square roots, "
+                                 "tolerance samples) per leaf; bytes are the points read and written"},
+        }
+        if rank == 0 and not args.no_cpu_baseline:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import oracle
+            sample = scenes_list[::args.cpu_sample_every]
+            t0 = time.perf_counter()
+            for sc in sample:
+                oracle.stroke_scene(sc)
+            dt = time.perf_counter() - t0
+            stroke_stage["cpu_baseline"] = {
+                "value": len(sample) / dt, "unit": "scenes/s (stroke pass only)", "cores": 1, "kind": "port",
+                "sample": f"every {args.cpu_sample_every}th scene ({len(sample)} scenes, {dt:.2f} s): restated "
+                          f"OutlineDash + OutlineStrokeToFill, one thread"}
+            stroke_stage["gpu_scenes_per_s"] = n_scenes / ((ms_dash + ms_stroke) * 1e-3)
+
     # roofline of the dominant kernel: binning (k_bin_fused, the three CTA classes, with the
     # classification and the class-3 passes that run empty here), timed by the library's
     # stage events on the frame's stream over the timed steps.  Algorithmic bytes: every leaf
@@ -390,13 +464,14 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_batched, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (exact-IEEE tiling), int32 fixed-point coverage", "data": "synthetic",
-            "config": workload_config(n_scenes, scenes_list, args.clips) | {"parallelism": f"replicas x{world}"},
+            "config": workload_config(n_scenes, scenes_list, args.clips, args.strokes) | {"parallelism": f"replicas x{world}"},
             "frame": "batched learned one-pass" if learned else "batched exact two-pass",
             "batched_exact": {"value": world * n_scenes / (ms_exact * 1e-3), "unit": UNIT, "ms_per_step": ms_exact},
             "plain": {"value": world * n_scenes / (ms_plain * 1e-3), "unit": UNIT, "ms_per_step": ms_plain,
                       "gpu_launches_per_step": launches_plain[-1]},
             "speedup_vs_plain": ms_plain / ms_batched,
             "sizer": sizer,
+            **({"stroke_stage": stroke_stage} if stroke_stage else {}),
             "e2e": {"value": world * n_scenes / (ms_e2e * 1e-3), "unit": UNIT, "ms_per_step": ms_e2e,
                     "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": img_bytes,
                     "images": "composited into pinned host memory (pf_set_host_image)"},

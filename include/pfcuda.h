@@ -335,6 +335,18 @@ typedef struct pf_outline {
 } pf_outline;
 int pf_read_outline(void *ctx, uint32_t scene, pf_outline *out);
 
+/* What the last upload's stroke pass did (all zero when it had no stroked path).  The device
+ * times are taken when the context has PF_CONFIG_STAGE_TIMING. */
+typedef struct pf_upload_stats {
+    uint32_t n_points, n_contours;   /* the fill outline the frames tile (all scenes)   */
+    uint32_t stroked_paths, dashed_paths;
+    uint32_t stroke_contours;        /* output contours of the stroke pass (all paths)  */
+    uint32_t dash_points;            /* points of the dashed contours                   */
+    float ms_dash;                   /* device time of the dash kernels                 */
+    float ms_stroke;                 /* device time of the stroke kernels               */
+} pf_upload_stats;
+int pf_upload_stats_get(void *ctx, pf_upload_stats *out);
+
 /* Canonical integer output of the last rendered scene (synchronises). */
 int pf_read_canon(void *ctx, pf_canon *out);
 int pf_read_canon_scene(void *ctx, uint32_t scene, pf_canon *out);

@@ -87,6 +87,8 @@ struct Ctx {
     DevBuf in_points, in_pflags, in_cstart, in_pstart, st_stroke, st_closed, st_dashes, st_scenes, st_cfirst;
     DevBuf dash_pts, dash_cnt, dash_end, dash_points, dash_flags, job_first, jobs, job_pts, st_bounds;
     uint32_t stroke_jobs = 0, stroke_dash_points = 0;  // of the last upload with strokes
+    pf_upload_stats ustats{};
+    cudaEvent_t sev[8] = {};  // stroke pass timing (stage timing on)
     uint32_t n_scenes = 0, n_paths = 0, n_contours = 0, n_points = 0, n_fb = 0;
     uint64_t image_bytes = 0;
     bool uploaded = false, rendered = false;
@@ -314,6 +316,15 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
     PF_CUDA(c->status.ensure(kStCount * 4));
     PF_CUDA(cudaMemsetAsync(c->status.p, 0, kStCount * 4, st));
     uint32_t *status = c->status.as<uint32_t>();
+    const bool timing = (c->flags & PF_CONFIG_STAGE_TIMING) != 0;
+    if (timing && !c->sev[0])
+        for (auto &e : c->sev) PF_CUDA(cudaEventCreate(&e));
+    auto mark = [&](int i) -> cudaError_t { return timing ? cudaEventRecord(c->sev[i], st) : cudaSuccess; };
+    c->ustats = pf_upload_stats{};
+    for (uint32_t p = 0; p < N; p++) {
+        c->ustats.stroked_paths += hs[p].line_width > 0.0f;
+        c->ustats.dashed_paths += hs[p].line_width > 0.0f && hs[p].dash_count != 0;
+    }
 
     StrokeIn in{};
     in.n_paths = N;
@@ -338,11 +349,13 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
 
     // dashing: counts, offsets, the dashed contours
     if (dashed) {
+        PF_CUDA(mark(0));
         PF_CUDA(launch_dash(in, false, status, st));
         PF_CUDA(scan_exclusive_u32(in.dash_pts, in.dash_pts, N, in.dash_pts + N, c->scan_temp.p, st, status));
         PF_CUDA(scan_exclusive_u32(in.dash_cnt, in.dash_cnt, N, in.dash_cnt + N, c->scan_temp.p, st, status));
         uint32_t tot[3];
         uint64_t wide = 0;  // the 64-bit total of the dash points (slots 16-17)
+        PF_CUDA(mark(1));
         PF_CUDA(cudaMemcpyAsync(&tot[0], in.dash_pts + N, 4, cudaMemcpyDeviceToHost, st));
         PF_CUDA(cudaMemcpyAsync(&tot[1], in.dash_cnt + N, 4, cudaMemcpyDeviceToHost, st));
         PF_CUDA(cudaMemcpyAsync(&wide, status + kStFill64, 8, cudaMemcpyDeviceToHost, st));
@@ -358,7 +371,9 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
         in.dash_points = c->dash_points.as<float2>();
         in.dash_flags = c->dash_flags.as<uint8_t>();
         in.dash_end = c->dash_end.as<uint32_t>();
+        PF_CUDA(mark(2));
         PF_CUDA(launch_dash(in, true, status, st));
+        PF_CUDA(mark(3));
     }
     // one job per output contour
     PF_CUDA(launch_stroke_jobs(in, false, st));
@@ -373,11 +388,13 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
     in.jobs = c->jobs.as<uint4>();
     in.job_pts = c->job_pts.as<uint32_t>();
     c->stroke_jobs = J;
+    PF_CUDA(mark(4));
     PF_CUDA(launch_stroke_jobs(in, true, st));
     PF_CUDA(launch_stroke(in, false, status, st));
     PF_CUDA(scan_exclusive_u32(in.job_pts, in.job_pts, J, in.job_pts + J, c->scan_temp.p, st, status));
     uint32_t tot[2];
     uint64_t wide = 0;  // the 64-bit total of the output points (slots 18-19)
+    PF_CUDA(mark(5));
     PF_CUDA(cudaMemcpyAsync(&tot[0], in.job_pts + J, 4, cudaMemcpyDeviceToHost, st));
     PF_CUDA(cudaMemcpyAsync(&wide, status + kStFill64 + 2, 8, cudaMemcpyDeviceToHost, st));
     if (int e = d2h_wait(c, &tot[1], status + kStErr, 1)) return e;
@@ -393,7 +410,9 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
     in.out_points = c->points.as<float2>();
     in.out_flags = c->pflags.as<uint8_t>();
     in.n_out_points = P;
+    PF_CUDA(mark(6));
     PF_CUDA(launch_stroke(in, true, status, st));
+    PF_CUDA(mark(7));
     // the new layout: per scene its first contour and point
     PF_CUDA(c->st_bounds.ensure((size_t(n) + 1) * 8));
     PF_CUDA(launch_scene_bounds(in, c->st_bounds.as<uint32_t>(), st));
@@ -417,6 +436,20 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
     PF_CUDA(cudaMemcpyAsync(c->scene_contour_first.p, ocf.data(), (size_t(n) + 1) * 4, cudaMemcpyHostToDevice, st));
     PF_CUDA(launch_outline_starts(in, c->scenes.as<SceneDev>(), c->cstart.as<uint32_t>(), c->pstart.as<uint32_t>(),
                                   st));
+    c->ustats.stroke_contours = J;
+    c->ustats.dash_points = dashed ? c->stroke_dash_points : 0u;
+    if (timing) {  // every marked pair brackets work enqueued back to back (no host wait inside)
+        PF_CUDA(cudaStreamSynchronize(st));
+        float a = 0.0f, b = 0.0f;
+        if (dashed) {
+            PF_CUDA(cudaEventElapsedTime(&a, c->sev[0], c->sev[1]));
+            PF_CUDA(cudaEventElapsedTime(&b, c->sev[2], c->sev[3]));
+            c->ustats.ms_dash = a + b;
+        }
+        PF_CUDA(cudaEventElapsedTime(&a, c->sev[4], c->sev[5]));
+        PF_CUDA(cudaEventElapsedTime(&b, c->sev[6], c->sev[7]));
+        c->ustats.ms_stroke = a + b;
+    }
     return PF_OK;
 }
 
@@ -560,6 +593,7 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
             return e;
         }
     } else {
+        c->ustats = pf_upload_stats{};
         PF_CUDA(cudaMemcpyAsync(c->scenes.p, c->h_scenes.data(), n * sizeof(SceneDev), cudaMemcpyHostToDevice,
                                 c->stream));
         PF_CUDA(cudaMemcpyAsync(c->scene_contour_first.p, scf.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
@@ -1416,6 +1450,8 @@ int pf_ctx_destroy(void *ctx) {
     for (DevBuf *b : bufs) b->release();
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
+    for (auto &e : c->sev)
+        if (e) cudaEventDestroy(e);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1481,6 +1517,16 @@ int pf_read_canon(void *ctx, pf_canon *out) {
     Ctx *c = as_ctx(ctx);
     if (!c || !out) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
     return read_canon(c, 0, out);
+}
+
+int pf_upload_stats_get(void *ctx, pf_upload_stats *out) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !out) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
+    *out = c->ustats;
+    out->n_points = c->n_points;
+    out->n_contours = c->n_contours;
+    return PF_OK;
 }
 
 int pf_read_outline(void *ctx, uint32_t scene, pf_outline *out) {

@@ -30,7 +30,7 @@ EXPORTS = [
     "pf_sizer_init", "pf_sizer_set_params", "pf_sizer_get_params", "pf_sizer_set_margin", "pf_sizer_predict",
     "pf_sizer_gradient", "pf_sizer_train", "pf_sizer_save", "pf_sizer_load", "pf_path_features", "pf_path_counts",
     "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags", "pf_sizer_predict_noalloc",
-    "pf_set_host_image", "pf_read_outline",
+    "pf_set_host_image", "pf_read_outline", "pf_upload_stats_get",
 ]
 
 N_FEATURES = 12
@@ -93,6 +93,12 @@ class OutlineOut(C.Structure):
         ("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_start", C.c_void_p),
         ("path_start", C.c_void_p), ("fill_rule", C.c_void_p),
     ]
+
+
+class UploadStats(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("n_points", "n_contours", "stroked_paths", "dashed_paths",
+                                          "stroke_contours", "dash_points")] + \
+               [("ms_dash", C.c_float), ("ms_stroke", C.c_float)]
 
 
 class PfError(RuntimeError):
@@ -222,6 +228,12 @@ class Renderer:
         self._check(self.lib.pf_read_image_scene(self.ctx, scene, C.c_void_p(out.ctypes.data), out.nbytes),
                     self.ctx)
         return out
+
+    def upload_stats(self) -> Dict[str, float]:
+        """The last upload's stroke pass: outline sizes, stroked/dashed paths, device times."""
+        r = UploadStats()
+        self._check(self.lib.pf_upload_stats_get(self.ctx, C.byref(r)), self.ctx)
+        return {n: getattr(r, n) for n, _ in r._fields_}
 
     def outline(self, scene: int = 0) -> Dict[str, np.ndarray]:
         """The scene's fill outline as the frames tile it (strokes converted)."""

@@ -393,12 +393,12 @@ def batched_clipped(n_scenes: int = 512, first_seed: int = 1000, n_clips: int = 
 def stroked(seed: int = 0, n_paths: int = 200, side: int = 1024, dash_share: float = 0.3,
             fill_share: float = 0.0) -> Scene:
     """Stroked paths (Canvas::stroke_path): 1-3 contours each, a random walk of 1-12 segments
-    (lines, quadratic and cubic curves), 40 % of the contours closed; line width log-uniform
-    0.5-24 px; caps, joins and miter limits (1-12) uniform; dash_share of the paths dashed with
-    a 2- or 4-entry pattern of 1-40 px (a third of them with a phase); fill_share of the paths
-    filled instead.  Colours are translucent or opaque, nonzero rule."""
+    (lines, quadratic and cubic curves, points uniform in a log-uniform 16 px-to-canvas box),
+    40 % of the contours closed; line width log-uniform 0.5-24 px; caps, joins and miter limits
+    (1-12) uniform; dash_share of the paths dashed with a 2- or 4-entry pattern of 1-40 px (a
+    third of them with a phase); fill_share of the paths filled instead.  Colours translucent
+    (40 %) or opaque, nonzero rule."""
     rng = Rng(seed, 8)
-    pts, fl, cstart, pstart, closed = [], [], [0], [0], []
     n = n_paths
     n_contours = rng.integers(1, 3, n)
     width = _log_uniform(rng, 0.5, 24.0, n)
@@ -407,48 +407,72 @@ def stroked(seed: int = 0, n_paths: int = 200, side: int = 1024, dash_share: flo
     miter = 1.0 + 11.0 * rng.uniform(n)
     dashed = rng.uniform(n) < dash_share
     filled = rng.uniform(n) < fill_share
-    dashes: list = []
+    box = _log_uniform(rng, 16.0, float(side), n)
+    origin = rng.uniform(2 * n).reshape(n, 2) * (side - box)[:, None]
+    k_path = np.repeat(np.arange(n), n_contours)                  # path of each contour
+    nk = len(k_path)
+    nseg = rng.integers(1, 12, nk)
+    kinds = rng.integers(0, 2, int(nseg.sum()))                   # 0 line, 1 quadratic, 2 cubic
+    seg_contour = np.repeat(np.arange(nk), nseg)
+    per_contour = 1 + np.bincount(seg_contour, weights=kinds + 1, minlength=nk).astype(np.int64)
+    cstart = np.zeros(nk + 1, np.int64)
+    np.cumsum(per_contour, out=cstart[1:])
+    n_pts = int(cstart[-1])
+    flags = np.zeros(n_pts, np.uint8)
+    # segment s starts after its contour's first point and the points of the segments before it
+    seg_first = np.zeros(len(kinds), np.int64)
+    np.cumsum(kinds + 1, out=seg_first)
+    seg_first -= kinds + 1
+    contour_seg0 = np.zeros(nk + 1, np.int64)
+    np.cumsum(nseg, out=contour_seg0[1:])
+    before = seg_first - np.repeat(np.concatenate([[0], np.cumsum(kinds + 1)])[contour_seg0[:-1]], nseg)
+    p0 = cstart[seg_contour] + 1 + before                          # first point after the segment start
+    flags[p0[kinds >= 1]] = 1
+    flags[p0[kinds == 2] + 1] = 2
+    u = rng.uniform(2 * n_pts).reshape(n_pts, 2)
+    pt_path = np.repeat(k_path, per_contour)
+    pts = origin[pt_path] + u * box[pt_path][:, None]
+    closed = (rng.uniform(nk) < 0.4).astype(np.uint8)
+    pstart = np.zeros(n + 1, np.int64)
+    np.cumsum(n_contours, out=pstart[1:])
     st = np.zeros(n, STROKE_DTYPE)
-    for p in range(n):
-        box = float(_log_uniform(rng, 16.0, float(side), 1)[0])
-        origin = rng.uniform(2) * (side - box)
-        for _ in range(int(n_contours[p])):
-            nseg = int(rng.integers(1, 12, 1)[0])
-            kinds = rng.integers(0, 2, nseg)
-            cur = origin + rng.uniform(2) * box
-            cp, cf = [cur], [0]
-            for k in kinds:
-                for _ in range(int(k)):  # control points
-                    cp.append(origin + rng.uniform(2) * box)
-                    cf.append(1 if len(cf) == 0 or cf[-1] == 0 else 2)
-                cp.append(origin + rng.uniform(2) * box)
-                cf.append(0)
-            pts.append(np.array(cp, np.float64))
-            fl.append(np.array(cf, np.uint8))
-            cstart.append(cstart[-1] + len(cp))
-            closed.append(1 if rng.uniform(1)[0] < 0.4 else 0)
-        pstart.append(len(cstart) - 1)
-        st[p]["line_width"] = 0.0 if filled[p] else width[p]
-        st[p]["miter_limit"] = miter[p]
-        st[p]["line_cap"] = caps[p]
-        st[p]["line_join"] = joins[p]
-        if dashed[p] and not filled[p]:
-            m = 2 if rng.uniform(1)[0] < 0.5 else 4
-            pat = 1.0 + 39.0 * rng.uniform(m)
-            st[p]["dash_first"] = len(dashes)
-            st[p]["dash_count"] = m
-            st[p]["dash_offset"] = float(rng.uniform(1)[0] * pat.sum()) if rng.uniform(1)[0] < 0.33 else 0.0
-            dashes.extend(pat.tolist())
+    st["line_width"] = np.where(filled, 0.0, width)
+    st["miter_limit"] = miter
+    st["line_cap"] = caps
+    st["line_join"] = joins
+    use = dashed & ~filled
+    m = np.where(rng.uniform(n) < 0.5, 2, 4) * use
+    first = np.zeros(n + 1, np.int64)
+    np.cumsum(m, out=first[1:])
+    pat = 1.0 + 39.0 * rng.uniform(int(first[-1]))
+    totals = np.add.reduceat(pat, first[:-1][use]) if use.any() else np.zeros(0)
+    phase = np.where(rng.uniform(n) < 0.33, rng.uniform(n), 0.0)
+    st["dash_first"] = first[:-1]
+    st["dash_count"] = m
+    offs = np.zeros(n)
+    offs[use] = phase[use] * totals
+    st["dash_offset"] = offs
     rgb = rng.integers(0, 0xFFFFFF, n).astype(np.uint32)
     alpha = np.where(rng.uniform(n) < 0.4, (rng.uniform(n) * 180 + 60).astype(np.uint32), 255)
-    sc = Scene(points=np.concatenate(pts).astype(np.float32), flags=np.concatenate(fl),
-               contour_start=np.asarray(cstart, np.uint32), path_start=np.asarray(pstart, np.uint32),
-               fill_rule=np.zeros(n, np.uint8), color=rgb | (alpha.astype(np.uint32) << np.uint32(24)),
-               width=float(side), height=float(side))
+    sc = Scene(points=pts.astype(np.float32), flags=flags, contour_start=cstart.astype(np.uint32),
+               path_start=pstart.astype(np.uint32), fill_rule=np.zeros(n, np.uint8),
+               color=rgb | (alpha.astype(np.uint32) << np.uint32(24)), width=float(side), height=float(side))
     sc.path_stroke = st
-    sc.contour_closed = np.asarray(closed, np.uint8)
-    sc.dashes = np.asarray(dashes if dashes else [1.0], np.float32)
+    sc.contour_closed = closed
+    sc.dashes = np.asarray(pat if len(pat) else [1.0], np.float32)
     return sc
+
+
+def batched_stroked(n_scenes: int = 512, first_seed: int = 1000, lo_paths: int = 16, hi_paths: int = 4096,
+                    sides=(256, 512, 1024, 2048), dash_share: float = 0.3) -> List[Scene]:
+    """The batched layout (log-uniform path counts, canvas sides) with stroked scenes."""
+    out = []
+    for i in range(n_scenes):
+        rng = Rng(first_seed + i, 4)
+        n = int(np.floor(_log_uniform(rng, float(lo_paths), float(hi_paths), 1))[0])
+        side = int(sides[int(rng.integers(0, len(sides) - 1, 1)[0])])
+        out.append(stroked(seed=first_seed + i, n_paths=n, side=side, dash_share=dash_share))
+    return out
 
 
 def mixed(seed: int = 7, n_paths: int = 8192, side: int = 4096) -> Scene:
