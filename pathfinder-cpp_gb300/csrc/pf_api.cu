@@ -86,6 +86,7 @@ struct Ctx {
     // stroked paths: the uploaded outline and what the upload's stroke pass works in
     DevBuf in_points, in_pflags, in_cstart, in_pstart, st_stroke, st_closed, st_dashes, st_scenes, st_cfirst;
     DevBuf dash_pts, dash_cnt, dash_end, dash_points, dash_flags, job_first, jobs, job_pts, st_bounds;
+    DevBuf job_units, job_nfwd, job_flags, job_cap1, job_end, units, unit_leaves, st_leaves, leaf_pts;
     uint32_t stroke_jobs = 0, stroke_dash_points = 0;  // of the last upload with strokes
     pf_upload_stats ustats{};
     cudaEvent_t sev[8] = {};  // stroke pass timing (stage timing on)
@@ -376,21 +377,80 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
         PF_CUDA(mark(3));
     }
     // one job per output contour
+    float ms_stroke = 0.0f;
+    auto span = [&]() -> int {  // after a synchronisation: the device time between marks 4 and 5
+        if (!timing) return PF_OK;
+        float t = 0.0f;
+        PF_CUDA(cudaEventElapsedTime(&t, c->sev[4], c->sev[5]));
+        ms_stroke += t;
+        return PF_OK;
+    };
+    auto read_u32 = [&](const uint32_t *dev, uint32_t &v) -> int {
+        PF_CUDA(mark(5));
+        if (int e = d2h_wait(c, &v, dev, 1)) return e;
+        return span();
+    };
+    PF_CUDA(mark(4));
     PF_CUDA(launch_stroke_jobs(in, false, st));
     PF_CUDA(scan_exclusive_u32(in.job_first, in.job_first, N, in.job_first + N, c->scan_temp.p, st, status));
     uint32_t J = 0;
-    if (int e = d2h_wait(c, &J, in.job_first + N, 1)) return e;
+    if (int e = read_u32(in.job_first + N, J)) return e;
     if (J >= (1u << 31)) return fail(c, PF_ERR_OVERFLOW, "stroked outline too large (2^31 contours)");
     PF_CUDA(c->jobs.ensure(size_t(J) * 16 + 16));
     PF_CUDA(c->job_pts.ensure((size_t(J) + 1) * 4));
+    PF_CUDA(c->job_units.ensure((size_t(J) + 1) * 4));
+    PF_CUDA(c->job_nfwd.ensure(size_t(J) * 4 + 16));
+    PF_CUDA(c->job_flags.ensure(size_t(J) * 4 + 16));
+    PF_CUDA(c->job_cap1.ensure(size_t(J) * 4 + 16));
+    PF_CUDA(c->job_end.ensure(size_t(J) * 4 + 16));
     PF_CUDA(c->scan_temp.ensure(scan_temp_bytes(J + 1)));
     in.n_jobs = J;
     in.jobs = c->jobs.as<uint4>();
     in.job_pts = c->job_pts.as<uint32_t>();
+    in.job_units = c->job_units.as<uint32_t>();
+    in.job_nfwd = c->job_nfwd.as<uint32_t>();
+    in.job_flags = c->job_flags.as<uint32_t>();
+    in.job_cap1 = c->job_cap1.as<uint32_t>();
+    in.job_end = c->job_end.as<uint32_t>();
     c->stroke_jobs = J;
+    // units: every stroked contour's segments, forward and backward
     PF_CUDA(mark(4));
     PF_CUDA(launch_stroke_jobs(in, true, st));
+    PF_CUDA(cudaMemsetAsync(in.job_flags, 0, size_t(J) * 4, st));
+    PF_CUDA(launch_units(in, false, st));
+    PF_CUDA(scan_exclusive_u32(in.job_units, in.job_units, J, in.job_units + J, c->scan_temp.p, st, status));
+    uint32_t U = 0;
+    if (int e = read_u32(in.job_units + J, U)) return e;
+    if (U >= (1u << 31)) return fail(c, PF_ERR_OVERFLOW, "stroked outline too large (2^31 segments)");
+    PF_CUDA(c->units.ensure(size_t(U) * 48 + 16));
+    PF_CUDA(c->unit_leaves.ensure((size_t(U) + 1) * 4));
+    PF_CUDA(c->scan_temp.ensure(scan_temp_bytes(U + 1)));
+    in.n_units = U;
+    in.units = c->units.as<float4>();
+    in.unit_leaves = c->unit_leaves.as<uint32_t>();
+    // leaves: the offset recursion of every unit
+    PF_CUDA(mark(4));
+    PF_CUDA(launch_units(in, true, st));
+    PF_CUDA(launch_unit_leaves(in, false, st));
+    PF_CUDA(scan_exclusive_u32(in.unit_leaves, in.unit_leaves, U, in.unit_leaves + U, c->scan_temp.p, st, status));
+    uint32_t NL = 0;
+    if (int e = read_u32(in.unit_leaves + U, NL)) return e;
+    if (NL >= (1u << 31)) return fail(c, PF_ERR_OVERFLOW, "stroked outline too large (2^31 offset pieces)");
+    PF_CUDA(c->st_leaves.ensure(size_t(NL) * 48 + 16));
+    PF_CUDA(c->leaf_pts.ensure((size_t(NL) + 1) * 4));
+    PF_CUDA(c->scan_temp.ensure(scan_temp_bytes(NL + 1)));
+    in.n_leaves = NL;
+    in.leaves = c->st_leaves.as<float4>();
+    in.leaf_pts = c->leaf_pts.as<uint32_t>();
+    // counts: joins and points per leaf, caps and closing joins per contour, the degenerate
+    // contours by the sequential kernel; then the contours' offsets
+    PF_CUDA(mark(4));
+    PF_CUDA(launch_unit_leaves(in, true, st));
+    PF_CUDA(launch_job_ends(in, false, st));
+    PF_CUDA(launch_leaf_pts(in, false, st));
     PF_CUDA(launch_stroke(in, false, status, st));
+    PF_CUDA(scan_exclusive_u32(in.leaf_pts, in.leaf_pts, NL, in.leaf_pts + NL, c->scan_temp.p, st, status));
+    PF_CUDA(launch_job_totals(in, status, st));
     PF_CUDA(scan_exclusive_u32(in.job_pts, in.job_pts, J, in.job_pts + J, c->scan_temp.p, st, status));
     uint32_t tot[2];
     uint64_t wide = 0;  // the 64-bit total of the output points (slots 18-19)
@@ -398,6 +458,7 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
     PF_CUDA(cudaMemcpyAsync(&tot[0], in.job_pts + J, 4, cudaMemcpyDeviceToHost, st));
     PF_CUDA(cudaMemcpyAsync(&wide, status + kStFill64 + 2, 8, cudaMemcpyDeviceToHost, st));
     if (int e = d2h_wait(c, &tot[1], status + kStErr, 1)) return e;
+    if (int e = span()) return e;
     if (wide >= (1ull << 31)) return fail(c, PF_ERR_OVERFLOW, "stroked outline too large (2^31 points)");
     if (tot[1] & kErrStroke)
         return fail(c, PF_ERR_KERNEL_LIMIT, "stroking hit a limit (a dash pattern over 2^22 steps on one path, "
@@ -411,6 +472,8 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
     in.out_flags = c->pflags.as<uint8_t>();
     in.n_out_points = P;
     PF_CUDA(mark(6));
+    PF_CUDA(launch_leaf_pts(in, true, st));
+    PF_CUDA(launch_job_ends(in, true, st));
     PF_CUDA(launch_stroke(in, true, status, st));
     PF_CUDA(mark(7));
     // the new layout: per scene its first contour and point
@@ -446,9 +509,8 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
             PF_CUDA(cudaEventElapsedTime(&b, c->sev[2], c->sev[3]));
             c->ustats.ms_dash = a + b;
         }
-        PF_CUDA(cudaEventElapsedTime(&a, c->sev[4], c->sev[5]));
         PF_CUDA(cudaEventElapsedTime(&b, c->sev[6], c->sev[7]));
-        c->ustats.ms_stroke = a + b;
+        c->ustats.ms_stroke = ms_stroke + b;
     }
     return PF_OK;
 }
@@ -1446,7 +1508,9 @@ int pf_ctx_destroy(void *ctx) {
                       &c->status, &c->scan_temp, &c->path_clip, &c->path_is_clip, &c->path_clip_rel,
                       &c->in_points, &c->in_pflags, &c->in_cstart, &c->in_pstart, &c->st_stroke, &c->st_closed,
                       &c->st_dashes, &c->st_scenes, &c->st_cfirst, &c->dash_pts, &c->dash_cnt, &c->dash_end,
-                      &c->dash_points, &c->dash_flags, &c->job_first, &c->jobs, &c->job_pts, &c->st_bounds};
+                      &c->dash_points, &c->dash_flags, &c->job_first, &c->jobs, &c->job_pts, &c->st_bounds,
+                      &c->job_units, &c->job_nfwd, &c->job_flags, &c->job_cap1, &c->job_end, &c->units,
+                      &c->unit_leaves, &c->st_leaves, &c->leaf_pts};
     for (DevBuf *b : bufs) b->release();
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);

@@ -218,10 +218,26 @@ struct StrokeIn {
     uint32_t *job_pts;                  // [n_jobs + 1] counts -> scanned
     float2 *out_points;
     uint8_t *out_flags;
+    // the segment-parallel stroker: one unit per input segment and direction, one leaf per
+    // offset piece; a job whose contour is degenerate is redone by the sequential kernel
+    uint32_t n_units, n_leaves;
+    uint32_t *job_units;                // [n_jobs + 1] counts -> scanned
+    uint32_t *job_nfwd;                 // [n_jobs] units of the forward direction
+    uint32_t *job_flags;                // [n_jobs] bit 0: done by the sequential kernel
+    uint32_t *job_cap1, *job_end;       // [n_jobs] points of the first cap / of the end (cap, join)
+    float4 *units;                      // [n_units][3] segment, (job, direction | index)
+    uint32_t *unit_leaves;              // [n_units + 1] counts -> scanned
+    float4 *leaves;                     // [n_leaves][3] piece, join point, (job, meta)
+    uint32_t *leaf_pts;                 // [n_leaves + 1] counts -> scanned
 };
 cudaError_t launch_dash(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);
 cudaError_t launch_stroke_jobs(const StrokeIn &in, bool fill, cudaStream_t st);
 cudaError_t launch_stroke(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);
+cudaError_t launch_units(const StrokeIn &in, bool write, cudaStream_t st);
+cudaError_t launch_unit_leaves(const StrokeIn &in, bool write, cudaStream_t st);
+cudaError_t launch_job_ends(const StrokeIn &in, bool write, cudaStream_t st);
+cudaError_t launch_leaf_pts(const StrokeIn &in, bool write, cudaStream_t st);
+cudaError_t launch_job_totals(const StrokeIn &in, uint32_t *status, cudaStream_t st);
 cudaError_t launch_outline_starts(const StrokeIn &in, const SceneDev *out_scenes, uint32_t *cstart,
                                   uint32_t *pstart, cudaStream_t st);
 cudaError_t launch_scene_bounds(const StrokeIn &in, uint32_t *out, cudaStream_t st);

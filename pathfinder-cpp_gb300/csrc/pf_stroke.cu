@@ -696,6 +696,8 @@ __global__ void __launch_bounds__(128) k_stroke(StrokeIn in, uint32_t *status) {
     if (j >= in.n_jobs) return;
     const uint4 job = in.jobs[j];
     const uint32_t kind = job.z & 3u;
+    // stroked contours go through the segment-parallel kernels unless marked degenerate
+    if (kind != kJobCopy && !(in.job_flags[j] & 1u)) return;
     Contour c;
     const bool from_dash = (job.z & 8u) != 0;
     c.p = (from_dash ? in.dash_points : in.points) + job.x;
@@ -709,10 +711,8 @@ __global__ void __launch_bounds__(128) k_stroke(StrokeIn in, uint32_t *status) {
                 in.out_points[base + i] = c.p[i];
                 in.out_flags[base + i] = c.f[i];
             }
-        else {
+        else
             in.job_pts[j] = c.n;
-            atomicAdd(reinterpret_cast<unsigned long long *>(status + kStFill64 + 2), (unsigned long long)c.n);
-        }
         return;
     }
     const pf_stroke st = in.stroke[job.w];
@@ -736,10 +736,359 @@ __global__ void __launch_bounds__(128) k_stroke(StrokeIn in, uint32_t *status) {
         close_join(o, c, st);
     }
     if (o.lost) atomicOr(&status[kStErr], kErrStroke);
-    if (!kWrite) {
-        in.job_pts[j] = o.n;
-        atomicAdd(reinterpret_cast<unsigned long long *>(status + kStFill64 + 2), (unsigned long long)o.n);
+    if (!kWrite) in.job_pts[j] = o.n;
+}
+
+
+// --- Segment-parallel stroking --------------------------------------------------------------
+// The sequential algorithm pushes, per input segment in order, the leaves of its offset
+// recursion, each preceded by the join with the contour's last two points.  When every leaf
+// is a valid segment (it then pushes at least two points), those two points are the previous
+// leaf's last two, so every leaf's join and points depend on that leaf and its predecessor
+// only; caps and the closing join depend on the first and last leaves.  Contours for which
+// this does not hold (an invalid leaf, a cap that searches back past the last leaf, one
+// direction empty) are marked and redone by the sequential k_stroke.
+
+// Unit record: float4 baseline, float4 control, float4 (kind, job, dir << 31 | index, -).
+__device__ __forceinline__ void put_seg(float4 *dst, const Seg &s, uint32_t w0, uint32_t w1, uint32_t w2) {
+    dst[0] = make_float4(s.b.f.x, s.b.f.y, s.b.t.x, s.b.t.y);
+    dst[1] = make_float4(s.c.f.x, s.c.f.y, s.c.t.x, s.c.t.y);
+    dst[2] = make_float4(__uint_as_float((uint32_t)s.kind), __uint_as_float(w0), __uint_as_float(w1),
+                         __uint_as_float(w2));
+}
+__device__ __forceinline__ Seg get_seg(const float4 *src, uint4 &meta) {
+    const float4 b = src[0], c = src[1], m = src[2];
+    meta = make_uint4(__float_as_uint(m.x), __float_as_uint(m.y), __float_as_uint(m.z), __float_as_uint(m.w));
+    return Seg{ls(mk(b.x, b.y), mk(b.z, b.w)), ls(mk(c.x, c.y), mk(c.z, c.w)), (int)meta.x};
+}
+
+__device__ __forceinline__ Contour job_contour(const StrokeIn &in, const uint4 &job) {
+    Contour c;
+    const bool from_dash = (job.z & 8u) != 0;
+    c.p = (from_dash ? in.dash_points : in.points) + job.x;
+    c.f = (from_dash ? in.dash_flags : in.flags) + job.x;
+    c.n = job.y;
+    c.closed = (job.z & 4u) != 0;
+    return c;
+}
+
+// count: job_units[j], job_nfwd[j]; write: the units (forward: SegmentsIter order; backward:
+// the closing line first, then the segments reversed, stroke.cpp:51-122).
+template <bool kWrite>
+__global__ void k_units(StrokeIn in) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= in.n_jobs) return;
+    const uint4 job = in.jobs[j];
+    const uint32_t kind = job.z & 3u;
+    uint32_t u = kWrite ? in.job_units[j] : 0u;
+    const uint32_t u0 = u;
+    if (kind == kJobCopy) {
+        if (!kWrite) in.job_units[j] = in.job_nfwd[j] = 0;
+        return;
     }
+    const Contour c = job_contour(in, job);
+    if (kind == kJobOpen || kind == kJobClosedFwd) {
+        SegIter it{&c, 0, true};
+        uint32_t idx = 0;
+        while (it.has_next) {
+            const Seg s = it.next();
+            if (s.kind == kNone) break;
+            if (kWrite) put_seg(in.units + 3 * (size_t)u, s, j, idx, 0);
+            u++;
+            idx++;
+        }
+    }
+    const uint32_t nfwd = u - u0;
+    if (kind == kJobOpen || kind == kJobClosedBwd) {
+        const int n = (int)c.n;
+        int tail = n - 1;
+        uint32_t idx = 0;
+        if (c.closed && n > 1 && !(vlen(vsub(c.at(0), c.at(n - 1))) <= kFloatEps)) {
+            if (kWrite) put_seg(in.units + 3 * (size_t)u, sline(ls(c.at(0), c.at(n - 1))), j, 1u << 31 | idx, 0);
+            u++;
+            idx++;
+        }
+        while (tail >= 0) {
+            if (c.f[tail] != kOn) break;
+            Seg s;
+            if (tail >= 3 && c.f[tail - 1] == kC1 && c.f[tail - 2] == kC0 && c.f[tail - 3] == kOn) {
+                s = scubic(ls(c.at(tail), c.at(tail - 3)), ls(c.at(tail - 1), c.at(tail - 2)));
+                tail -= 3;
+            } else if (tail >= 2 && c.f[tail - 1] == kC0 && c.f[tail - 2] == kOn) {
+                s = squad(ls(c.at(tail), c.at(tail - 2)), c.at(tail - 1));
+                tail -= 2;
+            } else if (tail >= 1 && c.f[tail - 1] == kOn) {
+                s = sline(ls(c.at(tail), c.at(tail - 1)));
+                tail -= 1;
+            } else {
+                break;
+            }
+            if (kWrite) put_seg(in.units + 3 * (size_t)u, s, j, 1u << 31 | idx, 0);
+            u++;
+            idx++;
+        }
+    }
+    if (!kWrite) {
+        in.job_units[j] = u - u0;
+        in.job_nfwd[j] = nfwd;
+    }
+}
+
+// count: unit_leaves[u]; write: the leaves of the unit's offset recursion (Segment::offset,
+// stroke.cpp:502-540), each the segment it pushes, its join point and (job, meta): meta =
+// kind | direction << 2 | (unit index > 0) << 3.  An invalid leaf marks the job.
+template <bool kWrite>
+__global__ void __launch_bounds__(128) k_unit_leaves(StrokeIn in) {
+    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= in.n_units) return;
+    uint4 um;
+    const Seg root = get_seg(in.units + 3 * (size_t)u, um);
+    const uint32_t job = um.y, dir = um.z >> 31, idx = um.z & 0x7fffffffu;
+    const float d = -fm(in.stroke[in.jobs[job].w].line_width, 0.5f);
+    uint32_t leaf = kWrite ? in.unit_leaves[u] : 0u;
+    const uint32_t l0 = leaf;
+    Seg stack[kStack];
+    uint8_t depth[kStack];
+    stack[0] = root;
+    depth[0] = 0;
+    int sp = 1;
+    const float tol2 = fm(kStrokeTol, kStrokeTol);
+    bool bad = false;
+    auto emit = [&](const Seg &s, V2 jp) {
+        bad |= !svalid(s);
+        if (kWrite) {
+            float4 *r = in.leaves + 3 * (size_t)leaf;
+            r[0] = make_float4(s.b.f.x, s.b.f.y, s.b.t.x, s.b.t.y);
+            r[1] = make_float4(s.c.f.x, s.c.f.y, s.c.t.x, s.c.t.y);
+            r[2] = make_float4(jp.y, __uint_as_float(job),
+                               __uint_as_float((uint32_t)s.kind | dir << 2 | (idx > 0 ? 8u : 0u)), jp.x);
+        }
+        leaf++;
+    };
+    while (sp > 0) {
+        sp--;
+        const Seg s = stack[sp];
+        const uint32_t dep = depth[sp];
+        if (!svalid(s)) continue;
+        const V2 jp = s.b.f;
+        if (lsqlen(s.b) < tol2 || dep >= 16) {
+            emit(s, jp);
+            continue;
+        }
+        const Seg cand = offset_once(s, d);
+        if (s.kind == kLine || within_tol(s, cand, d)) {
+            emit(cand, jp);
+            continue;
+        }
+        Seg a, b;
+        ssplit(s, 0.5f, a, b);
+        stack[sp] = b;
+        depth[sp] = (uint8_t)(dep + 1);
+        stack[sp + 1] = a;
+        depth[sp + 1] = (uint8_t)(dep + 1);
+        sp += 2;
+    }
+    if (!kWrite) in.unit_leaves[u] = leaf - l0;
+    // an invalid leaf, or a unit without leaves (a later leaf's predecessor would not be its
+    // own direction's), leaves the contour to the sequential kernel
+    if (!kWrite && (bad || leaf == l0)) atomicOr(&in.job_flags[job], 1u);
+}
+
+// A leaf record: float4 baseline, float4 control, float4 (join point y, job, meta, join point x);
+// the pushed segment's kind rides in the meta word.
+__device__ __forceinline__ Seg get_leaf(const StrokeIn &in, uint32_t l, V2 &jp, uint32_t &job, uint32_t &meta) {
+    const float4 *r = in.leaves + 3 * (size_t)l;
+    const float4 b = r[0], c = r[1], m = r[2];
+    job = __float_as_uint(m.y);
+    meta = __float_as_uint(m.z);
+    jp = mk(m.w, m.x);
+    return Seg{ls(mk(b.x, b.y), mk(b.z, b.w)), ls(mk(c.x, c.y), mk(c.z, c.w)), (int)(meta & 3u)};
+}
+// The points a segment pushes (contour.cpp:11-41), in order.
+__device__ __forceinline__ uint32_t seg_points(const Seg &s, V2 *p) {
+    uint32_t n = 0;
+    p[n++] = s.b.f;
+    if (s.kind != kLine) {
+        p[n++] = s.c.f;
+        if (s.kind != kQuad) p[n++] = s.c.t;
+    }
+    p[n++] = s.b.t;
+    return n;
+}
+
+__device__ __forceinline__ uint32_t first_leaf_of_job(const StrokeIn &in, uint32_t j) {
+    return in.unit_leaves[in.job_units[j]];
+}
+// Output position of a job's leaf: the job's start, the leaves before it, and (open
+// contours, backward leaves) the first cap.
+__device__ __forceinline__ uint32_t leaf_pos(const StrokeIn &in, uint32_t l, uint32_t job, uint32_t meta) {
+    const uint32_t l0 = first_leaf_of_job(in, job);
+    const bool open = (in.jobs[job].z & 3u) == kJobOpen;
+    return in.job_pts[job] + (in.leaf_pts[l] - in.leaf_pts[l0]) + (open && (meta & 4u) ? in.job_cap1[job] : 0u);
+}
+
+// count: leaf_pts[l] = the join before the leaf plus its points; write: those points.
+template <bool kWrite>
+__global__ void __launch_bounds__(128) k_leaf_pts(StrokeIn in) {
+    const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= in.n_leaves) return;
+    V2 jp;
+    uint32_t job, meta;
+    const Seg s = get_leaf(in, l, jp, job, meta);
+    if (in.job_flags[job] & 1u) {
+        if (!kWrite) in.leaf_pts[l] = 0;
+        return;
+    }
+    const pf_stroke st = in.stroke[in.jobs[job].w];
+    const float d = -fm(st.line_width, 0.5f);
+    const bool joins = (meta & 8u) && st.line_join != PF_JOIN_BEVEL;
+    Sink o;
+    o.n = 2;
+    o.lost = false;
+    o.pts = nullptr;
+    o.fl = nullptr;
+    if (joins) {  // the contour's last two points: the previous leaf's
+        V2 pj, pp[4];
+        uint32_t pjob, pmeta;
+        const Seg prev = get_leaf(in, l - 1, pj, pjob, pmeta);
+        const uint32_t k = seg_points(prev, pp);
+        o.ring[0] = pp[k - 2];
+        o.ring[1] = pp[k - 1];
+    }
+    if (kWrite) {
+        const uint32_t pos = leaf_pos(in, l, job, meta);
+        o.pts = in.out_points + pos - 2;
+        o.fl = in.out_flags + pos - 2;
+    }
+    if (joins) add_to_contour(o, s, d, st.line_join, jp, st.miter_limit);
+    else push_seg(o, s);
+    if (!kWrite) in.leaf_pts[l] = o.n - 2;
+}
+
+// A cap after leaf l (OutlineStrokeToFill::add_cap, stroke.cpp:206-258) with the search for
+// the tangent's start kept inside the leaf's points.  first: the leaf starts the contour (a
+// search that reaches its first point ends without a cap); otherwise leaving the leaf marks
+// the job.  Returns false when the job must be redone sequentially.
+__device__ bool leaf_cap(const StrokeIn &in, uint32_t l, const pf_stroke &st, bool first, float2 *pts, uint8_t *fl,
+                         uint32_t &count) {
+    V2 jp, p[4];
+    uint32_t job, meta;
+    const Seg s = get_leaf(in, l, jp, job, meta);
+    const uint32_t k = seg_points(s, p);
+    count = 0;
+    if (st.line_cap == PF_CAP_BUTT) return true;
+    const V2 p1 = p[k - 1];
+    int i = (int)k - 2;
+    for (;;) {
+        if (vsqlen(vsub(p1, p[i])) > kFloatEps) break;
+        if (i == 0) {
+            if (first) return true;
+            return false;
+        }
+        i--;
+    }
+    Sink o;
+    o.n = 2;
+    o.lost = false;
+    o.pts = pts ? pts - 2 : nullptr;
+    o.fl = fl ? fl - 2 : nullptr;
+    const V2 g = vnorm(vsub(p1, p[i]));
+    const float w = st.line_width;
+    if (st.line_cap == PF_CAP_SQUARE) {
+        const V2 off = vscale(g, fm(w, 0.5f));
+        const V2 p2 = vadd(p1, off);
+        const V2 p3 = vadd(p2, vmul(mk(g.y, g.x), mk(-w, w)));
+        o.push(p2, kOn);
+        o.push(p3, kOn);
+        o.push(vsub(p3, off), kOn);
+    } else {
+        const float sc = fm(w, 0.5f);
+        const V2 off = vmul(mk(g.y, g.x), mk(-1.0f, 1.0f));
+        const V2 tr = vadd(p1, vscale(off, fm(w, 0.5f)));
+        push_arc(o, xtranslate(xscale(mk(sc, sc)), tr), ls(mk(-off.x, -off.y), off));
+    }
+    count = o.n - 2;
+    return true;
+}
+
+// count: job_cap1[j], job_end[j] (and the marks for degenerate contours); write: the caps /
+// the closing join (push_stroked_contour, stroke.cpp:186-204).
+template <bool kWrite>
+__global__ void k_job_ends(StrokeIn in) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= in.n_jobs) return;
+    const uint4 job = in.jobs[j];
+    const uint32_t kind = job.z & 3u;
+    if (kind == kJobCopy || (in.job_flags[j] & 1u)) {
+        if (!kWrite) in.job_cap1[j] = in.job_end[j] = 0;
+        return;
+    }
+    const uint32_t u0 = in.job_units[j], u1 = in.job_units[j + 1];
+    const uint32_t l0 = in.unit_leaves[u0], l1 = in.unit_leaves[u1];
+    if (l0 == l1) {  // nothing pushed: no cap, no join
+        if (!kWrite) in.job_cap1[j] = in.job_end[j] = 0;
+        return;
+    }
+    const pf_stroke st = in.stroke[job.w];
+    const uint32_t base = kWrite ? in.job_pts[j] + (in.leaf_pts[l1] - in.leaf_pts[l0]) : 0u;
+    if (kind == kJobOpen) {
+        const uint32_t lb = in.unit_leaves[u0 + in.job_nfwd[j]];
+        if (lb == l0 || lb == l1) {  // one direction pushed nothing
+            if (!kWrite) atomicOr(&in.job_flags[j], 1u);
+            return;
+        }
+        uint32_t c1 = 0, c2 = 0;
+        const uint32_t pos1 = kWrite ? in.job_pts[j] + (in.leaf_pts[lb] - in.leaf_pts[l0]) : 0u;
+        bool ok = leaf_cap(in, lb - 1, st, lb - 1 == l0, kWrite ? in.out_points + pos1 : nullptr,
+                           kWrite ? in.out_flags + pos1 : nullptr, c1);
+        const uint32_t cap1 = kWrite ? in.job_cap1[j] : c1;
+        ok = ok && leaf_cap(in, l1 - 1, st, false, kWrite ? in.out_points + base + cap1 : nullptr,
+                            kWrite ? in.out_flags + base + cap1 : nullptr, c2);
+        if (!kWrite) {
+            if (!ok) atomicOr(&in.job_flags[j], 1u);
+            in.job_cap1[j] = c1;
+            in.job_end[j] = c2;
+        }
+        return;
+    }
+    // closed: the join from the last leaf back to the contour's first two points
+    V2 jp, a[4], z[4];
+    uint32_t jb, meta;
+    const uint32_t ka = seg_points(get_leaf(in, l0, jp, jb, meta), a);
+    const uint32_t kz = seg_points(get_leaf(in, l1 - 1, jp, jb, meta), z);
+    Sink o;
+    o.n = 2;
+    o.lost = false;
+    o.ring[0] = z[kz - 2];
+    o.ring[1] = z[kz - 1];
+    o.first[0] = a[0];
+    o.first[1] = a[1];
+    (void)ka;
+    o.pts = kWrite ? in.out_points + base - 2 : nullptr;
+    o.fl = kWrite ? in.out_flags + base - 2 : nullptr;
+    const Contour c = job_contour(in, job);
+    close_join(o, c, st);
+    if (!kWrite) {
+        in.job_cap1[j] = 0;
+        in.job_end[j] = o.n - 2;
+    }
+}
+
+// job_pts[j] for the segment-parallel jobs (the sequential kernel has set the others), and
+// the 64-bit total of all jobs beside the 32-bit scan.
+__global__ void k_job_totals(StrokeIn in, uint32_t *status) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= in.n_jobs) return;
+    const uint4 job = in.jobs[j];
+    uint32_t n;
+    if ((job.z & 3u) == kJobCopy || (in.job_flags[j] & 1u)) {
+        n = in.job_pts[j];
+    } else {
+        const uint32_t l0 = in.unit_leaves[in.job_units[j]], l1 = in.unit_leaves[in.job_units[j + 1]];
+        n = (in.leaf_pts[l1] - in.leaf_pts[l0]) + in.job_cap1[j] + in.job_end[j];
+        in.job_pts[j] = n;
+    }
+    atomicAdd(reinterpret_cast<unsigned long long *>(status + kStFill64 + 2), (unsigned long long)n);
 }
 
 // The new outline's per-scene offset arrays (the layout the upload uses: scene s's contour
@@ -798,6 +1147,45 @@ cudaError_t launch_stroke(const StrokeIn &in, bool write, uint32_t *status, cuda
     if (!in.n_jobs) return cudaSuccess;
     if (write) k_stroke<true><<<blocks(in.n_jobs, 128), 128, 0, st>>>(in, status);
     else k_stroke<false><<<blocks(in.n_jobs, 128), 128, 0, st>>>(in, status);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_units(const StrokeIn &in, bool write, cudaStream_t st) {
+    if (!in.n_jobs) return cudaSuccess;
+    if (write) k_units<true><<<blocks(in.n_jobs, 128), 128, 0, st>>>(in);
+    else k_units<false><<<blocks(in.n_jobs, 128), 128, 0, st>>>(in);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unit_leaves(const StrokeIn &in, bool write, cudaStream_t st) {
+    if (!in.n_units) return cudaSuccess;
+    if (write) k_unit_leaves<true><<<blocks(in.n_units, 128), 128, 0, st>>>(in);
+    else k_unit_leaves<false><<<blocks(in.n_units, 128), 128, 0, st>>>(in);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_job_ends(const StrokeIn &in, bool write, cudaStream_t st) {
+    if (!in.n_jobs) return cudaSuccess;
+    if (write) k_job_ends<true><<<blocks(in.n_jobs, 128), 128, 0, st>>>(in);
+    else k_job_ends<false><<<blocks(in.n_jobs, 128), 128, 0, st>>>(in);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_leaf_pts(const StrokeIn &in, bool write, cudaStream_t st) {
+    if (!in.n_leaves) return cudaSuccess;
+    if (write) k_leaf_pts<true><<<blocks(in.n_leaves, 128), 128, 0, st>>>(in);
+    else k_leaf_pts<false><<<blocks(in.n_leaves, 128), 128, 0, st>>>(in);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_job_totals(const StrokeIn &in, uint32_t *status, cudaStream_t st) {
+    if (!in.n_jobs) return cudaSuccess;
+    k_job_totals<<<blocks(in.n_jobs, 256), 256, 0, st>>>(in, status);
     count_launches(1);
     return cudaGetLastError();
 }
