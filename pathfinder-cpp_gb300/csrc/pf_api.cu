@@ -874,7 +874,7 @@ int stage_setup(Ctx *c, bool learned) {
     PF_CUDA(c->segs.ensure(size_t(c->n_segs) * sizeof(SegDev) + 16));
     PF_CUDA(c->seg_leaves.ensure((size_t(c->n_segs) + 1) * 4));
     PF_CUDA(c->seg_order.ensure(size_t(c->n_segs) * 4 + 16));
-    PF_CUDA(c->seg_ctl.ensure(256));
+    PF_CUDA(c->seg_ctl.ensure(seg_ctl_bytes()));
     PF_CUDA(c->row_paths.ensure(size_t(c->n_row_entries) * 16 + 16));
     const size_t T = c->n_tiles, K = c->n_cols;
     PF_CUDA(c->tile_fills.ensure(T * 4 + 16));

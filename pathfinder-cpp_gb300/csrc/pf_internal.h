@@ -262,6 +262,7 @@ cudaError_t launch_path_counts(const Batch &b, const uint2 *path_contours, uint3
 cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t st);
 // Orders the segments by estimated subdivision depth (seg_order); ctl holds 32 words.
 cudaError_t launch_seg_order(const Batch &b, uint32_t n_segs, uint32_t *ctl, cudaStream_t st);
+size_t seg_ctl_bytes();  // the per-block bucket counts launch_seg_order keeps in ctl
 // Binning by path: classify (leaf ranges, size classes), then bin every path (counts,
 // backdrops, fill offsets, fills).  A learned frame first lists its pooled lines by path:
 // count, scan pool_cnt, scatter.

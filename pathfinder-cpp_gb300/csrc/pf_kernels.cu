@@ -403,29 +403,54 @@ __device__ __forceinline__ int seg_bucket(const Batch &b, const SegDev &sg) {
     return d < kSegBuckets - 1 ? d : kSegBuckets - 1;
 }
 
-// ctl[0..15]: segments per bucket, then (scatter) ctl[16..31]: next slot per bucket
+// A fixed grid of kSegBlocks blocks walks the segments grid-stride.  The count pass leaves
+// each block's per-bucket counts in ctl[kSegBuckets * block + bucket]; the starts kernel
+// turns them into each block's first slot per bucket (buckets deepest first); the scatter
+// pass walks the same segments and places them from those slots.  Counters live in shared
+// memory: no global atomics (one hot global counter per bucket serialised millions of them).
+constexpr int kSegBlocks = 1216;  // 8 blocks per SM of 152
+
 template <bool kScatter>
 __global__ void __launch_bounds__(kThreads) k_seg_buckets(Batch b, uint32_t *ctl) {
-    const uint32_t i = global_tid();
+    __shared__ uint32_t s_cnt[kSegBuckets];
     const uint32_t n = b.status[kStSegs];
     const int lane = threadIdx.x & 31;
-    const int bk = i < n ? seg_bucket(b, b.segs[i]) : -1;
-    const unsigned group = __match_any_sync(0xffffffffu, bk);
-    if (bk < 0) return;
-    const int leader = __ffs(group) - 1;
-    uint32_t base = 0;
-    if (lane == leader) base = atomicAdd(&ctl[(kScatter ? kSegBuckets : 0) + bk], (uint32_t)__popc(group));
-    base = __shfl_sync(group, base, leader);
-    if (kScatter) b.seg_order[base + __popc(group & ((1u << lane) - 1u))] = i;
+    if (threadIdx.x < kSegBuckets)
+        s_cnt[threadIdx.x] = kScatter ? ctl[kSegBuckets * blockIdx.x + threadIdx.x] : 0u;
+    __syncthreads();
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const int bk = i < n ? seg_bucket(b, b.segs[i]) : -1;
+        const unsigned group = __match_any_sync(0xffffffffu, bk);
+        const int leader = __ffs(group) - 1;
+        uint32_t slot = 0;
+        if (bk >= 0 && lane == leader) slot = atomicAdd(&s_cnt[bk], (uint32_t)__popc(group));
+        slot = __shfl_sync(0xffffffffu, slot, leader);
+        if (kScatter && bk >= 0) b.seg_order[slot + __popc(group & ((1u << lane) - 1u))] = i;
+    }
+    __syncthreads();
+    if (!kScatter && threadIdx.x < kSegBuckets) ctl[kSegBuckets * blockIdx.x + threadIdx.x] = s_cnt[threadIdx.x];
 }
 
-// Bucket starts, deepest bucket first.
+// Every block's first slot per bucket, buckets deepest first (one thread per bucket).
 __global__ void k_seg_bucket_starts(uint32_t *ctl) {
-    if (threadIdx.x != 0) return;
-    uint32_t run = 0;
-    for (int bk = kSegBuckets - 1; bk >= 0; bk--) {
-        ctl[kSegBuckets + bk] = run;
-        run += ctl[bk];
+    __shared__ uint32_t total[kSegBuckets];
+    const int bk = threadIdx.x;
+    if (bk < kSegBuckets) {
+        uint32_t t = 0;
+        for (int blk = 0; blk < kSegBlocks; blk++) t += ctl[kSegBuckets * blk + bk];
+        total[bk] = t;
+    }
+    __syncthreads();
+    if (bk < kSegBuckets) {
+        uint32_t run = 0;
+        for (int d = kSegBuckets - 1; d > bk; d--) run += total[d];
+        for (int blk = 0; blk < kSegBlocks; blk++) {
+            const uint32_t c = ctl[kSegBuckets * blk + bk];
+            ctl[kSegBuckets * blk + bk] = run;
+            run += c;
+        }
     }
 }
 
@@ -1817,13 +1842,13 @@ cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStre
     return cudaGetLastError();
 }
 
+size_t seg_ctl_bytes() { return size_t(kSegBlocks) * kSegBuckets * 4; }
+
 cudaError_t launch_seg_order(const Batch &b, uint32_t n_segs, uint32_t *ctl, cudaStream_t st) {
     if (!n_segs) return cudaSuccess;
-    cudaError_t e = cudaMemsetAsync(ctl, 0, 2 * kSegBuckets * 4, st);
-    if (e != cudaSuccess) return e;
-    PF_LAUNCH(k_seg_buckets<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, ctl));
+    PF_LAUNCH(k_seg_buckets<false><<<kSegBlocks, kThreads, 0, st>>>(b, ctl));
     PF_LAUNCH(k_seg_bucket_starts<<<1, 32, 0, st>>>(ctl));
-    PF_LAUNCH(k_seg_buckets<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, ctl));
+    PF_LAUNCH(k_seg_buckets<true><<<kSegBlocks, kThreads, 0, st>>>(b, ctl));
     return cudaGetLastError();
 }
 

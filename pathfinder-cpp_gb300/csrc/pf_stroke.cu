@@ -1078,17 +1078,22 @@ __global__ void k_job_ends(StrokeIn in) {
 // the 64-bit total of all jobs beside the 32-bit scan.
 __global__ void k_job_totals(StrokeIn in, uint32_t *status) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= in.n_jobs) return;
-    const uint4 job = in.jobs[j];
-    uint32_t n;
-    if ((job.z & 3u) == kJobCopy || (in.job_flags[j] & 1u)) {
-        n = in.job_pts[j];
-    } else {
-        const uint32_t l0 = in.unit_leaves[in.job_units[j]], l1 = in.unit_leaves[in.job_units[j + 1]];
-        n = (in.leaf_pts[l1] - in.leaf_pts[l0]) + in.job_cap1[j] + in.job_end[j];
-        in.job_pts[j] = n;
+    unsigned long long n = 0;
+    if (j < in.n_jobs) {
+        const uint4 job = in.jobs[j];
+        if ((job.z & 3u) == kJobCopy || (in.job_flags[j] & 1u)) {
+            n = in.job_pts[j];
+        } else {
+            const uint32_t l0 = in.unit_leaves[in.job_units[j]], l1 = in.unit_leaves[in.job_units[j + 1]];
+            const uint32_t c = (in.leaf_pts[l1] - in.leaf_pts[l0]) + in.job_cap1[j] + in.job_end[j];
+            in.job_pts[j] = c;
+            n = c;
+        }
     }
-    atomicAdd(reinterpret_cast<unsigned long long *>(status + kStFill64 + 2), (unsigned long long)n);
+    // one atomic per warp (one hot address for millions of jobs otherwise)
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+    if ((threadIdx.x & 31) == 0 && n)
+        atomicAdd(reinterpret_cast<unsigned long long *>(status + kStFill64 + 2), n);
 }
 
 // The new outline's per-scene offset arrays (the layout the upload uses: scene s's contour
