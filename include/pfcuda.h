@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define PF_ABI_VERSION 3
+#define PF_ABI_VERSION 4
 
 typedef enum pf_status {
     PF_OK = 0,
@@ -73,6 +73,36 @@ typedef struct pf_stroke {
     float dash_offset;   /* the pattern's phase (the canvas passes 0)                      */
 } pf_stroke;
 
+/*
+ * Gradient paints (Paint::from_gradient, pathfinder/core/paint/paint.h:87-95; Gradient,
+ * core/paint/gradient.h): the path is filled with a 256-texel colour ramp (GradientTileBuilder::
+ * allocate, core/paint/gradient.cpp) sampled per pixel as tile.comp samples its colour texture:
+ * linearly filtered, clamped or repeated along the ramp, with the metadata (the gradient's
+ * texture transform and radial parameters) stored as half floats the way the reference's
+ * RGBA16F metadata texture stores them (core/renderer.cpp:167-250).
+ */
+#define PF_PAINT_SOLID 0u   /* the path's colour */
+#define PF_PAINT_LINEAR 1u  /* GradientLinear: t runs from line.from (0) to line.to (1) */
+#define PF_PAINT_RADIAL 2u  /* GradientRadial: circles (from, r0) to (to, r1), then transform */
+#define PF_WRAP_CLAMP 0u
+#define PF_WRAP_REPEAT 1u
+
+typedef struct pf_color_stop {
+    float offset;    /* position along the gradient, [0, 1] */
+    uint32_t color;  /* RGBA8, red in the low byte */
+} pf_color_stop;
+
+typedef struct pf_paint {
+    uint32_t type;        /* PF_PAINT_*                                              */
+    uint32_t wrap;        /* PF_WRAP_*                                               */
+    uint32_t stop_first;  /* the colour stops, in the order Gradient::add_color_stop  */
+    uint32_t stop_count;  /* receives them: stops[stop_first, stop_first + count)      */
+    float line[4];        /* from.x, from.y, to.x, to.y                               */
+    float radii[2];       /* PF_PAINT_RADIAL: r0, r1                                   */
+    float transform[6];   /* PF_PAINT_RADIAL: m11, m21, m12, m22, m13, m23 (x' = m11 x +
+                             m12 y + m13); the identity is {1, 0, 0, 1, 0, 0}            */
+} pf_paint;
+
 /* Point flags (pathfinder/core/data/data.h:120-129). */
 #define PF_POINT_ON_CURVE 0u
 #define PF_POINT_CONTROL_0 1u
@@ -112,6 +142,9 @@ typedef struct pf_stroke {
  *                 closing join when the contour is stroked; fills close every contour
  *   dashes        [n_dashes]: the dash patterns the strokes refer to; finite, >= 0, and each
  *                 pattern's total > 0
+ *   path_paint    [n_paths] or NULL (every path solid): each path's paint; a gradient path's
+ *                 colour entry is ignored (its base colour is opaque white, as from_gradient's)
+ *   stops         [n_stops]: the colour stops the gradients refer to
  */
 typedef struct pf_scene_view {
     const float *points;
@@ -132,6 +165,9 @@ typedef struct pf_scene_view {
     const uint8_t *contour_closed;  /* ABI 3 */
     const float *dashes;            /* ABI 3 */
     uint32_t n_dashes;              /* ABI 3 */
+    const pf_paint *path_paint;     /* ABI 4 */
+    const pf_color_stop *stops;     /* ABI 4 */
+    uint32_t n_stops;               /* ABI 4 */
 } pf_scene_view;
 
 /* Context configuration.  Zero-initialise and set what you need. */

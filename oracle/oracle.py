@@ -36,7 +36,7 @@ class SceneView(C.Structure):
         ("width", C.c_float), ("height", C.c_float), ("clear_color", C.c_uint32),
         ("path_clip", C.c_void_p), ("path_is_clip", C.c_void_p),
         ("path_stroke", C.c_void_p), ("contour_closed", C.c_void_p), ("dashes", C.c_void_p),
-        ("n_dashes", C.c_uint32),
+        ("n_dashes", C.c_uint32), ("path_paint", C.c_void_p), ("stops", C.c_void_p), ("n_stops", C.c_uint32),
     ]
 
 
@@ -87,6 +87,13 @@ def scene_view(scene) -> "tuple[SceneView, list]":
             d = np.ascontiguousarray(scene.dashes, np.float32)
             v.dashes, v.n_dashes = d.ctypes.data, len(d)
             arrs.append(d)
+    if getattr(scene, "path_paint", None) is not None:
+        pp = np.ascontiguousarray(scene.path_paint)
+        if pp.dtype.itemsize != 64:
+            raise ValueError("path_paint must use scenes.PAINT_DTYPE (pf_paint)")
+        st_ = np.ascontiguousarray(scene.stops)
+        v.path_paint, v.stops, v.n_stops = pp.ctypes.data, st_.ctypes.data, len(st_)
+        arrs += [pp, st_]
     return v, arrs
 
 
@@ -174,6 +181,47 @@ def stroke_scene(scene, reference: bool = False):
                 C.CDLL(None).free(C.c_void_p(getattr(o, name)))
         else:
             lib.pfo_outline_free(C.byref(o))
+
+
+class ColorStop(C.Structure):
+    _fields_ = [("offset", C.c_float), ("color", C.c_uint32)]
+
+
+def _ramps(scene, fn) -> np.ndarray:
+    """[n_paths, 256] ramps of the gradient paths (zeros for solid paths)."""
+    out = np.zeros((scene.n_paths, 256), np.uint32)
+    pp = getattr(scene, "path_paint", None)
+    if pp is None:
+        return out
+    stops = np.ascontiguousarray(scene.stops)
+    for p in range(scene.n_paths):
+        if pp[p]["type"] == 0:
+            continue
+        first, n = int(pp[p]["stop_first"]), int(pp[p]["stop_count"])
+        arr = (ColorStop * max(n, 1))(*[ColorStop(float(stops[first + i]["offset"]), int(stops[first + i]["color"]))
+                                        for i in range(n)])
+        ramp = (C.c_uint32 * 256)()
+        fn(arr, n, ramp)
+        out[p] = np.frombuffer(ramp, np.uint32)
+    return out
+
+
+def ramps(scene) -> np.ndarray:
+    """The restated gradient ramps (pf_paint.c)."""
+    return _ramps(scene, _lib(LIB_ORACLE).pfo_gradient_ramp)
+
+
+def reference_ramps(scene) -> np.ndarray:
+    """The reference's own Gradient ramps (GradientTileBuilder::allocate's sampling)."""
+    return _ramps(scene, _lib(LIB_REF).pfref_gradient_ramp)
+
+
+def half_trunc(values, reference: bool = False) -> np.ndarray:
+    """umHalf's float -> half -> float round trip (restated, or the reference's own)."""
+    lib = _lib(LIB_REF if reference else LIB_ORACLE)
+    fn = lib.pfref_half if reference else lib.pfo_half_trunc
+    fn.restype, fn.argtypes = C.c_float, [C.c_float]
+    return np.array([fn(float(v)) for v in np.asarray(values, np.float32)], np.float32)
 
 
 def fill_scene(scene):

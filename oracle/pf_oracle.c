@@ -451,6 +451,13 @@ static int validate(const pf_scene_view *s) {
     for (uint32_t c = 0; c < s->n_contours; c++)
         if (s->contour_start[c] > s->contour_start[c + 1]) return 1;
     if (!(s->width > 0.0f) || !(s->height > 0.0f)) return 1;
+    for (uint32_t p = 0; s->path_paint && p < s->n_paths; p++) {
+        const pf_paint *pp = &s->path_paint[p];
+        if (pp->type > PF_PAINT_RADIAL || pp->wrap > PF_WRAP_REPEAT) return 1;
+        if (pp->type != PF_PAINT_SOLID && ((uint64_t)pp->stop_first + pp->stop_count > s->n_stops ||
+                                           (pp->stop_count && !s->stops)))
+            return 1;
+    }
     if (s->path_clip || s->path_is_clip) {
         /* clip paths follow the draw paths, are not clipped, and draw paths name clip paths */
         if (!s->path_clip || !s->path_is_clip) return 1;
@@ -631,7 +638,7 @@ int pfo_tile_scene_mt(const pf_scene_view *s, int z_rule, int threads, pfo_resul
     out->z = (int32_t *)malloc(sizeof(int32_t) * (nfb ? nfb : 1));
     for (size_t i = 0; i < nfb; i++) out->z[i] = -1;
     for (uint32_t p = 0; p < n; p++) {
-        const int occludes = ((s->color[p] >> 24) & 0xffu) == 0xffu;
+        const int occludes = pfo_paint_is_opaque(s, p);  /* PaintMetadata::is_opaque */
         if (!occludes || is_clip_path(s, p)) continue;
         const path_ctx *pc = &pcs[p];
         const uint64_t tb = out->path_tile_first[p];
@@ -802,6 +809,8 @@ typedef struct {
     float *cov_out;
     uint32_t w, h;
     size_t first, step;
+    const uint32_t *ramps;      /* [n_paths][256] gradient ramps (gradient paths only) */
+    const float *meta;          /* [n_paths][12] their half-float metadata */
 } render_job;
 
 static void *render_worker(void *arg) {
@@ -833,9 +842,20 @@ static void *render_worker(void *arg) {
                 for (int k = 0; k < 256; k++) cov[k] = 1.0;
             }
             const uint32_t c = j->s->color[p];
-            const double pr = (c & 0xffu) / 255.0, pg = ((c >> 8) & 0xffu) / 255.0,
-                         pb = ((c >> 16) & 0xffu) / 255.0, pa = ((c >> 24) & 0xffu) / 255.0;
+            double pr = (c & 0xffu) / 255.0, pg = ((c >> 8) & 0xffu) / 255.0, pb = ((c >> 16) & 0xffu) / 255.0,
+                   pa = ((c >> 24) & 0xffu) / 255.0;
+            const pf_paint *pp = j->s->path_paint ? &j->s->path_paint[p] : NULL;
+            const int grad = pp && pp->type != PF_PAINT_SOLID;
             for (int k = 0; k < 256; k++) {
+                if (grad) {  /* tile.comp: the ramp's colour (SrcIn over the white base colour) */
+                    double g[4];
+                    pfo_paint_color(pp, j->meta + 12 * (size_t)p, j->ramps + 256 * (size_t)p,
+                                    fx * 16.0 + (k & 15) + 0.5, fy * 16.0 + (k >> 4) + 0.5, g);
+                    pr = g[0];
+                    pg = g[1];
+                    pb = g[2];
+                    pa = g[3];
+                }
                 const double a = pa * cov[k];
                 dest[k][0] = dest[k][0] * (1.0 - a) + pr * a;
                 dest[k][1] = dest[k][1] * (1.0 - a) + pg * a;
@@ -884,6 +904,19 @@ int pfo_render(const pf_scene_view *s, const pfo_result *r, uint8_t *rgba, float
     for (uint64_t t = 0; t < nt; t++) fill_first[t + 1] = fill_first[t] + r->tile_fill_count[t];
     for (uint32_t p = 0; p < r->n_paths; p++)
         for (uint64_t t = r->path_tile_first[p]; t < r->path_tile_first[p + 1]; t++) tile_path[t] = p;
+    uint32_t *ramps = NULL;
+    float *meta = NULL;
+    if (s->path_paint) {
+        ramps = (uint32_t *)calloc((size_t)r->n_paths * 256, sizeof(uint32_t));
+        meta = (float *)calloc((size_t)r->n_paths * 12, sizeof(float));
+        if (!ramps || !meta) return 1;
+        for (uint32_t p = 0; p < r->n_paths; p++) {
+            const pf_paint *pp = &s->path_paint[p];
+            if (pp->type == PF_PAINT_SOLID) continue;
+            pfo_gradient_ramp(s->stops + pp->stop_first, pp->stop_count, ramps + 256 * (size_t)p);
+            pfo_paint_meta(pp, meta + 12 * (size_t)p);
+        }
+    }
     if (threads < 1) threads = 1;
     render_job *jobs = (render_job *)calloc((size_t)threads, sizeof(render_job));
     pthread_t *th = (pthread_t *)calloc((size_t)threads, sizeof(pthread_t));
@@ -895,6 +928,8 @@ int pfo_render(const pf_scene_view *s, const pfo_result *r, uint8_t *rgba, float
         j->tile_path = tile_path;
         j->rgba = rgba;
         j->cov_out = coverage_f;
+        j->ramps = ramps;
+        j->meta = meta;
         j->w = (uint32_t)ceilf(s->width);
         j->h = (uint32_t)ceilf(s->height);
         j->first = (size_t)t;
@@ -916,5 +951,7 @@ int pfo_render(const pf_scene_view *s, const pfo_result *r, uint8_t *rgba, float
     free(th);
     free(fill_first);
     free(tile_path);
+    free(ramps);
+    free(meta);
     return 0;
 }

@@ -97,10 +97,25 @@ int pfo_stroke_scene(const pf_scene_view *scene, pfo_outline *out);
 int pfo_stroke_check(const pf_scene_view *scene);
 void pfo_outline_free(pfo_outline *o);
 
+/*
+ * Gradient paints (pf_paint.c): umHalf's truncating float -> half -> float round trip, the
+ * 256-texel ramp of a gradient's stops (bit-exact), whether a path's paint is opaque, the
+ * half-float metadata the shader reads and the straight-alpha colour at a pixel centre.
+ */
+float pfo_half_trunc(float f);
+void pfo_gradient_ramp(const pf_color_stop *stops, uint32_t n, uint32_t *ramp);
+int pfo_paint_is_opaque(const pf_scene_view *s, uint32_t p);
+void pfo_paint_meta(const pf_paint *pp, float meta[12]);
+void pfo_paint_color(const pf_paint *pp, const float meta[12], const uint32_t *ramp, double x, double y,
+                     double out[4]);
+
 /* Reference harness (oracle/_ref/libpfref.so): same output, z rule D3D9. */
 int pfref_tile_scene(const pf_scene_view *scene, pfo_result *out);
 /* The reference's own OutlineDash + OutlineStrokeToFill over the same scene. */
 int pfref_stroke_scene(const pf_scene_view *scene, pfo_outline *out);
+/* The reference's Gradient (add_color_stop, sample) for a ramp, and umHalf's round trip. */
+void pfref_gradient_ramp(const pf_color_stop *stops, uint32_t n, uint32_t *ramp);
+float pfref_half(float f);
 void pfref_free(pfo_result *r);
 
 #ifdef __cplusplus

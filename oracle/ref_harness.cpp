@@ -22,8 +22,11 @@
 #include "core/d3d9/scene_builder.h"
 #include "core/d3d9/tiler.h"
 #include "core/dash.h"
+#include "core/paint/gradient.h"
+#include "core/paint/paint.h"
 #include "core/scene.h"
 #include "core/stroke.h"
+#include <umHalf.h>
 
 #include "pf_oracle.h"
 
@@ -267,6 +270,16 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
         BuiltDrawPath bdp;
         bdp.path = bp;
         bdp.occludes = ((sv->color[p] >> 24) & 0xffu) == 0xffu;
+        if (sv->path_paint && sv->path_paint[p].type != PF_PAINT_SOLID) {
+            // PaintMetadata::is_opaque of a gradient paint (Paint::is_opaque, paint.cpp:9-19)
+            const pf_paint &pp = sv->path_paint[p];
+            const LineSegmentF line(pp.line[0], pp.line[1], pp.line[2], pp.line[3]);
+            Gradient g = pp.type == PF_PAINT_LINEAR ? Gradient::linear(line)
+                                                    : Gradient::radial(line, Vec2F(pp.radii[0], pp.radii[1]));
+            for (uint32_t i = 0; i < pp.stop_count; i++)
+                g.add_color_stop(ColorU(sv->stops[pp.stop_first + i].color), sv->stops[pp.stop_first + i].offset);
+            bdp.occludes = Paint::from_gradient(g).is_opaque();
+        }
         bdp.color_texture_info = nullptr;
         built[p] = bdp;
     }
@@ -414,6 +427,20 @@ extern "C" int pfref_stroke_scene(const pf_scene_view *sv, pfo_outline *out) {
     out->fill_rule = dup(rule);
     return 0;
 }
+
+// The reference's Gradient over the stops in order, sampled the way GradientTileBuilder::
+// allocate fills a ramp row (pathfinder/core/paint/gradient.cpp:61-110).
+extern "C" void pfref_gradient_ramp(const pf_color_stop *stops, uint32_t n, uint32_t *ramp) {
+    Gradient g = Gradient::linear(LineSegmentF());
+    for (uint32_t i = 0; i < n; i++) g.add_color_stop(ColorU(stops[i].color), stops[i].offset);
+    for (uint32_t x = 0; x < GRADIENT_TILE_LENGTH; x++) {
+        const ColorU c = g.sample(((float)x + 0.5f) / GRADIENT_TILE_LENGTH);
+        ramp[x] = uint32_t(c.r_) | uint32_t(c.g_) << 8 | uint32_t(c.b_) << 16 | uint32_t(c.a_) << 24;
+    }
+}
+
+// umHalf's float -> half -> float, as the metadata texture stores values.
+extern "C" float pfref_half(float f) { return float(half(f)); }
 
 extern "C" void pfref_free(pfo_result *r) {
     if (!r) return;

@@ -88,6 +88,10 @@ struct Ctx {
     DevBuf dash_pts, dash_cnt, dash_end, dash_points, dash_flags, job_first, jobs, job_pts, st_bounds;
     DevBuf job_units, job_nfwd, job_flags, job_cap1, job_end, units, unit_leaves, st_leaves, leaf_pts;
     uint32_t stroke_jobs = 0, stroke_dash_points = 0;  // of the last upload with strokes
+    // gradient paints: per uploaded path its gradient (kNone: solid), per gradient its paint,
+    // sorted stops, ramp and shader metadata; empty when the batch has no gradient
+    DevBuf path_grad, grad_paint, grad_stop_range, grad_stops, grad_meta, grad_ramp;
+    uint32_t n_grads = 0;
     pf_upload_stats ustats{};
     cudaEvent_t sev[8] = {};  // stroke pass timing (stage timing on)
     uint32_t n_scenes = 0, n_paths = 0, n_contours = 0, n_points = 0, n_fb = 0;
@@ -219,6 +223,23 @@ int validate_scene(Ctx *c, const pf_scene_view *s) {
             if (!(total > 0.0f) || !std::isfinite(total) || !std::isfinite(st.dash_offset))
                 return fail(c, PF_ERR_INVALID_ARGUMENT, "a dash pattern needs a finite positive total and phase");
         }
+    }
+    for (uint32_t p = 0; s->path_paint && p < s->n_paths; p++) {
+        // Paint::from_gradient (core/paint/paint.h:87-95)
+        const pf_paint &pp = s->path_paint[p];
+        if (pp.type > PF_PAINT_RADIAL || pp.wrap > PF_WRAP_REPEAT)
+            return fail(c, PF_ERR_INVALID_ARGUMENT, "unknown paint type or wrap mode");
+        if (pp.type == PF_PAINT_SOLID) continue;
+        if ((pp.stop_count && !s->stops) || uint64_t(pp.stop_first) + pp.stop_count > s->n_stops)
+            return fail(c, PF_ERR_INVALID_ARGUMENT, "a gradient's stops lie outside the stops array");
+        for (uint32_t i = 0; i < pp.stop_count; i++)
+            if (!std::isfinite(s->stops[pp.stop_first + i].offset))
+                return fail(c, PF_ERR_INVALID_ARGUMENT, "gradient stop offsets must be finite");
+        bool finite = true;
+        for (float v : pp.line) finite &= std::isfinite(v);
+        for (float v : pp.radii) finite &= std::isfinite(v);
+        for (float v : pp.transform) finite &= std::isfinite(v);
+        if (!finite) return fail(c, PF_ERR_INVALID_ARGUMENT, "gradient geometry must be finite");
     }
     if (s->path_clip || s->path_is_clip) {
         // Scene::push_draw_path / push_clip_path: clip paths come after every draw path, are not
@@ -618,6 +639,56 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
         PF_CUDA(cudaMemcpyAsync(c->path_is_clip.p, c->h_path_is_clip.data(), N, cudaMemcpyHostToDevice, c->stream));
     }
 
+    // gradient paints: the stops sorted as Gradient::add inserts them (before the first stop
+    // whose offset is not smaller), then ramps and metadata on the device
+    c->n_grads = 0;
+    {
+        std::vector<uint32_t> pg;
+        std::vector<pf_paint> gp;
+        std::vector<uint2> gr;
+        std::vector<pf_color_stop> gs;
+        for (uint32_t i = 0; i < n; i++) {
+            const pf_scene_view &s = scenes[i];
+            for (uint32_t p = 0; s.path_paint && p < s.n_paths; p++) {
+                const pf_paint &pp = s.path_paint[p];
+                if (pp.type == PF_PAINT_SOLID) continue;
+                if (pg.empty()) pg.assign(N, kNone);
+                pg[c->h_scenes[i].path_first + p] = (uint32_t)gp.size();
+                gp.push_back(pp);
+                const size_t first = gs.size();
+                for (uint32_t k = 0; k < pp.stop_count; k++) {
+                    const pf_color_stop stop = s.stops[pp.stop_first + k];
+                    size_t at = first;
+                    while (at < gs.size() && gs[at].offset < stop.offset) at++;
+                    gs.insert(gs.begin() + at, stop);
+                }
+                gr.push_back(make_uint2((uint32_t)first, pp.stop_count));
+            }
+        }
+        if (!gp.empty()) {
+            const size_t G = gp.size();
+            if (gs.empty()) gs.push_back(pf_color_stop{0.0f, 0u});
+            PF_CUDA(c->path_grad.ensure(size_t(N) * 4 + 16));
+            PF_CUDA(c->grad_paint.ensure(G * sizeof(pf_paint)));
+            PF_CUDA(c->grad_stop_range.ensure(G * 8));
+            PF_CUDA(c->grad_stops.ensure(gs.size() * sizeof(pf_color_stop)));
+            PF_CUDA(c->grad_meta.ensure(G * 64));
+            PF_CUDA(c->grad_ramp.ensure(G * 1024));
+            PF_CUDA(cudaMemcpyAsync(c->path_grad.p, pg.data(), size_t(N) * 4, cudaMemcpyHostToDevice, c->stream));
+            PF_CUDA(cudaMemcpyAsync(c->grad_paint.p, gp.data(), G * sizeof(pf_paint), cudaMemcpyHostToDevice,
+                                    c->stream));
+            PF_CUDA(cudaMemcpyAsync(c->grad_stop_range.p, gr.data(), G * 8, cudaMemcpyHostToDevice, c->stream));
+            PF_CUDA(cudaMemcpyAsync(c->grad_stops.p, gs.data(), gs.size() * sizeof(pf_color_stop),
+                                    cudaMemcpyHostToDevice, c->stream));
+            PF_CUDA(launch_gradients(c->grad_paint.as<pf_paint>(), c->grad_stop_range.as<uint2>(),
+                                     c->grad_stops.as<pf_color_stop>(), (uint32_t)G, c->grad_meta.as<float4>(),
+                                     c->grad_ramp.as<uint32_t>(), c->stream));
+            c->n_grads = (uint32_t)G;
+            // the staging vectors leave scope: wait for their copies
+            PF_CUDA(cudaStreamSynchronize(c->stream));
+        }
+    }
+
     // stroke outlines are filled nonzero (Canvas::stroke_path)
     std::vector<uint8_t> rules;
     if (strokes) {
@@ -685,6 +756,9 @@ Batch make_batch(Ctx *c) {
     b.path_clip_cat = clips ? c->path_clip.as<uint32_t>() : nullptr;
     b.path_is_clip_cat = clips ? c->path_is_clip.as<uint8_t>() : nullptr;
     b.path_clip_rel = clips ? c->path_clip_rel.as<uint32_t>() : nullptr;
+    b.path_grad = c->n_grads ? c->path_grad.as<uint32_t>() : nullptr;
+    b.grad_meta = c->n_grads ? c->grad_meta.as<float4>() : nullptr;
+    b.grad_ramp = c->n_grads ? c->grad_ramp.as<uint32_t>() : nullptr;
     b.n_scenes_all = c->n_scenes;
     b.scene_base = c->r_first;
     b.n_scenes = c->r_count;
@@ -1510,7 +1584,8 @@ int pf_ctx_destroy(void *ctx) {
                       &c->st_dashes, &c->st_scenes, &c->st_cfirst, &c->dash_pts, &c->dash_cnt, &c->dash_end,
                       &c->dash_points, &c->dash_flags, &c->job_first, &c->jobs, &c->job_pts, &c->st_bounds,
                       &c->job_units, &c->job_nfwd, &c->job_flags, &c->job_cap1, &c->job_end, &c->units,
-                      &c->unit_leaves, &c->st_leaves, &c->leaf_pts};
+                      &c->unit_leaves, &c->st_leaves, &c->leaf_pts, &c->path_grad, &c->grad_paint,
+                      &c->grad_stop_range, &c->grad_stops, &c->grad_meta, &c->grad_ramp};
     for (DevBuf *b : bufs) b->release();
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);

@@ -84,6 +84,11 @@ struct Batch {
                                          // no clip paths in the batch)
     const uint8_t *path_is_clip_cat;     // per uploaded path: 1 for a clip path
     uint32_t *path_clip_rel;             // [n_paths] the clip path within the frame, kNone
+    const uint32_t *path_grad;           // per uploaded path: its gradient, kNone (or null: no
+                                         // gradients in the batch)
+    const float4 *grad_meta;             // [gradients][4]: the shader's half-float metadata (3 x 4
+                                         // floats) and (type, wrap, opaque, -) as bits
+    const uint32_t *grad_ramp;           // [gradients][256] RGBA8 ramps
     const SceneDev *scenes;
     const uint32_t *scene_path_first;    // [n_scenes_all + 1]
     const uint32_t *scene_contour_first; // [n_scenes_all + 1]
@@ -241,6 +246,11 @@ cudaError_t launch_job_totals(const StrokeIn &in, uint32_t *status, cudaStream_t
 cudaError_t launch_outline_starts(const StrokeIn &in, const SceneDev *out_scenes, uint32_t *cstart,
                                   uint32_t *pstart, cudaStream_t st);
 cudaError_t launch_scene_bounds(const StrokeIn &in, uint32_t *out, cudaStream_t st);
+
+// Gradient paints at upload (pf_paint.cu): per gradient its ramp and shader metadata from its
+// sorted stops (stop_range[g] = first, count into stops) and its pf_paint.
+cudaError_t launch_gradients(const pf_paint *paints, const uint2 *stop_range, const pf_color_stop *stops,
+                             uint32_t n, float4 *meta, uint32_t *ramps, cudaStream_t st);
 
 // Stage launchers (all asynchronous on the given stream).
 cudaError_t launch_normalize(const Batch &b, uint2 *path_contours, cudaStream_t st);

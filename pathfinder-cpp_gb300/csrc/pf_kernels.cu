@@ -83,7 +83,11 @@ __global__ void k_normalize_paths(Batch b, uint2 *path_contours) {
     for (uint32_t c = c0; c < c1; c++) b.contour_path[c] = p;
     PathDev P{};
     P.scene = s;
-    P.flags = (b.fill_rule[pg] ? 1u : 0u) | (((b.color[pg] >> 24) == 0xffu) ? 2u : 0u);
+    // occludes: an opaque paint (PaintMetadata::is_opaque): an opaque colour, or a gradient
+    // whose stops are all opaque
+    bool opaque = (b.color[pg] >> 24) == 0xffu;
+    if (b.path_grad && b.path_grad[pg] != kNone) opaque = __float_as_uint(b.grad_meta[4 * b.path_grad[pg] + 3].z) != 0;
+    P.flags = (b.fill_rule[pg] ? 1u : 0u) | (opaque ? 2u : 0u);
     if (b.path_clip_cat) {
         // clip paths are tiled like the others but never drawn; a clipped path's clip is in its
         // scene, addressed here within the frame
@@ -1617,10 +1621,63 @@ __device__ __forceinline__ uint32_t fill_begin(const Batch &b, uint32_t p, uint3
     return gt == b.path_tiles[p] ? b.path_fill[p] : b.tile_fills[gt - 1];
 }
 
-// kClip: the batch has clip paths (a variant of its own, so that the clip code's registers
-// cost batches without clips nothing)
-template <bool kClip>
-__global__ void __launch_bounds__(kCompWarps * 32, (kClip ? 24 : 32) / kCompWarps) k_composite(Batch b) {
+// The colour (straight alpha) a gradient gives the pixel centred at (x, y): tile.comp's colour
+// texture coordinate (computeTileVaryings, tile.comp:694-724: the half-float transform times
+// the pixel centre), filterRadialGradient (tile.comp:319-347) for radial gradients, then a
+// linearly filtered fetch of the 256-texel ramp (clamped, or repeated for PF_WRAP_REPEAT).
+__device__ __forceinline__ float4 gradient_color(const Batch &b, uint32_t g, float x, float y) {
+    const float4 *m = b.grad_meta + 4 * g;
+    const float4 m0 = m[0], m1 = m[1], m3 = m[3];
+    const uint32_t type = __float_as_uint(m3.x);
+    const bool repeat = __float_as_uint(m3.y) == PF_WRAP_REPEAT;
+    float u;
+    if (type == PF_PAINT_LINEAR) {
+        u = m0.x * x + m0.z * y + m1.x;
+    } else {
+        const float4 m2 = m[2];
+        const float cx = m0.x * x + m0.z * y + m1.x, cy = m0.y * x + m0.w * y + m1.y;
+        const float dpx = cx - m1.z, dpy = cy - m1.w, dcx = m2.x, dcy = m2.y;
+        const float r0 = m2.z, dr = m2.w - r0;
+        const float a = dcx * dcx + dcy * dcy - dr * dr;
+        const float bb = dpx * dcx + dpy * dcy + r0 * dr;
+        const float c = dpx * dpx + dpy * dpy - r0 * r0;
+        const float disc = bb * bb - a * c;
+        if (!(disc > 0.0f)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // no real t (or the shader's 0)
+        const float sq = sqrtf(disc);
+        float t0 = (sq + bb) / a, t1 = (-sq + bb) / a;
+        if (t0 > t1) {
+            const float tmp = t0;
+            t0 = t1;
+            t1 = tmp;
+        }
+        u = t0 >= 0.0f ? t0 : t1;
+    }
+    if (!isfinite(u)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (repeat) u -= floorf(u);
+    const float s = u * 256.0f - 0.5f, f0 = floorf(s), f = s - f0;
+    int i0 = (int)fmaxf(fminf(f0, 1e9f), -1e9f), i1 = i0 + 1;
+    if (repeat) {
+        i0 &= 255;
+        i1 &= 255;
+    } else {
+        i0 = min(max(i0, 0), 255);
+        i1 = min(max(i1, 0), 255);
+    }
+    const uint32_t *ramp = b.grad_ramp + 256 * (size_t)g;
+    const uint32_t p0 = __ldg(ramp + i0), p1 = __ldg(ramp + i1);
+    const float inv = 1.0f / 255.0f;
+    float4 o;
+    o.x = ((float)(p0 & 0xffu) + ((float)(p1 & 0xffu) - (float)(p0 & 0xffu)) * f) * inv;
+    o.y = ((float)((p0 >> 8) & 0xffu) + ((float)((p1 >> 8) & 0xffu) - (float)((p0 >> 8) & 0xffu)) * f) * inv;
+    o.z = ((float)((p0 >> 16) & 0xffu) + ((float)((p1 >> 16) & 0xffu) - (float)((p0 >> 16) & 0xffu)) * f) * inv;
+    o.w = ((float)(p0 >> 24) + ((float)(p1 >> 24) - (float)(p0 >> 24)) * f) * inv;
+    return o;
+}
+
+// kClip: the batch has clip paths; kPaint: it has gradient paints (variants of their own, so
+// that their code's registers cost batches without them nothing)
+template <bool kClip, bool kPaint>
+__global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 32) / kCompWarps) k_composite(Batch b) {
     __shared__ int cells[kCompWarps][kCovCells];
     __shared__ FillPrep prep[kCompWarps][32];
     __shared__ int park[kCompWarps][8][32];  // kMaskBoth: the clip tile's |coverage|
@@ -1693,11 +1750,20 @@ __global__ void __launch_bounds__(kCompWarps * 32, (kClip ? 24 : 32) / kCompWarp
                 coverage_rule(raw, eo, cov);
             }
             const uint32_t color = v.color;
-            const float pr = (float)(color & 0xffu) * inv255, pg = (float)((color >> 8) & 0xffu) * inv255,
-                        pb = (float)((color >> 16) & 0xffu) * inv255, pa = (float)(color >> 24) * inv255;
+            float pr = (float)(color & 0xffu) * inv255, pg = (float)((color >> 8) & 0xffu) * inv255,
+                  pb = (float)((color >> 16) & 0xffu) * inv255, pa = (float)(color >> 24) * inv255;
+            const uint32_t grad = kPaint ? b.path_grad[b.path_base + v.p] : kNone;
             bool opaque = true;
 #pragma unroll
             for (int k = 0; k < 8; k++) {
+                if (kPaint && grad != kNone) {  // SrcIn over the opaque white base colour
+                    const float4 g = gradient_color(b, grad, (float)(fx * 16 + col) + 0.5f,
+                                                    (float)(fy * 16 + h * 8 + k) + 0.5f);
+                    pr = g.x;
+                    pg = g.y;
+                    pb = g.z;
+                    pa = g.w;
+                }
                 const float a = pa * cov[k], w = tr[k] * a;
                 ar[k] += w * pr;
                 ag[k] += w * pg;
@@ -1938,10 +2004,15 @@ cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st) {
 
 cudaError_t launch_composite(const Batch &b, cudaStream_t st) {
     if (b.n_fb) {
-        if (b.path_clip_cat)
-            PF_LAUNCH(k_composite<true><<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
+        const unsigned grid = grid_for(b.n_fb, kCompWarps);
+        if (b.path_clip_cat && b.path_grad)
+            PF_LAUNCH(k_composite<true, true><<<grid, kCompWarps * 32, 0, st>>>(b));
+        else if (b.path_clip_cat)
+            PF_LAUNCH(k_composite<true, false><<<grid, kCompWarps * 32, 0, st>>>(b));
+        else if (b.path_grad)
+            PF_LAUNCH(k_composite<false, true><<<grid, kCompWarps * 32, 0, st>>>(b));
         else
-            PF_LAUNCH(k_composite<false><<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
+            PF_LAUNCH(k_composite<false, false><<<grid, kCompWarps * 32, 0, st>>>(b));
     }
     return cudaGetLastError();
 }

@@ -53,7 +53,7 @@ class SceneView(C.Structure):
         ("width", C.c_float), ("height", C.c_float), ("clear_color", C.c_uint32),
         ("path_clip", C.c_void_p), ("path_is_clip", C.c_void_p),
         ("path_stroke", C.c_void_p), ("contour_closed", C.c_void_p), ("dashes", C.c_void_p),
-        ("n_dashes", C.c_uint32),
+        ("n_dashes", C.c_uint32), ("path_paint", C.c_void_p), ("stops", C.c_void_p), ("n_stops", C.c_uint32),
     ]
 
 
@@ -157,6 +157,13 @@ def scene_view(scene) -> "tuple[SceneView, list]":
         d = np.ascontiguousarray(scene.dashes, np.float32)
         v.dashes, v.n_dashes = d.ctypes.data, len(d)
         arrs.append(d)
+    if getattr(scene, "path_paint", None) is not None:
+        pp = np.ascontiguousarray(scene.path_paint)
+        if pp.dtype.itemsize != 64:
+            raise ValueError("path_paint must use scenes.PAINT_DTYPE (pf_paint)")
+        st_ = np.ascontiguousarray(scene.stops)
+        v.path_paint, v.stops, v.n_stops = pp.ctypes.data, st_.ctypes.data, len(st_)
+        arrs += [pp, st_]
     return v, arrs
 
 

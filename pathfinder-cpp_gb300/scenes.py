@@ -36,6 +36,12 @@ STROKE_DTYPE = np.dtype([("line_width", "<f4"), ("miter_limit", "<f4"), ("line_c
                          ("line_join", "u1"), ("reserved", "<u2"), ("dash_first", "<u4"),
                          ("dash_count", "<u4"), ("dash_offset", "<f4")])
 CAP_BUTT, CAP_SQUARE, CAP_ROUND = 0, 1, 2
+# pf_paint / pf_color_stop (include/pfcuda.h): gradient paints
+PAINT_DTYPE = np.dtype([("type", "<u4"), ("wrap", "<u4"), ("stop_first", "<u4"), ("stop_count", "<u4"),
+                        ("line", "<f4", (4,)), ("radii", "<f4", (2,)), ("transform", "<f4", (6,))])
+STOP_DTYPE = np.dtype([("offset", "<f4"), ("color", "<u4")])
+PAINT_SOLID, PAINT_LINEAR, PAINT_RADIAL = 0, 1, 2
+WRAP_CLAMP, WRAP_REPEAT = 0, 1
 JOIN_MITER, JOIN_BEVEL, JOIN_ROUND = 0, 1, 2
 
 _GOLDEN = np.uint64(0x9E3779B97F4A7C15)
@@ -104,6 +110,8 @@ class Scene:
     path_stroke: Optional[np.ndarray] = None   # STROKE_DTYPE [N]: how each path is stroked
     contour_closed: Optional[np.ndarray] = None  # uint8 [C] Contour::closed (strokes only)
     dashes: Optional[np.ndarray] = None        # float32 [D] dash patterns of the strokes
+    path_paint: Optional[np.ndarray] = None    # PAINT_DTYPE [N]: solid or gradient paint per path
+    stops: Optional[np.ndarray] = None         # STOP_DTYPE [S] colour stops of the gradients
 
     @property
     def n_paths(self) -> int:
@@ -473,6 +481,69 @@ def batched_stroked(n_scenes: int = 512, first_seed: int = 1000, lo_paths: int =
         side = int(sides[int(rng.integers(0, len(sides) - 1, 1)[0])])
         out.append(stroked(seed=first_seed + i, n_paths=n, side=side, dash_share=dash_share))
     return out
+
+
+def with_gradients(sc: Scene, seed: int, share: float = 0.5) -> Scene:
+    """`sc` with a share of its paths painted with gradients (Paint::from_gradient): half
+    linear, half radial (two circles, a quarter of them under a rotation and scale), 2-5 stops
+    (unsorted, sometimes repeated offsets, 40 % of the gradients with translucent stops), 30 %
+    repeating.  Geometry is drawn around each path's bounding box."""
+    rng = Rng(seed, 9)
+    n = sc.n_paths
+    pts = sc.points.astype(np.float64)
+    cs, ps = sc.contour_start.astype(np.int64), sc.path_start.astype(np.int64)
+    pt_first, pt_end = cs[ps[:-1]], cs[ps[1:]]
+    grad = rng.uniform(n) < share
+    kind = np.where(rng.uniform(n) < 0.5, PAINT_LINEAR, PAINT_RADIAL)
+    wrap = np.where(rng.uniform(n) < 0.3, WRAP_REPEAT, WRAP_CLAMP)
+    nstops = rng.integers(2, 5, n)
+    translucent = rng.uniform(n) < 0.4
+    paint = np.zeros(n, PAINT_DTYPE)
+    paint["transform"] = [1, 0, 0, 1, 0, 0]
+    stops = []
+    u = rng.uniform(8 * n).reshape(n, 8)
+    for p in range(n):
+        if not grad[p] or pt_end[p] == pt_first[p]:
+            continue
+        q = pts[pt_first[p]:pt_end[p]]
+        lo, hi = q.min(axis=0), q.max(axis=0)
+        size = np.maximum(hi - lo, 1.0)
+        a = lo + u[p, 0:2] * size
+        b = lo + u[p, 2:4] * size
+        paint[p]["type"] = kind[p]
+        paint[p]["wrap"] = wrap[p]
+        paint[p]["stop_first"] = len(stops)
+        paint[p]["stop_count"] = nstops[p]
+        paint[p]["line"] = [a[0], a[1], b[0], b[1]]
+        if kind[p] == PAINT_RADIAL:
+            r1 = 0.1 * size.max() + u[p, 4] * size.max()
+            paint[p]["radii"] = [u[p, 5] * 0.3 * r1, r1]
+            if u[p, 6] < 0.25:  # a rotation and scale about the first centre
+                c, s_ = 0.8 + 0.4 * u[p, 7], 0.5 * u[p, 6]
+                paint[p]["transform"] = [c, s_, -s_, c, a[0] - c * a[0] + s_ * a[1], a[1] - s_ * a[0] - c * a[1]]
+        offs = rng.uniform(int(nstops[p]))
+        if nstops[p] > 2 and u[p, 7] < 0.2:
+            offs[1] = offs[0]
+        cols = rng.integers(0, 0xFFFFFF, int(nstops[p])).astype(np.uint32)
+        alpha = np.where(translucent[p] & (rng.uniform(int(nstops[p])) < 0.6),
+                         (rng.uniform(int(nstops[p])) * 200 + 30).astype(np.uint32), 255)
+        for o_, c_, a_ in zip(offs, cols, alpha):
+            stops.append((o_, int(c_) | (int(a_) << 24)))
+    out = dataclasses.replace(sc)
+    out.path_paint = paint
+    out.stops = np.asarray(stops if stops else [(0.0, 0)], STOP_DTYPE)
+    return out
+
+
+def gradient_scene(seed: int = 0, n_paths: int = 240, side: int = 1024, share: float = 0.6) -> Scene:
+    """Large paths (scenes.large_single's families) with gradient paints."""
+    return with_gradients(large_single(seed=seed, n_paths=n_paths, side=side), seed, share)
+
+
+def batched_gradients(n_scenes: int = 512, first_seed: int = 1000, share: float = 0.5, **kw) -> List[Scene]:
+    """The batched scenes with gradient paints on a share of the paths."""
+    return [with_gradients(sc, first_seed + i, share)
+            for i, sc in enumerate(batched(n_scenes=n_scenes, first_seed=first_seed, **kw))]
 
 
 def mixed(seed: int = 7, n_paths: int = 8192, side: int = 4096) -> Scene:

@@ -40,11 +40,15 @@ def load_golden(name):
                  path_is_clip=d["path_is_clip"] if "path_is_clip" in d else None,
                  path_stroke=d["path_stroke"] if "path_stroke" in d else None,
                  contour_closed=d["contour_closed"] if "contour_closed" in d else None,
-                 dashes=d["dashes"] if "dashes" in d else None)
+                 dashes=d["dashes"] if "dashes" in d else None,
+                 path_paint=d["path_paint"] if "path_paint" in d else None,
+                 stops=d["stops"] if "stops" in d else None)
     ref = {k: d["ref_" + k] for k in CANON_KEYS}
     for k in OUTLINE_KEYS:
         if "out_" + k in d:
             ref["out_" + k] = d["out_" + k]
+    if "ref_ramps" in d:
+        ref["ramps"] = d["ref_ramps"]
     return sc, ref
 
 

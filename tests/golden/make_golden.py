@@ -38,6 +38,7 @@ CANON_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha",
 INPUT_KEYS = ["points", "flags", "contour_start", "path_start", "fill_rule", "color"]
 CLIP_KEYS = ["path_clip", "path_is_clip"]  # stored when the scene has clip paths
 STROKE_KEYS = ["path_stroke", "contour_closed", "dashes"]  # stored when the scene has strokes
+PAINT_KEYS = ["path_paint", "stops"]  # stored when the scene has gradient paints (with ref_ramps)
 # the reference's stroke outline (OutlineDash + OutlineStrokeToFill), stored as out_<key>
 OUTLINE_KEYS = ["points", "flags", "contour_start", "path_start", "fill_rule"]
 
@@ -259,6 +260,51 @@ def stroke_scenes():
     return out
 
 
+def with_paints(sc: S.Scene, paints) -> S.Scene:
+    """paints: per path None (solid) or (type, wrap, stops [(offset, rgba)], line, radii, transform)."""
+    pp = np.zeros(sc.n_paths, S.PAINT_DTYPE)
+    pp["transform"] = [1, 0, 0, 1, 0, 0]
+    stops = []
+    for p, paint in enumerate(paints):
+        if paint is None:
+            continue
+        kind, wrap, st, line, radii, xf = paint
+        pp[p]["type"], pp[p]["wrap"] = kind, wrap
+        pp[p]["stop_first"], pp[p]["stop_count"] = len(stops), len(st)
+        pp[p]["line"], pp[p]["radii"] = line, radii
+        if xf is not None:
+            pp[p]["transform"] = xf
+        stops.extend((o, int(S.pack_rgba(*c))) for o, c in st)
+    sc.path_paint = pp
+    sc.stops = np.asarray(stops if stops else [(0.0, 0)], S.STOP_DTYPE)
+    return sc
+
+
+def gradient_scenes():
+    """Gradient paints (Paint::from_gradient): linear and radial, clamped and repeated, opaque
+    and translucent stops, unsorted and repeated offsets, a transformed radial gradient."""
+    L, R, C, P = S.PAINT_LINEAR, S.PAINT_RADIAL, S.WRAP_CLAMP, S.WRAP_REPEAT
+    red, green, blue, white = (255, 0, 0, 255), (0, 160, 0, 255), (0, 0, 255, 255), (255, 255, 255, 255)
+    half = (20, 40, 200, 128)
+    out = {}
+    rects = [poly(4, 4, 60, 4, 60, 60, 4, 60), poly(68, 4, 124, 4, 124, 60, 68, 60),
+             poly(4, 68, 60, 68, 60, 124, 4, 124), poly(68, 68, 124, 68, 124, 124, 68, 124),
+             poly(30, 30, 98, 40, 64, 100)]
+    out["grad_linear"] = with_paints(build_scene([([r], 0, white) for r in rects], 128, 128, clear=0xff202020), [
+        (L, C, [(0.0, red), (1.0, blue)], [4, 0, 60, 0], [0, 0], None),
+        (L, P, [(0.5, green), (0.0, red), (1.0, blue)], [70, 6, 90, 30], [0, 0], None),
+        (L, C, [(0.2, half), (0.8, (200, 200, 0, 60))], [4, 124, 60, 68], [0, 0], None),
+        (L, C, [(0.3, red), (0.3, green), (0.7, blue)], [68, 68, 124, 124], [0, 0], None),
+        (L, C, [(0.5, (255, 128, 0, 200))], [30, 30, 98, 100], [0, 0], None)])
+    out["grad_radial"] = with_paints(build_scene([([r], 0, white) for r in rects], 128, 128, clear=0xff000000), [
+        (R, C, [(0.0, white), (1.0, blue)], [32, 32, 32, 32], [0, 28], None),
+        (R, P, [(0.0, red), (0.5, green), (1.0, red)], [96, 32, 100, 28], [0, 12], None),
+        (R, C, [(0.0, half), (1.0, (250, 250, 250, 40))], [20, 100, 44, 90], [6, 30], None),
+        (R, C, [(0.0, green), (1.0, red)], [96, 96, 96, 96], [0, 24], [0.8, 0.45, -0.45, 0.8, 60.0, -24.0]),
+        (R, P, [(0.0, blue), (1.0, white)], [64, 64, 70, 60], [10, 40], None)])
+    return out
+
+
 def generator_scenes():
     return {
         "gen_plain_small_s1": S.plain_small(seed=1, n_paths=24, side=256),
@@ -268,6 +314,7 @@ def generator_scenes():
         "gen_batched_scene_s5": S.batched(n_scenes=3, first_seed=5, hi_paths=64)[2],
         "gen_clipped_s6": S.clipped(seed=6, n_paths=60, side=256, n_clips=4),
         "gen_stroked_s7": S.stroked(seed=7, n_paths=40, side=256, dash_share=0.4, fill_share=0.2),
+        "gen_gradient_s8": S.gradient_scene(seed=8, n_paths=60, side=256),
     }
 
 
@@ -295,6 +342,7 @@ def main() -> None:
     small = dict(edge_scenes())
     small.update(clip_scenes())
     small.update(stroke_scenes())
+    small.update(gradient_scenes())
     small.update(generator_scenes())
     for name, sc in small.items():
         ref = oracle.reference_tile_scene(sc)
@@ -305,6 +353,9 @@ def main() -> None:
             arrays.update({k: getattr(sc, k) for k in STROKE_KEYS})
             outline = oracle.stroke_scene(sc, reference=True)
             arrays.update({"out_" + k: getattr(outline, k) for k in OUTLINE_KEYS})
+        if sc.path_paint is not None:
+            arrays.update({k: getattr(sc, k) for k in PAINT_KEYS})
+            arrays["ref_ramps"] = oracle.reference_ramps(sc)
         arrays["meta"] = np.asarray([sc.width, sc.height, sc.clear], np.float64)
         for k in CANON_KEYS:
             arrays["ref_" + k] = ref[k]

@@ -1,0 +1,120 @@
+"""Gradient paints on the GPU against the oracle.
+
+A gradient path is filled with its 256-texel ramp (the reference's GradientTileBuilder rows,
+bit-exact in the oracle) sampled per pixel as tile.comp samples its colour texture, from the
+half-float metadata the reference's RGBA16F texture holds.  Tile data stays bit-exact (a
+gradient occludes when all its stops are opaque).  Pixels: the composite works in float, the
+oracle in double; both follow the same formulas.  Linear gradients are continuous in the pixel
+centre, so they stay within one RGBA8 code.  A radial gradient has two discontinuities of its
+own (the discriminant's sign, and the choice between the two roots where the smaller one
+crosses zero), where float and double may fall on different sides: pixels within a small
+distance of those edges may differ by more, and there are few of them.
+"""
+import numpy as np
+import pytest
+
+import scenes as S
+from conftest import TILE_KEYS, load_golden
+
+pytestmark = pytest.mark.gpu
+
+LIST_KEYS = ["fb_tiles", "z", "fb_list_first", "fb_list"]
+PIXEL_TOL = 1
+RADIAL_EDGE_SHARE = 2e-3   # pixels beyond PIXEL_TOL allowed in scenes with radial gradients
+
+
+def _pixels(img, ref, radial, label):
+    diff = np.abs(img.astype(np.int32) - ref.astype(np.int32)).max(axis=2)
+    over = int((diff > PIXEL_TOL).sum())
+    print(f"{label}: pixel max err {diff.max()}, {over} of {diff.size} beyond {PIXEL_TOL}")
+    if radial:
+        assert over <= RADIAL_EDGE_SHARE * diff.size
+    else:
+        assert over == 0
+
+
+def _has_radial(sc):
+    return bool(np.any(sc.path_paint["type"] == S.PAINT_RADIAL))
+
+
+@pytest.mark.parametrize("name", ["grad_linear", "grad_radial", "gen_gradient_s8"])
+def test_gradient_fixture_tiles_and_pixels(renderer, oracle_mod, name):
+    sc, ref = load_golden(name)
+    renderer.upload(sc)
+    renderer.render()
+    got, img = renderer.canon(), renderer.image()
+    for k in TILE_KEYS:
+        assert np.array_equal(got[k], ref[k]), k
+    want, _ = oracle_mod.render(sc, threads=8)
+    _pixels(img, want, _has_radial(sc), name)
+
+
+@pytest.mark.parametrize("seed,n_paths,side", [(61, 300, 1024), (62, 1200, 2048)])
+def test_gradient_scene_tiles_and_pixels(renderer, oracle_mod, seed, n_paths, side):
+    sc = S.gradient_scene(seed=seed, n_paths=n_paths, side=side)
+    renderer.upload(sc)
+    renderer.render()
+    got, img = renderer.canon(), renderer.image()
+    want = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D11, threads=8)
+    for k in TILE_KEYS + LIST_KEYS:
+        assert np.array_equal(got[k], want[k]), k
+    ref, _ = oracle_mod.render(sc, threads=16)
+    _pixels(img, ref, _has_radial(sc), f"gradient s{seed}")
+
+
+def test_linear_gradients_only_within_one_code(renderer, oracle_mod):
+    sc = S.gradient_scene(seed=63, n_paths=400, side=1024, share=0.8)
+    sc.path_paint["type"][sc.path_paint["type"] == S.PAINT_RADIAL] = S.PAINT_LINEAR
+    renderer.upload(sc)
+    renderer.render()
+    ref, _ = oracle_mod.render(sc, threads=16)
+    _pixels(renderer.image(), ref, False, "linear only")
+
+
+def test_batch_mixing_gradients_strokes_clips(renderer):
+    scs = [S.gradient_scene(seed=71, n_paths=200, side=512), S.stroked(seed=72, n_paths=80, side=512),
+           S.clipped(seed=73, n_paths=120, side=512), S.with_gradients(S.plain_small(seed=74, n_paths=60, side=256), 74)]
+    renderer.upload(scs)
+    renderer.render()
+    batch = [(renderer.canon(i), renderer.image(i)) for i in range(len(scs))]
+    for i, sc in enumerate(scs):
+        renderer.upload(sc)
+        renderer.render()
+        for k in TILE_KEYS + LIST_KEYS:
+            assert np.array_equal(batch[i][0][k], renderer.canon()[k]), (i, k)
+        assert np.array_equal(batch[i][1], renderer.image())
+
+
+def test_learned_frame_with_gradients_equals_exact(pf):
+    scs = S.batched_gradients(n_scenes=4, first_seed=81, hi_paths=300)
+    with pf.Renderer(device=0) as r:
+        r.upload(scs)
+        r.sizer_load()
+        r.render()
+        exact = [r.image(i) for i in range(len(scs))]
+        for _ in range(3):
+            assert r.render_learned()["overflow"] == 0
+            for i in range(len(scs)):
+                assert np.array_equal(r.image(i), exact[i])
+
+
+def test_invalid_paints_are_rejected(renderer, pf):
+    sc = S.gradient_scene(seed=91, n_paths=20, side=256, share=1.0)
+    g = int(np.nonzero(sc.path_paint["type"] > 0)[0][0])
+    cases = []
+    for field, value in (("type", 7), ("wrap", 2), ("stop_first", len(sc.stops))):
+        pp = sc.path_paint.copy()
+        pp[field][g] = value
+        cases.append(S.Scene(**{**sc.__dict__, "path_paint": pp}))
+    pp = sc.path_paint.copy()
+    pp["line"][g][0] = np.nan
+    cases.append(S.Scene(**{**sc.__dict__, "path_paint": pp}))
+    st = sc.stops.copy()
+    st["offset"][0] = np.inf
+    cases.append(S.Scene(**{**sc.__dict__, "stops": st}))
+    for bad in cases:
+        with pytest.raises(pf.PfError) as e:
+            renderer.upload(bad)
+        assert e.value.status == 1
+    renderer.upload(sc)
+    renderer.render()

@@ -57,6 +57,31 @@ def test_stroke_layout_checks(oracle_mod):
         oracle_mod.stroke_scene(S.Scene(**{**sc.__dict__, "path_stroke": st}))
 
 
+GRADIENT = [n for n in golden_names() if n.startswith("grad_") or n.startswith("gen_gradient")]
+
+
+@pytest.mark.parametrize("name", GRADIENT)
+def test_restated_gradient_ramps_match_reference_golden(oracle_mod, name):
+    """GradientTileBuilder's ramp rows (Gradient::add / sample, ColorF lerp, 8-bit truncation),
+    restated, against the reference's own stored ramps."""
+    sc, ref = load_golden(name)
+    assert np.array_equal(oracle_mod.ramps(sc), ref["ramps"])
+
+
+def test_restated_gradients_and_half_floats_match_live_reference(oracle_mod):
+    import scenes as S
+    if not oracle_mod.have_reference():
+        pytest.skip("reference harness not built")
+    rng = np.random.default_rng(5)
+    vals = np.concatenate([rng.standard_normal(4000) * 10 ** rng.uniform(-9, 6, 4000),
+                           [0.0, -0.0, 65504.0, 7e4, 1e-8, -3e-6, np.inf, -np.inf, np.nan]]).astype(np.float32)
+    a, b = oracle_mod.half_trunc(vals), oracle_mod.half_trunc(vals, reference=True)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    sc = S.gradient_scene(seed=31, n_paths=150, side=512, share=1.0)
+    assert np.array_equal(oracle_mod.ramps(sc), oracle_mod.reference_ramps(sc))
+    assert oracle_mod.compare(oracle_mod.tile_scene(sc, oracle_mod.Z_D3D9), oracle_mod.reference_tile_scene(sc)) == []
+
+
 def _digest(a):
     a = np.ascontiguousarray(a)
     return hashlib.sha256(a.dtype.str.encode() + str(a.shape).encode() + a.tobytes()).hexdigest()
