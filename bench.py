@@ -65,6 +65,9 @@ def parse_args():
     ap.add_argument("--strokes", action="store_true",
                     help="the batched scenes as stroked paths (scenes.batched_stroked: 30%% dashed); the upload "
                          "strokes them on the GPU, and the line reports that stage too")
+    ap.add_argument("--gradients", action="store_true",
+                    help="the batched scenes with half of the paths painted with gradients "
+                         "(scenes.batched_gradients: linear and radial, clamped and repeated)")
     ap.add_argument("--clips", type=int, default=0,
                     help="clip paths per scene (0: none): the batched scenes with that many clip shapes "
                          "each, 60%% of the draw paths clipped")
@@ -79,12 +82,14 @@ def make_scenes(args, first_seed):
     import scenes as S
     if args.strokes:
         return S.batched_stroked(n_scenes=args.scenes, first_seed=first_seed)
+    if args.gradients:
+        return S.batched_gradients(n_scenes=args.scenes, first_seed=first_seed)
     if args.clips > 0:
         return S.batched_clipped(n_scenes=args.scenes, first_seed=first_seed, n_clips=args.clips)
     return S.batched(n_scenes=args.scenes, first_seed=first_seed)
 
 
-def workload_config(n_scenes, scenes_list, clips=0, strokes=False):
+def workload_config(n_scenes, scenes_list, clips=0, strokes=False, gradients=False):
     import numpy as np
     desc = ("batched: %d scenes, paths/scene log-uniform 16-4096 (cubic 8-24 seg, control points "
             "uniform over the canvas), canvas side in {256,512,1024,2048}, seeds 1000+i" % n_scenes)
@@ -93,6 +98,8 @@ def workload_config(n_scenes, scenes_list, clips=0, strokes=False):
                 "{256,512,1024,2048}, seeds 1000+i; every path stroked (1-3 contours of 1-12 line/quad/cubic "
                 "segments in a log-uniform box, 40%% closed, width 0.5-24 px, caps/joins uniform), 30%% "
                 "dashed" % n_scenes)
+    if gradients:
+        desc += "; half of the paths painted with gradients (linear and radial, 2-5 stops, 30%% repeating)"
     if clips:
         desc += "; %d clip paths per scene (cubic 3-8 seg, a quarter to a whole canvas wide), 60%% of the " \
                 "draw paths clipped" % clips
@@ -174,13 +181,16 @@ def pack_pinned(scenes_list):
         keys += [("path_clip", np.uint32), ("path_is_clip", np.uint8)]
     if has("path_stroke"):
         keys += [("path_stroke", S.STROKE_DTYPE), ("contour_closed", np.uint8), ("dashes", np.float32)]
+    if has("path_paint"):
+        keys += [("path_paint", S.PAINT_DTYPE), ("stops", S.STOP_DTYPE)]
 
     def field(s, k):
         a = getattr(s, k)
         if a is None:  # a scene without clips or strokes in a batch with some
             defaults = {"path_clip": np.full(s.n_paths, 0xFFFFFFFF, np.uint32),
                         "path_stroke": np.zeros(s.n_paths, S.STROKE_DTYPE),
-                        "contour_closed": np.zeros(s.n_contours, np.uint8), "dashes": np.zeros(0, np.float32)}
+                        "contour_closed": np.zeros(s.n_contours, np.uint8), "dashes": np.zeros(0, np.float32),
+                        "path_paint": np.zeros(s.n_paths, S.PAINT_DTYPE), "stops": np.zeros(0, S.STOP_DTYPE)}
             a = defaults.get(k, np.zeros(s.n_paths, np.uint8))
         return a
 
@@ -205,6 +215,8 @@ def pack_pinned(scenes_list):
         if "path_stroke" in ptrs:
             v.path_stroke, v.contour_closed, v.dashes = ptrs["path_stroke"], ptrs["contour_closed"], ptrs["dashes"]
             v.n_dashes = len(field(s, "dashes"))
+        if "path_paint" in ptrs:
+            v.path_paint, v.stops, v.n_stops = ptrs["path_paint"], ptrs["stops"], len(field(s, "stops"))
         views.append(v)
     h2d = sum(offs.values())
     return bufs, views, h2d
@@ -244,7 +256,7 @@ def run_reference(args, scenes_list):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 tiling, f64 coverage",
-        "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list, args.clips, args.strokes),
+        "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list, args.clips, args.strokes, args.gradients),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -464,7 +476,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_batched, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (exact-IEEE tiling), int32 fixed-point coverage", "data": "synthetic",
-            "config": workload_config(n_scenes, scenes_list, args.clips, args.strokes) | {"parallelism": f"replicas x{world}"},
+            "config": workload_config(n_scenes, scenes_list, args.clips, args.strokes, args.gradients) | {"parallelism": f"replicas x{world}"},
             "frame": "batched learned one-pass" if learned else "batched exact two-pass",
             "batched_exact": {"value": world * n_scenes / (ms_exact * 1e-3), "unit": UNIT, "ms_per_step": ms_exact},
             "plain": {"value": world * n_scenes / (ms_plain * 1e-3), "unit": UNIT, "ms_per_step": ms_plain,
