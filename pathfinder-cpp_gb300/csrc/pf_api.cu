@@ -87,6 +87,7 @@ struct Ctx {
     DevBuf in_points, in_pflags, in_cstart, in_pstart, st_stroke, st_closed, st_dashes, st_scenes, st_cfirst;
     DevBuf dash_pts, dash_cnt, dash_end, dash_points, dash_flags, job_first, jobs, job_pts, st_bounds;
     DevBuf job_units, job_nfwd, job_flags, job_cap1, job_end, units, unit_leaves, st_leaves, leaf_pts;
+    DevBuf st_order_ctl, unit_order, dash_order;
     uint32_t stroke_jobs = 0, stroke_dash_points = 0;  // of the last upload with strokes
     // gradient paints: per uploaded path its gradient (kNone: solid), per gradient its paint,
     // sorted stops, ramp and shader metadata; empty when the batch has no gradient
@@ -369,9 +370,16 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
     in.job_first = c->job_first.as<uint32_t>();
     PF_CUDA(c->scan_temp.ensure(scan_temp_bytes(N + 1)));
 
-    // dashing: counts, offsets, the dashed contours
+    PF_CUDA(c->st_order_ctl.ensure(stroke_order_ctl_bytes()));
+    // dashing: counts, offsets, the dashed contours (the dashed paths taken longest first)
     if (dashed) {
         PF_CUDA(mark(0));
+        PF_CUDA(c->dash_order.ensure(size_t(N) * 4 + 16));
+        PF_CUDA(cudaMemsetAsync(in.dash_pts, 0, size_t(N) * 4, st));
+        PF_CUDA(cudaMemsetAsync(in.dash_cnt, 0, size_t(N) * 4, st));
+        PF_CUDA(launch_stroke_order(in, 1, c->st_order_ctl.as<uint32_t>(), c->dash_order.as<uint32_t>(), st));
+        in.dash_order = c->dash_order.as<uint32_t>();
+        in.n_dashed = c->ustats.dashed_paths;
         PF_CUDA(launch_dash(in, false, status, st));
         PF_CUDA(scan_exclusive_u32(in.dash_pts, in.dash_pts, N, in.dash_pts + N, c->scan_temp.p, st, status));
         PF_CUDA(scan_exclusive_u32(in.dash_cnt, in.dash_cnt, N, in.dash_cnt + N, c->scan_temp.p, st, status));
@@ -449,9 +457,12 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
     in.n_units = U;
     in.units = c->units.as<float4>();
     in.unit_leaves = c->unit_leaves.as<uint32_t>();
-    // leaves: the offset recursion of every unit
+    // leaves: the offset recursion of every unit (units taken most work first)
+    PF_CUDA(c->unit_order.ensure(size_t(U) * 4 + 16));
     PF_CUDA(mark(4));
     PF_CUDA(launch_units(in, true, st));
+    PF_CUDA(launch_stroke_order(in, 0, c->st_order_ctl.as<uint32_t>(), c->unit_order.as<uint32_t>(), st));
+    in.unit_order = c->unit_order.as<uint32_t>();
     PF_CUDA(launch_unit_leaves(in, false, st));
     PF_CUDA(scan_exclusive_u32(in.unit_leaves, in.unit_leaves, U, in.unit_leaves + U, c->scan_temp.p, st, status));
     uint32_t NL = 0;
@@ -1585,7 +1596,8 @@ int pf_ctx_destroy(void *ctx) {
                       &c->dash_points, &c->dash_flags, &c->job_first, &c->jobs, &c->job_pts, &c->st_bounds,
                       &c->job_units, &c->job_nfwd, &c->job_flags, &c->job_cap1, &c->job_end, &c->units,
                       &c->unit_leaves, &c->st_leaves, &c->leaf_pts, &c->path_grad, &c->grad_paint,
-                      &c->grad_stop_range, &c->grad_stops, &c->grad_meta, &c->grad_ramp};
+                      &c->grad_stop_range, &c->grad_stops, &c->grad_meta, &c->grad_ramp, &c->st_order_ctl,
+                      &c->unit_order, &c->dash_order};
     for (DevBuf *b : bufs) b->release();
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);

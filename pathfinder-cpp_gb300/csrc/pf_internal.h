@@ -234,7 +234,12 @@ struct StrokeIn {
     uint32_t *unit_leaves;              // [n_units + 1] counts -> scanned
     float4 *leaves;                     // [n_leaves][3] piece, join point, (job, meta)
     uint32_t *leaf_pts;                 // [n_leaves + 1] counts -> scanned
+    const uint32_t *unit_order;         // [n_units] units, the most work first (or null)
+    const uint32_t *dash_order;         // [n_dashed] the dashed paths, the most work first
+    uint32_t n_dashed;
 };
+size_t stroke_order_ctl_bytes();
+cudaError_t launch_stroke_order(const StrokeIn &in, int what, uint32_t *ctl, uint32_t *order, cudaStream_t st);
 cudaError_t launch_dash(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);
 cudaError_t launch_stroke_jobs(const StrokeIn &in, bool fill, cudaStream_t st);
 cudaError_t launch_stroke(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);

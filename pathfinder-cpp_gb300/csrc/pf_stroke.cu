@@ -547,10 +547,12 @@ __device__ __forceinline__ uint2 path_contours(const StrokeIn &in, uint32_t p) {
 // dash_pts[p] / dash_cnt[p] (scanned), their ends in dash_end.
 template <bool kWrite>
 __global__ void k_dash(StrokeIn in, uint32_t *status) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= in.n_paths) return;
+    // the dashed paths, largest first (dash_order); every other path's counts are zeroed
+    // before the count pass
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= in.n_dashed) return;
+    const uint32_t p = in.dash_order[t];
     const pf_stroke &st = path_stroke(in, p);
-    if (!kWrite) in.dash_pts[p] = in.dash_cnt[p] = 0;  // also what a failed path leaves
     if (!stroked(in, p) || st.dash_count == 0) return;
     // DashState::DashState, dash.cpp:9-29
     const float *dashes = in.dashes + st.dash_first;
@@ -839,8 +841,9 @@ __global__ void k_units(StrokeIn in) {
 // kind | direction << 2 | (unit index > 0) << 3.  An invalid leaf marks the job.
 template <bool kWrite>
 __global__ void __launch_bounds__(128) k_unit_leaves(StrokeIn in) {
-    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= in.n_units) return;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= in.n_units) return;
+    const uint32_t u = in.unit_order ? in.unit_order[t] : t;
     uint4 um;
     const Seg root = get_seg(in.units + 3 * (size_t)u, um);
     const uint32_t job = um.y, dir = um.z >> 31, idx = um.z & 0x7fffffffu;
@@ -1096,6 +1099,83 @@ __global__ void k_job_totals(StrokeIn in, uint32_t *status) {
         atomicAdd(reinterpret_cast<unsigned long long *>(status + kStFill64 + 2), n);
 }
 
+// --- Work ordering ---------------------------------------------------------------------------
+// A warp's lanes run their items in step, so a warp takes as long as its longest item.  Items
+// are bucketed by an estimate of their work, largest first: units by kind and the flatness of
+// their control polygon (lines split never; curves split more the more they bend), dashed paths
+// by their point count.  A fixed grid counts the buckets per block in shared memory, a single
+// block turns the counts into each block's first slot, and the grid places the items.
+constexpr int kOrderBuckets = 16;
+constexpr int kOrderBlocks = 608;  // 4 per SM of 152
+
+__device__ __forceinline__ int unit_bucket(const StrokeIn &in, uint32_t u) {
+    uint4 m;
+    const Seg s = get_seg(in.units + 3 * (size_t)u, m);
+    if (s.kind == kLine) return 0;
+    const V2 p0 = s.b.f, p3 = s.b.t, c0 = s.c.f;
+    const V2 c1 = s.kind == kQuad ? s.c.f : s.c.t;
+    const float ux = 3.0f * c0.x - 2.0f * p0.x - p3.x, uy = 3.0f * c0.y - 2.0f * p0.y - p3.y;
+    const float vx = 3.0f * c1.x - 2.0f * p3.x - p0.x, vy = 3.0f * c1.y - 2.0f * p3.y - p0.y;
+    const float f = fmaxf(ux * ux, vx * vx) + fmaxf(uy * uy, vy * vy);
+    if (!(f > 1.0f)) return 1;
+    const int d = 1 + (int)ceilf(__log2f(f) * 0.25f);
+    return d < kOrderBuckets - 1 ? d : kOrderBuckets - 1;
+}
+
+__device__ __forceinline__ int dash_bucket(const StrokeIn &in, uint32_t p) {
+    if (!stroked(in, p) || path_stroke(in, p).dash_count == 0) return -1;
+    const uint2 kr = path_contours(in, p);
+    uint32_t pts = 0;
+    for (uint32_t k = kr.x; k < kr.y; k++) pts += raw_contour(in, k).n;
+    const int d = pts ? 32 - __clz(pts) : 0;
+    return d < kOrderBuckets - 1 ? d : kOrderBuckets - 1;
+}
+
+// kWhat 0: units, 1: dashed paths.  ctl[kOrderBuckets * block + bucket].
+template <int kWhat, bool kScatter>
+__global__ void __launch_bounds__(256) k_order(StrokeIn in, uint32_t *ctl, uint32_t *order) {
+    __shared__ uint32_t s_cnt[kOrderBuckets];
+    const uint32_t n = kWhat == 0 ? in.n_units : in.n_paths;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < kOrderBuckets) s_cnt[threadIdx.x] = kScatter ? ctl[kOrderBuckets * blockIdx.x + threadIdx.x] : 0u;
+    __syncthreads();
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const int bk = i < n ? (kWhat == 0 ? unit_bucket(in, i) : dash_bucket(in, i)) : -1;
+        const unsigned group = __match_any_sync(0xffffffffu, bk);
+        const int leader = __ffs(group) - 1;
+        uint32_t slot = 0;
+        if (bk >= 0 && lane == leader) slot = atomicAdd(&s_cnt[bk], (uint32_t)__popc(group));
+        slot = __shfl_sync(0xffffffffu, slot, leader);
+        if (kScatter && bk >= 0) order[slot + __popc(group & ((1u << lane) - 1u))] = i;
+    }
+    __syncthreads();
+    if (!kScatter && threadIdx.x < kOrderBuckets) ctl[kOrderBuckets * blockIdx.x + threadIdx.x] = s_cnt[threadIdx.x];
+}
+
+// Each block's first slot per bucket, largest bucket first; ctl[kOrderBuckets * kOrderBlocks]
+// receives the number of items placed.
+__global__ void k_order_starts(uint32_t *ctl) {
+    __shared__ uint32_t total[kOrderBuckets];
+    const int bk = threadIdx.x;
+    if (bk < kOrderBuckets) {
+        uint32_t t = 0;
+        for (int blk = 0; blk < kOrderBlocks; blk++) t += ctl[kOrderBuckets * blk + bk];
+        total[bk] = t;
+    }
+    __syncthreads();
+    if (bk < kOrderBuckets) {
+        uint32_t run = 0;
+        for (int d = kOrderBuckets - 1; d > bk; d--) run += total[d];
+        for (int blk = 0; blk < kOrderBlocks; blk++) {
+            const uint32_t c = ctl[kOrderBuckets * blk + bk];
+            ctl[kOrderBuckets * blk + bk] = run;
+            run += c;
+        }
+        if (bk == 0) ctl[kOrderBuckets * kOrderBlocks] = run;
+    }
+}
+
 // The new outline's per-scene offset arrays (the layout the upload uses: scene s's contour
 // offsets at cstart_base = its first contour + s, path offsets at pstart_base).
 __global__ void k_outline_starts(StrokeIn in, const SceneDev *out_scenes, uint32_t *cstart, uint32_t *pstart) {
@@ -1133,10 +1213,30 @@ __global__ void k_scene_bounds(StrokeIn in, uint32_t *out) {
 static uint32_t blocks(uint32_t n, uint32_t t) { return (n + t - 1) / t; }
 
 cudaError_t launch_dash(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st) {
-    if (!in.n_paths) return cudaSuccess;
-    if (write) k_dash<true><<<blocks(in.n_paths, 128), 128, 0, st>>>(in, status);
-    else k_dash<false><<<blocks(in.n_paths, 128), 128, 0, st>>>(in, status);
+    if (!in.n_dashed) return cudaSuccess;
+    if (write) k_dash<true><<<blocks(in.n_dashed, 64), 64, 0, st>>>(in, status);
+    else k_dash<false><<<blocks(in.n_dashed, 64), 64, 0, st>>>(in, status);
     count_launches(1);
+    return cudaGetLastError();
+}
+
+size_t stroke_order_ctl_bytes() { return (size_t(kOrderBuckets) * kOrderBlocks + 1) * 4; }
+
+// what: 0 units (order: [n_units]), 1 dashed paths (order: [n_paths]; the count lands in
+// ctl[kOrderBuckets * kOrderBlocks])
+cudaError_t launch_stroke_order(const StrokeIn &in, int what, uint32_t *ctl, uint32_t *order, cudaStream_t st) {
+    if (what == 0) {
+        if (!in.n_units) return cudaSuccess;
+        k_order<0, false><<<kOrderBlocks, 256, 0, st>>>(in, ctl, order);
+        k_order_starts<<<1, 32, 0, st>>>(ctl);
+        k_order<0, true><<<kOrderBlocks, 256, 0, st>>>(in, ctl, order);
+    } else {
+        if (!in.n_paths) return cudaSuccess;
+        k_order<1, false><<<kOrderBlocks, 256, 0, st>>>(in, ctl, order);
+        k_order_starts<<<1, 32, 0, st>>>(ctl);
+        k_order<1, true><<<kOrderBlocks, 256, 0, st>>>(in, ctl, order);
+    }
+    count_launches(3);
     return cudaGetLastError();
 }
 
