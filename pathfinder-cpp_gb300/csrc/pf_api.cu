@@ -93,6 +93,7 @@ struct Ctx {
     // sorted stops, ramp and shader metadata; empty when the batch has no gradient
     DevBuf path_grad, grad_paint, grad_stop_range, grad_stops, grad_meta, grad_ramp;
     uint32_t n_grads = 0;
+    std::vector<uint32_t> h_grad_sbase;  // the scenes' first stops (kept until the upload's copies end)
     pf_upload_stats ustats{};
     cudaEvent_t sev[8] = {};  // stroke pass timing (stage timing on)
     uint32_t n_scenes = 0, n_paths = 0, n_contours = 0, n_points = 0, n_fb = 0;
@@ -233,6 +234,7 @@ int validate_scene(Ctx *c, const pf_scene_view *s) {
         if (pp.type == PF_PAINT_SOLID) continue;
         if ((pp.stop_count && !s->stops) || uint64_t(pp.stop_first) + pp.stop_count > s->n_stops)
             return fail(c, PF_ERR_INVALID_ARGUMENT, "a gradient's stops lie outside the stops array");
+        if (pp.stop_count > 1024) return fail(c, PF_ERR_INVALID_ARGUMENT, "at most 1024 stops per gradient");
         for (uint32_t i = 0; i < pp.stop_count; i++)
             if (!std::isfinite(s->stops[pp.stop_first + i].offset))
                 return fail(c, PF_ERR_INVALID_ARGUMENT, "gradient stop offsets must be finite");
@@ -650,53 +652,60 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
         PF_CUDA(cudaMemcpyAsync(c->path_is_clip.p, c->h_path_is_clip.data(), N, cudaMemcpyHostToDevice, c->stream));
     }
 
-    // gradient paints: the stops sorted as Gradient::add inserts them (before the first stop
-    // whose offset is not smaller), then ramps and metadata on the device
+    PF_CUDA(cudaMemcpyAsync(c->scene_path_first.p, spf.data(), (n + 1) * 4, cudaMemcpyHostToDevice, c->stream));
+    // gradient paints: the paths' pf_paint records and every scene's stops go to the device as
+    // given; the device numbers the gradients, orders each one's stops and builds its ramp and
+    // metadata (no host pass over stops, no extra synchronisation)
     c->n_grads = 0;
     {
-        std::vector<uint32_t> pg;
-        std::vector<pf_paint> gp;
-        std::vector<uint2> gr;
-        std::vector<pf_color_stop> gs;
+        uint64_t G = 0, S = 0;
+        std::vector<uint32_t> sbase(n + 1, 0);
+        bool any = false;
         for (uint32_t i = 0; i < n; i++) {
             const pf_scene_view &s = scenes[i];
-            for (uint32_t p = 0; s.path_paint && p < s.n_paths; p++) {
-                const pf_paint &pp = s.path_paint[p];
-                if (pp.type == PF_PAINT_SOLID) continue;
-                if (pg.empty()) pg.assign(N, kNone);
-                pg[c->h_scenes[i].path_first + p] = (uint32_t)gp.size();
-                gp.push_back(pp);
-                const size_t first = gs.size();
-                for (uint32_t k = 0; k < pp.stop_count; k++) {
-                    const pf_color_stop stop = s.stops[pp.stop_first + k];
-                    size_t at = first;
-                    while (at < gs.size() && gs[at].offset < stop.offset) at++;
-                    gs.insert(gs.begin() + at, stop);
-                }
-                gr.push_back(make_uint2((uint32_t)first, pp.stop_count));
-            }
+            sbase[i] = (uint32_t)S;
+            if (!s.path_paint) continue;
+            any = true;
+            S += s.n_stops;
+            for (uint32_t p = 0; p < s.n_paths; p++) G += s.path_paint[p].type != PF_PAINT_SOLID;
         }
-        if (!gp.empty()) {
-            const size_t G = gp.size();
-            if (gs.empty()) gs.push_back(pf_color_stop{0.0f, 0u});
+        sbase[n] = (uint32_t)S;
+        if (any && G) {
+            if (S >= (1ull << 31)) return fail(c, PF_ERR_OVERFLOW, "too many gradient stops (2^31)");
+            PF_CUDA(c->grad_paint.ensure(size_t(N) * sizeof(pf_paint) + 16));
+            PF_CUDA(c->grad_stops.ensure(size_t(S) * sizeof(pf_color_stop) + 16));
+            PF_CUDA(c->grad_stop_range.ensure((size_t(n) + 1) * 4 + 4 * (size_t(N) + 1) + 4 * G + 64));
             PF_CUDA(c->path_grad.ensure(size_t(N) * 4 + 16));
-            PF_CUDA(c->grad_paint.ensure(G * sizeof(pf_paint)));
-            PF_CUDA(c->grad_stop_range.ensure(G * 8));
-            PF_CUDA(c->grad_stops.ensure(gs.size() * sizeof(pf_color_stop)));
             PF_CUDA(c->grad_meta.ensure(G * 64));
             PF_CUDA(c->grad_ramp.ensure(G * 1024));
-            PF_CUDA(cudaMemcpyAsync(c->path_grad.p, pg.data(), size_t(N) * 4, cudaMemcpyHostToDevice, c->stream));
-            PF_CUDA(cudaMemcpyAsync(c->grad_paint.p, gp.data(), G * sizeof(pf_paint), cudaMemcpyHostToDevice,
+            CopyPlan pp, ss;
+            for (uint32_t i = 0; i < n; i++) {
+                const pf_scene_view &s = scenes[i];
+                char *dst = c->grad_paint.as<char>() + uint64_t(c->h_scenes[i].path_first) * sizeof(pf_paint);
+                if (s.path_paint) pp.add(dst, s.path_paint, uint64_t(s.n_paths) * sizeof(pf_paint));
+                else PF_CUDA(cudaMemsetAsync(dst, 0, uint64_t(s.n_paths) * sizeof(pf_paint), c->stream));
+                if (s.path_paint && s.n_stops)
+                    ss.add(c->grad_stops.as<char>() + uint64_t(sbase[i]) * sizeof(pf_color_stop), s.stops,
+                           uint64_t(s.n_stops) * sizeof(pf_color_stop));
+            }
+            PF_CUDA(pp.run(c->stream));
+            PF_CUDA(ss.run(c->stream));
+            // grad_stop_range holds the scene stop bases, the per-path gradient flags (scanned)
+            // and the gradient -> path map
+            uint32_t *bases = c->grad_stop_range.as<uint32_t>();
+            uint32_t *flags = bases + (n + 1);
+            uint32_t *grad_path = flags + (N + 1);
+            c->h_grad_sbase = sbase;
+            PF_CUDA(cudaMemcpyAsync(bases, c->h_grad_sbase.data(), (size_t(n) + 1) * 4, cudaMemcpyHostToDevice,
                                     c->stream));
-            PF_CUDA(cudaMemcpyAsync(c->grad_stop_range.p, gr.data(), G * 8, cudaMemcpyHostToDevice, c->stream));
-            PF_CUDA(cudaMemcpyAsync(c->grad_stops.p, gs.data(), gs.size() * sizeof(pf_color_stop),
-                                    cudaMemcpyHostToDevice, c->stream));
-            PF_CUDA(launch_gradients(c->grad_paint.as<pf_paint>(), c->grad_stop_range.as<uint2>(),
-                                     c->grad_stops.as<pf_color_stop>(), (uint32_t)G, c->grad_meta.as<float4>(),
-                                     c->grad_ramp.as<uint32_t>(), c->stream));
+            PF_CUDA(c->scan_temp.ensure(scan_temp_bytes(N + 1)));
+            PF_CUDA(c->status.ensure(kStCount * 4));
+            PF_CUDA(launch_gradient_index(c->grad_paint.as<pf_paint>(), N, flags, c->path_grad.as<uint32_t>(),
+                                          grad_path, c->scan_temp.p, c->status.as<uint32_t>(), c->stream));
+            PF_CUDA(launch_gradients(c->grad_paint.as<pf_paint>(), grad_path, c->scene_path_first.as<uint32_t>(),
+                                     n, bases, c->grad_stops.as<pf_color_stop>(), (uint32_t)G,
+                                     c->grad_meta.as<float4>(), c->grad_ramp.as<uint32_t>(), c->stream));
             c->n_grads = (uint32_t)G;
-            // the staging vectors leave scope: wait for their copies
-            PF_CUDA(cudaStreamSynchronize(c->stream));
         }
     }
 
@@ -725,7 +734,6 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
         col.add(c->color.as<char>() + uint64_t(S.path_first) * 4, s.color, uint64_t(s.n_paths) * 4);
     }
     for (CopyPlan *cp : {&pts, &fl, &csp, &psp, &fr, &col}) PF_CUDA(cp->run(c->stream));
-    PF_CUDA(cudaMemcpyAsync(c->scene_path_first.p, spf.data(), (n + 1) * 4, cudaMemcpyHostToDevice, c->stream));
     PF_CUDA(cudaMemcpyAsync(c->scene_fb_first.p, c->h_scene_fb_first.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
                             c->stream));
     PF_CUDA(cudaMemcpyAsync(c->scene_row_first.p, c->h_scene_row_first.data(), (n + 1) * 4, cudaMemcpyHostToDevice,

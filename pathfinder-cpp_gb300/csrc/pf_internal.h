@@ -252,10 +252,16 @@ cudaError_t launch_outline_starts(const StrokeIn &in, const SceneDev *out_scenes
                                   uint32_t *pstart, cudaStream_t st);
 cudaError_t launch_scene_bounds(const StrokeIn &in, uint32_t *out, cudaStream_t st);
 
-// Gradient paints at upload (pf_paint.cu): per gradient its ramp and shader metadata from its
-// sorted stops (stop_range[g] = first, count into stops) and its pf_paint.
-cudaError_t launch_gradients(const pf_paint *paints, const uint2 *stop_range, const pf_color_stop *stops,
-                             uint32_t n, float4 *meta, uint32_t *ramps, cudaStream_t st);
+// Gradient paints at upload (pf_paint.cu).  paints: every uploaded path's pf_paint; stops: every
+// scene's stops, scene s's from stop_base[s].  launch_gradient_index numbers the gradient paths
+// (path_grad[p], kNone for solid ones; grad_path[g]); launch_gradients orders each gradient's
+// stops as Gradient::add does and builds its ramp and shader metadata.
+constexpr uint32_t kMaxGradientStops = 1024;
+cudaError_t launch_gradient_index(const pf_paint *paints, uint32_t n_paths, uint32_t *flags, uint32_t *path_grad,
+                                  uint32_t *grad_path, void *scan_temp, uint32_t *status, cudaStream_t st);
+cudaError_t launch_gradients(const pf_paint *paints, const uint32_t *grad_path, const uint32_t *scene_path_first,
+                             uint32_t n_scenes, const uint32_t *stop_base, const pf_color_stop *stops, uint32_t n,
+                             float4 *meta, uint32_t *ramps, cudaStream_t st);
 
 // Stage launchers (all asynchronous on the given stream).
 cudaError_t launch_normalize(const Batch &b, uint2 *path_contours, cudaStream_t st);

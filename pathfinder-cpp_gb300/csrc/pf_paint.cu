@@ -49,15 +49,53 @@ __device__ float half_trunc(float f) {
     return __uint_as_float(sign | ((hexp - 15 + 127) << 23) | (hfrac << 13));
 }
 
-__global__ void __launch_bounds__(256) k_gradients(const pf_paint *paints, const uint2 *stop_range,
-                                                   const pf_color_stop *stops, uint32_t n, float4 *meta,
-                                                   uint32_t *ramps) {
+__device__ __forceinline__ uint32_t upper_bound(const uint32_t *a, uint32_t n, uint32_t v) {
+    uint32_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] <= v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_gradient_flags(const pf_paint *paints, uint32_t n, uint32_t *flags) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) flags[p] = paints[p].type != PF_PAINT_SOLID ? 1u : 0u;
+}
+
+__global__ void k_gradient_index(const pf_paint *paints, uint32_t n, const uint32_t *scanned, uint32_t *path_grad,
+                                 uint32_t *grad_path) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const bool g = paints[p].type != PF_PAINT_SOLID;
+    path_grad[p] = g ? scanned[p] : kNone;
+    if (g) grad_path[scanned[p]] = p;
+}
+
+__global__ void __launch_bounds__(256) k_gradients(const pf_paint *paints, const uint32_t *grad_path,
+                                                   const uint32_t *scene_path_first, uint32_t n_scenes,
+                                                   const uint32_t *stop_base, const pf_color_stop *stops, uint32_t n,
+                                                   float4 *meta, uint32_t *ramps) {
+    __shared__ pf_color_stop st[kMaxGradientStops];
     const uint32_t g = blockIdx.x;
     if (g >= n) return;
-    const pf_paint pp = paints[g];
-    const uint2 sr = stop_range[g];
-    const pf_color_stop *st = stops + sr.x;
-    const uint32_t cnt = sr.y;
+    const uint32_t path = grad_path[g];
+    const pf_paint pp = paints[path];
+    const uint32_t scene = upper_bound(scene_path_first, n_scenes + 1, path) - 1;
+    const pf_color_stop *src = stops + stop_base[scene] + pp.stop_first;
+    const uint32_t cnt = min(pp.stop_count, kMaxGradientStops);
+    if (threadIdx.x == 0) {
+        // Gradient::add: each stop goes before the first stop whose offset is not smaller
+        for (uint32_t i = 0; i < cnt; i++) {
+            const pf_color_stop s = src[i];
+            uint32_t at = 0;
+            while (at < i && st[at].offset < s.offset) at++;
+            for (uint32_t k = i; k > at; k--) st[k] = st[k - 1];
+            st[at] = s;
+        }
+    }
+    __syncthreads();
     // Gradient::sample((x + 0.5) / 256)
     const uint32_t x = threadIdx.x;
     float t = fd(fa((float)x, 0.5f), 256.0f);
@@ -124,10 +162,23 @@ __global__ void __launch_bounds__(256) k_gradients(const pf_paint *paints, const
 
 }  // namespace
 
-cudaError_t launch_gradients(const pf_paint *paints, const uint2 *stop_range, const pf_color_stop *stops,
-                             uint32_t n, float4 *meta, uint32_t *ramps, cudaStream_t st) {
+cudaError_t launch_gradient_index(const pf_paint *paints, uint32_t n_paths, uint32_t *flags, uint32_t *path_grad,
+                                  uint32_t *grad_path, void *scan_temp, uint32_t *status, cudaStream_t st) {
+    if (!n_paths) return cudaSuccess;
+    const uint32_t blocks = (n_paths + 255) / 256;
+    k_gradient_flags<<<blocks, 256, 0, st>>>(paints, n_paths, flags);
+    cudaError_t e = scan_exclusive_u32(flags, flags, n_paths, flags + n_paths, scan_temp, st, status + kStErr);
+    if (e != cudaSuccess) return e;
+    k_gradient_index<<<blocks, 256, 0, st>>>(paints, n_paths, flags, path_grad, grad_path);
+    count_launches(2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gradients(const pf_paint *paints, const uint32_t *grad_path, const uint32_t *scene_path_first,
+                             uint32_t n_scenes, const uint32_t *stop_base, const pf_color_stop *stops, uint32_t n,
+                             float4 *meta, uint32_t *ramps, cudaStream_t st) {
     if (!n) return cudaSuccess;
-    k_gradients<<<n, 256, 0, st>>>(paints, stop_range, stops, n, meta, ramps);
+    k_gradients<<<n, 256, 0, st>>>(paints, grad_path, scene_path_first, n_scenes, stop_base, stops, n, meta, ramps);
     count_launches(1);
     return cudaGetLastError();
 }
