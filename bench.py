@@ -71,6 +71,10 @@ def parse_args():
     ap.add_argument("--clips", type=int, default=0,
                     help="clip paths per scene (0: none): the batched scenes with that many clip shapes "
                          "each, 60%% of the draw paths clipped")
+    ap.add_argument("--svg", action="store_true",
+                    help="SVG documents: the batch is N seeded documents (svg_docs.random_document, shapes per "
+                         "document log-uniform 16-1024) parsed on the host by pf_svg_parse; the line adds an "
+                         "svg_stage whose end-to-end step parses the documents' text too")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-frames", action="store_true",
                     help="only the batched exact and learned frames (warm-up + steps each), a short summary "
@@ -78,8 +82,20 @@ def parse_args():
     return ap.parse_args()
 
 
+def svg_texts(n, first_seed):
+    """n seeded SVG documents with 16-1024 shapes each (log-uniform)."""
+    import numpy as np
+    import svg_docs
+    rng = np.random.default_rng(first_seed)
+    sizes = np.exp(rng.uniform(np.log(16), np.log(1024), n)).astype(int)
+    return [svg_docs.random_document(first_seed + i, n_shapes=int(sizes[i])) for i in range(n)]
+
+
 def make_scenes(args, first_seed):
     import scenes as S
+    if args.svg:
+        import pfcuda
+        return [pfcuda.parse_svg(t) for t in svg_texts(args.scenes, first_seed)]
     if args.strokes:
         return S.batched_stroked(n_scenes=args.scenes, first_seed=first_seed)
     if args.gradients:
@@ -89,7 +105,7 @@ def make_scenes(args, first_seed):
     return S.batched(n_scenes=args.scenes, first_seed=first_seed)
 
 
-def workload_config(n_scenes, scenes_list, clips=0, strokes=False, gradients=False):
+def workload_config(n_scenes, scenes_list, clips=0, strokes=False, gradients=False, svg=False):
     import numpy as np
     desc = ("batched: %d scenes, paths/scene log-uniform 16-4096 (cubic 8-24 seg, control points "
             "uniform over the canvas), canvas side in {256,512,1024,2048}, seeds 1000+i" % n_scenes)
@@ -98,6 +114,10 @@ def workload_config(n_scenes, scenes_list, clips=0, strokes=False, gradients=Fal
                 "{256,512,1024,2048}, seeds 1000+i; every path stroked (1-3 contours of 1-12 line/quad/cubic "
                 "segments in a log-uniform box, 40%% closed, width 0.5-24 px, caps/joins uniform), 30%% "
                 "dashed" % n_scenes)
+    if svg:
+        desc = ("svg: %d seeded SVG documents (svg_docs.random_document, seeds 1000+i, 16-1024 shapes each: "
+                "rect/circle/ellipse/line/poly/path with all path commands, nested transforms, fills, strokes "
+                "with caps/joins/dashes, linear and radial gradients), parsed by pf_svg_parse" % n_scenes)
     if gradients:
         desc += "; half of the paths painted with gradients (linear and radial, 2-5 stops, 30%% repeating)"
     if clips:
@@ -256,7 +276,7 @@ def run_reference(args, scenes_list):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 tiling, f64 coverage",
-        "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list, args.clips, args.strokes, args.gradients),
+        "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list, args.clips, args.strokes, args.gradients, args.svg),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -372,6 +392,45 @@ def main():
     for _ in range(max(1, args.warmup // 2)):
         e2e_step()
     ms_e2e, _ = timed(e2e_step, args.steps)
+
+    # SVG documents end to end (--svg): every step parses the documents' text on the host
+    # (pf_svg_parse on a thread pool; ctypes releases the interpreter lock), uploads straight
+    # from the parser's arrays, renders and delivers the images to pinned host memory
+    svg_stage = None
+    if args.svg:
+        import concurrent.futures as cf
+        texts = [t.encode() for t in svg_texts(args.scenes, replica_first_seed(rank))]
+        n_threads = min(16, os.cpu_count() or 1)
+        pool = cf.ThreadPoolExecutor(n_threads)
+        parse_ms = []
+
+        def svg_step():
+            t0 = time.perf_counter()
+            docs = list(pool.map(pfcuda.SvgDocument, texts))
+            parse_ms.append((time.perf_counter() - t0) * 1e3)
+            r.upload_views([d.view for d in docs])
+            s = frame()
+            r.read_images(img_host.data_ptr(), img_bytes)
+            for d in docs:
+                d.close()
+            return s
+        for _ in range(max(1, args.warmup // 2)):
+            svg_step()
+        parse_ms.clear()
+        ms_svg, _ = timed(svg_step, args.steps)
+        t0 = time.perf_counter()
+        for t in texts[:64]:
+            pfcuda.SvgDocument(t).close()
+        one_thread_ms = (time.perf_counter() - t0) * 1e3 * len(texts) / 64
+        mb = sum(len(t) for t in texts) / 1e6
+        svg_stage = {
+            "e2e": {"value": world * n_scenes / (ms_svg * 1e-3), "unit": UNIT, "ms_per_step": ms_svg,
+                    "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": img_bytes,
+                    "includes": "host parse of the text + pageable H2D upload + frame + images to host"},
+            "parse_ms": sum(parse_ms) / len(parse_ms), "parse_threads": n_threads,
+            "parse_ms_one_thread_est": one_thread_ms, "text_mb": mb,
+            "parse_mb_per_s": mb / (sum(parse_ms) / len(parse_ms) * 1e-3),
+        }
     r.set_host_image(None)
 
     # one more (untimed) frame with the composite's work counters on, for the roofline's bytes
@@ -476,7 +535,7 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_batched, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (exact-IEEE tiling), int32 fixed-point coverage", "data": "synthetic",
-            "config": workload_config(n_scenes, scenes_list, args.clips, args.strokes, args.gradients) | {"parallelism": f"replicas x{world}"},
+            "config": workload_config(n_scenes, scenes_list, args.clips, args.strokes, args.gradients, args.svg) | {"parallelism": f"replicas x{world}"},
             "frame": "batched learned one-pass" if learned else "batched exact two-pass",
             "batched_exact": {"value": world * n_scenes / (ms_exact * 1e-3), "unit": UNIT, "ms_per_step": ms_exact},
             "plain": {"value": world * n_scenes / (ms_plain * 1e-3), "unit": UNIT, "ms_per_step": ms_plain,
@@ -484,6 +543,7 @@ def main():
             "speedup_vs_plain": ms_plain / ms_batched,
             "sizer": sizer,
             **({"stroke_stage": stroke_stage} if stroke_stage else {}),
+            **({"svg_stage": svg_stage} if svg_stage else {}),
             "e2e": {"value": world * n_scenes / (ms_e2e * 1e-3), "unit": UNIT, "ms_per_step": ms_e2e,
                     "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": img_bytes,
                     "images": "composited into pinned host memory (pf_set_host_image)"},

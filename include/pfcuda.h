@@ -403,6 +403,21 @@ int pf_read_coverage(void *ctx, float *out, size_t capacity_floats, uint64_t *n_
 int pf_draw(void *ctx, const pf_scene_view *scene, uint8_t *rgba, size_t capacity_bytes,
             pf_frame_stats *stats);
 
+/*
+ * SVG ingestion (host only, no device): the work of SvgScene::SvgScene
+ * (pathfinder/core/svg.cpp:135-205): nanosvg's nsvgParse(text, "px", dpi) replayed through
+ * the canvas.  Each shape gives a fill path (when its fill paint is visible) and a stroke path
+ * (when its stroke paint is visible and its width positive), the stroke as the shape's
+ * contours plus a pf_stroke the upload converts on the GPU (dashes at phase 0, as
+ * Canvas::stroke_path dashes).  Colour, linear and radial gradient paints.  The text is copied;
+ * the scene's arrays belong to the pf_svg and stay valid until pf_svg_free.  width and height
+ * are the document's size in px.  A document without a shape gives a scene of no paths.
+ */
+typedef struct pf_svg pf_svg;
+int pf_svg_parse(const char *text, size_t length, float dpi, pf_svg **out);
+int pf_svg_scene(const pf_svg *svg, pf_scene_view *out);
+void pf_svg_free(pf_svg *svg);
+
 #ifdef __cplusplus
 }
 #endif

@@ -216,6 +216,49 @@ def reference_ramps(scene) -> np.ndarray:
     return _ramps(scene, _lib(LIB_REF).pfref_gradient_ramp)
 
 
+class SvgOut(C.Structure):
+    _fields_ = [("n_points", C.c_uint32), ("n_contours", C.c_uint32), ("n_paths", C.c_uint32),
+                ("n_dashes", C.c_uint32), ("n_stops", C.c_uint32), ("width", C.c_float), ("height", C.c_float),
+                ("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_start", C.c_void_p),
+                ("contour_closed", C.c_void_p), ("path_start", C.c_void_p), ("fill_rule", C.c_void_p),
+                ("color", C.c_void_p), ("path_stroke", C.c_void_p), ("dashes", C.c_void_p),
+                ("path_paint", C.c_void_p), ("stops", C.c_void_p), ("ramps", C.c_void_p)]
+
+
+def reference_svg_scene(text, dpi: float = 96.0) -> Dict[str, np.ndarray]:
+    """The reference's nanosvg + SvgScene replay of an SVG document, in the scene layout:
+    points, flags, contour_start, contour_closed, path_start, fill_rule, color, dashes (typed);
+    path_stroke, path_paint, stops as raw bytes (pf_stroke 24 B, pf_paint 64 B, pf_color_stop
+    8 B per item); ramps [n_paths, 256] of the reference's Gradient; width and height."""
+    lib = _lib(LIB_REF)
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    lib.pfref_svg_scene.argtypes = [C.c_char_p, C.c_size_t, C.c_float, C.POINTER(SvgOut)]
+    lib.pfref_svg_free.argtypes, lib.pfref_svg_free.restype = [C.POINTER(SvgOut)], None
+    o = SvgOut()
+    st = lib.pfref_svg_scene(data, len(data), dpi, C.byref(o))
+    if st != 0:
+        raise RuntimeError(f"pfref_svg_scene failed with status {st}")
+    try:
+        n_p, n_c, n_n = o.n_points, o.n_contours, o.n_paths
+        return {
+            "points": _arr(o.points, 2 * n_p, np.float32).reshape(-1, 2),
+            "flags": _arr(o.point_flags, n_p, np.uint8),
+            "contour_start": _arr(o.contour_start, n_c + 1, np.uint32),
+            "contour_closed": _arr(o.contour_closed, n_c, np.uint8),
+            "path_start": _arr(o.path_start, n_n + 1, np.uint32),
+            "fill_rule": _arr(o.fill_rule, n_n, np.uint8),
+            "color": _arr(o.color, n_n, np.uint32),
+            "dashes": _arr(o.dashes, o.n_dashes, np.float32),
+            "path_stroke": _arr(o.path_stroke, 24 * n_n, np.uint8),
+            "path_paint": _arr(o.path_paint, 64 * n_n, np.uint8),
+            "stops": _arr(o.stops, 8 * o.n_stops, np.uint8),
+            "ramps": _arr(o.ramps, 256 * n_n, np.uint32).reshape(-1, 256),
+            "width": np.float32(o.width), "height": np.float32(o.height),
+        }
+    finally:
+        lib.pfref_svg_free(C.byref(o))
+
+
 def half_trunc(values, reference: bool = False) -> np.ndarray:
     """umHalf's float -> half -> float round trip (restated, or the reference's own)."""
     lib = _lib(LIB_REF if reference else LIB_ORACLE)

@@ -118,6 +118,34 @@ void pfref_gradient_ramp(const pf_color_stop *stops, uint32_t n, uint32_t *ramp)
 float pfref_half(float f);
 void pfref_free(pfo_result *r);
 
+/*
+ * SVG: the reference's nanosvg (nsvgParse(text, "px", dpi), third_party/nanosvg.h) replayed as
+ * SvgScene::SvgScene does (core/svg.cpp:135-205) through the reference's own Path2d and Paint,
+ * written as a scene in pf_scene_view's layout: per shape a fill path when Canvas::fill_path
+ * would draw one, then a stroke path (its contours plus a pf_stroke, dash phase 0) when
+ * Canvas::stroke_path would.  stops are nanosvg's, in the order add_color_stop receives them;
+ * ramps holds, per path, the 256 texels of the reference Gradient's ramp (zero for colour paints).
+ */
+typedef struct pfo_svg {
+    uint32_t n_points, n_contours, n_paths, n_dashes, n_stops;
+    float width, height;
+    float *points;             /* [n_points][2] */
+    uint8_t *point_flags;      /* [n_points] */
+    uint32_t *contour_start;   /* [n_contours + 1] */
+    uint8_t *contour_closed;   /* [n_contours] */
+    uint32_t *path_start;      /* [n_paths + 1] */
+    uint8_t *fill_rule;        /* [n_paths] */
+    uint32_t *color;           /* [n_paths] */
+    pf_stroke *path_stroke;    /* [n_paths] */
+    float *dashes;             /* [n_dashes] */
+    pf_paint *path_paint;      /* [n_paths] */
+    pf_color_stop *stops;      /* [n_stops] */
+    uint32_t *ramps;           /* [n_paths][256] */
+} pfo_svg;
+/* 0 ok; 1 nanosvg returned no image */
+int pfref_svg_scene(const char *text, size_t length, float dpi, pfo_svg *out);
+void pfref_svg_free(pfo_svg *s);
+
 #ifdef __cplusplus
 }
 #endif

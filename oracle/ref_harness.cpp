@@ -11,6 +11,8 @@
 //      threaded so alpha-tile ids come out in a fixed order;
 //   build_tile_batches_for_draw_path_display_item  pathfinder/core/d3d9/scene_builder.cpp:18-95
 //     (visible tiles in path order and the z-buffer).
+//   nsvgParse (third_party/nanosvg.h) with SvgScene's replay through Path2d and Paint
+//     (pathfinder/core/svg.cpp:63-205), for the SVG ingestion's pin.
 // SceneBuilderD3D9::build itself is bypassed because it needs a GPU Renderer for the palette.
 #include <algorithm>
 #include <climits>
@@ -27,6 +29,11 @@
 #include "core/scene.h"
 #include "core/stroke.h"
 #include <umHalf.h>
+
+#include <string>
+#include "core/path2d.h"
+#define NANOSVG_IMPLEMENTATION
+#include <nanosvg.h>
 
 #include "pf_oracle.h"
 
@@ -461,4 +468,171 @@ extern "C" void pfref_free(pfo_result *r) {
     std::free(r->tile_clip);
     std::free(r->tile_dest_backdrop);
     std::memset(r, 0, sizeof(*r));
+}
+
+// SvgScene::SvgScene (pathfinder/core/svg.cpp:135-205) up to the canvas: the Path2d of each
+// shape, its fill and stroke paints from convert_nsvg_paint (svg.cpp:63-133), and the canvas's
+// own tests (Canvas::fill_path / stroke_path / push_path, canvas.cpp:180-300) of which paths
+// are drawn.  The canvas itself is not linked (it pulls in the GPU renderers).
+namespace {
+Paint harness_paint(const NSVGpaint &np) {
+    Paint paint;
+    if (np.type == NSVG_PAINT_COLOR) {
+        paint = Paint::from_color(ColorU(np.color));
+    } else if (np.type == NSVG_PAINT_LINEAR_GRADIENT || np.type == NSVG_PAINT_RADIAL_GRADIENT) {
+        NSVGgradient *g = np.gradient;
+        Transform2 gradient_xform(g->xform2), path_xform(g->xform3);
+        Gradient gradient;
+        if (np.type == NSVG_PAINT_LINEAR_GRADIENT) {
+            Vec2F from = {g->x1, g->y1}, to = {g->x2, g->y2};
+            from = path_xform * gradient_xform * from;
+            to = path_xform * gradient_xform * to;
+            gradient = Gradient::linear(LineSegmentF(from, to));
+        } else {
+            gradient = Gradient::radial(LineSegmentF(Vec2F(g->cx, g->cy), Vec2F(g->fx, g->fy)), Vec2F(0.0, g->r));
+            std::get<GradientRadial>(gradient.geometry).transform = path_xform * gradient_xform;
+        }
+        if (g->spread == NSVG_SPREAD_REPEAT) gradient.wrap = GradientWrap::Repeat;
+        for (int i = 0; i < g->nstops; i++) gradient.add_color_stop(ColorU(g->stops[i].color), g->stops[i].offset);
+        paint = Paint::from_gradient(gradient);
+    }
+    return paint;
+}
+}  // namespace
+
+extern "C" int pfref_svg_scene(const char *text, size_t length, float dpi, pfo_svg *out) {
+    std::memset(out, 0, sizeof(*out));
+    std::string copy(text, length);
+    NSVGimage *image = nsvgParse(&copy[0], "px", dpi);
+    if (!image) return 1;
+    std::vector<float> pts, dashes;
+    std::vector<uint8_t> flags, closed, rule;
+    std::vector<uint32_t> cstart{0}, pstart{0}, color, ramps;
+    std::vector<pf_stroke> strokes;
+    std::vector<pf_paint> paints;
+    std::vector<pf_color_stop> stops;
+    auto push = [&](const Outline &outline, const Paint &paint, const NSVGpaint &np, uint8_t fill_rule,
+                    const pf_stroke &st) {
+        for (const Contour &c : outline.contours) {
+            for (size_t i = 0; i < c.points.size(); i++) {
+                pts.push_back(c.points[i].x);
+                pts.push_back(c.points[i].y);
+                flags.push_back(static_cast<uint8_t>(c.flags[i]));
+            }
+            cstart.push_back(static_cast<uint32_t>(flags.size()));
+            closed.push_back(c.closed ? 1 : 0);
+        }
+        pstart.push_back(static_cast<uint32_t>(cstart.size() - 1));
+        rule.push_back(fill_rule);
+        strokes.push_back(st);
+        const ColorU base = paint.get_base_color();
+        color.push_back(uint32_t(base.r_) | uint32_t(base.g_) << 8 | uint32_t(base.b_) << 16 | uint32_t(base.a_) << 24);
+        pf_paint pp;
+        std::memset(&pp, 0, sizeof pp);
+        pp.transform[0] = pp.transform[3] = 1.0f;
+        uint32_t ramp[GRADIENT_TILE_LENGTH] = {0};
+        if (const auto overlay = paint.get_overlay()) {
+            const Gradient &g = std::get<Gradient>(overlay->contents);
+            if (const auto *lin = std::get_if<GradientLinear>(&g.geometry)) {
+                pp.type = PF_PAINT_LINEAR;
+                pp.line[0] = lin->line.from().x, pp.line[1] = lin->line.from().y;
+                pp.line[2] = lin->line.to().x, pp.line[3] = lin->line.to().y;
+            } else {
+                const auto &rad = std::get<GradientRadial>(g.geometry);
+                pp.type = PF_PAINT_RADIAL;
+                pp.line[0] = rad.line.from().x, pp.line[1] = rad.line.from().y;
+                pp.line[2] = rad.line.to().x, pp.line[3] = rad.line.to().y;
+                pp.radii[0] = rad.radii.x, pp.radii[1] = rad.radii.y;
+                pp.transform[0] = rad.transform.m11(), pp.transform[1] = rad.transform.m21();
+                pp.transform[2] = rad.transform.m12(), pp.transform[3] = rad.transform.m22();
+                pp.transform[4] = rad.transform.m13(), pp.transform[5] = rad.transform.m23();
+            }
+            pp.wrap = g.wrap == GradientWrap::Repeat ? PF_WRAP_REPEAT : PF_WRAP_CLAMP;
+            pp.stop_first = static_cast<uint32_t>(stops.size());
+            pp.stop_count = static_cast<uint32_t>(np.gradient->nstops);
+            for (int i = 0; i < np.gradient->nstops; i++)
+                stops.push_back(pf_color_stop{np.gradient->stops[i].offset, np.gradient->stops[i].color});
+            for (uint32_t x = 0; x < GRADIENT_TILE_LENGTH; x++) {
+                const ColorU c = g.sample(((float)x + 0.5f) / GRADIENT_TILE_LENGTH);
+                ramp[x] = uint32_t(c.r_) | uint32_t(c.g_) << 8 | uint32_t(c.b_) << 16 | uint32_t(c.a_) << 24;
+            }
+        }
+        paints.push_back(pp);
+        ramps.insert(ramps.end(), ramp, ramp + GRADIENT_TILE_LENGTH);
+    };
+    for (NSVGshape *shape = image->shapes; shape; shape = shape->next) {
+        Path2d path;
+        for (NSVGpath *np = shape->paths; np; np = np->next) {
+            path.move_to(np->pts[0], np->pts[1]);
+            for (int i = 0; i < np->npts - 3; i += 3) {
+                const float *q = &np->pts[i * 2];
+                path.cubic_to(q[2], q[3], q[4], q[5], q[6], q[7]);
+            }
+            if (np->closed) path.close_path();
+        }
+        const Paint fill = harness_paint(shape->fill);
+        if (fill.is_visible() && fill.get_base_color().is_visible()) {
+            pf_stroke none;
+            std::memset(&none, 0, sizeof none);
+            push(path.into_outline(), fill, shape->fill,
+                 shape->fillRule == NSVG_FILLRULE_EVENODD ? PF_FILL_EVEN_ODD : PF_FILL_NONZERO, none);
+        }
+        const Paint stroke = harness_paint(shape->stroke);
+        if (stroke.is_visible() && shape->strokeWidth > 0 && stroke.get_base_color().is_visible()) {
+            pf_stroke st;
+            std::memset(&st, 0, sizeof st);
+            st.line_width = shape->strokeWidth;
+            st.miter_limit = shape->miterLimit;
+            st.line_cap = shape->strokeLineCap == NSVG_CAP_ROUND    ? PF_CAP_ROUND
+                          : shape->strokeLineCap == NSVG_CAP_SQUARE ? PF_CAP_SQUARE
+                                                                    : PF_CAP_BUTT;
+            st.line_join = shape->strokeLineJoin == NSVG_JOIN_ROUND   ? PF_JOIN_ROUND
+                           : shape->strokeLineJoin == NSVG_JOIN_BEVEL ? PF_JOIN_BEVEL
+                                                                      : PF_JOIN_MITER;
+            if (shape->strokeDashCount > 0) {
+                st.dash_first = static_cast<uint32_t>(dashes.size());
+                st.dash_count = static_cast<uint32_t>(shape->strokeDashCount);
+                dashes.insert(dashes.end(), shape->strokeDashArray, shape->strokeDashArray + shape->strokeDashCount);
+            }
+            push(path.into_outline(), stroke, shape->stroke, PF_FILL_NONZERO, st);
+        }
+    }
+    out->width = image->width;
+    out->height = image->height;
+    nsvgDelete(image);
+    out->n_points = static_cast<uint32_t>(flags.size());
+    out->n_contours = static_cast<uint32_t>(cstart.size() - 1);
+    out->n_paths = static_cast<uint32_t>(color.size());
+    out->n_dashes = static_cast<uint32_t>(dashes.size());
+    out->n_stops = static_cast<uint32_t>(stops.size());
+    out->points = dup(pts);
+    out->point_flags = dup(flags);
+    out->contour_start = dup(cstart);
+    out->contour_closed = dup(closed);
+    out->path_start = dup(pstart);
+    out->fill_rule = dup(rule);
+    out->color = dup(color);
+    out->path_stroke = dup(strokes);
+    out->dashes = dup(dashes);
+    out->path_paint = dup(paints);
+    out->stops = dup(stops);
+    out->ramps = dup(ramps);
+    return 0;
+}
+
+extern "C" void pfref_svg_free(pfo_svg *s) {
+    if (!s) return;
+    std::free(s->points);
+    std::free(s->point_flags);
+    std::free(s->contour_start);
+    std::free(s->contour_closed);
+    std::free(s->path_start);
+    std::free(s->fill_rule);
+    std::free(s->color);
+    std::free(s->path_stroke);
+    std::free(s->dashes);
+    std::free(s->path_paint);
+    std::free(s->stops);
+    std::free(s->ramps);
+    std::memset(s, 0, sizeof(*s));
 }

@@ -16,7 +16,9 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpfcuda.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include")]
+# host code without FMA contraction: the SVG parser and the host-side arithmetic follow the
+# reference operation by operation on x86 and on Arm
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(ROOT, "include")]
 
 
 def sources():

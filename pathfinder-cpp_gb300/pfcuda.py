@@ -30,7 +30,7 @@ EXPORTS = [
     "pf_sizer_init", "pf_sizer_set_params", "pf_sizer_get_params", "pf_sizer_set_margin", "pf_sizer_predict",
     "pf_sizer_gradient", "pf_sizer_train", "pf_sizer_save", "pf_sizer_load", "pf_path_features", "pf_path_counts",
     "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags", "pf_sizer_predict_noalloc",
-    "pf_set_host_image", "pf_read_outline", "pf_upload_stats_get",
+    "pf_set_host_image", "pf_read_outline", "pf_upload_stats_get", "pf_svg_parse", "pf_svg_scene", "pf_svg_free",
 ]
 
 N_FEATURES = 12
@@ -122,6 +122,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         for name in EXPORTS:
             if name != "pf_last_error":
                 getattr(lib, name).restype = C.c_int
+        lib.pf_svg_parse.argtypes = [C.c_char_p, C.c_size_t, C.c_float, C.POINTER(C.c_void_p)]
+        lib.pf_svg_scene.argtypes = [C.c_void_p, C.c_void_p]
+        lib.pf_svg_free.argtypes, lib.pf_svg_free.restype = [C.c_void_p], None
         _lib = lib
     return _lib
 
@@ -172,6 +175,67 @@ def _arr(ptr, n, dtype):
         return np.zeros(0, dtype)
     buf = (C.c_char * (int(n) * np.dtype(dtype).itemsize)).from_address(ptr)
     return np.frombuffer(buf, dtype=dtype).copy()
+
+
+class SvgDocument:
+    """A parsed SVG document (pf_svg): its scene view points into the parser's own arrays, so
+    ``Renderer.upload_views([doc.view])`` hands the document to the GPU without a copy.
+
+    The reference's SvgScene (pathfinder/core/svg.cpp:135-205): nanosvg's parse replayed through
+    the canvas, one fill path and one stroke path per shape where their paints are visible.
+    Strokes stay strokes (path_stroke); the upload converts them on the GPU.  Host code: no GPU
+    is needed to parse."""
+
+    def __init__(self, text, dpi: float = 96.0):
+        self.lib = load()
+        data = text.encode() if isinstance(text, str) else bytes(text)
+        self.handle = C.c_void_p()
+        st = self.lib.pf_svg_parse(data, len(data), dpi, C.byref(self.handle))
+        if st != PF_OK:
+            raise PfError(st, "pf_svg_parse failed")
+        self.view = SceneView()
+        self.lib.pf_svg_scene(self.handle, C.byref(self.view))
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.pf_svg_free(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def scene(self):
+        """The document as a scenes.Scene (numpy copies of the view's arrays)."""
+        import scenes as S
+        v = self.view
+        n_p, n_c, n_n = v.n_points, v.n_contours, v.n_paths
+        sc = S.Scene(points=_arr(v.points, 2 * n_p, np.float32).reshape(-1, 2),
+                     flags=_arr(v.point_flags, n_p, np.uint8),
+                     contour_start=_arr(v.contour_start, n_c + 1, np.uint32),
+                     path_start=_arr(v.path_start, n_n + 1, np.uint32),
+                     fill_rule=_arr(v.fill_rule, n_n, np.uint8), color=_arr(v.color, n_n, np.uint32),
+                     width=float(v.width), height=float(v.height))
+        sc.path_stroke = _arr(v.path_stroke, n_n, S.STROKE_DTYPE)
+        sc.contour_closed = _arr(v.contour_closed, n_c, np.uint8)
+        sc.dashes = _arr(v.dashes, v.n_dashes, np.float32)
+        sc.path_paint = _arr(v.path_paint, n_n, S.PAINT_DTYPE)
+        sc.stops = _arr(v.stops, v.n_stops, S.STOP_DTYPE)
+        return sc
+
+
+def parse_svg(text, dpi: float = 96.0):
+    """An SVG document as a scenes.Scene (see :class:`SvgDocument`)."""
+    with SvgDocument(text, dpi) as doc:
+        return doc.scene()
 
 
 class Renderer:

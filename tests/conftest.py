@@ -29,6 +29,16 @@ def golden_names():
     return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(GOLDEN, "*.npz")))
 
 
+def golden_with(key):
+    """Names of the golden fixtures that hold the array ``key``."""
+    out = []
+    for name in golden_names():
+        with np.load(os.path.join(GOLDEN, name + ".npz")) as d:
+            if key in d.files:
+                out.append(name)
+    return out
+
+
 def load_golden(name):
     import scenes as S
     d = np.load(os.path.join(GOLDEN, name + ".npz"))

@@ -31,6 +31,7 @@ sys.path.insert(0, os.path.join(ROOT, "pathfinder-cpp_gb300"))
 
 import oracle  # noqa: E402
 import scenes as S  # noqa: E402
+import svg_docs  # noqa: E402
 
 CANON_KEYS = ["path_rect", "path_tile_first", "path_column_first", "tile_alpha", "tile_backdrop",
               "tile_fill_count", "fills", "column_backdrop", "fb_tiles", "z", "fb_list_first", "fb_list",
@@ -318,6 +319,28 @@ def generator_scenes():
     }
 
 
+def svg_scenes():
+    """SVG documents through the reference's nanosvg + SvgScene replay (the harness): the scene
+    the reference's canvas builds, stored with the document's text (svg_text) so the parser can be
+    checked against it where the reference is absent.  Paint arrays are kept only when the
+    document has a gradient."""
+    docs = {k: v for k, v in svg_docs.HAND.items() if k != "svg_empty"}
+    docs.update({f"svg_random_s{seed}": svg_docs.random_document(seed) for seed in (101, 102, 103)})
+    out = {}
+    for name, text in docs.items():
+        r = oracle.reference_svg_scene(text)
+        sc = S.Scene(points=r["points"], flags=r["flags"], contour_start=r["contour_start"],
+                     path_start=r["path_start"], fill_rule=r["fill_rule"], color=r["color"],
+                     width=float(r["width"]), height=float(r["height"]))
+        sc.path_stroke = r["path_stroke"].view(S.STROKE_DTYPE)
+        sc.contour_closed, sc.dashes = r["contour_closed"], r["dashes"]
+        paint = r["path_paint"].view(S.PAINT_DTYPE)
+        if np.any(paint["type"] != S.PAINT_SOLID):
+            sc.path_paint, sc.stops = paint, r["stops"].view(S.STOP_DTYPE)
+        out[name] = (sc, text)
+    return out
+
+
 def full_scenes():
     return {"plain_small_1024": S.plain_small()}
 
@@ -344,6 +367,9 @@ def main() -> None:
     small.update(stroke_scenes())
     small.update(gradient_scenes())
     small.update(generator_scenes())
+    texts = {}
+    for name, (sc, text) in svg_scenes().items():
+        small[name], texts[name] = sc, text
     for name, sc in small.items():
         ref = oracle.reference_tile_scene(sc)
         arrays = {k: getattr(sc, k) for k in INPUT_KEYS}
@@ -357,6 +383,8 @@ def main() -> None:
             arrays.update({k: getattr(sc, k) for k in PAINT_KEYS})
             arrays["ref_ramps"] = oracle.reference_ramps(sc)
         arrays["meta"] = np.asarray([sc.width, sc.height, sc.clear], np.float64)
+        if name in texts:
+            arrays["svg_text"] = np.frombuffer(texts[name].encode(), np.uint8)
         for k in CANON_KEYS:
             arrays["ref_" + k] = ref[k]
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)

@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 import scenes as S
-from conftest import TILE_KEYS, load_golden
+from conftest import TILE_KEYS, golden_with, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -37,7 +37,7 @@ def _has_radial(sc):
     return bool(np.any(sc.path_paint["type"] == S.PAINT_RADIAL))
 
 
-@pytest.mark.parametrize("name", ["grad_linear", "grad_radial", "gen_gradient_s8"])
+@pytest.mark.parametrize("name", golden_with("ref_ramps"))
 def test_gradient_fixture_tiles_and_pixels(renderer, oracle_mod, name):
     sc, ref = load_golden(name)
     renderer.upload(sc)

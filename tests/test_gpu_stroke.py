@@ -10,13 +10,13 @@ import numpy as np
 import pytest
 
 import scenes as S
-from conftest import OUTLINE_KEYS, TILE_KEYS, golden_names, load_golden
+from conftest import OUTLINE_KEYS, TILE_KEYS, golden_with, load_golden
 
 pytestmark = pytest.mark.gpu
 
 LIST_KEYS = ["fb_tiles", "z", "fb_list_first", "fb_list"]
 PIXEL_TOL = 1
-STROKED = [n for n in golden_names() if n.startswith("stroke_") or n.startswith("gen_stroked")]
+STROKED = golden_with("out_points")
 
 
 def _same_outline(got, want):

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import CANON_KEYS, GOLDEN, OUTLINE_KEYS, golden_names, load_golden
+from conftest import CANON_KEYS, GOLDEN, OUTLINE_KEYS, golden_names, golden_with, load_golden
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -18,7 +18,7 @@ def test_restated_tiler_matches_reference_golden(oracle_mod, name):
         assert np.array_equal(ours[k], ref[k]), k
 
 
-STROKED = [n for n in golden_names() if n.startswith("stroke_") or n.startswith("gen_stroked")]
+STROKED = golden_with("out_points")
 
 
 @pytest.mark.parametrize("name", STROKED)
@@ -57,7 +57,7 @@ def test_stroke_layout_checks(oracle_mod):
         oracle_mod.stroke_scene(S.Scene(**{**sc.__dict__, "path_stroke": st}))
 
 
-GRADIENT = [n for n in golden_names() if n.startswith("grad_") or n.startswith("gen_gradient")]
+GRADIENT = golden_with("ref_ramps")
 
 
 @pytest.mark.parametrize("name", GRADIENT)
