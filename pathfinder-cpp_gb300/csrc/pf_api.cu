@@ -104,7 +104,7 @@ struct Ctx {
     DevBuf contour_point_first, contour_path, paths, path_tiles, path_cols, contour_segs, path_contours, path_bounds;
     // learned sizer: weights (bf16 used by the kernels, fp32 master + Adam moments for training)
     DevBuf sz_w, sz_master, sz_m, sz_v, sz_grad, sz_loss, sz_feat, sz_target, sz_index, sz_pred;
-    DevBuf path_feat, path_pred, path_leaf_first, path_leaf_budget, path_leaf_cursor, path_fill_budget;
+    DevBuf path_feat, contour_feat, path_pred, path_leaf_first, path_leaf_budget, path_leaf_cursor, path_fill_budget;
     DevBuf bin_list, bin_ctl, path_leaf_range;
     int sz_step = 0;
     bool sz_ready = false;
@@ -940,13 +940,15 @@ int stage_setup(Ctx *c, bool learned) {
     PF_CUDA(launch_path_offsets(b, st));
     if (learned) {
         PF_CUDA(c->path_feat.ensure(size_t(N) * kSizerIn * 4 + 16));
+        PF_CUDA(c->contour_feat.ensure(size_t(C) * 32 + 32));
         PF_CUDA(c->path_pred.ensure(size_t(N) * kSizerOut * 4 + 16));
         PF_CUDA(c->path_leaf_first.ensure((size_t(N) + 1) * 4));
         PF_CUDA(c->path_leaf_budget.ensure(size_t(N) * 4 + 16));
         PF_CUDA(c->path_leaf_cursor.ensure(size_t(N) * 4 + 16));
         PF_CUDA(c->path_fill_budget.ensure((size_t(N) + 1) * 4));
         b = make_batch(c);
-        PF_CUDA(launch_features(b, c->path_contours.as<uint2>(), c->path_feat.as<float>(), st));
+        PF_CUDA(launch_features(b, c->path_contours.as<uint2>(), c->contour_feat.as<float4>(), c->path_feat.as<float>(),
+                                st));
         PF_CUDA(launch_mlp_predict(c->sz_w.as<__nv_bfloat16>(), c->path_feat.as<float>(), N, c->path_pred.as<float>(),
                                    st));
         PF_CUDA(launch_budgets(b, c->path_pred.as<float>(), c->sz_mul, c->sz_add, b.path_leaf_first,
@@ -1149,7 +1151,7 @@ std::vector<void *> frame_buffers(const Ctx *c) {
     const DevBuf *bufs[] = {&c->status, &c->contour_point_first, &c->contour_path, &c->paths, &c->path_tiles,
                             &c->path_cols, &c->path_contours, &c->path_bounds, &c->row_first, &c->bin_list,
                             &c->bin_ctl, &c->path_leaf_range, &c->path_fill, &c->path_cls, &c->bin_stage,
-                            &c->path_feat, &c->path_pred, &c->path_leaf_first, &c->path_leaf_budget,
+                            &c->path_feat, &c->contour_feat, &c->path_pred, &c->path_leaf_first, &c->path_leaf_budget,
                             &c->path_leaf_cursor, &c->path_fill_budget, &c->segs, &c->seg_leaves, &c->seg_order,
                             &c->seg_ctl, &c->row_paths, &c->tile_fills, &c->tile_state, &c->col_above,
                             &c->col_final, &c->leaves, &c->pool_path, &c->pool_idx, &c->pool_cnt, &c->fills,
@@ -1588,7 +1590,7 @@ int pf_ctx_destroy(void *ctx) {
     drop_graph(c);
     drop_host_image(c);
     DevBuf *bufs[] = {&c->sz_w, &c->sz_master, &c->sz_m, &c->sz_v, &c->sz_grad, &c->sz_loss, &c->sz_feat,
-                      &c->sz_target, &c->sz_index, &c->sz_pred, &c->path_feat, &c->path_pred, &c->path_leaf_first,
+                      &c->sz_target, &c->sz_index, &c->sz_pred, &c->path_feat, &c->contour_feat, &c->path_pred, &c->path_leaf_first,
                       &c->path_leaf_budget, &c->path_leaf_cursor, &c->path_fill_budget, &c->path_bounds,
                       &c->bin_list, &c->bin_ctl, &c->path_leaf_range,
                       &c->points, &c->pflags, &c->cstart, &c->pstart, &c->fill_rule, &c->color, &c->scenes,
@@ -2022,7 +2024,9 @@ int pf_path_features(void *ctx, float *out, size_t capacity_floats) {
     if (capacity_floats < n * kSizerIn) return fail(c, PF_ERR_INVALID_ARGUMENT, "buffer too small");
     PF_CUDA(c->path_feat.ensure(n * kSizerIn * 4 + 16));
     Batch b = make_batch(c);
-    PF_CUDA(launch_features(b, c->path_contours.as<uint2>(), c->path_feat.as<float>(), c->stream));
+    PF_CUDA(c->contour_feat.ensure(size_t(c->r_contours) * 32 + 32));
+    PF_CUDA(launch_features(b, c->path_contours.as<uint2>(), c->contour_feat.as<float4>(), c->path_feat.as<float>(),
+                            c->stream));
     PF_CUDA(cudaMemcpyAsync(out, c->path_feat.p, n * kSizerIn * 4, cudaMemcpyDeviceToHost, c->stream));
     PF_CUDA(cudaStreamSynchronize(c->stream));
     return PF_OK;

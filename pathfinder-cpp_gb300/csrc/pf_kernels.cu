@@ -1248,7 +1248,27 @@ __global__ void __launch_bounds__(kPrepThreads) k_bin_large_prep(Batch b) {
         unsigned long long sum = 0;
         for (uint32_t x = tid; x < rw; x += kPrepThreads) {
             int32_t run = b.col_above[cb + x];
-            for (uint32_t y = 0; y < rh; y++) {
+            uint32_t y = 0;
+            // eight rows at a time: their counters and deltas are loaded before any of the
+            // eight states is rewritten, so the loads overlap instead of following each store
+            for (; y + 8 <= rh; y += 8) {
+                uint32_t cnt[8];
+                uint16_t state[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const uint32_t t = tb + (y + k) * rw + x;
+                    cnt[k] = b.tile_fills[t];
+                    state[k] = b.tile_state[t];
+                }
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const uint32_t t = tb + (y + k) * rw + x;
+                    b.tile_state[t] = (uint16_t)((uint32_t)(uint8_t)(int8_t)run | (cnt[k] ? 0x100u : 0u));
+                    run += (int8_t)(state[k] & 0xffu);
+                    sum += cnt[k];
+                }
+            }
+            for (; y < rh; y++) {
                 const uint32_t t = tb + y * rw + x, c = b.tile_fills[t];
                 const int8_t delta = (int8_t)(b.tile_state[t] & 0xffu);
                 b.tile_state[t] = (uint16_t)((uint32_t)(uint8_t)(int8_t)run | (c ? 0x100u : 0u));
@@ -1270,11 +1290,17 @@ __global__ void __launch_bounds__(kPrepThreads) k_bin_large_prep(Batch b) {
             s_base = (uint32_t)base;
         }
         __syncthreads();
+        // exclusive scan of the counters into write cursors, four consecutive tiles a thread
         uint32_t carry = s_base;
-        for (uint32_t t0 = 0; t0 < T; t0 += kPrepThreads) {
-            const uint32_t t = t0 + tid;
-            const uint32_t v = t < T ? b.tile_fills[tb + t] : 0u;
-            uint32_t incl = v;
+        for (uint32_t t0 = 0; t0 < T; t0 += 4 * kPrepThreads) {
+            const uint32_t t = t0 + 4 * tid;
+            uint32_t v[4], own = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                v[k] = t + k < T ? b.tile_fills[tb + t + k] : 0u;
+                own += v[k];
+            }
+            uint32_t incl = own;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t n = __shfl_up_sync(0xffffffffu, incl, o);
@@ -1287,7 +1313,12 @@ __global__ void __launch_bounds__(kPrepThreads) k_bin_large_prep(Batch b) {
                 if (k < warp) before += s_warp[k];
                 chunk_total += s_warp[k];
             }
-            if (t < T) b.tile_fills[tb + t] = carry + before + incl - v;
+            uint32_t cur = carry + before + incl - own;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (t + k < T) b.tile_fills[tb + t + k] = cur;
+                cur += v[k];
+            }
             carry += chunk_total;
             __syncthreads();
         }

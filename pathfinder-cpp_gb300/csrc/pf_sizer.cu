@@ -32,34 +32,86 @@ __device__ __forceinline__ float turn(float2 a, float2 b, float2 c) {
     return fabsf(atan2f(cr, dt));
 }
 
-// One warp per path: features from the path's points and point flags (they do not need the
-// segment records, so they are ready before the first host synchronisation of a frame) and
-// its bounds / tile rect (after k_path_setup):
+// Per contour: its point-flag counts, control-polygon length and summed turning angle
+// (closed around the contour).  Paths sum them over their contours, so a path of thousands of
+// contours (a dashed stroke's outline) costs its warp one strided pass over those sums.  A
+// thread takes its contour alone up to kBigContour points; longer contours are taken by the
+// whole warp afterwards, one at a time, so no thread walks thousands of points.
+constexpr uint32_t kBigContour = 64;
+
+__device__ __forceinline__ void point_terms(const Batch &b, uint32_t a, uint32_t n, uint32_t i, float &n_on,
+                                            float &n_c0, float &n_c1, float &length, float &turning) {
+    const uint8_t f = b.flags[a + i];
+    n_on += f == 0;
+    n_c0 += f == 1;
+    n_c1 += f == 2;
+    if (n > 1) {
+        const float2 q0 = b.points[a + (i == 0 ? n - 1 : i - 1)], q1 = b.points[a + i],
+                     q2 = b.points[a + (i + 1 == n ? 0 : i + 1)];
+        length += leg_len(q1, q2);
+        turning += turn(q0, q1, q2);
+    }
+}
+
+__global__ void k_contour_features(Batch b, float4 *cf) {
+    const uint32_t c = global_tid();
+    const int lane = threadIdx.x & 31;
+    const bool in = c < b.n_contours;
+    uint32_t a = 0, n = 0;
+    if (in) {
+        a = b.contour_point_first[c];
+        n = b.contour_point_first[c + 1] - a;
+    }
+    const bool big = in && n > kBigContour;
+    if (in && !big) {
+        float n_on = 0, n_c0 = 0, n_c1 = 0, length = 0, turning = 0;
+        for (uint32_t i = 0; i < n; i++) point_terms(b, a, n, i, n_on, n_c0, n_c1, length, turning);
+        cf[2 * (size_t)c] = make_float4(n_on, n_c0, n_c1, length);
+        cf[2 * (size_t)c + 1] = make_float4(turning, 0.0f, 0.0f, 0.0f);
+    }
+    unsigned pending = __ballot_sync(0xffffffffu, big);
+    while (pending) {
+        const int src = __ffs(pending) - 1;
+        pending &= pending - 1;
+        const uint32_t ba = __shfl_sync(0xffffffffu, a, src), bn = __shfl_sync(0xffffffffu, n, src);
+        float n_on = 0, n_c0 = 0, n_c1 = 0, length = 0, turning = 0;
+        for (uint32_t i = lane; i < bn; i += 32) point_terms(b, ba, bn, i, n_on, n_c0, n_c1, length, turning);
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            n_on += __shfl_xor_sync(0xffffffffu, n_on, d);
+            n_c0 += __shfl_xor_sync(0xffffffffu, n_c0, d);
+            n_c1 += __shfl_xor_sync(0xffffffffu, n_c1, d);
+            length += __shfl_xor_sync(0xffffffffu, length, d);
+            turning += __shfl_xor_sync(0xffffffffu, turning, d);
+        }
+        if (lane == src) {
+            cf[2 * (size_t)c] = make_float4(n_on, n_c0, n_c1, length);
+            cf[2 * (size_t)c + 1] = make_float4(turning, 0.0f, 0.0f, 0.0f);
+        }
+    }
+}
+
+// One warp per path: features from its contours' sums and its bounds / tile rect (after
+// k_path_setup); they need no segment records, so they are ready before the first host
+// synchronisation of a frame:
 //   0 segments   1 lines   2 quadratics   3 cubics   4 contours   5 box width   6 box height
 //   7 box area   8 control-polygon length   9 summed turning angle   10 tiles in the rect
 //   11 even-odd flag
 // (log1p of every count / length; the reference's outlines are already in canvas space, so
 // the transform-scale feature is replaced by the tile count of the clipped rect).
-__global__ void k_features(Batch b, const uint2 *path_contours, float *feat) {
+__global__ void k_features(Batch b, const uint2 *path_contours, const float4 *cf, float *feat) {
     const uint32_t p = global_tid() >> 5;
     const int lane = threadIdx.x & 31;
     if (p >= b.n_paths) return;
     const uint2 cr = path_contours[p];
     float n_on = 0, n_c0 = 0, n_c1 = 0, length = 0, turning = 0;
-    for (uint32_t c = cr.x; c < cr.y; c++) {
-        const uint32_t a = b.contour_point_first[c], e = b.contour_point_first[c + 1], n = e - a;
-        for (uint32_t i = lane; i < n; i += 32) {
-            const uint8_t f = b.flags[a + i];
-            n_on += f == 0;
-            n_c0 += f == 1;
-            n_c1 += f == 2;
-            if (n > 1) {
-                const float2 q0 = b.points[a + (i == 0 ? n - 1 : i - 1)], q1 = b.points[a + i],
-                             q2 = b.points[a + (i + 1 == n ? 0 : i + 1)];
-                length += leg_len(q1, q2);
-                turning += turn(q0, q1, q2);
-            }
-        }
+    for (uint32_t c = cr.x + lane; c < cr.y; c += 32) {
+        const float4 u = cf[2 * (size_t)c], v = cf[2 * (size_t)c + 1];
+        n_on += u.x;
+        n_c0 += u.y;
+        n_c1 += u.z;
+        length += u.w;
+        turning += v.x;
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) {
@@ -275,10 +327,15 @@ __global__ void k_adam(float *master, __nv_bfloat16 *w, float *grad, float *m, f
 
 }  // namespace
 
-cudaError_t launch_features(const Batch &b, const uint2 *path_contours, float *feat, cudaStream_t st) {
+cudaError_t launch_features(const Batch &b, const uint2 *path_contours, float4 *contour_scratch, float *feat,
+                            cudaStream_t st) {
     if (b.n_paths) {
+        if (b.n_contours) {
+            k_contour_features<<<(b.n_contours + kThreads - 1) / kThreads, kThreads, 0, st>>>(b, contour_scratch);
+            count_launches(1);
+        }
         k_features<<<(unsigned)((uint64_t(b.n_paths) * 32 + kThreads - 1) / kThreads), kThreads, 0, st>>>(
-            b, path_contours, feat);
+            b, path_contours, contour_scratch, feat);
         count_launches(1);
     }
     return cudaGetLastError();

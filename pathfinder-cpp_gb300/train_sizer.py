@@ -2,8 +2,9 @@
 
     python pathfinder-cpp_gb300/train_sizer.py --out pathfinder-cpp_gb300/weights/sizer.bin
 
-1. Training paths come from the three single-scene generators (the 240-path cubic
-   generator at every batched canvas side, the large mixed scene and the glyph scene),
+1. Training paths come from the single-scene generators (the 240-path cubic generator at
+   every batched canvas side, the large mixed scene, the glyph scene, stroked scenes whose
+   stroke outlines the upload builds) and from seeded SVG documents parsed by pf_svg_parse,
    about 2 M paths by default.  Each scene is rendered with the exact two-pass frame; its
    per-path features and exact leaf-line / fill counts are the inputs and labels
    (targets are log1p of the counts).
@@ -46,17 +47,23 @@ def _fold_standardisation(params: np.ndarray, mu: np.ndarray, sd: np.ndarray) ->
 
 def training_scenes(target_paths: int, seed0: int = 100):
     """Yield scenes from the three generators until about target_paths paths."""
+    import svg_docs
     n = 0
     k = 0
     sides = (256, 512, 1024, 2048)
     while n < target_paths:
-        kind = k % 4
+        kind = k % 6
         if kind in (0, 1):
-            sc = S.plain_small(seed=seed0 + k, n_paths=2048, side=sides[(k // 4) % 4])
+            sc = S.plain_small(seed=seed0 + k, n_paths=2048, side=sides[(k // 6) % 4])
         elif kind == 2:
             sc = S.large_single(seed=seed0 + k, n_paths=20000, side=4096)
-        else:
+        elif kind == 3:
             sc = S.glyphs(seed=seed0 + k, n_paths=60000, side=2048)
+        elif kind == 4:
+            sc = S.stroked(seed=seed0 + k, n_paths=4096, side=sides[(k // 6) % 4], dash_share=0.3,
+                           fill_share=0.2)
+        else:
+            sc = pfcuda.parse_svg(svg_docs.random_document(50_000 + k, n_shapes=(256, 1024, 4096)[(k // 6) % 3]))
         n += sc.n_paths
         k += 1
         yield sc
@@ -116,6 +123,29 @@ def evaluate(r: pfcuda.Renderer, sc, mul: float, add: float, pool: float, repeat
     }
 
 
+def held_out_batches_():
+    """Batches unlike any training scene's seeds: the benchmark's kinds at a smaller count."""
+    import svg_docs
+    yield "batched_64", S.batched(n_scenes=64, first_seed=9000)
+    yield "batched_stroked_64", S.batched_stroked(n_scenes=64, first_seed=9100)
+    rng = np.random.default_rng(9200)
+    sizes = np.exp(rng.uniform(np.log(16), np.log(1024), 64)).astype(int)
+    yield "svg_64", [pfcuda.parse_svg(svg_docs.random_document(9200 + i, n_shapes=int(sizes[i]))) for i in range(64)]
+
+
+def evaluate_batch(r: pfcuda.Renderer, scs, repeats: int = 3):
+    """The learned frame over a batch: overflow (frame redone exactly) and equality with the exact frame."""
+    r.upload(scs)
+    r.render()
+    exact = [r.image(i) for i in range(len(scs))]
+    over = [r.render_learned()["overflow"] for _ in range(repeats)]
+    same = all(np.array_equal(r.image(i), exact[i]) for i in range(len(scs)))
+    paths_over, pool_used = r.sizer_last_frame()
+    return {"scenes": len(scs), "paths": int(sum(s.n_paths for s in scs)), "frames_redone_exactly": int(sum(over)),
+            "paths_over_budget": int(paths_over), "spill_pool_slots_used": int(pool_used),
+            "learned_equals_exact": bool(same)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.join(HERE, "weights", "sizer.bin"))
@@ -151,12 +181,14 @@ def main():
     r.sizer_save(args.out)
 
     held_out = evaluate(r, S.mixed(seed=7, n_paths=8192, side=4096), args.mul, args.add, args.pool)
+    held_out_batches = {name: evaluate_batch(r, scs) for name, scs in held_out_batches_()}
     report = {
         "training_paths": int(len(tr)), "validation_paths": int(n_val), "epochs": args.epochs,
         "batch": args.batch, "lr": args.lr, "epoch_mse": [float(v) for v in losses],
         "validation_mse": val_mse, "collect_s": t_collect, "train_s": t_train,
         "margin": {"mul": args.mul, "add": args.add, "pool": args.pool},
         "held_out_mixed_8192_4096": held_out,
+        "held_out_batches": held_out_batches,
     }
     with open(os.path.splitext(args.out)[0] + "_report.json", "w") as f:
         json.dump(report, f, indent=1)
