@@ -101,3 +101,16 @@ def test_learned_frame_on_documents_equals_exact(pf):
                 assert np.array_equal(r.image(i), exact[i])
     for d in docs:
         d.close()
+
+
+def test_document_without_shapes_renders_clear(pf, renderer):
+    with pf.SvgDocument(svg_docs.HAND["svg_empty"]) as doc:
+        assert doc.view.n_paths == 0
+        renderer.upload_views([doc.view])
+    renderer.render()
+    img = renderer.image()
+    assert img.shape == (32, 64, 4) and not img.any()
+    with pf.SvgDocument("<svg></svg>") as doc:
+        with pytest.raises(pf.PfError) as e:
+            renderer.upload_views([doc.view])
+        assert e.value.status == 1
