@@ -352,6 +352,18 @@ int pf_image_bytes(void *ctx, uint64_t *bytes);
 int pf_image_offset(void *ctx, uint32_t scene, uint64_t *offset);
 int pf_read_images(void *ctx, uint8_t *dst, size_t capacity_bytes);
 
+/*
+ * The last frame's images to host memory without holding up the next frame: the images are
+ * snapshotted on the device (on the context's stream) and copied to dst on a copy stream of the
+ * context; the call returns at once, and later uploads and frames run while the copy does.
+ * pf_images_wait blocks until the last such copy is complete; dst must not be read before.  A
+ * later pf_read_images_async waits on the device for the previous copy before it snapshots
+ * again.  With a host image target (pf_set_host_image) the images are already in host memory
+ * and are copied to dst at once.  dst should be pinned for the copy to run asynchronously.
+ */
+int pf_read_images_async(void *ctx, uint8_t *dst, size_t capacity_bytes);
+int pf_images_wait(void *ctx);
+
 /* Device pointer and pitch of the last rendered image (valid until the next
  * render on this context). */
 int pf_image_device_ptr(void *ctx, void **rgba, uint32_t *width_px, uint32_t *height_px);

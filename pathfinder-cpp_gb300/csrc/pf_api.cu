@@ -119,7 +119,14 @@ struct Ctx {
     uint8_t *host_img_dev = nullptr;  // the same memory as the device addresses it
     size_t host_img_bytes = 0;
     bool host_img_registered = false; // pinned by this context (unpinned when replaced)
-    uint32_t *h_status = nullptr;  // pinned
+    // asynchronous image readback (pf_read_images_async): a device snapshot of the images and
+    // its copy to the host on a stream of its own
+    DevBuf image_snap;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t snap_done = nullptr, copy_done = nullptr;
+    bool copy_pending = false;
+    uint32_t *h_status = nullptr;      // pinned
+    uint32_t *h_status_dev = nullptr;  // the same memory as the device addresses it
 
     // the scene range of the last frame and its totals
     uint32_t r_first = 0, r_count = 0, r_paths = 0, r_contours = 0, r_fb = 0, r_rows = 0;
@@ -837,7 +844,7 @@ Batch make_batch(Ctx *c) {
 
 int read_status(Ctx *c) {
     if (c->capturing) return PF_OK;  // the captured frame's totals are already in h_status
-    PF_CUDA(cudaMemcpyAsync(c->h_status, c->status.p, kStCount * 4, cudaMemcpyDeviceToHost, c->stream));
+    PF_CUDA(launch_copy_words(c->h_status_dev, c->status.as<uint32_t>(), kStCount, c->stream));
     PF_CUDA(cudaStreamSynchronize(c->stream));
     c->syncs++;
     return PF_OK;
@@ -1498,6 +1505,63 @@ extern "C" int pf_read_images(void *ctx, uint8_t *dst, size_t capacity_bytes) {
     return PF_OK;
 }
 
+// The images of the last frame to host memory without holding up the next frame: a
+// device-to-device snapshot on the frame's stream (HBM speed), then the snapshot's copy to dst
+// on the context's copy stream, which runs while later uploads and frames proceed.  The next
+// snapshot waits, on the device, for the previous copy to have left the snapshot buffer.
+extern "C" int pf_read_images_async(void *ctx, uint8_t *dst, size_t capacity_bytes) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !dst) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->rendered) return fail(c, PF_ERR_NOT_READY, "nothing rendered");
+    if (capacity_bytes < c->image_bytes) return fail(c, PF_ERR_INVALID_ARGUMENT, "image buffer too small");
+    cudaSetDevice(c->device);
+    if (c->host_img) {  // the frame already wrote the images into host memory
+        if (dst != c->host_img) {
+            PF_CUDA(cudaStreamSynchronize(c->stream));
+            std::memcpy(dst, c->host_img, c->image_bytes);
+        }
+        return PF_OK;
+    }
+    if (!c->copy_stream) {
+        PF_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        PF_CUDA(cudaEventCreateWithFlags(&c->snap_done, cudaEventDisableTiming));
+        PF_CUDA(cudaEventCreateWithFlags(&c->copy_done, cudaEventDisableTiming));
+    }
+    if (c->copy_pending) {
+        if (c->image_snap.cap < c->image_bytes || !c->image_snap.p) {
+            // the snapshot buffer grows: the copy still reading it must finish first
+            PF_CUDA(cudaEventSynchronize(c->copy_done));
+            c->copy_pending = false;
+        } else {
+            PF_CUDA(cudaStreamWaitEvent(c->stream, c->copy_done, 0));
+        }
+    }
+    PF_CUDA(c->image_snap.ensure(c->image_bytes));
+    PF_CUDA(cudaMemcpyAsync(c->image_snap.p, c->image.p, c->image_bytes, cudaMemcpyDeviceToDevice, c->stream));
+    PF_CUDA(cudaEventRecord(c->snap_done, c->stream));
+    PF_CUDA(cudaStreamWaitEvent(c->copy_stream, c->snap_done, 0));
+    // in 32 MB pieces: a frame's own small device-to-host reads (its status words) would
+    // otherwise queue behind the whole copy on the copy engine
+    constexpr size_t kPiece = size_t(32) << 20;
+    for (size_t off = 0; off < c->image_bytes; off += kPiece)
+        PF_CUDA(cudaMemcpyAsync(dst + off, c->image_snap.as<uint8_t>() + off, std::min(kPiece, c->image_bytes - off),
+                                cudaMemcpyDeviceToHost, c->copy_stream));
+    PF_CUDA(cudaEventRecord(c->copy_done, c->copy_stream));
+    c->copy_pending = true;
+    return PF_OK;
+}
+
+extern "C" int pf_images_wait(void *ctx) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    if (c->copy_pending) {
+        cudaSetDevice(c->device);
+        PF_CUDA(cudaEventSynchronize(c->copy_done));
+        c->copy_pending = false;
+    }
+    return PF_OK;
+}
+
 // Frames composite straight into host memory over the GPU's coherent link (NVLink-C2C on
 // GB300): the pixels cross to the host while the composite runs, and no copy follows the
 // frame.  The buffer is pinned and mapped here unless the caller pinned it already (then it
@@ -1570,7 +1634,8 @@ int pf_ctx_create(const pf_config *config, void **out) {
         e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
         c->own_stream = e == cudaSuccess;
     }
-    if (e == cudaSuccess) e = cudaMallocHost(&c->h_status, kStCount * 4);
+    if (e == cudaSuccess) e = cudaHostAlloc(&c->h_status, kStCount * 4, cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&c->h_status_dev), c->h_status, 0);
     for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
     if (e == cudaSuccess) e = c->status.ensure(kStCount * 4);
     if (e != cudaSuccess) {
@@ -1587,6 +1652,12 @@ int pf_ctx_destroy(void *ctx) {
     if (!c) return PF_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copy_stream) {
+        cudaStreamSynchronize(c->copy_stream);
+        cudaStreamDestroy(c->copy_stream);
+    }
+    if (c->snap_done) cudaEventDestroy(c->snap_done);
+    if (c->copy_done) cudaEventDestroy(c->copy_done);
     drop_graph(c);
     drop_host_image(c);
     DevBuf *bufs[] = {&c->sz_w, &c->sz_master, &c->sz_m, &c->sz_v, &c->sz_grad, &c->sz_loss, &c->sz_feat,
@@ -1605,7 +1676,7 @@ int pf_ctx_destroy(void *ctx) {
                       &c->st_dashes, &c->st_scenes, &c->st_cfirst, &c->dash_pts, &c->dash_cnt, &c->dash_end,
                       &c->dash_points, &c->dash_flags, &c->job_first, &c->jobs, &c->job_pts, &c->st_bounds,
                       &c->job_units, &c->job_nfwd, &c->job_flags, &c->job_cap1, &c->job_end, &c->units,
-                      &c->unit_leaves, &c->st_leaves, &c->leaf_pts, &c->path_grad, &c->grad_paint,
+                      &c->unit_leaves, &c->st_leaves, &c->leaf_pts, &c->path_grad, &c->grad_paint, &c->image_snap,
                       &c->grad_stop_range, &c->grad_stops, &c->grad_meta, &c->grad_ramp, &c->st_order_ctl,
                       &c->unit_order, &c->dash_order};
     for (DevBuf *b : bufs) b->release();

@@ -241,6 +241,7 @@ struct StrokeIn {
 size_t stroke_order_ctl_bytes();
 cudaError_t launch_stroke_order(const StrokeIn &in, int what, uint32_t *ctl, uint32_t *order, cudaStream_t st);
 cudaError_t launch_dash(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);
+cudaError_t launch_copy_words(uint32_t *dst, const uint32_t *src, uint32_t n, cudaStream_t st);
 cudaError_t launch_stroke_jobs(const StrokeIn &in, bool fill, cudaStream_t st);
 cudaError_t launch_stroke(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);
 cudaError_t launch_units(const StrokeIn &in, bool write, cudaStream_t st);

@@ -2026,6 +2026,17 @@ cudaError_t launch_pool_lists(const Batch &b, bool scatter, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+// Status words to pinned host memory by a kernel rather than a copy-engine transfer, so a
+// frame's readback never queues behind a large device-to-host copy (pf_read_images_async).
+__global__ void k_copy_words(uint32_t *dst, const uint32_t *src, uint32_t n) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+cudaError_t launch_copy_words(uint32_t *dst, const uint32_t *src, uint32_t n, cudaStream_t st) {
+    if (n) PF_LAUNCH(k_copy_words<<<1, 64, 0, st>>>(dst, src, n));
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st) {
     if (!b.n_rows) return cudaSuccess;
     if (write) PF_LAUNCH(k_rows<true><<<b.n_rows, kRowThreads, 0, st>>>(b));

@@ -31,6 +31,7 @@ EXPORTS = [
     "pf_sizer_gradient", "pf_sizer_train", "pf_sizer_save", "pf_sizer_load", "pf_path_features", "pf_path_counts",
     "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags", "pf_sizer_predict_noalloc",
     "pf_set_host_image", "pf_read_outline", "pf_upload_stats_get", "pf_svg_parse", "pf_svg_scene", "pf_svg_free",
+    "pf_read_images_async", "pf_images_wait",
 ]
 
 N_FEATURES = 12
@@ -362,6 +363,14 @@ class Renderer:
     def read_images(self, dst_ptr: int, capacity: int) -> None:
         """Copy every image of the batch into host memory at dst_ptr (one transfer)."""
         self._check(self.lib.pf_read_images(self.ctx, C.c_void_p(dst_ptr), C.c_size_t(capacity)), self.ctx)
+
+    def read_images_async(self, dst_ptr: int, capacity: int) -> None:
+        """Start delivering the last frame's images to dst (pinned host memory); returns at once.
+        Call images_wait() before reading dst."""
+        self._check(self.lib.pf_read_images_async(self.ctx, C.c_void_p(dst_ptr), C.c_size_t(capacity)), self.ctx)
+
+    def images_wait(self) -> None:
+        self._check(self.lib.pf_images_wait(self.ctx), self.ctx)
 
     def set_host_image(self, host_ptr: Optional[int], capacity: int = 0) -> None:
         """Composite later frames straight into host memory at host_ptr (None: device images)."""

@@ -35,4 +35,6 @@ def test_null_arguments_are_rejected_without_a_device(pf):
     assert lib.pf_scene_upload(None, None) == 1
     assert lib.pf_render(None, None) == 1
     assert lib.pf_ctx_destroy(None) == 0
+    assert lib.pf_read_images_async(None, None, 0) == 1
+    assert lib.pf_images_wait(None) == 1
     assert isinstance(lib.pf_last_error(None), bytes)
