@@ -161,6 +161,13 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def wait_first(self, timeout: float = 10.0):
+        """Block until nvidia-smi has printed its first sample (its start-up stays out of the
+        timed regions)."""
+        t0 = time.time()
+        while self.proc and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.05)
+
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -345,14 +352,15 @@ def main():
         r.render()
     ms_exact, stats_e = timed(lambda: r.render(), args.steps)
 
-    # 2. batched learned one-pass frame (the headline), inputs resident
+    # 2. batched learned one-pass frame (the headline), inputs resident.  Clocks are sampled
+    #    from here through the end-to-end runs.
     frame = r.render_learned if learned else r.render
-    for _ in range(args.warmup):
-        frame()
     clocks = ClockSampler(local_rank)
     clocks.start()
+    clocks.wait_first()
+    for _ in range(args.warmup):
+        frame()
     ms_batched, stats_b = timed(frame, args.steps)
-    clk = clocks.stop()
     st = stats_b[-1]
     sizer = None
     if learned:
@@ -362,6 +370,7 @@ def main():
                  "exact_host_syncs": stats_e[-1]["host_syncs"]}
 
     if args.profile_frames:
+        clocks.stop()
         if rank == 0:
             print(json.dumps({"profile_frames": True, "exact_ms": ms_exact, "learned_ms": ms_batched,
                               "exact_stats": stats_e[-1], "learned_stats": st}), flush=True)
@@ -418,6 +427,7 @@ def main():
         e2e_step_host()
     ms_e2e_host, _ = timed(e2e_step_host, args.steps)
     r.set_host_image(None)
+    clk = clocks.stop()
 
     # SVG documents end to end (--svg): every step parses the documents' text on the host
     # (pf_svg_parse on a thread pool; ctypes releases the interpreter lock), uploads straight

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <mutex>
 #include <new>
 #include <string>
@@ -21,6 +22,8 @@
 using namespace pfc;
 
 namespace {
+
+constexpr size_t kStageBytes = 64 << 10;  // mapped host staging for small device reads
 
 struct DevBuf {
     void *p = nullptr;
@@ -127,6 +130,7 @@ struct Ctx {
     bool copy_pending = false;
     uint32_t *h_status = nullptr;      // pinned
     uint32_t *h_status_dev = nullptr;  // the same memory as the device addresses it
+    uint8_t *h_stage = nullptr, *h_stage_dev = nullptr;  // mapped staging for small reads
 
     // the scene range of the last frame and its totals
     uint32_t r_first = 0, r_count = 0, r_paths = 0, r_contours = 0, r_fb = 0, r_rows = 0;
@@ -300,10 +304,29 @@ struct CopyPlan {
     }
 };
 
+// Device to host and wait.  Small reads go through a kernel into mapped host memory, not the
+// copy engine, so they never queue behind an image copy (pf_read_images_async).
 template <class T>
 int d2h_wait(Ctx *c, T *host, const void *dev, size_t count) {
-    PF_CUDA(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+    const size_t bytes = count * sizeof(T);
+    if (bytes <= kStageBytes) {
+        PF_CUDA(launch_copy_bytes(c->h_stage_dev, static_cast<const uint8_t *>(dev), (uint32_t)bytes, c->stream));
+        PF_CUDA(cudaStreamSynchronize(c->stream));
+        std::memcpy(host, c->h_stage, bytes);
+        return PF_OK;
+    }
+    PF_CUDA(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->stream));
     PF_CUDA(cudaStreamSynchronize(c->stream));
+    return PF_OK;
+}
+
+// Single words from device memory, gathered by one kernel into mapped host memory, and wait.
+int read_words(Ctx *c, std::initializer_list<const uint32_t *> src, uint32_t *out) {
+    WordSources s{};
+    for (const uint32_t *p : src) s.p[s.n++] = p;
+    PF_CUDA(launch_gather_words(reinterpret_cast<uint32_t *>(c->h_stage_dev), s, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    std::memcpy(out, c->h_stage, s.n * 4);
     return PF_OK;
 }
 
@@ -392,13 +415,13 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
         PF_CUDA(launch_dash(in, false, status, st));
         PF_CUDA(scan_exclusive_u32(in.dash_pts, in.dash_pts, N, in.dash_pts + N, c->scan_temp.p, st, status));
         PF_CUDA(scan_exclusive_u32(in.dash_cnt, in.dash_cnt, N, in.dash_cnt + N, c->scan_temp.p, st, status));
-        uint32_t tot[3];
-        uint64_t wide = 0;  // the 64-bit total of the dash points (slots 16-17)
+        uint32_t tot[3], w[5];
         PF_CUDA(mark(1));
-        PF_CUDA(cudaMemcpyAsync(&tot[0], in.dash_pts + N, 4, cudaMemcpyDeviceToHost, st));
-        PF_CUDA(cudaMemcpyAsync(&tot[1], in.dash_cnt + N, 4, cudaMemcpyDeviceToHost, st));
-        PF_CUDA(cudaMemcpyAsync(&wide, status + kStFill64, 8, cudaMemcpyDeviceToHost, st));
-        if (int e = d2h_wait(c, &tot[2], status + kStErr, 1)) return e;
+        if (int e = read_words(c, {in.dash_pts + N, in.dash_cnt + N, status + kStFill64, status + kStFill64 + 1,
+                                   status + kStErr}, w))
+            return e;
+        tot[0] = w[0], tot[1] = w[1], tot[2] = w[4];
+        const uint64_t wide = uint64_t(w[2]) | uint64_t(w[3]) << 32;  // the dash points' 64-bit total
         if (tot[2] & kErrStroke)
             return fail(c, PF_ERR_KERNEL_LIMIT, "a dash pattern needs more than 2^22 steps on one path");
         if (tot[2]) return fail(c, PF_ERR_CUDA, "dash pass failed");
@@ -493,12 +516,12 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
     PF_CUDA(scan_exclusive_u32(in.leaf_pts, in.leaf_pts, NL, in.leaf_pts + NL, c->scan_temp.p, st, status));
     PF_CUDA(launch_job_totals(in, status, st));
     PF_CUDA(scan_exclusive_u32(in.job_pts, in.job_pts, J, in.job_pts + J, c->scan_temp.p, st, status));
-    uint32_t tot[2];
-    uint64_t wide = 0;  // the 64-bit total of the output points (slots 18-19)
+    uint32_t tot[2], w[4];
     PF_CUDA(mark(5));
-    PF_CUDA(cudaMemcpyAsync(&tot[0], in.job_pts + J, 4, cudaMemcpyDeviceToHost, st));
-    PF_CUDA(cudaMemcpyAsync(&wide, status + kStFill64 + 2, 8, cudaMemcpyDeviceToHost, st));
-    if (int e = d2h_wait(c, &tot[1], status + kStErr, 1)) return e;
+    if (int e = read_words(c, {in.job_pts + J, status + kStFill64 + 2, status + kStFill64 + 3, status + kStErr}, w))
+        return e;
+    tot[0] = w[0], tot[1] = w[3];
+    const uint64_t wide = uint64_t(w[1]) | uint64_t(w[2]) << 32;  // the output points' 64-bit total
     if (int e = span()) return e;
     if (wide >= (1ull << 31)) return fail(c, PF_ERR_OVERFLOW, "stroked outline too large (2^31 points)");
     if (tot[1] & kErrStroke)
@@ -1636,6 +1659,8 @@ int pf_ctx_create(const pf_config *config, void **out) {
     }
     if (e == cudaSuccess) e = cudaHostAlloc(&c->h_status, kStCount * 4, cudaHostAllocMapped);
     if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&c->h_status_dev), c->h_status, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc(&c->h_stage, kStageBytes, cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&c->h_stage_dev), c->h_stage, 0);
     for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
     if (e == cudaSuccess) e = c->status.ensure(kStCount * 4);
     if (e != cudaSuccess) {
@@ -1685,6 +1710,7 @@ int pf_ctx_destroy(void *ctx) {
     for (auto &e : c->sev)
         if (e) cudaEventDestroy(e);
     if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->own_stream) cudaStreamDestroy(c->stream);
     delete c;
     return PF_OK;

@@ -242,6 +242,13 @@ size_t stroke_order_ctl_bytes();
 cudaError_t launch_stroke_order(const StrokeIn &in, int what, uint32_t *ctl, uint32_t *order, cudaStream_t st);
 cudaError_t launch_dash(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);
 cudaError_t launch_copy_words(uint32_t *dst, const uint32_t *src, uint32_t n, cudaStream_t st);
+// up to 8 single words gathered into dst[0, n)
+struct WordSources {
+    const uint32_t *p[8];
+    uint32_t n;
+};
+cudaError_t launch_gather_words(uint32_t *dst, const WordSources &s, cudaStream_t st);
+cudaError_t launch_copy_bytes(uint8_t *dst, const uint8_t *src, uint32_t n, cudaStream_t st);
 cudaError_t launch_stroke_jobs(const StrokeIn &in, bool fill, cudaStream_t st);
 cudaError_t launch_stroke(const StrokeIn &in, bool write, uint32_t *status, cudaStream_t st);
 cudaError_t launch_units(const StrokeIn &in, bool write, cudaStream_t st);

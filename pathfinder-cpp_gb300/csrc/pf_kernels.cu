@@ -2037,6 +2037,25 @@ cudaError_t launch_copy_words(uint32_t *dst, const uint32_t *src, uint32_t n, cu
     return cudaGetLastError();
 }
 
+// Small device reads (totals, flags, per-scene bounds) into mapped host memory the same way.
+__global__ void k_copy_bytes(uint8_t *dst, const uint8_t *src, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
+__global__ void k_gather_words(uint32_t *dst, WordSources s) {
+    if (threadIdx.x < s.n) dst[threadIdx.x] = *s.p[threadIdx.x];
+}
+
+cudaError_t launch_copy_bytes(uint8_t *dst, const uint8_t *src, uint32_t n, cudaStream_t st) {
+    if (n) PF_LAUNCH(k_copy_bytes<<<std::min<uint32_t>((n + 255) / 256, 64), 256, 0, st>>>(dst, src, n));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gather_words(uint32_t *dst, const WordSources &s, cudaStream_t st) {
+    if (s.n) PF_LAUNCH(k_gather_words<<<1, 32, 0, st>>>(dst, s));
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st) {
     if (!b.n_rows) return cudaSuccess;
     if (write) PF_LAUNCH(k_rows<true><<<b.n_rows, kRowThreads, 0, st>>>(b));
