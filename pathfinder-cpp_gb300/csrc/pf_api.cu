@@ -982,11 +982,10 @@ int stage_setup(Ctx *c, bool learned) {
         PF_CUDA(launch_mlp_predict(c->sz_w.as<__nv_bfloat16>(), c->path_feat.as<float>(), N, c->path_pred.as<float>(),
                                    st));
         PF_CUDA(launch_budgets(b, c->path_pred.as<float>(), c->sz_mul, c->sz_add, b.path_leaf_first,
-                               c->path_fill_budget.as<uint32_t>(), st));
+                               c->path_fill_budget.as<uint32_t>(), b.path_leaf_cursor, st));
         PF_CUDA(cudaMemcpyAsync(b.path_leaf_budget, b.path_leaf_first, size_t(N) * 4, cudaMemcpyDeviceToDevice, st));
         PF_CUDA(cudaMemsetAsync(b.path_leaf_first + N, 0, 4, st));
         PF_CUDA(cudaMemsetAsync(c->path_fill_budget.as<uint32_t>() + N, 0, 4, st));
-        PF_CUDA(cudaMemsetAsync(b.path_leaf_cursor, 0, size_t(N) * 4, st));
         if (int e = scan(c, b.path_leaf_first, N + 1, kStLeafBudget)) return e;
         if (int e = scan(c, c->path_fill_budget.as<uint32_t>(), N + 1, kStFillBudget)) return e;
     }

@@ -286,7 +286,7 @@ cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t
 cudaError_t launch_features(const Batch &b, const uint2 *path_contours, float4 *contour_scratch, float *feat,
                             cudaStream_t st);
 cudaError_t launch_budgets(const Batch &b, const float *pred, float mul, float add, uint32_t *leaf_budget,
-                           uint32_t *fill_budget, cudaStream_t st);
+                           uint32_t *fill_budget, uint32_t *leaf_cursor, cudaStream_t st);
 cudaError_t launch_path_counts(const Batch &b, const uint2 *path_contours, uint32_t *leaves, uint32_t *fills,
                                cudaStream_t st);
 cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t st);

@@ -751,6 +751,11 @@ __global__ void __launch_bounds__(kThreads, 5) k_flatten_budget(Batch b, uint32_
     const uint32_t i = b.seg_order ? b.seg_order[t] : t;
     const SegDev sg = b.segs[i];
     const uint32_t region = b.path_leaf_first[sg.path], budget = b.path_leaf_budget[sg.path];
+    // the segment's first leaf: the slot of the segment's index within its path (the budget
+    // covers every segment), so a line segment writes without an atomic and consecutive
+    // segments of a path write consecutive slots
+    const uint32_t own = region + (i - b.contour_segs[b.path_contours[sg.path].x]);
+    bool own_done = false;
     // pending leaves, in registers (an indexed array would live in local memory)
     float4 q0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), q1 = q0, q2 = q0, q3 = q0;
     uint32_t npend = 0;
@@ -783,12 +788,17 @@ __global__ void __launch_bounds__(kThreads, 5) k_flatten_budget(Batch b, uint32_
     };
     auto emit = [&](float x0, float y0, float x1, float y1) {
         const float4 v = make_float4(x0, y0, x1, y1);
+        produced++;
+        if (!own_done) {
+            b.leaves[own] = v;
+            own_done = true;
+            return;
+        }
         if (npend == 0) q0 = v;
         else if (npend == 1) q1 = v;
         else if (npend == 2) q2 = v;
         else q3 = v;
         if (++npend == (uint32_t)kLeafBatch) flush();
-        produced++;
     };
     const float2 p0 = b.points[sg.a];
     switch (sg.kind) {

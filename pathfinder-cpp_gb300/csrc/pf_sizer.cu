@@ -143,15 +143,20 @@ __global__ void k_features(Batch b, const uint2 *path_contours, const float4 *cf
 }
 
 // Per-path leaf budget (and fill estimate) from the sizer's prediction:
-// budget = ceil(expm1(prediction) * mul + add).
+// budget = ceil(expm1(prediction) * mul + add), and at least the path's segment count: every
+// segment yields at least one leaf, and a segment's first leaf goes to the slot of its own
+// index in the path's region (k_flatten_budget), so the region's write cursor starts past them.
 __global__ void k_budgets(Batch b, const float *pred, float mul, float add, uint32_t *leaf_budget,
-                          uint32_t *fill_budget) {
+                          uint32_t *fill_budget, uint32_t *leaf_cursor) {
     const uint32_t p = global_tid();
     if (p >= b.n_paths) return;
     const float l = fmaxf(expm1f(fminf(pred[2 * p + 0], 30.0f)), 0.0f);
     const float f = fmaxf(expm1f(fminf(pred[2 * p + 1], 30.0f)), 0.0f);
-    leaf_budget[p] = (uint32_t)fminf(ceilf(l * mul + add), 1.0e9f);
+    const uint2 cr = b.path_contours[p];
+    const uint32_t n_segs = b.contour_segs[cr.y] - b.contour_segs[cr.x];
+    leaf_budget[p] = max((uint32_t)fminf(ceilf(l * mul + add), 1.0e9f), n_segs);
     fill_budget[p] = (uint32_t)fminf(ceilf(f * mul + add), 1.0e9f);
+    leaf_cursor[p] = n_segs;
 }
 
 // Exact per-path counts of the last exact frame (training labels): leaf lines and fills.
@@ -342,10 +347,10 @@ cudaError_t launch_features(const Batch &b, const uint2 *path_contours, float4 *
 }
 
 cudaError_t launch_budgets(const Batch &b, const float *pred, float mul, float add, uint32_t *leaf_budget,
-                           uint32_t *fill_budget, cudaStream_t st) {
+                           uint32_t *fill_budget, uint32_t *leaf_cursor, cudaStream_t st) {
     if (b.n_paths) {
         k_budgets<<<(b.n_paths + kThreads - 1) / kThreads, kThreads, 0, st>>>(b, pred, mul, add, leaf_budget,
-                                                                             fill_budget);
+                                                                             fill_budget, leaf_cursor);
         count_launches(1);
     }
     return cudaGetLastError();
