@@ -943,7 +943,7 @@ int begin_frame(Ctx *c, uint32_t first, uint32_t count) {
     PF_CUDA(bin_stage_bytes(&stage_bytes));
     PF_CUDA(c->bin_stage.ensure(stage_bytes));
     PF_CUDA(c->path_cls.ensure(size_t(N) + 16));
-    PF_CUDA(c->bin_ctl.ensure(64));
+    PF_CUDA(c->bin_ctl.ensure(1024));
     PF_CUDA(c->path_leaf_range.ensure(size_t(N) * 8 + 16));
     if (!c->h_path_clip.empty()) PF_CUDA(c->path_clip_rel.ensure(size_t(N) * 4 + 16));
     return PF_OK;
@@ -1015,7 +1015,7 @@ int stage_setup(Ctx *c, bool learned) {
 int bin_and_composite(Ctx *c, Batch b, bool learned) {
     cudaStream_t st = c->stream;
     for (int attempt = 0;; attempt++) {
-        PF_CUDA(cudaMemsetAsync(b.bin_ctl, 0, 64, st));
+        PF_CUDA(cudaMemsetAsync(b.bin_ctl, 0, 1024, st));
         PF_CUDA(cudaMemsetAsync(b.status + kStFill64, 0, 8, st));
         PF_CUDA(launch_bin_classify(b, learned, st));
         PF_CUDA(launch_bin_paths(b, st));

@@ -855,6 +855,11 @@ constexpr uint32_t kCtaMaxLeaves = 1u << 22;
 // bin_ctl slots: paths per CTA class, work tickets per CTA class, tickets of the class-3
 // zeroing and set-up passes, and at slot 12 a 64-bit word: class-3 paths << 40 | their lines.
 enum : int { kCtlCount = 0, kCtlTicket = 4, kCtlTicketZero = 8, kCtlTicketPrep = 9, kCtl3 = 12 };
+// and from slot 16 the CTA classes' paths counted by log2 of their leaf lines (3 x 32), then
+// the write cursors of those buckets (3 x 32): each class's list runs from its largest paths to
+// its smallest, so the last CTAs to start take the shortest paths
+enum : int { kCtlBucket = 16, kCtlCursor = 16 + 3 * 32, kCtlWords = 16 + 6 * 32 };
+static_assert(kCtlWords * 4 <= 1024, "bin_ctl holds 1024 bytes");
 constexpr uint64_t kLow40 = (1ull << 40) - 1;
 
 __device__ __forceinline__ unsigned long long *ctl3_word(const Batch &b) {
@@ -926,6 +931,15 @@ __device__ __forceinline__ void add_delta_u16(uint16_t *a, int d, uint32_t *stat
 // Leaf ranges of every path and the size classes.  Classes 0-2 are listed with one atomic per
 // warp and class; class-3 paths take a 64-bit atomic that also hands out their offsets in the
 // class-3 line numbering the global passes stride over.
+// log2 of a path's leaf lines (its range and its spill-pool lines), after k_bin_classify
+// stored the range
+__device__ __forceinline__ int bin_bucket(const Batch &b, uint32_t p) {
+    const uint2 range = b.path_leaf_range[p];
+    uint32_t n = range.y - range.x;
+    if (b.pool_cnt) n += b.pool_cnt[p] - b.pool_cnt[(int64_t)p - 1];
+    return 31 - __clz(max(n, 1u));
+}
+
 __global__ void k_bin_classify(Batch b, bool learned) {
     const uint32_t p = global_tid();
     const int lane = threadIdx.x & 31;
@@ -956,13 +970,41 @@ __global__ void k_bin_classify(Batch b, bool learned) {
 #pragma unroll
     for (int c = 0; c < kCtaClasses; c++) {
         const uint32_t m = __ballot_sync(0xffffffffu, cls == c);
-        if (!m) continue;
-        const int leader = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&b.bin_ctl[kCtlCount + c], (uint32_t)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (cls == c) b.bin_list[(size_t)c * b.n_paths + base + __popc(m & ((1u << lane) - 1u))] = p;
+        if (m && lane == __ffs(m) - 1) atomicAdd(&b.bin_ctl[kCtlCount + c], (uint32_t)__popc(m));
     }
+    // the bucket of a CTA-class path: log2 of its leaf lines
+    const int key = cls >= 0 && cls < kCtaClasses ? cls * 32 + bin_bucket(b, p) : -1;
+    const unsigned g = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && lane == __ffs(g) - 1) atomicAdd(&b.bin_ctl[kCtlBucket + key], (uint32_t)__popc(g));
+}
+
+// The buckets' cursors, largest lines first within each class.
+__global__ void k_bin_bucket_starts(Batch b) {
+    const int c = threadIdx.x;
+    if (c >= kCtaClasses) return;
+    uint32_t off = 0;
+    for (int k = 31; k >= 0; k--) {
+        b.bin_ctl[kCtlCursor + c * 32 + k] = off;
+        off += b.bin_ctl[kCtlBucket + c * 32 + k];
+    }
+}
+
+// Each CTA-class path into its class list at its bucket's cursor.
+__global__ void k_bin_scatter(Batch b) {
+    const uint32_t p = global_tid();
+    const int lane = threadIdx.x & 31;
+    int key = -1;
+    if (p < b.n_paths) {
+        const int cls = (int)(int8_t)b.path_cls[p];
+        if (cls >= 0 && cls < kCtaClasses) key = cls * 32 + bin_bucket(b, p);
+    }
+    const unsigned g = __match_any_sync(0xffffffffu, key);
+    if (key < 0) return;
+    const int leader = __ffs(g) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&b.bin_ctl[kCtlCursor + key], (uint32_t)__popc(g));
+    base = __shfl_sync(g, base, leader);
+    b.bin_list[(size_t)(key >> 5) * b.n_paths + base + __popc(g & ((1u << lane) - 1u))] = p;
 }
 
 // Tiles a line's walk visits at most (its end points' tile distance, before clipping, plus one):
@@ -1965,7 +2007,11 @@ cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t 
 }
 
 cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st) {
-    if (b.n_paths) PF_LAUNCH(k_bin_classify<<<grid_for(b.n_paths), kThreads, 0, st>>>(b, learned));
+    if (b.n_paths) {
+        PF_LAUNCH(k_bin_classify<<<grid_for(b.n_paths), kThreads, 0, st>>>(b, learned));
+        PF_LAUNCH(k_bin_bucket_starts<<<1, 32, 0, st>>>(b));
+        PF_LAUNCH(k_bin_scatter<<<grid_for(b.n_paths), kThreads, 0, st>>>(b));
+    }
     return cudaGetLastError();
 }
 
