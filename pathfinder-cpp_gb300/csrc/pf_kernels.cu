@@ -745,7 +745,7 @@ __device__ void walk_line_warp(const WalkCtx &w, float4 f, OnFill &&on_fill, OnD
 // redone by the exact two-pass method.
 constexpr int kLeafBatch = 4;
 
-__global__ void __launch_bounds__(kThreads, 5) k_flatten_budget(Batch b, uint32_t n_segs) {
+__global__ void __launch_bounds__(kThreads, 4) k_flatten_budget(Batch b, uint32_t n_segs) {
     const uint32_t t = global_tid();
     if (t >= n_segs || t >= b.status[kStSegs]) return;
     const uint32_t i = b.seg_order ? b.seg_order[t] : t;
