@@ -242,8 +242,9 @@ struct GradStop {
 struct GradData {
     std::string id, ref;
     int type = kLinear;
-    Coord x1{0.0f, kPercent}, y1{0.0f, kPercent}, x2{100.0f, kPercent}, y2{0.0f, kPercent};
-    Coord cx{50.0f, kPercent}, cy{50.0f, kPercent}, r{50.0f, kPercent}, fx{0.0f, kUser}, fy{0.0f, kUser};
+    // nanosvg keeps the linear and radial coordinates in one union, so x1/cx, y1/cy, x2/r and
+    // y2/fx share a slot (an attribute of the other kind lands in it); fy has its own
+    Coord u[5] = {{0.0f, kUser}, {0.0f, kUser}, {0.0f, kUser}, {0.0f, kUser}, {0.0f, kUser}};
     int spread = 0;  // pad, reflect, repeat
     bool object_space = true;
     float xform[6];
@@ -487,16 +488,16 @@ bool create_gradient(Parser &p, const char *id, const float *lb, PaintDesc &out)
     Grad g{};
     g.type = data->type;
     if (data->type == kLinear) {
-        g.x1 = p.to_pixels(data->x1, ox, sw);
-        g.y1 = p.to_pixels(data->y1, oy, sh);
-        g.x2 = p.to_pixels(data->x2, ox, sw);
-        g.y2 = p.to_pixels(data->y2, oy, sh);
+        g.x1 = p.to_pixels(data->u[0], ox, sw);
+        g.y1 = p.to_pixels(data->u[1], oy, sh);
+        g.x2 = p.to_pixels(data->u[2], ox, sw);
+        g.y2 = p.to_pixels(data->u[3], oy, sh);
     } else {
-        g.cx = p.to_pixels(data->cx, ox, sw);
-        g.cy = p.to_pixels(data->cy, oy, sh);
-        g.fx = p.to_pixels(data->fx, ox, sw);
-        g.fy = p.to_pixels(data->fy, oy, sh);
-        g.r = p.to_pixels(data->r, 0, sl);
+        g.cx = p.to_pixels(data->u[0], ox, sw);
+        g.cy = p.to_pixels(data->u[1], oy, sh);
+        g.fx = p.to_pixels(data->u[3], ox, sw);
+        g.fy = p.to_pixels(data->u[4], oy, sh);
+        g.r = p.to_pixels(data->u[2], 0, sl);
     }
     std::memcpy(g.xform2, data->xform, sizeof g.xform2);
     std::memcpy(g.xform3, p.cur().xform, sizeof g.xform3);
@@ -1277,6 +1278,11 @@ void parse_svg(Parser &p, const char **attr) {
 void parse_gradient(Parser &p, const char **attr, int type) {
     GradData g;
     g.type = type;
+    if (type == kLinear) {  // x1 0%, y1 0%, x2 100%, y2 0%
+        g.u[0] = {0.0f, kPercent}, g.u[1] = {0.0f, kPercent}, g.u[2] = {100.0f, kPercent}, g.u[3] = {0.0f, kPercent};
+    } else {  // cx, cy, r 50%
+        g.u[0] = {50.0f, kPercent}, g.u[1] = {50.0f, kPercent}, g.u[2] = {50.0f, kPercent};
+    }
     xf_identity(g.xform);
     for (int i = 0; attr[i]; i += 2) {
         if (std::strcmp(attr[i], "id") == 0) {
@@ -1285,15 +1291,15 @@ void parse_gradient(Parser &p, const char **attr, int type) {
             const char *n = attr[i], *v = attr[i + 1];
             if (std::strcmp(n, "gradientUnits") == 0) g.object_space = std::strcmp(v, "objectBoundingBox") == 0;
             else if (std::strcmp(n, "gradientTransform") == 0) parse_transform(g.xform, v);
-            else if (std::strcmp(n, "cx") == 0) g.cx = parse_coord_raw(v);
-            else if (std::strcmp(n, "cy") == 0) g.cy = parse_coord_raw(v);
-            else if (std::strcmp(n, "r") == 0) g.r = parse_coord_raw(v);
-            else if (std::strcmp(n, "fx") == 0) g.fx = parse_coord_raw(v);
-            else if (std::strcmp(n, "fy") == 0) g.fy = parse_coord_raw(v);
-            else if (std::strcmp(n, "x1") == 0) g.x1 = parse_coord_raw(v);
-            else if (std::strcmp(n, "y1") == 0) g.y1 = parse_coord_raw(v);
-            else if (std::strcmp(n, "x2") == 0) g.x2 = parse_coord_raw(v);
-            else if (std::strcmp(n, "y2") == 0) g.y2 = parse_coord_raw(v);
+            else if (std::strcmp(n, "cx") == 0) g.u[0] = parse_coord_raw(v);
+            else if (std::strcmp(n, "cy") == 0) g.u[1] = parse_coord_raw(v);
+            else if (std::strcmp(n, "r") == 0) g.u[2] = parse_coord_raw(v);
+            else if (std::strcmp(n, "fx") == 0) g.u[3] = parse_coord_raw(v);
+            else if (std::strcmp(n, "fy") == 0) g.u[4] = parse_coord_raw(v);
+            else if (std::strcmp(n, "x1") == 0) g.u[0] = parse_coord_raw(v);
+            else if (std::strcmp(n, "y1") == 0) g.u[1] = parse_coord_raw(v);
+            else if (std::strcmp(n, "x2") == 0) g.u[2] = parse_coord_raw(v);
+            else if (std::strcmp(n, "y2") == 0) g.u[3] = parse_coord_raw(v);
             else if (std::strcmp(n, "spreadMethod") == 0) {
                 if (std::strcmp(v, "pad") == 0) g.spread = 0;
                 else if (std::strcmp(v, "reflect") == 0) g.spread = 1;

@@ -47,6 +47,13 @@ HAND = {
  stroke-dasharray="5,3,1" stroke-dashoffset="2"/>
 <rect x="0" y="0" width="10" height="10" fill="red" opacity="0.5" display="none"/></svg>""",
     "svg_empty": """<?xml version="1.0"?><!-- nothing to draw --><svg width="64" height="32"></svg>""",
+    # attributes of the other gradient kind land in the shared coordinate slots (x1/cx, y1/cy,
+    # x2/r, y2/fx), and a gradient without stops leaves its shape unpainted
+    "svg_gradient_slots": """<svg width="100" height="100"><defs>
+<linearGradient id="a" cx="0.2" r="0.9"><stop offset="0" stop-color="red"/><stop offset="1" stop-color="blue"/></linearGradient>
+<radialGradient id="b" x1="0.2" x2="0.7" y2="0.4" fy="0.1"><stop offset="0" stop-color="red"/><stop offset="1" stop-color="#0f08"/></radialGradient>
+<linearGradient id="c"/></defs>
+<rect width="50" height="50" fill="url(#a)"/><circle cx="70" cy="70" r="25" fill="url(#b)" stroke="url(#c)"/></svg>""",
 }
 
 _NAMED = ["red", "green", "blue", "yellow", "cyan", "magenta", "black", "grey", "gray", "white", "navy", "olive"]
