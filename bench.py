@@ -280,7 +280,7 @@ def run_reference(args, scenes_list):
     sample = f"every {args.cpu_sample_every}th scene of the batch ({n} scenes), restated d3d9 tiler + FP64 " \
              f"coverage and src-over composite"
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 tiling, f64 coverage",
         "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list, args.clips, args.strokes, args.gradients, args.svg),
