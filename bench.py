@@ -281,6 +281,7 @@ def run_reference(args, scenes_list):
              f"coverage and src-over composite"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "runs_on": f"host CPU only, {threads} threads; no GPU is used (n_gpus is the launch's N)",
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 tiling, f64 coverage",
         "data": "synthetic", "config": workload_config(len(scenes_list), scenes_list, args.clips, args.strokes, args.gradients, args.svg),

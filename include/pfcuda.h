@@ -315,8 +315,9 @@ int pf_set_host_image(void *ctx, void *host, size_t bytes);
 
 /*
  * pf_sizer_predict without any device allocation, for callers that cannot call cudaMalloc
- * (a render loop that must not stall the device, a CUDA-graph capture in progress, or GPU
- * memory owned by another allocator).  No counterpart in the reference.  Features and
+ * (a render loop that must not stall the device, or GPU memory owned by another allocator).
+ * No counterpart in the reference.  It waits on the context's stream for its results before it
+ * returns, as pf_sizer_predict does.  Features and
  * predictions are staged in a fixed device array of 16384 paths (about 0.9 MB, held by every
  * GPU that loads the library until exit); larger n is rejected with PF_ERR_INVALID_ARGUMENT.
  * The first call on a device looks the array up (cudaGetSymbolAddress) - make it before any

@@ -22,7 +22,22 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_ORACLE = os.path.join(HERE, "_build", "libpforacle.so")
 LIB_REF = os.path.join(HERE, "_ref", "libpfref.so")
-REF_ROOT = os.environ.get("PF_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root() -> str:
+    """The reference checkout: PF_REFERENCE_ROOT, else the default of the oracle's Makefile
+    (the one recipe that names where the checkout lies)."""
+    env = os.environ.get("PF_REFERENCE_ROOT")
+    if env:
+        return env
+    try:
+        out = subprocess.run(["make", "-s", "-C", HERE, "ref-root"], capture_output=True, text=True, timeout=30)
+        return out.stdout.strip() if out.returncode == 0 else ""
+    except (OSError, subprocess.SubprocessError):
+        return ""
+
+
+REF_ROOT = _reference_root()
 
 Z_D3D9 = 0
 Z_D3D11 = 1

@@ -2178,12 +2178,12 @@ int pf_render_learned(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_fra
 // Sizer prediction that allocates nothing.
 //
 // Some callers cannot call cudaMalloc: a render loop that plans the next frame's buffers
-// while it must not stall the device (cudaMalloc can synchronise it), code recording a
-// CUDA-graph capture (a plain cudaMalloc is not allowed there), or a host whose GPU memory
-// belongs to another allocator (an engine's own pool) and may not grow.  For them this
+// while it must not stall the device (cudaMalloc can synchronise it), or a host whose GPU
+// memory belongs to another allocator (an engine's own pool) and may not grow.  For them this
 // variant of pf_sizer_predict stages features and predictions in a fixed, file-scope device
 // array instead of context buffers.  It needs a context that already holds sizer weights
-// (pf_sizer_load / pf_sizer_init, which do allocate, once).
+// (pf_sizer_load / pf_sizer_init, which do allocate, once).  Like pf_sizer_predict it waits
+// on the context's stream for its results before it returns.
 //
 // Limit: kNoAllocMaxPaths paths per call (the array is (12 + 2) floats per path, about
 // 0.9 MB, and every GPU that loads this library keeps it until the process exits).

@@ -1,7 +1,7 @@
 """Generate the golden fixtures from the reference's own d3d9 tiler.
 
-Run in a checkout next to the reference sources (the reference tree is read from
-PF_REFERENCE_ROOT, default /root/reference):
+Run in a checkout next to the reference sources (the reference tree is the one
+oracle.REF_ROOT names: PF_REFERENCE_ROOT, else the oracle Makefile's default):
 
     python tests/golden/make_golden.py
 

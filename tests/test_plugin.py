@@ -21,7 +21,9 @@ def test_plugin_packs_reference_scene(tmp_path, oracle_mod, pf):
     oracle_mod.build(reference=True)
     objs = sorted(glob.glob(os.path.join(ROOT, "oracle", "_ref", "obj", "**", "*.o"), recursive=True))
     exe = str(tmp_path / "plugin_driver")
-    cmd = ["g++", "-std=c++17", "-O1", "-msse4.1", "-DPATHFINDER_ENABLE_SIMD", "-DPATHFINDER_ENABLE_COMPUTE",
+    import platform
+    simd = ["-msse4.1"] if platform.machine() in ("x86_64", "AMD64") else []  # Arm: sse2neon.h
+    cmd = ["g++", "-std=c++17", "-O1", *simd, "-DPATHFINDER_ENABLE_SIMD", "-DPATHFINDER_ENABLE_COMPUTE",
            f"-I{ref}/pathfinder", f"-I{ref}/third_party", f"-I{ref}/third_party/umHalf",
            f"-I{ROOT}/include", f"-I{ROOT}/oracle", f"-I{ROOT}/pathfinder-cpp_gb300/plugin", "-w",
            os.path.join(ROOT, "tests", "plugin", "plugin_driver.cpp"),

@@ -1,7 +1,7 @@
 """pf_sizer_predict_noalloc: the sizer's prediction without any device allocation.
 
-Callers that cannot call cudaMalloc (a render loop that must not stall the device, a
-CUDA-graph capture in progress, GPU memory owned by another allocator) use this entry point;
+Callers that cannot call cudaMalloc (a render loop that must not stall the device, GPU memory
+owned by another allocator) use this entry point;
 it stages its data in a fixed device array of the library instead of context buffers.  The
 test calls it through the C-ABI twice in a row and checks it against pf_sizer_predict, the
 allocating entry point, with the tolerance of the other sizer-prediction test; it also checks
