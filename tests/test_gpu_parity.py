@@ -5,6 +5,9 @@ column sums) must be bit-exact; composite lists and z follow the d3d11 z rule;
 RGBA8 pixels must be within 1/255 (one code) of the FP64 analytic-area oracle
 and alpha-tile coverage within 1/255 of it.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
@@ -61,6 +64,11 @@ def test_coverage_within_tolerance_of_fp64_oracle(renderer, oracle_mod, name):
     assert got.shape == want.shape
     err = np.abs(got - want)
     print(f"{name}: coverage max err {err.max():.3e} mean {err.mean():.3e} over {got.shape[0]} alpha tiles")
+    path = os.environ.get("PF_PARITY_LOG")
+    if path:
+        with open(path, "a") as f:
+            f.write(json.dumps({"config": f"coverage:{name}", "alpha_tiles": int(got.shape[0]),
+                                "coverage_max_err": float(err.max()), "coverage_mean_err": float(err.mean())}) + "\n")
     assert err.max() <= COVERAGE_TOL
 
 
