@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define PF_ABI_VERSION 4
+#define PF_ABI_VERSION 5
 
 typedef enum pf_status {
     PF_OK = 0,
@@ -103,6 +103,13 @@ typedef struct pf_paint {
                              m12 y + m13); the identity is {1, 0, 0, 1, 0, 0}            */
 } pf_paint;
 
+/* What a frame does with the destination image before it composites (the tile shader's load
+ * actions, pathfinder/shaders/d3d11/tile.comp:9-10, 744-757; Renderer::draw's
+ * clear_dst_texture, pathfinder/core/d3d11/renderer.cpp:376-380). */
+#define PF_LOAD_CLEAR 0u /* every pixel starts as clear_color                                    */
+#define PF_LOAD_LOAD 1u  /* every pixel starts as the image already there (the last frame's image,
+                            or what pf_write_image put there)                                     */
+
 /* Point flags (pathfinder/core/data/data.h:120-129). */
 #define PF_POINT_ON_CURVE 0u
 #define PF_POINT_CONTROL_0 1u
@@ -122,9 +129,9 @@ typedef struct pf_paint {
  *   fill_rule     [n_paths]     PF_FILL_*
  *   color         [n_paths]     RGBA8 solid paint, red in the low byte;
  *                               src-over (pathfinder/shaders/d3d11/tile.comp:841)
- *   width,height  canvas size in pixels (Scene view box = (0,0,width,height);
- *                 its right edge is rounded up to a multiple of 16 as in
- *                 Scene::set_view_box, pathfinder/core/scene.cpp:170-179)
+ *   width,height  size of the destination image in pixels (ceil(width) x ceil(height)
+ *                 RGBA8); framebuffer tiles cover it from (0, 0), as the tile shader's
+ *                 dispatch covers the destination texture (renderer.cpp:371, 443)
  *   clear_color   RGBA8 colour the destination is cleared to
  *   path_clip     [n_paths] or NULL: the scene-local index of the clip path of each path, or
  *                 PF_NO_CLIP (DrawPath::clip_path, pathfinder/core/data/path.h:36)
@@ -145,6 +152,16 @@ typedef struct pf_paint {
  *   path_paint    [n_paths] or NULL (every path solid): each path's paint; a gradient path's
  *                 colour entry is ignored (its base colour is opaque white, as from_gradient's)
  *   stops         [n_stops]: the colour stops the gradients refer to
+ *   view_box      [4] or NULL: the scene's view box (Scene::set_view_box,
+ *                 pathfinder/core/scene.cpp:169-176) as left, top, right, bottom; NULL is
+ *                 (0, 0, width, height).  Its right edge is rounded up to a multiple of 16 as
+ *                 set_view_box does.  Path tile rects are the paths' bounds intersected with it
+ *                 (core/d3d9/tiler.cpp:317-335) and lines are clipped to its left, right and
+ *                 bottom edges (tiler.cpp:141-153); tiles keep canvas coordinates, so a tile
+ *                 (x, y) lands on pixels [16x, 16x + 16) x [16y, 16y + 16) of the image, and a
+ *                 tile outside the image is never composited.  Coordinates in [-65536, 65536],
+ *                 left <= right, top <= bottom.
+ *   load_action   PF_LOAD_CLEAR or PF_LOAD_LOAD
  */
 typedef struct pf_scene_view {
     const float *points;
@@ -168,6 +185,8 @@ typedef struct pf_scene_view {
     const pf_paint *path_paint;     /* ABI 4 */
     const pf_color_stop *stops;     /* ABI 4 */
     uint32_t n_stops;               /* ABI 4 */
+    const float *view_box;          /* ABI 5 */
+    uint32_t load_action;           /* ABI 5 */
 } pf_scene_view;
 
 /* Context configuration.  Zero-initialise and set what you need. */
@@ -199,8 +218,9 @@ typedef struct pf_frame_stats {
 } pf_frame_stats;
 
 #define PF_CONFIG_STAGE_TIMING 0x1u
-/* Count the composite's work (entries, composited fills) into pf_frame_stats; off by default
- * because the counters cost a few atomics per block. */
+/* Count the composite's work (entries, composited fills) and the draw paths' alpha and visible
+ * tiles into pf_frame_stats; off by default because the counters cost a few atomics per block
+ * and a pass over the tile states. */
 #define PF_CONFIG_FRAME_COUNTERS 0x2u
 
 /*
@@ -279,11 +299,31 @@ int pf_render_scenes(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_fram
  * set-up instead of the exact method's count-then-allocate passes).  Output is identical
  * to pf_render_scenes.  If a prediction is too small the frame is redone by the exact
  * method and stats->overflow is set.  Needs sizer weights (pf_sizer_load / _init).
- * Once such a frame has run, it is recorded as a CUDA graph; the next learned frames over
- * the same scene range replay it (one launch, one synchronisation: stats->host_syncs == 1)
- * until the scenes, the sizer, the flags, the host image target or a buffer changes.
+ * The second such frame in a row over the same upload and scene range is recorded as a CUDA
+ * graph and replayed, and later ones replay it (one launch, one synchronisation:
+ * stats->host_syncs == 1) until the scenes, the sizer, the flags, the host image target or a
+ * buffer changes.
  */
 int pf_render_learned(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats);
+
+/*
+ * The frame to use by default: the learned frame where it pays, else the exact one.  The context
+ * times both frames on the device over the workload (the scene range and its totals of paths,
+ * contours and points: a later upload of scenes of the same size keeps what was measured) as they
+ * run: the first calls run the exact frame until it is timed, the next ones the learned frame
+ * until its time is known (neither frame's first run is timed, nor a learned frame that records
+ * its CUDA graph; its replay is), and from then on the faster of the two, re-timing the learned
+ * frame whenever it runs.  A learned frame that has
+ * to be redone exactly (stats->overflow) counts as the slower one.  Without sizer weights every
+ * call runs the exact frame.  Output is identical whichever runs.  No counterpart in the reference
+ * (its count-then-allocate loop always runs, renderer.cpp:540-577).
+ */
+#define PF_FRAME_EXACT 0
+#define PF_FRAME_LEARNED 1
+int pf_render_auto(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats);
+/* What pf_render_auto did: the frame its last call ran (PF_FRAME_*), the settled choice (-1 while
+ * it is still timing), and the two device times it measured (0 until measured). */
+int pf_auto_choice(void *ctx, int *last, int *choice, float *exact_ms, float *learned_ms);
 
 /*
  * Learned sizer: features (12 per path) -> 64 -> 64 -> (log1p leaf lines, log1p fills),
@@ -364,6 +404,15 @@ int pf_read_images(void *ctx, uint8_t *dst, size_t capacity_bytes);
  */
 int pf_read_images_async(void *ctx, uint8_t *dst, size_t capacity_bytes);
 int pf_images_wait(void *ctx);
+
+/*
+ * Put pixels into scene `scene`'s destination image (RGBA8, width_px * height_px * 4 bytes, as
+ * pf_read_image returns them), for a later frame with PF_LOAD_LOAD to composite over: the
+ * reference's write into the destination texture (CommandEncoder::write_texture,
+ * pathfinder/gpu/command_encoder.h) before Renderer::draw(..., clear_dst_texture = false).
+ * Call it after the upload (an upload may reallocate the images).  Synchronises.
+ */
+int pf_write_image(void *ctx, uint32_t scene, const uint8_t *rgba, size_t bytes);
 
 /* Device pointer and pitch of the last rendered image (valid until the next
  * render on this context). */

@@ -52,6 +52,7 @@ class SceneView(C.Structure):
         ("path_clip", C.c_void_p), ("path_is_clip", C.c_void_p),
         ("path_stroke", C.c_void_p), ("contour_closed", C.c_void_p), ("dashes", C.c_void_p),
         ("n_dashes", C.c_uint32), ("path_paint", C.c_void_p), ("stops", C.c_void_p), ("n_stops", C.c_uint32),
+        ("view_box", C.c_void_p), ("load_action", C.c_uint32),
     ]
 
 
@@ -109,6 +110,11 @@ def scene_view(scene) -> "tuple[SceneView, list]":
         st_ = np.ascontiguousarray(scene.stops)
         v.path_paint, v.stops, v.n_stops = pp.ctypes.data, st_.ctypes.data, len(st_)
         arrs += [pp, st_]
+    if getattr(scene, "view_box", None) is not None:
+        vb = np.ascontiguousarray(scene.view_box, np.float32)
+        v.view_box = vb.ctypes.data
+        arrs.append(vb)
+    v.load_action = int(getattr(scene, "load_action", 0))
     return v, arrs
 
 
@@ -326,8 +332,9 @@ def reference_tile_scene(scene) -> Dict[str, np.ndarray]:
 
 
 def render(scene, z_rule: int = Z_D3D11, threads: int = 1, coverage: bool = False,
-           tiled: Optional[Dict[str, np.ndarray]] = None):
-    """FP64 analytic-area coverage + src-over composite; returns (rgba u8 [H,W,4], coverage|None)."""
+           tiled: Optional[Dict[str, np.ndarray]] = None, dest: Optional[np.ndarray] = None):
+    """FP64 analytic-area coverage + src-over composite; returns (rgba u8 [H,W,4], coverage|None).
+    A scene with load_action 1 composites over ``dest`` (u8 [H,W,4]; zeros when None)."""
     lib = _lib(LIB_ORACLE)
     scene = fill_scene(scene)
     v, keep = scene_view(scene)
@@ -339,6 +346,8 @@ def render(scene, z_rule: int = Z_D3D11, threads: int = 1, coverage: bool = Fals
         w = int(np.ceil(scene.width))
         h = int(np.ceil(scene.height))
         rgba = np.zeros((h, w, 4), np.uint8)
+        if dest is not None:
+            rgba[...] = np.asarray(dest, np.uint8).reshape(h, w, 4)
         cov = np.zeros((int(r.n_tiles), 16, 16), np.float32) if coverage else None
         st = lib.pfo_render(C.byref(v), C.byref(r), C.c_void_p(rgba.ctypes.data),
                             C.c_void_p(cov.ctypes.data if cov is not None else 0), C.c_int(threads))

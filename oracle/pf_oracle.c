@@ -330,12 +330,7 @@ static void tile_contour(path_ctx *pc, const float *pts, const uint8_t *fl, uint
 /* ------------------------------------------------------------------------ */
 /* Tiler::Tiler + generate_tiles + prepare_tiles (tiler.cpp:317-439)          */
 
-typedef struct {
-    float vb_right, vb_bottom;
-    int32_t rect[4];
-} path_setup;
-
-static void path_rect(const pf_scene_view *s, uint32_t p, float vb_right, float vb_bottom, int32_t r[4]) {
+static void path_rect(const pf_scene_view *s, uint32_t p, const float vb[4], int32_t r[4]) {
     /* Outline::bounds = union of the contours' point bounds */
     float l = 1.0f, t = 1.0f, rr = 0.0f, b = 0.0f;
     int valid = 0;
@@ -354,18 +349,19 @@ static void path_rect(const pf_scene_view *s, uint32_t p, float vb_right, float 
             }
         }
     }
-    /* RectF::intersection with the view box (0, 0, vb_right, vb_bottom) */
+    /* RectF::intersection with the view box vb = (left, top, right, bottom)
+     * (common/math/rect.h:160-172): an invalid {1, 1, 0, 0} when they do not meet */
     float il, it, ir, ib;
-    if (l > vb_right || rr < 0.0f || t > vb_bottom || b < 0.0f) {
+    if (l > vb[2] || rr < vb[0] || t > vb[3] || b < vb[1]) {
         il = 1.0f;
         it = 1.0f;
         ir = 0.0f;
         ib = 0.0f;
     } else {
-        il = l < 0.0f ? 0.0f : l;
-        it = t < 0.0f ? 0.0f : t;
-        ir = vb_right < rr ? vb_right : rr;
-        ib = vb_bottom < b ? vb_bottom : b;
+        il = l < vb[0] ? vb[0] : l;
+        it = t < vb[1] ? vb[1] : t;
+        ir = vb[2] < rr ? vb[2] : rr;
+        ib = vb[3] < b ? vb[3] : b;
     }
     const float inv = 1.0f / (float)TILE;
     r[0] = (int32_t)floorf(il * inv);
@@ -382,13 +378,24 @@ static float view_box_right(float width) {
     return (float)w;
 }
 
+/* The scene's view box as Scene::set_view_box stores it (scene.cpp:169-176): the given rect, or
+ * (0, 0, width, height), with its right edge rounded up to a multiple of 16. */
+static void scene_view_box(const pf_scene_view *s, float vb[4]) {
+    vb[0] = s->view_box ? s->view_box[0] : 0.0f;
+    vb[1] = s->view_box ? s->view_box[1] : 0.0f;
+    vb[2] = view_box_right(s->view_box ? s->view_box[2] : s->width);
+    vb[3] = s->view_box ? s->view_box[3] : s->height;
+}
+
 static int tile_path(const pf_scene_view *s, uint32_t p, path_ctx *pc) {
     memset(pc, 0, sizeof(*pc));
-    pc->vb_left = 0.0f;
-    pc->vb_right = view_box_right(s->width);
-    pc->vb_bottom = s->height;
+    float vb[4];
+    scene_view_box(s, vb);
+    pc->vb_left = vb[0];
+    pc->vb_right = vb[2];
+    pc->vb_bottom = vb[3];
     int32_t r[4];
-    path_rect(s, p, pc->vb_right, pc->vb_bottom, r);
+    path_rect(s, p, vb, r);
     pc->rx0 = r[0];
     pc->ry0 = r[1];
     pc->rx1 = r[2];
@@ -629,9 +636,22 @@ int pfo_tile_scene_mt(const pf_scene_view *s, int z_rule, int threads, pfo_resul
 
     /* z-buffer and composite lists (scene_builder.cpp:18-95; propagate.comp:190-205; sort.comp);
      * clip paths are not drawn */
-    const float vbr = view_box_right(s->width);
-    const uint32_t fbw = (uint32_t)ceilf(vbr / (float)TILE);
-    const uint32_t fbh = (uint32_t)ceilf(s->height / (float)TILE);
+    /* the framebuffer tile grid: d3d9's z-buffer covers the view box's tile rect
+     * (round_rect_out_to_tile_bounds(view_box), scene_builder.cpp:50-54); the d3d11 tile pass
+     * covers the destination image from tile (0, 0) (renderer.cpp:371, 443), and a tile outside
+     * it is never composited */
+    float vb[4];
+    scene_view_box(s, vb);
+    int32_t fx0 = 0, fy0 = 0;
+    uint32_t fbw = (uint32_t)ceilf(view_box_right(s->width) / (float)TILE);
+    uint32_t fbh = (uint32_t)ceilf(s->height / (float)TILE);
+    if (z_rule == PFO_Z_D3D9) {
+        const float inv = 1.0f / (float)TILE;
+        fx0 = (int32_t)floorf(vb[0] * inv);
+        fy0 = (int32_t)floorf(vb[1] * inv);
+        fbw = (uint32_t)((int32_t)ceilf(vb[2] * inv) - fx0);
+        fbh = (uint32_t)((int32_t)ceilf(vb[3] * inv) - fy0);
+    }
     const size_t nfb = (size_t)fbw * fbh;
     out->fb_tiles_x = fbw;
     out->fb_tiles_y = fbh;
@@ -648,7 +668,9 @@ int pfo_tile_scene_mt(const pf_scene_view *s, int z_rule, int threads, pfo_resul
                 const int8_t b = out->tile_backdrop[g];
                 if (out->tile_alpha[g] || b == 0) continue;
                 if (z_rule == PFO_Z_D3D11 && s->fill_rule[p] == PF_FILL_EVEN_ODD && (abs((int)b) % 2) == 0) continue;
-                const size_t fb = (size_t)(pc->ry0 + y) * fbw + (size_t)(pc->rx0 + x);
+                const int32_t tx = pc->rx0 + x - fx0, ty = pc->ry0 + y - fy0;
+                if (tx < 0 || ty < 0 || tx >= (int32_t)fbw || ty >= (int32_t)fbh) continue;
+                const size_t fb = (size_t)ty * fbw + (size_t)tx;
                 if ((int32_t)p > out->z[fb]) out->z[fb] = (int32_t)p;
             }
     }
@@ -670,7 +692,9 @@ int pfo_tile_scene_mt(const pf_scene_view *s, int z_rule, int threads, pfo_resul
                 for (int32_t x = 0; x < pc->rw; x++) {
                     const uint64_t g = tb + (uint64_t)y * pc->rw + x;
                     if (!out->tile_alpha[g] && out->tile_backdrop[g] == 0) continue;
-                    const size_t fb = (size_t)(pc->ry0 + y) * fbw + (size_t)(pc->rx0 + x);
+                    const int32_t tx = pc->rx0 + x - fx0, ty = pc->ry0 + y - fy0;
+                    if (tx < 0 || ty < 0 || tx >= (int32_t)fbw || ty >= (int32_t)fbh) continue;
+                    const size_t fb = (size_t)ty * fbw + (size_t)tx;
                     if ((int32_t)p < out->z[fb]) continue;
                     if (pass == 0) out->fb_list_first[fb + 1]++;
                     else out->fb_list[cur[fb]++] = (uint32_t)g;
@@ -825,6 +849,13 @@ static void *render_worker(void *arg) {
     for (size_t fb = j->first; fb < nfb; fb += j->step) {
         const uint32_t fx = (uint32_t)(fb % r->fb_tiles_x), fy = (uint32_t)(fb / r->fb_tiles_x);
         for (int k = 0; k < 256; k++) {
+            const uint32_t px = fx * 16 + (uint32_t)(k & 15), py = fy * 16 + (uint32_t)(k >> 4);
+            if (j->s->load_action == PF_LOAD_LOAD && px < j->w && py < j->h) {
+                /* LOAD_ACTION_LOAD (tile.comp:744-757): start from the pixel already there */
+                const uint8_t *d = j->rgba + ((size_t)py * j->w + px) * 4;
+                for (int ch = 0; ch < 4; ch++) dest[k][ch] = d[ch] / 255.0;
+                continue;
+            }
             dest[k][0] = cr;
             dest[k][1] = cg;
             dest[k][2] = cb;

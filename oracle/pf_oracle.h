@@ -66,7 +66,9 @@ int pfo_tile_scene_mt(const pf_scene_view *scene, int z_rule, int threads, pfo_r
 
 /*
  * FP64 analytic-area coverage and src-over composite of a tiled scene.
- * rgba: width_px*height_px*4 bytes (RGBA8).  coverage_f (optional, may be
+ * rgba: width_px*height_px*4 bytes (RGBA8); with load_action PF_LOAD_LOAD it holds
+ * the destination to composite over on entry.  The tiled result must use the d3d11
+ * framebuffer grid (PFO_Z_D3D11: tiles from (0, 0) over the image).  coverage_f (optional, may be
  * NULL): [n_tiles*256] float coverage of every alpha tile after the fill
  * rule, row-major 16x16 (solid and empty tiles are left untouched).
  * first_tile/n_tiles_limit restrict the coverage pass to a tile range (use

@@ -67,7 +67,10 @@ extern "C" int pfref_tile_scene(const pf_scene_view *sv, pfo_result *out) {
     if (!sv || !out) return 1;
     std::memset(out, 0, sizeof(*out));
 
-    Scene scene(0, RectF(Vec2F(0.0f, 0.0f), Vec2F(sv->width, sv->height)));
+    const RectF given = sv->view_box ? RectF(Vec2F(sv->view_box[0], sv->view_box[1]),
+                                             Vec2F(sv->view_box[2], sv->view_box[3]))
+                                     : RectF(Vec2F(0.0f, 0.0f), Vec2F(sv->width, sv->height));
+    Scene scene(0, given);
     const RectF view_box = scene.get_view_box();
 
     HarnessBuilder builder;

@@ -117,6 +117,7 @@ struct Ctx {
     DevBuf tile_fills, tile_state, col_above, col_final, fills, path_fill, path_cls, bin_stage;
     DevBuf row_first, row_paths, scene_row_first;
     DevBuf z, fb_count, list, image, status, scan_temp;
+    DevBuf canon_state, canon_clip;  // clipped frames: tile states after the clip rules (read-back only)
     // host image target (pf_set_host_image): frames composite straight into this host buffer
     uint8_t *host_img = nullptr;      // host address
     uint8_t *host_img_dev = nullptr;  // the same memory as the device addresses it
@@ -159,11 +160,34 @@ struct Ctx {
     std::vector<void *> lg_ptrs;        // the buffers it uses, by address
     bool capturing = false;             // recording the graph: no host synchronisation
     bool learned_done = false;          // the last learned frame ran the learned path to the end
+    // The graph is recorded on the second learned frame in a row over the same upload, range,
+    // flags and buffers (a frame after every upload never replays: recording it would be wasted)
+    struct {
+        bool valid = false;
+        uint64_t epoch = 0;
+        uint32_t first = 0, count = 0, flags = 0;
+        std::vector<void *> ptrs;
+        uint32_t status[kStCount] = {};  // the totals the plain frame sized its buffers for
+    } lg_prev;
+    int lg_kind = 0;  // the last learned frame: 0 plain, 1 recorded then replayed, 2 replayed
+
+    // pf_render_auto: the device times of the exact and the learned frame over a workload (the
+    // scene range and the upload's totals), measured as they run; the faster one runs once both
+    // are known
+    uint64_t upload_epoch = 0;
+    struct {
+        uint64_t sig[5] = {~0ull, 0, 0, 0, 0};  // first, count, paths, contours, points of the range
+        float exact_ms = -1.0f, learned_ms = -1.0f;  // < 0: not measured
+        int exact_runs = 0, learned_runs = 0;  // frames run over the workload (the first is not timed)
+        int last = PF_FRAME_EXACT;     // the frame the last auto call ran
+    } au;
+    cudaEvent_t au_ev[2] = {};
 };
 
 thread_local std::string g_last_error;
 
 void drop_graph(Ctx *c);
+void forget_learned(Ctx *c);
 
 int fail(Ctx *c, int code, const std::string &msg) {
     if (c) c->err = msg;
@@ -197,6 +221,15 @@ int validate_scene(Ctx *c, const pf_scene_view *s) {
         return fail(c, PF_ERR_INVALID_ARGUMENT, "canvas size must be finite, positive and at most 65536");
     if (!s->path_start || !s->contour_start)
         return fail(c, PF_ERR_INVALID_ARGUMENT, "path_start and contour_start are required");
+    if (s->load_action > PF_LOAD_LOAD) return fail(c, PF_ERR_INVALID_ARGUMENT, "unknown load action");
+    if (s->view_box) {
+        const float *v = s->view_box;
+        for (int k = 0; k < 4; k++)
+            if (!std::isfinite(v[k]) || std::fabs(v[k]) > 65536.0f)
+                return fail(c, PF_ERR_INVALID_ARGUMENT, "view box coordinates must be finite and within 65536");
+        if (!(v[0] <= v[2]) || !(v[1] <= v[3]))
+            return fail(c, PF_ERR_INVALID_ARGUMENT, "the view box needs left <= right and top <= bottom");
+    }
     if (s->n_paths && (!s->fill_rule || !s->color))
         return fail(c, PF_ERR_INVALID_ARGUMENT, "fill_rule and color are required");
     if (s->n_points && (!s->points || !s->point_flags))
@@ -581,7 +614,7 @@ int stroke_upload(Ctx *c, const pf_scene_view *scenes, uint32_t n, const std::ve
 
 int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     if (!scenes || n == 0) return fail(c, PF_ERR_INVALID_ARGUMENT, "no scenes");
-    drop_graph(c);
+    forget_learned(c);
     uint64_t P = 0, C = 0, N = 0, fb = 0, img = 0, cs = 0, ps = 0;
     c->h_scenes.assign(n, SceneDev{});
     c->h_scene_fb_first.assign(n + 1, 0);
@@ -593,9 +626,14 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
         if (st) return st;
         const pf_scene_view &s = scenes[i];
         SceneDev &S = c->h_scenes[i];
-        S.vb_right = view_box_right(s.width);
-        S.vb_bottom = s.height;
-        S.fbw = (uint32_t)std::ceil(S.vb_right / kTile);
+        // the view box (Scene::set_view_box rounds its right edge up to a multiple of 16);
+        // framebuffer tiles cover the destination image from (0, 0)
+        S.vb_left = s.view_box ? s.view_box[0] : 0.0f;
+        S.vb_top = s.view_box ? s.view_box[1] : 0.0f;
+        S.vb_right = view_box_right(s.view_box ? s.view_box[2] : s.width);
+        S.vb_bottom = s.view_box ? s.view_box[3] : s.height;
+        S.load = s.load_action;
+        S.fbw = (uint32_t)std::ceil(view_box_right(s.width) / kTile);
         S.fbh = (uint32_t)std::ceil(s.height / kTile);
         S.fb_first = (uint32_t)fb;
         S.img_w = (uint32_t)std::ceil(s.width);
@@ -661,7 +699,12 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     PF_CUDA(c->scene_contour_first.ensure((n + 1) * 4));
     PF_CUDA(c->scene_fb_first.ensure((n + 1) * 4));
     PF_CUDA(c->scene_row_first.ensure((n + 1) * 4));
-    PF_CUDA(c->image.ensure(img + 256));
+    {
+        // a new image buffer starts transparent, so a first frame with PF_LOAD_LOAD loads zeros
+        void *const before = c->image.p;
+        PF_CUDA(c->image.ensure(img + 256));
+        if (c->image.p != before) PF_CUDA(cudaMemsetAsync(c->image.p, 0, c->image.cap, c->stream));
+    }
     bool clips = false;
     for (uint32_t i = 0; i < n; i++) clips |= scenes[i].path_clip != nullptr;
     c->h_path_clip.clear();
@@ -785,6 +828,7 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     PF_CUDA(cudaStreamSynchronize(c->stream));
     c->uploaded = true;
     c->rendered = false;
+    c->upload_epoch++;
     return PF_OK;
 }
 
@@ -1024,6 +1068,7 @@ int bin_and_composite(Ctx *c, Batch b, bool learned) {
         record(c, 5);
         PF_CUDA(launch_composite(b, st));
         record(c, 6);
+        if (b.counters) PF_CUDA(launch_tile_counts(b, st));
         if (int e = read_status(c)) return e;
         const uint32_t err = c->h_status[kStErr];
         const uint64_t need = uint64_t(c->h_status[kStFill64]) | uint64_t(c->h_status[kStFill64 + 1]) << 32;
@@ -1040,7 +1085,8 @@ int bin_and_composite(Ctx *c, Batch b, bool learned) {
         b.fill_cap = (uint32_t)std::min<size_t>(c->fills.cap / 8, 0xffffffffu);
         // clear the error word and the composite's counters before the second run
         const uint32_t zero = 0;
-        for (int slot : {(int)kStErr, (int)kStListFills, (int)kStEntries, (int)kStWalkChunks})
+        for (int slot : {(int)kStErr, (int)kStListFills, (int)kStEntries, (int)kStWalkChunks, (int)kStAlphaTiles,
+                         (int)kStVisible})
             PF_CUDA(cudaMemcpyAsync(b.status + slot, &zero, 4, cudaMemcpyHostToDevice, st));
     }
 }
@@ -1063,7 +1109,9 @@ int finish_frame(Ctx *c, uint32_t first, uint32_t count, uint64_t launches0, pf_
         stats->composite_entries = c->n_list;
         stats->framebuffer_tiles = NFB;
         stats->composited_fills = c->h_status[kStListFills];
-        stats->alpha_tiles = 0;
+        // alpha and visible tiles are counted with PF_CONFIG_FRAME_COUNTERS (else 0)
+        stats->alpha_tiles = c->h_status[kStAlphaTiles];
+        stats->visible_tiles = c->h_status[kStVisible];
         stats->kernel_launches = (uint32_t)(launches() - launches0);
         stats->host_syncs = c->syncs;
         if ((c->flags & PF_CONFIG_STAGE_TIMING) && !c->capturing) {
@@ -1196,6 +1244,12 @@ void drop_graph(Ctx *c) {
     c->lg_exec = nullptr;
 }
 
+// The scenes or the sizer changed: no graph, and no plain frame to record one from.
+void forget_learned(Ctx *c) {
+    drop_graph(c);
+    c->lg_prev.valid = false;
+}
+
 // Records the learned frame over [first, first + count) as a graph, right after the same frame
 // ran with the same buffers.  A failure leaves the plain path in use.
 void capture_learned(Ctx *c, uint32_t first, uint32_t count) {
@@ -1274,13 +1328,95 @@ int replay_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats
 
 int render_learned(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
     if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights loaded");
-    const int r = replay_learned(c, first, count, stats);
+    c->lg_kind = 2;
+    int r = replay_learned(c, first, count, stats);
     if (r != kReplayMiss) return r;
+    auto &pv = c->lg_prev;
+    if (pv.valid && pv.epoch == c->upload_epoch && pv.first == first && pv.count == count && pv.flags == c->flags &&
+        pv.ptrs == frame_buffers(c)) {
+        // the last frame ran this one plainly with these buffers: record it (with the totals that
+        // frame sized the buffers for) and replay it
+        std::memcpy(c->h_status, pv.status, sizeof pv.status);
+        capture_learned(c, first, count);
+        c->lg_kind = 1;
+        r = replay_learned(c, first, count, stats);
+        if (r != kReplayMiss) return r;
+    }
+    pv.valid = false;
     pf_frame_stats local;
     pf_frame_stats *st = stats ? stats : &local;
+    c->lg_kind = 0;
     const int e = render_learned_frame(c, first, count, st);
-    if (e == PF_OK && c->learned_done) capture_learned(c, first, count);
+    if (e == PF_OK && c->learned_done) {
+        pv.valid = true;
+        pv.epoch = c->upload_epoch;
+        pv.first = first;
+        pv.count = count;
+        pv.flags = c->flags;
+        pv.ptrs = frame_buffers(c);
+        std::memcpy(pv.status, c->h_status, sizeof pv.status);
+    }
     return e;
+}
+
+// A frame between two device events; *ms is its time on the device (the frame ends with a host
+// synchronisation, so the events have completed by then).
+template <class F>
+int timed_frame(Ctx *c, float *ms, F &&frame) {
+    if (!c->au_ev[0]) {
+        PF_CUDA(cudaEventCreate(&c->au_ev[0]));
+        PF_CUDA(cudaEventCreate(&c->au_ev[1]));
+    }
+    PF_CUDA(cudaEventRecord(c->au_ev[0], c->stream));
+    const int e = frame();
+    if (e != PF_OK) return e;
+    PF_CUDA(cudaEventRecord(c->au_ev[1], c->stream));
+    PF_CUDA(cudaEventSynchronize(c->au_ev[1]));
+    PF_CUDA(cudaEventElapsedTime(ms, c->au_ev[0], c->au_ev[1]));
+    return PF_OK;
+}
+
+// The frame the library picks.  With sizer weights it times, on the device, the exact frame and
+// the learned frame over the workload - the scene range and the totals of its paths, contours and
+// points, so a new upload of scenes of the same size keeps what was measured - and runs the
+// faster one once both are known.  Each frame's first run over the workload is not timed (it may
+// grow buffers), nor is a learned frame that records its graph (the next one, a replay, is); a
+// learned frame that had to be redone exactly counts as the slower one.  Without weights: the
+// exact frame.
+int render_auto(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
+    auto &a = c->au;
+    if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
+    if (count == 0 || first >= c->n_scenes || count > c->n_scenes - first)
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "scene range out of bounds");
+    a.last = PF_FRAME_EXACT;
+    if (!c->sz_ready) return render_exact(c, first, count, stats);
+    const SceneDev &s0 = c->h_scenes[first], &s1 = c->h_scenes[first + count - 1];
+    const uint64_t sig[5] = {first, count, uint64_t(s1.path_end - s0.path_first),
+                             uint64_t(s1.contour_end - s0.contour_first), uint64_t(s1.point_end - s0.point_first)};
+    if (std::memcmp(sig, a.sig, sizeof sig) != 0) {
+        std::memcpy(a.sig, sig, sizeof sig);
+        a.exact_ms = a.learned_ms = -1.0f;
+        a.exact_runs = a.learned_runs = 0;
+    }
+    pf_frame_stats local;
+    pf_frame_stats *st = stats ? stats : &local;
+    float ms = 0.0f;
+    if (a.exact_ms < 0.0f) {
+        const int e = timed_frame(c, &ms, [&] { return render_exact(c, first, count, st); });
+        if (e == PF_OK && a.exact_runs++ > 0) a.exact_ms = ms;
+        return e;
+    }
+    if (a.learned_ms < 0.0f || a.learned_ms < a.exact_ms) {
+        a.last = PF_FRAME_LEARNED;
+        const int e = timed_frame(c, &ms, [&] { return render_learned(c, first, count, st); });
+        if (e != PF_OK) return e;
+        if (st->overflow) a.learned_ms = 2.0f * a.exact_ms + 1.0f;  // redone exactly: the exact frame wins
+        else if (c->lg_kind == 2 || (c->lg_kind == 0 && a.learned_runs > 0))
+            a.learned_ms = ms;  // a replay, or a plain frame after the first: the frame as it runs
+        a.learned_runs++;
+        return e;
+    }
+    return render_exact(c, first, count, st);
 }
 
 template <class T>
@@ -1304,6 +1440,13 @@ int dump_lists(Ctx *c) {
     PF_CUDA(c->list.ensure(size_t(c->h_status[kStList]) * 4 + 16));
     b = make_batch(c);
     PF_CUDA(launch_list_dump(b, true, c->stream));
+    if (!c->h_path_clip.empty()) {
+        // the clip rules as the composite applies them, tile by tile
+        PF_CUDA(c->canon_state.ensure(size_t(c->n_tiles) * 4 + 16));
+        PF_CUDA(c->canon_clip.ensure(size_t(c->n_tiles) * 4 + 16));
+        PF_CUDA(launch_clip_dump(b, c->n_tiles, c->canon_state.as<uint32_t>(), c->canon_clip.as<uint32_t>(),
+                                 c->stream));
+    }
     PF_CUDA(cudaStreamSynchronize(c->stream));
     c->lists_dumped = true;
     return PF_OK;
@@ -1341,17 +1484,25 @@ int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
     }
     // every path's fills are one block from path_fill[p], grouped by tile; tile_fills[t] is one
     // past the last fill of tile t
-    std::vector<uint32_t> tend, pfill;
-    std::vector<uint16_t> state;
+    std::vector<uint32_t> tend, pfill, state, clip_tile;
+    std::vector<uint16_t> state16;
+    const bool clips = !c->h_path_clip.empty();
     if (int e = d2h(c, tend, c->tile_fills.as<uint32_t>() + t0, size_t(t1 - t0))) return e;
     if (int e = d2h(c, pfill, c->path_fill.as<uint32_t>() + p0, np)) return e;
-    if (int e = d2h(c, state, c->tile_state.as<uint16_t>() + t0, t1 - t0)) return e;
+    if (clips) {
+        // tile states after the clip rules, as the GPU applied them (k_clip_dump)
+        if (int e = d2h(c, state, c->canon_state.as<uint32_t>() + t0, t1 - t0)) return e;
+        if (int e = d2h(c, clip_tile, c->canon_clip.as<uint32_t>() + t0, t1 - t0)) return e;
+    } else if (int e = d2h(c, state16, c->tile_state.as<uint16_t>() + t0, t1 - t0)) {
+        return e;
+    }
     if (int e = d2h(c, h.col_backdrop, c->col_final.as<int32_t>() + k0, k1 - k0)) return e;
     if (int e = d2h(c, h.z, c->z.as<int32_t>() + fb0, size_t(S.fbw) * S.fbh)) return e;
     std::vector<uint32_t> fbc;
     if (int e = d2h(c, fbc, c->fb_count.as<uint32_t>() + fb0, size_t(S.fbw) * S.fbh + 1)) return e;
     PF_CUDA(cudaStreamSynchronize(c->stream));
     const size_t nt = t1 - t0;
+    if (!clips) state.assign(state16.begin(), state16.end());
     // gather the paths' blocks in path order (one copy per run of blocks adjacent on the device)
     std::vector<uint64_t> blk(np + 1, 0);
     for (uint32_t p = 0; p < np; p++) {
@@ -1400,42 +1551,17 @@ int read_canon(Ctx *c, uint32_t si, pf_canon *out) {
             d[3] = uint16_t(keys[k]);
         }
     }
-    // clipped draw tiles (Tiler::prepare_tiles, pathfinder/core/d3d9/tiler.cpp:386-431), as the
-    // kernels apply them on the fly; clip paths are not clipped, so their tiles read as stored
+    // clipped draw tiles (Tiler::prepare_tiles, pathfinder/core/d3d9/tiler.cpp:386-431): the
+    // mask source, the clip tile and the draw tile's own backdrop, from the states k_clip_dump
+    // wrote with the composite's own clip rules
     h.mask.assign(nt, 0);
     h.clip.assign(nt, UINT64_MAX);
     h.dest_backdrop.assign(nt, 0);
-    for (uint32_t p = 0; !c->h_path_clip.empty() && p < np; p++) {
-        const uint32_t k = c->h_path_clip[S.path_first + p];
-        if (k == PF_NO_CLIP) continue;
-        const int32_t *R = &h.rect[4 * p], *CR = &h.rect[4 * k];
-        const int32_t w = R[2] - R[0], cw = CR[2] - CR[0];
-        for (int32_t y = R[1]; y < R[3]; y++)
-            for (int32_t x = R[0]; x < R[2]; x++) {
-                const uint64_t g = h.tile_first[p] + uint64_t(y - R[1]) * w + uint64_t(x - R[0]);
-                if (x < CR[0] || x >= CR[2] || y < CR[1] || y >= CR[3]) {
-                    h.alpha[g] = 0;
-                    h.backdrop[g] = 0;
-                    continue;
-                }
-                const uint64_t gc = h.tile_first[k] + uint64_t(y - CR[1]) * cw + uint64_t(x - CR[0]);
-                const bool ca = h.alpha[gc] != 0, da = h.alpha[g] != 0;
-                const int8_t cbd = h.backdrop[gc], dbd = h.backdrop[g];
-                if (ca && da) {
-                    h.mask[g] = 2;
-                    h.clip[g] = gc;
-                    h.dest_backdrop[g] = dbd;
-                    h.backdrop[g] = 0;
-                } else if (ca && dbd != 0) {
-                    h.mask[g] = 1;
-                    h.clip[g] = gc;
-                    h.alpha[g] = 1;
-                    h.backdrop[g] = cbd;
-                } else if (!ca && cbd == 0) {
-                    h.alpha[g] = 0;
-                    h.backdrop[g] = 0;
-                }
-            }
+    for (size_t t = 0; clips && t < nt; t++) {
+        const uint32_t mode = (state[t] >> 9) & 3u;
+        h.mask[t] = (uint8_t)mode;
+        if (mode != 0) h.clip[t] = uint64_t(clip_tile[t]) - t0;
+        if (mode == 2) h.dest_backdrop[t] = (int8_t)((state[t] >> 16) & 0xffu);
     }
     for (auto &z : h.z)
         if (z >= 0) z -= (int32_t)p0;
@@ -1682,7 +1808,7 @@ int pf_ctx_destroy(void *ctx) {
     }
     if (c->snap_done) cudaEventDestroy(c->snap_done);
     if (c->copy_done) cudaEventDestroy(c->copy_done);
-    drop_graph(c);
+    forget_learned(c);
     drop_host_image(c);
     DevBuf *bufs[] = {&c->sz_w, &c->sz_master, &c->sz_m, &c->sz_v, &c->sz_grad, &c->sz_loss, &c->sz_feat,
                       &c->sz_target, &c->sz_index, &c->sz_pred, &c->path_feat, &c->contour_feat, &c->path_pred, &c->path_leaf_first,
@@ -1708,6 +1834,10 @@ int pf_ctx_destroy(void *ctx) {
         if (e) cudaEventDestroy(e);
     for (auto &e : c->sev)
         if (e) cudaEventDestroy(e);
+    for (auto &e : c->au_ev)
+        if (e) cudaEventDestroy(e);
+    c->canon_state.release();
+    c->canon_clip.release();
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->own_stream) cudaStreamDestroy(c->stream);
@@ -1767,6 +1897,26 @@ int pf_image_device_ptr(void *ctx, void **rgba, uint32_t *width_px, uint32_t *he
     *rgba = (c->host_img_dev ? c->host_img_dev : c->image.as<uint8_t>()) + c->h_scenes[c->r_first].img_offset;
     if (width_px) *width_px = c->h_scenes[c->r_first].img_w;
     if (height_px) *height_px = c->h_scenes[c->r_first].img_h;
+    return PF_OK;
+}
+
+int pf_write_image(void *ctx, uint32_t scene, const uint8_t *rgba, size_t bytes) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !rgba) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
+    if (scene >= c->n_scenes) return fail(c, PF_ERR_INVALID_ARGUMENT, "scene index out of range");
+    const SceneDev &S = c->h_scenes[scene];
+    const size_t need = size_t(S.img_w) * S.img_h * 4;
+    if (bytes != need) return fail(c, PF_ERR_INVALID_ARGUMENT, "pf_write_image needs width_px * height_px * 4 bytes");
+    PF_CUDA(cudaSetDevice(c->device));
+    if (c->host_img) {
+        // frames composite into the host image target: the destination lives there
+        PF_CUDA(cudaStreamSynchronize(c->stream));
+        std::memcpy(c->host_img + S.img_offset, rgba, need);
+        return PF_OK;
+    }
+    PF_CUDA(cudaMemcpyAsync(c->image.as<uint8_t>() + S.img_offset, rgba, need, cudaMemcpyHostToDevice, c->stream));
+    PF_CUDA(cudaStreamSynchronize(c->stream));
     return PF_OK;
 }
 
@@ -1920,7 +2070,7 @@ extern "C" {
 int pf_sizer_init(void *ctx, uint64_t seed) {
     Ctx *c = as_ctx(ctx);
     if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
-    drop_graph(c);
+    forget_learned(c);
     cudaSetDevice(c->device);
     // He-uniform initialisation from a splitmix64 stream
     std::vector<float> w(kSizerParams, 0.0f);
@@ -1946,7 +2096,7 @@ int pf_sizer_param_count(void) { return kSizerParams; }
 int pf_sizer_set_params(void *ctx, const float *params, size_t n) {
     Ctx *c = as_ctx(ctx);
     if (!c || !params || n != (size_t)kSizerParams) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad sizer parameters");
-    drop_graph(c);
+    forget_learned(c);
     cudaSetDevice(c->device);
     return sizer_upload(c, params);
 }
@@ -1963,7 +2113,7 @@ int pf_sizer_get_params(void *ctx, float *params, size_t n) {
 int pf_sizer_set_margin(void *ctx, float mul, float add, float pool) {
     Ctx *c = as_ctx(ctx);
     if (!c || !(mul > 0.0f) || !(add >= 0.0f) || !(pool >= 0.0f)) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad margin");
-    drop_graph(c);
+    forget_learned(c);
     c->sz_mul = mul;
     c->sz_add = add;
     c->sz_pool = pool;
@@ -2022,7 +2172,7 @@ int pf_sizer_train(void *ctx, const float *feat, const float *target, uint32_t n
     Ctx *c = as_ctx(ctx);
     if (!c || !feat || !target || n == 0 || batch == 0) return fail(c, PF_ERR_INVALID_ARGUMENT, "bad arguments");
     if (!c->sz_ready) return fail(c, PF_ERR_NOT_READY, "no sizer weights");
-    drop_graph(c);
+    forget_learned(c);
     cudaSetDevice(c->device);
     if (int e = upload_dataset(c, feat, target, n)) return e;
     PF_CUDA(c->sz_index.ensure(size_t(n) * 4 + 16));
@@ -2089,7 +2239,7 @@ int pf_sizer_save(void *ctx, const char *path) {
 int pf_sizer_load(void *ctx, const char *path) {
     Ctx *c = as_ctx(ctx);
     if (!c || !path) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
-    drop_graph(c);
+    forget_learned(c);
     cudaSetDevice(c->device);
     FILE *f = std::fopen(path, "rb");
     if (!f) return fail(c, PF_ERR_INVALID_ARGUMENT, std::string("cannot read ") + path);
@@ -2170,6 +2320,27 @@ int pf_render_learned(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_fra
     if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
     cudaSetDevice(c->device);
     return render_learned(c, first_scene, n_scenes, stats);
+}
+
+int pf_render_auto(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    cudaSetDevice(c->device);
+    return render_auto(c, first_scene, n_scenes, stats);
+}
+
+int pf_auto_choice(void *ctx, int *last, int *choice, float *exact_ms, float *learned_ms) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    const auto &a = c->au;
+    if (last) *last = a.last;
+    if (choice)
+        *choice = !c->sz_ready ? PF_FRAME_EXACT
+                  : (a.exact_ms < 0.0f || a.learned_ms < 0.0f) ? -1
+                  : a.learned_ms < a.exact_ms ? PF_FRAME_LEARNED : PF_FRAME_EXACT;
+    if (exact_ms) *exact_ms = a.exact_ms > 0.0f ? a.exact_ms : 0.0f;
+    if (learned_ms) *learned_ms = a.learned_ms > 0.0f ? a.learned_ms : 0.0f;
+    return PF_OK;
 }
 
 }  // extern "C"

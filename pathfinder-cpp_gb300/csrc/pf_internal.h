@@ -39,8 +39,9 @@ enum : uint32_t {
 
 // Per scene of a batch (device).
 struct SceneDev {
+    float vb_left, vb_top;  // view box (Scene::set_view_box): tiling clips against it
     float vb_right;       // view box right edge, rounded up to a multiple of 16
-    float vb_bottom;      // view box bottom edge (canvas height)
+    float vb_bottom;      // view box bottom edge
     uint32_t fbw, fbh;    // framebuffer tiles across / down
     uint32_t fb_first;    // first framebuffer tile of this scene in the batch
     uint32_t img_w, img_h;
@@ -51,6 +52,7 @@ struct SceneDev {
     uint32_t point_first, point_end;
     uint32_t cstart_base, pstart_base;  // offsets of the scene's offset arrays
     uint32_t row_first;                  // first framebuffer-tile row of this scene in the batch
+    uint32_t load;                       // PF_LOAD_LOAD: composite over the image already there
 };
 
 // Per draw path (device), written by the set-up kernel.
@@ -175,7 +177,7 @@ enum : int {
     kStTiles = 2,
     kStCols = 3,
     kStLeaves = 4,
-    // slot 5 is unused (fills are counted in the 64-bit kStFill64)
+    kStAlphaTiles = 5, // frame counters: alpha tiles of the draw paths
     kStList = 6,
     kStListFills = 7,  // fills of the alpha tiles that made it into composite lists
     kStRows = 8,       // entries of the per-row path lists
@@ -188,6 +190,7 @@ enum : int {
     kStWalkChunks = 15,// composite: 32-candidate chunks walked (all framebuffer tiles)
     kStFill64 = 16,    // two words: fills reserved by the frame's paths (64-bit)
     kStPoolListed = 18,// learned frame: pooled lines listed by path
+    kStVisible = 19,   // frame counters: visible tiles of the draw paths (alpha, or a nonzero backdrop)
     kStCount = 20,
 };
 
@@ -279,7 +282,11 @@ cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st)
 cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st);
 cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_composite(const Batch &b, cudaStream_t st);
+// Frame counters: alpha and visible tiles of the draw paths into the status words.
+cudaError_t launch_tile_counts(const Batch &b, cudaStream_t st);
 cudaError_t launch_list_dump(const Batch &b, bool write, cudaStream_t st);
+// Canonical output of clipped frames: every tile's state after the clip rules and its clip tile.
+cudaError_t launch_clip_dump(const Batch &b, uint32_t n_tiles, uint32_t *state, uint32_t *clip, cudaStream_t st);
 cudaError_t launch_coverage_dump(const Batch &b, const uint32_t *tiles, uint32_t n, float *out, cudaStream_t st);
 
 // Learned sizer (pf_sizer.cu).

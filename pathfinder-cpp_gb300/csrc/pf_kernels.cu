@@ -139,14 +139,15 @@ __global__ void k_path_setup(Batch b, const uint2 *path_contours) {
         r = 0.0f;
         bt = 0.0f;
     }
-    if (l > S.vb_right || r < 0.0f || t > S.vb_bottom || bt < 0.0f) {
+    // RectF::intersection with the view box (common/math/rect.h:160-172)
+    if (l > S.vb_right || r < S.vb_left || t > S.vb_bottom || bt < S.vb_top) {
         il = 1.0f;
         it = 1.0f;
         ir = 0.0f;
         ib = 0.0f;
     } else {
-        il = l < 0.0f ? 0.0f : l;
-        it = t < 0.0f ? 0.0f : t;
+        il = l < S.vb_left ? S.vb_left : l;
+        it = t < S.vb_top ? S.vb_top : t;
         ir = S.vb_right < r ? S.vb_right : r;
         ib = S.vb_bottom < bt ? S.vb_bottom : bt;
     }
@@ -504,12 +505,12 @@ __global__ void __launch_bounds__(kThreads) k_flatten(Batch b, uint32_t n_segs) 
 
 struct WalkCtx {
     int32_t rx0, ry0, rx1, ry1, rw, rh;
-    float vb_right, vb_bottom;
+    float vb_left, vb_right, vb_bottom;  // the clip box: the view box with its top at -infinity
 };
 
 __device__ __forceinline__ int outcode(const WalkCtx &w, float x, float y) {
     int o = 0;
-    if (x < 0.0f) o |= 1;
+    if (x < w.vb_left) o |= 1;
     else if (x > w.vb_right) o |= 2;
     if (y > w.vb_bottom) o |= 8;
     return o;
@@ -530,8 +531,8 @@ __device__ __forceinline__ int clip_line(const WalkCtx &w, float &x0, float &y0,
         const int oc = clip_from ? of : ot;
         float px = clip_from ? x0 : x1, py = clip_from ? y0 : y1;
         if (oc & 1) {
-            px = 0.0f;
-            py = lerp_clamped(y0, y1, fdiv(fsub(0.0f, x0), fsub(x1, x0)));
+            px = w.vb_left;
+            py = lerp_clamped(y0, y1, fdiv(fsub(w.vb_left, x0), fsub(x1, x0)));
         } else if (oc & 2) {
             px = w.vb_right;
             py = lerp_clamped(y0, y1, fdiv(fsub(w.vb_right, x0), fsub(x1, x0)));
@@ -906,6 +907,7 @@ __device__ __forceinline__ WalkCtx walk_ctx(const Batch &b, const PathDev &P) {
     w.ry1 = P.ry1;
     w.rw = max(P.rx1 - P.rx0, 0);
     w.rh = max(P.ry1 - P.ry0, 0);
+    w.vb_left = S.vb_left;
     w.vb_right = S.vb_right;
     w.vb_bottom = S.vb_bottom;
     return w;
@@ -1416,9 +1418,12 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(Batch b) {
         const uint32_t p = base + threadIdx.x;
         bool spans = false;
         int4 rect = make_int4(0, 0, 0, 0);
+        int32_t cx0 = 0, cx1 = 0;  // the rect's columns inside the framebuffer
         if (p < p1) {
             rect = *reinterpret_cast<const int4 *>(&b.paths[p].rx0);
-            spans = rect.y <= y && y < rect.w && rect.x < rect.z && !(b.paths[p].flags & kPathIsClip);
+            cx0 = max(rect.x, 0);
+            cx1 = min(rect.z, (int32_t)S.fbw);
+            spans = rect.y <= y && y < rect.w && cx0 < cx1 && !(b.paths[p].flags & kPathIsClip);
         }
         const uint32_t ballot = __ballot_sync(0xffffffffu, spans);
         if (lane == 0) warp_counts[warp] = __popc(ballot);
@@ -1439,12 +1444,13 @@ __global__ void __launch_bounds__(kRowThreads) k_rows(Batch b) {
             // adding fx >= rx0 brings it back into range)
             const uint32_t row_tile = b.paths[p].tile_first + (uint32_t)(y - rect.y) * (uint32_t)(rect.z - rect.x) -
                                       (uint32_t)rect.x;
-            // flags: bit 0 even-odd, bit 1 occludes, bit 2 this row is the rect's first row,
-            // bit 4 the path is clipped
+            // flags: bit 0 even-odd, bit 1 occludes, bit 2 the rect's first tile (its first
+            // row, first column) is in this row of the framebuffer, bit 4 the path is clipped
             const bool clipped = b.path_clip_cat && b.path_clip_rel[p] != kNone;
+            const bool first = y == rect.y && rect.x >= 0;
             if (out + rank < b.row_cap)
-                b.row_paths[out + rank] = make_uint4(p, (uint32_t)rect.x | ((uint32_t)rect.z << 16), row_tile,
-                                                     b.paths[p].flags | (y == rect.y ? 4u : 0u) |
+                b.row_paths[out + rank] = make_uint4(p, (uint32_t)cx0 | ((uint32_t)cx1 << 16), row_tile,
+                                                     b.paths[p].flags | (first ? 4u : 0u) |
                                                          (clipped ? kRowClipped : 0u));
         }
         out += chunk_total;
@@ -1641,6 +1647,7 @@ __device__ __forceinline__ void apply_clip(const Batch &b, uint32_t p, int32_t t
         c.st = 0x100u | kMaskClip << 9 | (uint32_t)(uint8_t)cbd;
         c.f0 = gc == C.tile_first ? b.path_fill[cp] : b.tile_fills[gc - 1];
         c.f1 = b.tile_fills[gc];
+        c.gc = gc;
     } else if (!ca && cbd == 0) {
         c.st = 0;
     }
@@ -1858,13 +1865,21 @@ __global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 3
         }, chunks);
         const uint32_t px = fx * 16 + (uint32_t)col;
         if (px < S.img_w) {
-            const float cr = (float)(S.clear & 0xffu) * inv255, cg = (float)((S.clear >> 8) & 0xffu) * inv255,
-                        cb = (float)((S.clear >> 16) & 0xffu) * inv255, ca = (float)(S.clear >> 24) * inv255;
+            float cr = (float)(S.clear & 0xffu) * inv255, cg = (float)((S.clear >> 8) & 0xffu) * inv255,
+                  cb = (float)((S.clear >> 16) & 0xffu) * inv255, ca = (float)(S.clear >> 24) * inv255;
             uchar4 *img = reinterpret_cast<uchar4 *>(b.image + S.img_offset);
 #pragma unroll
             for (int k = 0; k < 8; k++) {
                 const uint32_t py = fy * 16 + (uint32_t)(h * 8 + k);
                 if (py < S.img_h) {
+                    if (S.load == PF_LOAD_LOAD) {
+                        // LOAD_ACTION_LOAD (tile.comp:744-757): start from the pixel already there
+                        const uchar4 d = img[(size_t)py * S.img_w + px];
+                        cr = (float)d.x * inv255;
+                        cg = (float)d.y * inv255;
+                        cb = (float)d.z * inv255;
+                        ca = (float)d.w * inv255;
+                    }
                     img[(size_t)py * S.img_w + px] =
                         make_uchar4((unsigned char)__float2uint_rn(__saturatef(ar[k] + tr[k] * cr) * 255.0f),
                                     (unsigned char)__float2uint_rn(__saturatef(ag[k] + tr[k] * cg) * 255.0f),
@@ -1889,6 +1904,39 @@ __global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 3
             const int slot = threadIdx.x == 0 ? kStEntries : (threadIdx.x == 1 ? kStListFills : kStWalkChunks);
             if (v) atomicAdd(&b.status[slot], v);
         }
+    }
+}
+
+// Frame counters: the draw paths' alpha tiles and visible tiles (an alpha tile or a nonzero
+// backdrop: the tiles build_tile_batches keeps, core/d3d9/scene_builder.cpp:57-63).  One block
+// per path, over its tile states.
+__global__ void __launch_bounds__(kThreads) k_tile_counts(Batch b) {
+    __shared__ uint32_t red[2][kThreads / 32];
+    const uint32_t p = blockIdx.x;
+    const PathDev P = b.paths[p];
+    uint32_t alpha = 0, visible = 0;
+    if (!(P.flags & kPathIsClip)) {
+        const uint32_t T = (uint32_t)max(P.rx1 - P.rx0, 0) * (uint32_t)max(P.ry1 - P.ry0, 0);
+        for (uint32_t t = threadIdx.x; t < T; t += kThreads) {
+            const uint32_t st = b.tile_state[P.tile_first + t];
+            alpha += (st >> 8) & 1u;
+            visible += (st & 0x1ffu) != 0;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        alpha += __shfl_down_sync(0xffffffffu, alpha, o);
+        visible += __shfl_down_sync(0xffffffffu, visible, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = alpha;
+        red[1][threadIdx.x >> 5] = visible;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        uint32_t v = 0;
+        for (int w = 0; w < kThreads / 32; w++) v += red[threadIdx.x][w];
+        if (v) atomicAdd(&b.status[threadIdx.x == 0 ? kStAlphaTiles : kStVisible], v);
     }
 }
 
@@ -1924,6 +1972,26 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_list_dump(Batch b) {
         if (kWrite) b.z[fb] = z;
         else b.fb_count[fb] = n;
     }
+}
+
+// Every tile of the frame after the clip rules, for the canonical output (not part of a frame):
+// the state the composite's walk sees - apply_clip, the same function, on each tile of a
+// clipped path - and the clip tile whose mask it takes (kNone if none).  state[t] holds the
+// int8 backdrop in bits 0-7, the alpha flag in bit 8, the mask source in bits 9-10 and, for
+// kMaskBoth, the draw tile's own backdrop in bits 16-23.  One thread per tile.
+__global__ void __launch_bounds__(kThreads) k_clip_dump(Batch b, uint32_t n_tiles, uint32_t *state, uint32_t *clip) {
+    const uint32_t t = global_tid();
+    if (t >= n_tiles) return;
+    const uint32_t p = upper_bound(b.path_tiles, b.n_paths + 1, t) - 1;
+    Cand c{0, t, b.tile_state[t], 0, 0, 0, 0, kNone};
+    if (b.path_clip_rel[p] != kNone && !(b.paths[p].flags & kPathIsClip)) {
+        const PathDev P = b.paths[p];
+        const uint32_t local = t - P.tile_first, rw = (uint32_t)(P.rx1 - P.rx0);
+        apply_clip(b, p, P.rx0 + (int32_t)(local % rw), P.ry0 + (int32_t)(local / rw), c);
+        if (mask_mode(c.st) == kMaskOwn) c.gc = kNone;
+    }
+    state[t] = c.st;
+    clip[t] = c.gc;
 }
 
 // Coverage of listed alpha tiles after the fill rule (test output; one warp per tile).
@@ -2134,10 +2202,20 @@ cudaError_t launch_composite(const Batch &b, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_tile_counts(const Batch &b, cudaStream_t st) {
+    if (b.n_paths) PF_LAUNCH(k_tile_counts<<<b.n_paths, kThreads, 0, st>>>(b));
+    return cudaGetLastError();
+}
+
 cudaError_t launch_list_dump(const Batch &b, bool write, cudaStream_t st) {
     if (!b.n_fb) return cudaSuccess;
     if (write) PF_LAUNCH(k_list_dump<true><<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
     else PF_LAUNCH(k_list_dump<false><<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clip_dump(const Batch &b, uint32_t n_tiles, uint32_t *state, uint32_t *clip, cudaStream_t st) {
+    if (n_tiles && b.path_clip_cat) PF_LAUNCH(k_clip_dump<<<grid_for(n_tiles), kThreads, 0, st>>>(b, n_tiles, state, clip));
     return cudaGetLastError();
 }
 

@@ -31,7 +31,7 @@ EXPORTS = [
     "pf_sizer_gradient", "pf_sizer_train", "pf_sizer_save", "pf_sizer_load", "pf_path_features", "pf_path_counts",
     "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags", "pf_sizer_predict_noalloc",
     "pf_set_host_image", "pf_read_outline", "pf_upload_stats_get", "pf_svg_parse", "pf_svg_scene", "pf_svg_free",
-    "pf_read_images_async", "pf_images_wait",
+    "pf_read_images_async", "pf_images_wait", "pf_write_image", "pf_render_auto", "pf_auto_choice",
 ]
 
 N_FEATURES = 12
@@ -55,6 +55,7 @@ class SceneView(C.Structure):
         ("path_clip", C.c_void_p), ("path_is_clip", C.c_void_p),
         ("path_stroke", C.c_void_p), ("contour_closed", C.c_void_p), ("dashes", C.c_void_p),
         ("n_dashes", C.c_uint32), ("path_paint", C.c_void_p), ("stops", C.c_void_p), ("n_stops", C.c_uint32),
+        ("view_box", C.c_void_p), ("load_action", C.c_uint32),
     ]
 
 
@@ -168,6 +169,13 @@ def scene_view(scene) -> "tuple[SceneView, list]":
         st_ = np.ascontiguousarray(scene.stops)
         v.path_paint, v.stops, v.n_stops = pp.ctypes.data, st_.ctypes.data, len(st_)
         arrs += [pp, st_]
+    if getattr(scene, "view_box", None) is not None:
+        vb = np.ascontiguousarray(scene.view_box, np.float32)
+        if vb.shape != (4,):
+            raise ValueError("view_box is (left, top, right, bottom)")
+        v.view_box = vb.ctypes.data
+        arrs.append(vb)
+    v.load_action = int(getattr(scene, "load_action", 0))
     return v, arrs
 
 
@@ -301,6 +309,15 @@ class Renderer:
                     self.ctx)
         return out
 
+    def write_image(self, scene: int, rgba: np.ndarray) -> None:
+        """Put pixels into a scene's destination image, for a frame with load_action 1 (LOAD)."""
+        w, h = self._sizes[scene]
+        rgba = np.ascontiguousarray(rgba, np.uint8)
+        if rgba.size != w * h * 4:
+            raise ValueError(f"scene {scene} needs a {h}x{w}x4 image")
+        self._check(self.lib.pf_write_image(self.ctx, scene, C.c_void_p(rgba.ctypes.data), C.c_size_t(rgba.nbytes)),
+                    self.ctx)
+
     def upload_stats(self) -> Dict[str, float]:
         """The last upload's stroke pass: outline sizes, stroked/dashed paths, device times."""
         r = UploadStats()
@@ -391,6 +408,25 @@ class Renderer:
             count = len(self._sizes) - first
         self._check(self.lib.pf_render_learned(self.ctx, first, count, C.byref(st)), self.ctx)
         return st.to_dict()
+
+    def render_auto(self, first: int = 0, count: Optional[int] = None) -> Dict[str, float]:
+        """The frame the library picks: the learned one where it measured faster, else the exact one."""
+        st = FrameStats()
+        if count is None:
+            count = len(self._sizes) - first
+        self._check(self.lib.pf_render_auto(self.ctx, first, count, C.byref(st)), self.ctx)
+        return st.to_dict()
+
+    def last_auto_choice(self) -> Dict[str, object]:
+        """What render_auto did: the frame its last call ran, the settled choice (None while it is
+        still timing) and the device times it measured."""
+        last, choice = C.c_int(), C.c_int()
+        ems, lms = C.c_float(), C.c_float()
+        self._check(self.lib.pf_auto_choice(self.ctx, C.byref(last), C.byref(choice), C.byref(ems), C.byref(lms)),
+                    self.ctx)
+        names = {0: "exact", 1: "learned"}
+        return {"last": names[last.value], "choice": names.get(choice.value), "exact_ms": ems.value,
+                "learned_ms": lms.value}
 
     def sizer_init(self, seed: int = 0) -> None:
         self._check(self.lib.pf_sizer_init(self.ctx, C.c_uint64(seed)), self.ctx)

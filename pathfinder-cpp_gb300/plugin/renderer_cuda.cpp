@@ -9,7 +9,6 @@
 namespace Pathfinder {
 
 void SceneBuilderCuda::build(Scene *scene, Renderer *renderer) {
-    (void)renderer;
     this->scene = scene;
     points_.clear();
     flags_.clear();
@@ -65,9 +64,24 @@ void SceneBuilderCuda::build(Scene *scene, Renderer *renderer) {
         view_.path_clip = path_clip_.data();
         view_.path_is_clip = path_is_clip_.data();
     }
-    view_.width = vb.width();
-    view_.height = vb.height();
-    view_.clear_color = 0;
+    // the view box with its origin (Scene::set_view_box); the image is the destination texture
+    // (the tile pass covers it from (0, 0), core/d3d11/renderer.cpp:371, 443), or the view box's
+    // lower-right corner when no destination is set
+    view_box_[0] = vb.left;
+    view_box_[1] = vb.top;
+    view_box_[2] = vb.right;
+    view_box_[3] = vb.bottom;
+    view_.view_box = view_box_;
+    const std::shared_ptr<Texture> dest = renderer ? renderer->get_dest_texture() : nullptr;
+    if (dest) {
+        view_.width = float(dest->get_size().x);
+        view_.height = float(dest->get_size().y);
+    } else {
+        view_.width = vb.right > 1.0f ? vb.right : 1.0f;
+        view_.height = vb.bottom > 1.0f ? vb.bottom : 1.0f;
+    }
+    view_.clear_color = 0;  // RendererD3D11::clear_color is transparent black (renderer.h:77)
+    view_.load_action = PF_LOAD_CLEAR;
 }
 
 RendererCuda::RendererCuda(const std::shared_ptr<Device> &device, const std::shared_ptr<Queue> &queue,
@@ -98,11 +112,14 @@ void RendererCuda::draw(const std::shared_ptr<SceneBuilder> &scene_builder, bool
         return;
     }
     pf_scene_view view = builder->view();
-    if (!clear_dst_texture) view.clear_color = 0;
+    const size_t w = static_cast<size_t>(std::ceil(view.width)), h = static_cast<size_t>(std::ceil(view.height));
+    // LOAD_ACTION_LOAD: composite over what this renderer last put into the destination
+    const bool load = !clear_dst_texture && pixels_.size() == w * h * 4;
+    view.load_action = load ? PF_LOAD_LOAD : PF_LOAD_CLEAR;
     int st = pf_scene_upload(ctx_, &view);
+    if (st == PF_OK && load) st = pf_write_image(ctx_, 0, pixels_.data(), pixels_.size());
     if (st == PF_OK) st = learned_ ? pf_render_learned(ctx_, 0, 1, &stats_) : pf_render(ctx_, &stats_);
     if (st == PF_OK) {
-        const size_t w = static_cast<size_t>(std::ceil(view.width)), h = static_cast<size_t>(std::ceil(view.height));
         pixels_.resize(w * h * 4);
         st = pf_read_image(ctx_, pixels_.data(), pixels_.size());
         if (st == PF_OK && dest_texture_) {

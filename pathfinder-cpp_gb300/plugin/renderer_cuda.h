@@ -41,12 +41,16 @@ private:
     std::vector<uint8_t> flags_;
     std::vector<uint32_t> contour_start_, path_start_, color_, path_clip_;
     std::vector<uint8_t> fill_rule_, path_is_clip_;
+    float view_box_[4] = {};
     pf_scene_view view_{};
 };
 
 /// Runs the GPU-driven frame on CUDA (Renderer, pathfinder/core/renderer.h:58-139).  The
 /// RGBA8 result is written into the destination texture through the device's own command
-/// encoder, so the rest of the application sees a normal Pathfinder texture.
+/// encoder, so the rest of the application sees a normal Pathfinder texture.  draw() with
+/// clear_dst_texture = false composites over the destination (LOAD_ACTION_LOAD,
+/// core/d3d11/renderer.cpp:376-380): the pixels this renderer last wrote into it, handed back to
+/// the frame with pf_write_image (the Device interface has no texture read-back).
 class RendererCuda : public Renderer {
 public:
     RendererCuda(const std::shared_ptr<Device> &device, const std::shared_ptr<Queue> &queue, int cuda_device = 0);

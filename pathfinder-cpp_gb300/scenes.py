@@ -112,6 +112,8 @@ class Scene:
     dashes: Optional[np.ndarray] = None        # float32 [D] dash patterns of the strokes
     path_paint: Optional[np.ndarray] = None    # PAINT_DTYPE [N]: solid or gradient paint per path
     stops: Optional[np.ndarray] = None         # STOP_DTYPE [S] colour stops of the gradients
+    view_box: Optional[np.ndarray] = None      # float32 [4] left, top, right, bottom (None: the canvas)
+    load_action: int = 0                       # 0 clear to `clear`, 1 composite over the image there
 
     @property
     def n_paths(self) -> int:

@@ -52,7 +52,8 @@ def load_golden(name):
                  contour_closed=d["contour_closed"] if "contour_closed" in d else None,
                  dashes=d["dashes"] if "dashes" in d else None,
                  path_paint=d["path_paint"] if "path_paint" in d else None,
-                 stops=d["stops"] if "stops" in d else None)
+                 stops=d["stops"] if "stops" in d else None,
+                 view_box=d["view_box"] if "view_box" in d else None)
     ref = {k: d["ref_" + k] for k in CANON_KEYS}
     for k in OUTLINE_KEYS:
         if "out_" + k in d:

@@ -3,7 +3,7 @@
 Run in a checkout next to the reference sources (the reference tree is the one
 oracle.REF_ROOT names: PF_REFERENCE_ROOT, else the oracle Makefile's default):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [fixture names]   # all fixtures when no name is given
 
 For every scene below it builds oracle/_ref/libpfref.so (the reference's Tiler,
 ObjectBuilder and SceneBuilderD3D9 compiled from their sources, driven by
@@ -319,6 +319,25 @@ def generator_scenes():
     }
 
 
+def with_view_box(sc: S.Scene, box) -> S.Scene:
+    sc.view_box = np.asarray(box, np.float32)
+    return sc
+
+
+def view_box_scenes():
+    """Scenes whose view box (Scene::set_view_box) is not the canvas: an inner box with a
+    fractional origin, a box reaching above and left of the canvas (negative tile coordinates)
+    and past its right and bottom edges, and a clipped scene inside a box."""
+    wide = S.large_single(seed=12, n_paths=60, side=640)
+    wide.points = (wide.points.astype(np.float64) * 1.25 - 96.0).astype(np.float32)  # some paths off canvas
+    return {
+        "view_box_inner": with_view_box(S.plain_small(seed=9, n_paths=40, side=512), [37.5, 21.25, 401.7, 389.0]),
+        "view_box_outside": with_view_box(S.Scene(**{**wide.__dict__, "width": 480.0, "height": 400.0}),
+                                          [-70.3, -33.0, 530.0, 470.5]),
+        "view_box_clipped": with_view_box(S.clipped(seed=13, n_paths=50, side=256, n_clips=3), [64.0, 40.0, 200.0, 230.0]),
+    }
+
+
 def svg_scenes():
     """SVG documents through the reference's nanosvg + SvgScene replay (the harness): the scene
     the reference's canvas builds, stored with the document's text (svg_text) so the parser can be
@@ -367,10 +386,14 @@ def main() -> None:
     small.update(stroke_scenes())
     small.update(gradient_scenes())
     small.update(generator_scenes())
+    small.update(view_box_scenes())
     texts = {}
     for name, (sc, text) in svg_scenes().items():
         small[name], texts[name] = sc, text
+    only = set(sys.argv[1:])  # names to (re)write; all when none are given
     for name, sc in small.items():
+        if only and name not in only:
+            continue
         ref = oracle.reference_tile_scene(sc)
         arrays = {k: getattr(sc, k) for k in INPUT_KEYS}
         if sc.path_clip is not None:
@@ -382,6 +405,8 @@ def main() -> None:
         if sc.path_paint is not None:
             arrays.update({k: getattr(sc, k) for k in PAINT_KEYS})
             arrays["ref_ramps"] = oracle.reference_ramps(sc)
+        if sc.view_box is not None:
+            arrays["view_box"] = sc.view_box
         arrays["meta"] = np.asarray([sc.width, sc.height, sc.clear], np.float64)
         if name in texts:
             arrays["svg_text"] = np.frombuffer(texts[name].encode(), np.uint8)
@@ -389,6 +414,8 @@ def main() -> None:
             arrays["ref_" + k] = ref[k]
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrays)
         print(f"{name}: {sc.n_paths} paths, {len(ref['fills'])} fills, {int(ref['tile_alpha'].sum())} alpha tiles")
+    if only:
+        return
     digests = {}
     for name, sc in full_scenes().items():
         ref = oracle.reference_tile_scene(sc)

@@ -1,6 +1,7 @@
 // Builds a scene through the reference's own API (Path2d, Paint, Scene::push_draw_path and
-// push_clip_path), packs it with the drop-in SceneBuilderCuda, and tiles the packed scene with
-// both the reference's d3d9 tiler (through the harness) and the restated oracle.  Prints "OK <fills>" when the two
+// push_clip_path, a view box with an origin), packs it with the drop-in SceneBuilderCuda, and
+// tiles the packed scene with both the reference's d3d9 tiler (through the harness) and the
+// restated oracle.  Prints "OK <fills>" when the two
 // agree and the packed colours / fill rules / clip assignments are the ones the scene holds.
 #include <cstdio>
 #include <cstring>
@@ -13,7 +14,9 @@
 using namespace Pathfinder;
 
 int main() {
-    Scene scene(0, RectF({0.f, 0.f}, {300.f, 200.f}));
+    // a view box with an origin: tiles and lines are clipped to it (Scene::set_view_box rounds
+    // its right edge up to 304)
+    Scene scene(0, RectF({12.5f, 7.0f}, {300.f, 200.f}));
     // two clip paths (Scene::push_clip_path): a diamond and an even-odd ring
     uint32_t clip_ids[2];
     {
@@ -64,6 +67,9 @@ int main() {
     builder.build(&scene, nullptr);
     const pf_scene_view &v = builder.view();
     if (v.n_paths != 10 || !v.path_clip || !v.path_is_clip) return std::printf("FAIL paths %u\n", v.n_paths), 1;
+    if (!v.view_box || v.view_box[0] != 12.5f || v.view_box[1] != 7.0f || v.view_box[2] != 304.f ||
+        v.view_box[3] != 200.f || v.load_action != PF_LOAD_CLEAR)
+        return std::printf("FAIL view box\n"), 1;
     for (uint32_t i = 0; i < 10; i++) {
         const uint32_t want = i >= 8 ? PF_NO_CLIP : i % 4 == 3 ? PF_NO_CLIP : 8 + clip_ids[i % 2];
         if (v.path_clip[i] != want || v.path_is_clip[i] != (i >= 8)) return std::printf("FAIL clip %u\n", i), 1;

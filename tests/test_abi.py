@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol(pf):
 
 
 def test_abi_version(pf):
-    assert pf.load().pf_abi_version() == 4
+    assert pf.load().pf_abi_version() == 5
 
 
 def test_null_arguments_are_rejected_without_a_device(pf):

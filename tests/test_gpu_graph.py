@@ -1,7 +1,8 @@
 """The learned frame replayed as a CUDA graph equals the frame it was captured from.
 
-After a learned frame has run with its buffers sized, the library records it as a graph;
-later learned frames over the same scenes replay it (one launch, one synchronisation).
+The second learned frame in a row over the same scenes (the first one has sized the buffers)
+is recorded as a graph and replayed; later learned frames replay it (one launch, one
+synchronisation).
 Any change of scenes, sizer, buffers or flags drops the graph.
 """
 import numpy as np
@@ -33,10 +34,10 @@ def test_replayed_learned_frame_equals_exact_frame(pf):
         r.sizer_load()
         r.render()
         exact = _outputs(r, len(scs))
-        first = r.render_learned()            # plain learned frame, then captured
+        first = r.render_learned()            # plain learned frame
         assert first["host_syncs"] >= 2
         _same(_outputs(r, len(scs)), exact)
-        for _ in range(3):                    # replays
+        for _ in range(3):                    # recorded and replayed, then replays
             st = r.render_learned()
             assert st["host_syncs"] == 1, st
             assert st["overflow"] == 0

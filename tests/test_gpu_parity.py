@@ -77,6 +77,9 @@ def test_plain_small_full_size(renderer, oracle_mod):
     stats, got, img = render(renderer, sc)
     want = oracle_mod.tile_scene(sc, oracle_mod.Z_D3D11, threads=8)
     assert_canon(got, want, TILE_KEYS + LIST_KEYS)
+    # the frame counters (the session renderer has them on): alpha and visible tiles
+    assert stats["alpha_tiles"] == int(want["tile_alpha"].sum())
+    assert stats["visible_tiles"] == int(((want["tile_alpha"] != 0) | (want["tile_backdrop"] != 0)).sum())
     ref_img, _ = oracle_mod.render(sc, threads=16)
     diff = np.abs(img.astype(np.int32) - ref_img.astype(np.int32))
     print(f"plain_small: {stats['fills']} fills, pixel max err {diff.max()} mean {diff.mean():.2e}")
