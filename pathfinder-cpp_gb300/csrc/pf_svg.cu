@@ -6,20 +6,57 @@
 // (Canvas::stroke_path: dash, stroke-to-fill).  Here one pass writes the scene arrays directly:
 // the fill as a path, the stroke as a path with a pf_stroke (the GPU strokes it at upload).
 //
-// What is followed, and where (nanosvg.h / core):
-//   XML tokenising                nsvg__parseXML, nsvg__parseElement        :240-345
-//   numbers                       nsvg__parseNumber, nsvg__atof              :1087-1187
-//   path data, shapes             nsvg__parsePath, nsvg__parseRect/Circle/Ellipse/Line/Poly,
-//                                 nsvg__pathArcTo, nsvg__lineTo (lines become cubics)  :698-741, 1901-2563
-//   attributes, style, transforms nsvg__parseAttr, nsvg__parseStyle, nsvg__parseTransform :1523-1900
-//   colours                       hex, rgb(), the basic named colours (others read as gray)
-//   gradients                     nsvg__parseGradient(Stop), nsvg__createGradient   :807-896, 2619-2730
-//   view box and units            nsvg__scaleToViewbox                       :2813-2942
-//   scene assembly                SvgScene (core/svg.cpp:158-196), Path2d::move_to / cubic_to /
-//                                 close_path (core/path2d.cpp), Canvas::fill_path / stroke_path
-//                                 (core/canvas.cpp:265-300), convert_nsvg_paint (svg.cpp:63-133)
-// Float arithmetic follows those functions operation by operation (this file is compiled
-// without FMA contraction), so the scene's points are the reference's bit for bit.
+// Two kinds of code are in this file.
+//
+// * Written for this library: the tag reader (read_tag / parse_document), the element and
+//   attribute dispatch tables (kElements, kAttrRules), style declarations (apply_style), units,
+//   colours, url() and dash lists, and the scene assembly (SceneOut, convert_paint,
+//   emit_contours, pf_svg_parse).  They accept exactly the documents nanosvg accepts and read them
+//   the same way (that is what makes the scene equal to the reference's), but they are not
+//   nanosvg's code.
+// * ALTERED FROM NANOSVG (the notice below applies to these parts): the arithmetic whose
+//   operation order fixes the output bits - the number reader (parse_atof, parse_number,
+//   next_path_item), the 2x3 transforms and transform lists (xf_*, transform_args,
+//   parse_transform), curve bounds (eval_bezier, curve_bounds, local_bounds), path data and
+//   shapes (parse_path, arc_to, parse_rect / circle / ellipse / line / poly, Parser::move_to /
+//   line_to / cubic_to / add_path), gradients (parse_gradient, parse_stop, create_gradient) and
+//   the view-box scaling (scale_to_viewbox).  They are restated in this library's own types and
+//   names from nanosvg.h (nsvg__atof, nsvg__parseNumber, nsvg__xform*, nsvg__parseTransform,
+//   nsvg__pathArcTo, nsvg__parsePath, nsvg__parseRect..Poly, nsvg__createGradient,
+//   nsvg__scaleToViewbox), and altered: zeros where nanosvg reads memory it never wrote (a
+//   transform item without its arguments, the inverse of a singular transform), no parser-state
+//   allocation, C++ containers for its linked lists.
+//
+// Float arithmetic follows nanosvg operation by operation (this file is compiled without FMA
+// contraction), so the scene's points are the reference's bit for bit.
+//
+// nanosvg's notice, which travels with the altered parts:
+//
+//   Copyright (c) 2013-14 Mikko Mononen memon@inside.org
+//
+//   This software is provided 'as-is', without any express or implied
+//   warranty.  In no event will the authors be held liable for any damages
+//   arising from the use of this software.
+//
+//   Permission is granted to anyone to use this software for any purpose,
+//   including commercial applications, and to alter it and redistribute it
+//   freely, subject to the following restrictions:
+//
+//   1. The origin of this software must not be misrepresented; you must not
+//   claim that you wrote the original software. If you use this software
+//   in a product, an acknowledgment in the product documentation would be
+//   appreciated but is not required.
+//   2. Altered source versions must be plainly marked as such, and must not be
+//   misrepresented as being the original software.
+//   3. This notice may not be removed or altered from any source distribution.
+//
+//   The SVG parser is based on Anti-Grain Geometry 2.4 SVG example
+//   Copyright (C) 2002-2004 Maxim Shemanarev (McSeem) (http://www.antigrain.com/)
+//
+//   Arc calculation code based on canvg (https://code.google.com/p/canvg/)
+//
+//   Bounding box calculation based on http://blog.hackers-cafe.net/2009/06/how-to-calculate-bezier-curves-bounding.html
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -35,7 +72,6 @@ constexpr float kPi = 3.14159265358979323846264338327f;  // NSVG_PI
 constexpr float kKappa90 = 0.5522847493f;                // NSVG_KAPPA90
 constexpr int kMaxAttr = 128;
 constexpr int kMaxDashes = 8;
-constexpr int kMaxXmlAttribs = 256;
 
 enum Units { kUser, kPx, kPt, kPc, kMm, kCm, kIn, kPercent, kEm, kEx };
 enum Paint { kNone = 0, kColor = 1, kLinear = 2, kRadial = 3 };
@@ -309,7 +345,7 @@ struct Parser {
     float view_minx = 0, view_miny = 0, view_width = 0, view_height = 0;
     int align_x = kAlignMin, align_y = kAlignMin, align_type = kAlignNone;
     float dpi = 96.0f;
-    bool path_flag = false, defs_flag = false;
+    bool defs_flag = false;
 
     Parser() {
         std::memset(attr, 0, sizeof attr);
@@ -537,7 +573,9 @@ void Parser::add_shape() {
             out.type = kColor;
             out.color = color | (uint32_t)(opacity * 255) << 24;
         } else if (has == 2) {
-            float inv[6], lb[4];
+            // a singular transform leaves nanosvg's inverse unwritten (it resets the transform
+            // instead); here that inverse is zero, so the shape's local bounds are zero
+            float inv[6] = {0, 0, 0, 0, 0, 0}, lb[4] = {0, 0, 0, 0};
             float xf[6];
             std::memcpy(xf, a.xform, sizeof xf);
             xf_inverse(inv, xf);
@@ -551,16 +589,18 @@ void Parser::add_shape() {
 }
 
 // --- attributes ----------------------------------------------------------------------------------
+// A length's unit is named by the first characters after its number: the two-letter CSS units and
+// '%' (anything else is a user unit).
 int parse_units(const char *u) {
-    if (u[0] == 'p' && u[1] == 'x') return kPx;
-    if (u[0] == 'p' && u[1] == 't') return kPt;
-    if (u[0] == 'p' && u[1] == 'c') return kPc;
-    if (u[0] == 'm' && u[1] == 'm') return kMm;
-    if (u[0] == 'c' && u[1] == 'm') return kCm;
-    if (u[0] == 'i' && u[1] == 'n') return kIn;
+    static const struct {
+        char c0, c1;
+        int unit;
+    } kUnits[] = {{'p', 'x', kPx}, {'p', 't', kPt}, {'p', 'c', kPc}, {'m', 'm', kMm}, {'c', 'm', kCm},
+                  {'i', 'n', kIn}, {'e', 'm', kEm}, {'e', 'x', kEx}};
     if (u[0] == '%') return kPercent;
-    if (u[0] == 'e' && u[1] == 'm') return kEm;
-    if (u[0] == 'e' && u[1] == 'x') return kEx;
+    if (u[0] == '\0') return kUser;
+    for (const auto &k : kUnits)
+        if (u[0] == k.c0 && u[1] == k.c1) return k.unit;
     return kUser;
 }
 Coord parse_coord_raw(const char *s) {
@@ -578,68 +618,64 @@ bool is_coordinate(const char *s) {
     return is_digit(*s) || *s == '.';
 }
 
-uint32_t parse_color_hex(const char *s) {
-    unsigned r = 0, g = 0, b = 0;
-    if (std::sscanf(s, "#%2x%2x%2x", &r, &g, &b) == 3) return rgb(r, g, b);
-    if (std::sscanf(s, "#%1x%1x%1x", &r, &g, &b) == 3) return rgb(r * 17, g * 17, b * 17);
-    return rgb(128, 128, 128);
+// Colours: "#rrggbb" / "#rgb" (read with the C library's %x conversions, white space and all),
+// "rgb(r, g, b)" with integers (%u) or with percentages, and the colour keywords the reference's
+// build of nanosvg knows (its short table: other names, and anything malformed, read as gray).
+constexpr uint32_t kGray = 128u | 128u << 8 | 128u << 16;
+
+uint32_t hex_color(const char *s) {
+    unsigned c[3] = {0, 0, 0};
+    if (std::sscanf(s, "#%2x%2x%2x", &c[0], &c[1], &c[2]) == 3) return rgb(c[0], c[1], c[2]);
+    if (std::sscanf(s, "#%1x%1x%1x", &c[0], &c[1], &c[2]) == 3) return rgb(17 * c[0], 17 * c[1], 17 * c[2]);
+    return kGray;
 }
-uint32_t parse_color_rgb(const char *s) {
-    unsigned ri[3];
-    float rf[3];
-    if (std::sscanf(s, "rgb(%u, %u, %u)", &ri[0], &ri[1], &ri[2]) != 3) {
-        const char delim[3] = {',', ',', ')'};
-        s += 4;
-        int i;
-        for (i = 0; i < 3; i++) {
-            while (*s && is_space(*s)) s++;
-            if (*s == '+') s++;
-            if (!*s) break;
-            rf[i] = (float)parse_atof(s);
-            while (*s && is_digit(*s)) s++;
-            if (*s == '.') {
-                s++;
-                if (!is_digit(*s)) break;
-                while (*s && is_digit(*s)) s++;
-            }
-            if (*s == '%') s++;
-            else break;
-            while (is_space(*s)) s++;
-            if (*s == delim[i]) s++;
-            else break;
-        }
-        if (i == 3) {
-            ri[0] = (unsigned)std::round(rf[0] * 2.55f);
-            ri[1] = (unsigned)std::round(rf[1] * 2.55f);
-            ri[2] = (unsigned)std::round(rf[2] * 2.55f);
-        } else {
-            ri[0] = ri[1] = ri[2] = 128;
-        }
+
+// One "<number>%" component of rgb(...), then white space and the expected delimiter; false when
+// the text does not have that form.
+bool percent_component(const char *&s, char delim, float &out) {
+    while (*s && is_space(*s)) s++;
+    if (*s == '+') s++;
+    if (!*s) return false;
+    out = (float)parse_atof(s);
+    while (is_digit(*s)) s++;
+    if (*s == '.') {
+        if (!is_digit(*++s)) return false;
+        while (is_digit(*s)) s++;
     }
-    for (unsigned &v : ri)
-        if (v > 255) v = 255;
-    return rgb(ri[0], ri[1], ri[2]);
+    if (*s++ != '%') return false;
+    while (*s && is_space(*s)) s++;  // (nanosvg's loop here also steps over the string's end)
+    return *s++ == delim;
 }
-// The colour keywords nanosvg knows as the reference builds it (its basic table, without
-// NANOSVG_ALL_COLOR_KEYWORDS); any other name reads as gray, as unknown names do.
-uint32_t parse_color_name(const char *s) {
-    static const struct {
-        const char *name;
-        uint8_t r, g, b;
-    } kNames[] = {{"red", 255, 0, 0},       {"green", 0, 128, 0},   {"blue", 0, 0, 255},
-                  {"yellow", 255, 255, 0},  {"cyan", 0, 255, 255},  {"magenta", 255, 0, 255},
-                  {"black", 0, 0, 0},       {"grey", 128, 128, 128}, {"gray", 128, 128, 128},
-                  {"white", 255, 255, 255}};
-    for (const auto &n : kNames)
-        if (std::strcmp(n.name, s) == 0) return rgb(n.r, n.g, n.b);
-    return rgb(128, 128, 128);
+
+uint32_t function_color(const char *s) {
+    unsigned v[3];
+    if (std::sscanf(s, "rgb(%u, %u, %u)", &v[0], &v[1], &v[2]) != 3) {
+        const char *q = s + 4;
+        float f[3];
+        if (!percent_component(q, ',', f[0]) || !percent_component(q, ',', f[1]) || !percent_component(q, ')', f[2]))
+            return kGray;
+        for (int k = 0; k < 3; k++) v[k] = (unsigned)std::round(f[k] * 2.55f);
+    }
+    return rgb(v[0] > 255 ? 255 : v[0], v[1] > 255 ? 255 : v[1], v[2] > 255 ? 255 : v[2]);
 }
+
+uint32_t keyword_color(const char *s) {
+    static const std::pair<const char *, uint32_t> kWords[] = {  // sorted by name
+        {"black", 0x000000u}, {"blue", 0xff0000u},    {"cyan", 0xffff00u},  {"gray", 0x808080u},
+        {"green", 0x008000u}, {"grey", 0x808080u},    {"magenta", 0xff00ffu}, {"red", 0x0000ffu},
+        {"white", 0xffffffu}, {"yellow", 0x00ffffu}};
+    const auto *end = kWords + sizeof kWords / sizeof kWords[0];
+    const auto *it = std::lower_bound(kWords, end, s, [](const std::pair<const char *, uint32_t> &w, const char *k) {
+        return std::strcmp(w.first, k) < 0;
+    });
+    return it != end && std::strcmp(it->first, s) == 0 ? it->second : kGray;
+}
+
 uint32_t parse_color(const char *s) {
     while (*s == ' ') ++s;
-    const size_t len = std::strlen(s);
-    if (len >= 1 && *s == '#') return parse_color_hex(s);
-    if (len >= 4 && s[0] == 'r' && s[1] == 'g' && s[2] == 'b' && s[3] == '(') return parse_color_rgb(s);
-    return parse_color_name(s);
+    if (*s == '#') return hex_color(s);
+    if (std::strncmp(s, "rgb(", 4) == 0) return function_color(s);
+    return keyword_color(s);
 }
 float parse_opacity(const char *s) {
     float v = (float)parse_atof(s);
@@ -729,148 +765,145 @@ void parse_transform(float *xform, const char *str) {
     }
 }
 
-void parse_url(char *id, const char *str) {
-    int i = 0;
-    str += 4;
-    if (*str && *str == '#') str++;
-    while (i < 63 && *str && *str != ')') id[i++] = *str++;
-    id[i] = '\0';
+// "url(#name)" (the '#' optional): the name, up to 63 characters or the ')'.
+void url_target(char *id, const char *value) {
+    const char *q = value + 4;
+    if (*q == '#') q++;
+    size_t n = 0;
+    while (n < 63 && q[n] && q[n] != ')') n++;
+    std::memcpy(id, q, n);
+    id[n] = '\0';
 }
 
-const char *next_dash_item(const char *s, char *it) {
-    int n = 0;
-    it[0] = '\0';
-    while (*s && (is_space(*s) || *s == ',')) s++;
-    while (*s && (!is_space(*s) && *s != ',')) {
-        if (n < 63) it[n++] = *s;
-        s++;
-    }
-    it[n++] = '\0';
-    return s;
-}
-
-int parse_dash_array(Parser &p, const char *str, float *dashes) {
-    char item[64];
-    int count = 0;
-    float sum = 0.0f;
+// stroke-dasharray: "none" (anything starting with 'n'), or lengths split by white space and
+// commas, at most kMaxDashes kept (absolute values); a pattern whose sum is not above 1e-6 is
+// no pattern.  Each length is read from at most 63 of its characters.
+int dash_pattern(Parser &p, const char *str, float *dashes) {
     if (str[0] == 'n') return 0;
-    while (*str) {
-        str = next_dash_item(str, item);
-        if (!*item) break;
+    int count = 0;
+    const char *q = str;
+    for (;;) {
+        while (*q && (is_space(*q) || *q == ',')) q++;
+        const char *b = q;
+        while (*q && !is_space(*q) && *q != ',') q++;
+        if (q == b) break;
+        char item[64];
+        const size_t n = std::min<size_t>(size_t(q - b), 63);
+        std::memcpy(item, b, n);
+        item[n] = '\0';
         if (count < kMaxDashes) dashes[count++] = std::fabs(parse_coord(p, item, 0.0f, p.actual_length()));
     }
+    float sum = 0.0f;
     for (int i = 0; i < count; i++) sum += dashes[i];
-    if (sum <= 1e-6f) count = 0;
-    return count;
+    return sum <= 1e-6f ? 0 : count;
 }
 
-void parse_style(Parser &p, const char *str);
+// Presentation attributes and style properties (the ones the reference's nanosvg build reads),
+// applied to the current attribute state: one handler per name, found by binary search.
+void apply_style(Parser &p, const char *text);
 
-bool parse_attr(Parser &p, const char *name, const char *value) {
-    Attr &a = p.cur();
-    if (std::strcmp(name, "style") == 0) {
-        parse_style(p, value);
-    } else if (std::strcmp(name, "display") == 0) {
-        if (std::strcmp(value, "none") == 0) a.visible = 0;
-    } else if (std::strcmp(name, "fill") == 0) {
-        if (std::strcmp(value, "none") == 0) {
-            a.has_fill = 0;
-        } else if (std::strncmp(value, "url(", 4) == 0) {
-            a.has_fill = 2;
-            parse_url(a.fill_grad, value);
-        } else {
-            a.has_fill = 1;
-            a.fill_color = parse_color(value);
-        }
-    } else if (std::strcmp(name, "opacity") == 0) {
-        a.opacity = parse_opacity(value);
-    } else if (std::strcmp(name, "fill-opacity") == 0) {
-        a.fill_opacity = parse_opacity(value);
-    } else if (std::strcmp(name, "stroke") == 0) {
-        if (std::strcmp(value, "none") == 0) {
-            a.has_stroke = 0;
-        } else if (std::strncmp(value, "url(", 4) == 0) {
-            a.has_stroke = 2;
-            parse_url(a.stroke_grad, value);
-        } else {
-            a.has_stroke = 1;
-            a.stroke_color = parse_color(value);
-        }
-    } else if (std::strcmp(name, "stroke-width") == 0) {
-        a.stroke_width = parse_coord(p, value, 0.0f, p.actual_length());
-    } else if (std::strcmp(name, "stroke-dasharray") == 0) {
-        a.dash_count = parse_dash_array(p, value, a.dashes);
-    } else if (std::strcmp(name, "stroke-dashoffset") == 0) {
-        a.dash_offset = parse_coord(p, value, 0.0f, p.actual_length());
-    } else if (std::strcmp(name, "stroke-opacity") == 0) {
-        a.stroke_opacity = parse_opacity(value);
-    } else if (std::strcmp(name, "stroke-linecap") == 0) {
-        a.cap = std::strcmp(value, "round") == 0 ? 1 : std::strcmp(value, "square") == 0 ? 2 : 0;
-    } else if (std::strcmp(name, "stroke-linejoin") == 0) {
-        a.join = std::strcmp(value, "round") == 0 ? 1 : std::strcmp(value, "bevel") == 0 ? 2 : 0;
-    } else if (std::strcmp(name, "stroke-miterlimit") == 0) {
-        float v = (float)parse_atof(value);
-        a.miter = v < 0.0f ? 0.0f : v;
-    } else if (std::strcmp(name, "fill-rule") == 0) {
-        a.fill_rule = std::strcmp(value, "evenodd") == 0 ? 1 : 0;
-    } else if (std::strcmp(name, "font-size") == 0) {
-        a.font_size = parse_coord(p, value, 0.0f, p.actual_length());
-    } else if (std::strcmp(name, "transform") == 0) {
-        float xf[6];
-        parse_transform(xf, value);
-        xf_premultiply(a.xform, xf);
-    } else if (std::strcmp(name, "stop-color") == 0) {
-        a.stop_color = parse_color(value);
-    } else if (std::strcmp(name, "stop-opacity") == 0) {
-        a.stop_opacity = parse_opacity(value);
-    } else if (std::strcmp(name, "offset") == 0) {
-        a.stop_offset = parse_coord(p, value, 0.0f, 1.0f);
-    } else if (std::strcmp(name, "id") == 0) {
-        std::strncpy(a.id, value, 63);
-        a.id[63] = '\0';
+// "none", "url(#id)" (a gradient, kind 2) or a colour (kind 1)
+void paint_attr(const char *v, char &kind, uint32_t &color, char *grad) {
+    if (std::strcmp(v, "none") == 0) {
+        kind = 0;
+    } else if (std::strncmp(v, "url(", 4) == 0) {
+        kind = 2;
+        url_target(grad, v);
     } else {
-        return false;
+        kind = 1;
+        color = parse_color(v);
     }
+}
+
+using AttrFn = void (*)(Parser &, Attr &, const char *);
+struct AttrRule {
+    const char *name;
+    AttrFn apply;
+};
+
+const AttrRule kAttrRules[] = {  // sorted by name (strcmp)
+    {"display", [](Parser &, Attr &a, const char *v) { if (std::strcmp(v, "none") == 0) a.visible = 0; }},
+    {"fill", [](Parser &, Attr &a, const char *v) { paint_attr(v, a.has_fill, a.fill_color, a.fill_grad); }},
+    {"fill-opacity", [](Parser &, Attr &a, const char *v) { a.fill_opacity = parse_opacity(v); }},
+    {"fill-rule", [](Parser &, Attr &a, const char *v) { a.fill_rule = std::strcmp(v, "evenodd") == 0; }},
+    {"font-size", [](Parser &p, Attr &a, const char *v) { a.font_size = parse_coord(p, v, 0.0f, p.actual_length()); }},
+    {"id", [](Parser &, Attr &a, const char *v) {
+         std::strncpy(a.id, v, 63);
+         a.id[63] = '\0';
+     }},
+    {"offset", [](Parser &p, Attr &a, const char *v) { a.stop_offset = parse_coord(p, v, 0.0f, 1.0f); }},
+    {"opacity", [](Parser &, Attr &a, const char *v) { a.opacity = parse_opacity(v); }},
+    {"stop-color", [](Parser &, Attr &a, const char *v) { a.stop_color = parse_color(v); }},
+    {"stop-opacity", [](Parser &, Attr &a, const char *v) { a.stop_opacity = parse_opacity(v); }},
+    {"stroke", [](Parser &, Attr &a, const char *v) { paint_attr(v, a.has_stroke, a.stroke_color, a.stroke_grad); }},
+    {"stroke-dasharray", [](Parser &p, Attr &a, const char *v) { a.dash_count = dash_pattern(p, v, a.dashes); }},
+    {"stroke-dashoffset",
+     [](Parser &p, Attr &a, const char *v) { a.dash_offset = parse_coord(p, v, 0.0f, p.actual_length()); }},
+    {"stroke-linecap", [](Parser &, Attr &a, const char *v) {
+         a.cap = std::strcmp(v, "round") == 0 ? 1 : std::strcmp(v, "square") == 0 ? 2 : 0;
+     }},
+    {"stroke-linejoin", [](Parser &, Attr &a, const char *v) {
+         a.join = std::strcmp(v, "round") == 0 ? 1 : std::strcmp(v, "bevel") == 0 ? 2 : 0;
+     }},
+    {"stroke-miterlimit", [](Parser &, Attr &a, const char *v) {
+         const float m = (float)parse_atof(v);
+         a.miter = m < 0.0f ? 0.0f : m;
+     }},
+    {"stroke-opacity", [](Parser &, Attr &a, const char *v) { a.stroke_opacity = parse_opacity(v); }},
+    {"stroke-width",
+     [](Parser &p, Attr &a, const char *v) { a.stroke_width = parse_coord(p, v, 0.0f, p.actual_length()); }},
+    {"style", [](Parser &p, Attr &, const char *v) { apply_style(p, v); }},
+    {"transform", [](Parser &, Attr &a, const char *v) {
+         float xf[6];
+         parse_transform(xf, v);
+         xf_premultiply(a.xform, xf);
+     }},
+};
+
+// Applies a known attribute to the current state; false for a name no rule has.
+bool parse_attr(Parser &p, const char *name, const char *value) {
+    const AttrRule *end = kAttrRules + sizeof kAttrRules / sizeof kAttrRules[0];
+    const AttrRule *r = std::lower_bound(kAttrRules, end, name,
+                                         [](const AttrRule &a, const char *n) { return std::strcmp(a.name, n) < 0; });
+    if (r == end || std::strcmp(r->name, name) != 0) return false;
+    r->apply(p, p.cur(), value);
     return true;
 }
 
-bool parse_name_value(Parser &p, const char *start, const char *end) {
-    char name[512], value[512];
-    const char *str = start;
-    while (str < end && *str != ':') ++str;
-    const char *val = str;
-    while (str > start && (*str == ':' || is_space(*str))) --str;
-    ++str;
-    int n = (int)(str - start);
-    if (n > 511) n = 511;
-    if (n) std::memcpy(name, start, n);
-    name[n] = 0;
-    while (val < end && (*val == ':' || is_space(*val))) ++val;
-    n = (int)(end - val);
-    if (n > 511) n = 511;
-    if (n) std::memcpy(value, val, n);
-    value[n] = 0;
-    return parse_attr(p, name, value);
-}
-
-void parse_style(Parser &p, const char *str) {
-    while (*str) {
-        while (*str && is_space(*str)) ++str;
-        const char *start = str;
-        while (*str && *str != ';') ++str;
-        const char *end = str;
-        while (end > start && (*end == ';' || is_space(*end))) --end;
-        ++end;
-        parse_name_value(p, start, end);
-        if (*str) ++str;
+// A style attribute: declarations split at ';'; in each, the name is what precedes the first
+// ':' and the value what follows it, each trimmed of white space (and of the ':' and ';'
+// separators next to it), at most 511 characters each.  Empty declarations are skipped.  A
+// declaration without ':' is its own name with an empty value, unless a ';' follows it at once:
+// nanosvg then reads the ';' into the name, which names no attribute.
+void apply_style(Parser &p, const char *text) {
+    const char *q = text;
+    while (*q) {
+        while (*q && is_space(*q)) q++;
+        const char *b = q;
+        while (*q && *q != ';') q++;
+        const char *e = q;
+        if (*q) q++;
+        while (e > b && (is_space(e[-1]) || e[-1] == ';')) e--;
+        if (e == b) continue;
+        const char *colon = b;
+        while (colon < e && *colon != ':') colon++;
+        if (colon == e && *e == ';') continue;
+        const char *ne = colon;
+        while (ne > b && (is_space(ne[-1]) || ne[-1] == ':')) ne--;
+        const char *vb = colon;
+        while (vb < e && (is_space(*vb) || *vb == ':')) vb++;
+        char name[512], value[512];
+        const size_t nn = std::min<size_t>(size_t(ne - b), 511), nv = std::min<size_t>(size_t(e - vb), 511);
+        std::memcpy(name, b, nn);
+        name[nn] = '\0';
+        std::memcpy(value, vb, nv);
+        value[nv] = '\0';
+        parse_attr(p, name, value);
     }
 }
 
 void parse_attribs(Parser &p, const char **attr) {
-    for (int i = 0; attr[i]; i += 2) {
-        if (std::strcmp(attr[i], "style") == 0) parse_style(p, attr[i + 1]);
-        else parse_attr(p, attr[i], attr[i + 1]);
-    }
+    for (int i = 0; attr[i]; i += 2) parse_attr(p, attr[i], attr[i + 1]);
 }
 
 // --- path data -----------------------------------------------------------------------------------
@@ -1239,39 +1272,58 @@ void parse_poly(Parser &p, const char **attr, bool close) {
     p.add_shape();
 }
 
+// The <svg> element: presentation attributes, then its size, view box and alignment.
+// Four numbers separated by white space, commas or '%'.  False when the text ends before the
+// fourth: nanosvg then stops reading the element's attributes.
+bool svg_view_box(Parser &p, const char *s) {
+    float *dst[4] = {&p.view_minx, &p.view_miny, &p.view_width, &p.view_height};
+    char buf[64];
+    for (int k = 0; k < 4; k++) {
+        if (k) {
+            while (*s && (is_space(*s) || *s == '%' || *s == ',')) s++;
+            if (!*s) return false;
+        }
+        s = parse_number(s, buf, 64);
+        *dst[k] = (float)parse_atof(buf);
+    }
+    return true;
+}
+
+void svg_align(Parser &p, const char *v) {
+    // "none", or an x and a y alignment keyword and "meet" / "slice" anywhere in the value
+    if (std::strstr(v, "none")) {
+        p.align_type = kAlignNone;
+        return;
+    }
+    static const struct {
+        const char *word;
+        int *(*field)(Parser &);
+        int value;
+    } kWords[] = {{"xMin", [](Parser &q) { return &q.align_x; }, kAlignMin},
+                  {"xMid", [](Parser &q) { return &q.align_x; }, kAlignMid},
+                  {"xMax", [](Parser &q) { return &q.align_x; }, kAlignMax},
+                  {"yMin", [](Parser &q) { return &q.align_y; }, kAlignMin},
+                  {"yMid", [](Parser &q) { return &q.align_y; }, kAlignMid},
+                  {"yMax", [](Parser &q) { return &q.align_y; }, kAlignMax}};
+    bool x_done = false, y_done = false;
+    for (const auto &w : kWords) {
+        bool &done = w.word[0] == 'x' ? x_done : y_done;
+        if (!done && std::strstr(v, w.word)) {
+            *w.field(p) = w.value;
+            done = true;
+        }
+    }
+    p.align_type = std::strstr(v, "slice") ? kAlignSlice : kAlignMeet;
+}
+
 void parse_svg(Parser &p, const char **attr) {
     for (int i = 0; attr[i]; i += 2) {
-        if (parse_attr(p, attr[i], attr[i + 1])) continue;
-        if (std::strcmp(attr[i], "width") == 0) {
-            p.width = parse_coord(p, attr[i + 1], 0.0f, 0.0f);
-        } else if (std::strcmp(attr[i], "height") == 0) {
-            p.height = parse_coord(p, attr[i + 1], 0.0f, 0.0f);
-        } else if (std::strcmp(attr[i], "viewBox") == 0) {
-            const char *s = attr[i + 1];
-            char buf[64];
-            float *dst[4] = {&p.view_minx, &p.view_miny, &p.view_width, &p.view_height};
-            for (int k = 0; k < 4; k++) {
-                if (k) {
-                    while (*s && (is_space(*s) || *s == '%' || *s == ',')) s++;
-                    if (!*s) return;
-                }
-                s = parse_number(s, buf, 64);
-                *dst[k] = (float)parse_atof(buf);
-            }
-        } else if (std::strcmp(attr[i], "preserveAspectRatio") == 0) {
-            const char *v = attr[i + 1];
-            if (std::strstr(v, "none")) {
-                p.align_type = kAlignNone;
-            } else {
-                if (std::strstr(v, "xMin")) p.align_x = kAlignMin;
-                else if (std::strstr(v, "xMid")) p.align_x = kAlignMid;
-                else if (std::strstr(v, "xMax")) p.align_x = kAlignMax;
-                if (std::strstr(v, "yMin")) p.align_y = kAlignMin;
-                else if (std::strstr(v, "yMid")) p.align_y = kAlignMid;
-                else if (std::strstr(v, "yMax")) p.align_y = kAlignMax;
-                p.align_type = std::strstr(v, "slice") ? kAlignSlice : kAlignMeet;
-            }
-        }
+        const char *n = attr[i], *v = attr[i + 1];
+        if (parse_attr(p, n, v)) continue;
+        if (std::strcmp(n, "width") == 0) p.width = parse_coord(p, v, 0.0f, 0.0f);
+        else if (std::strcmp(n, "height") == 0) p.height = parse_coord(p, v, 0.0f, 0.0f);
+        else if (std::strcmp(n, "viewBox") == 0 && !svg_view_box(p, v)) return;
+        else if (std::strcmp(n, "preserveAspectRatio") == 0) svg_align(p, v);
     }
 }
 
@@ -1329,122 +1381,129 @@ void parse_stop(Parser &p, const char **attr) {
     stops.insert(stops.begin() + idx, GradStop{a.stop_color | (uint32_t)(a.stop_opacity * 255) << 24, a.stop_offset});
 }
 
-void start_element(Parser &p, const char *el, const char **attr) {
-    if (p.defs_flag) {
-        if (std::strcmp(el, "linearGradient") == 0) parse_gradient(p, attr, kLinear);
-        else if (std::strcmp(el, "radialGradient") == 0) parse_gradient(p, attr, kRadial);
-        else if (std::strcmp(el, "stop") == 0) parse_stop(p, attr);
-        return;
-    }
-    if (std::strcmp(el, "g") == 0) {
-        p.push();
-        parse_attribs(p, attr);
-    } else if (std::strcmp(el, "path") == 0) {
-        if (p.path_flag) return;
-        p.push();
-        parse_path(p, attr);
-        p.pop();
-    } else if (std::strcmp(el, "rect") == 0) {
-        p.push();
-        parse_rect(p, attr);
-        p.pop();
-    } else if (std::strcmp(el, "circle") == 0) {
-        p.push();
-        parse_circle(p, attr);
-        p.pop();
-    } else if (std::strcmp(el, "ellipse") == 0) {
-        p.push();
-        parse_ellipse(p, attr);
-        p.pop();
-    } else if (std::strcmp(el, "line") == 0) {
-        p.push();
-        parse_line(p, attr);
-        p.pop();
-    } else if (std::strcmp(el, "polyline") == 0) {
-        p.push();
-        parse_poly(p, attr, false);
-        p.pop();
-    } else if (std::strcmp(el, "polygon") == 0) {
-        p.push();
-        parse_poly(p, attr, true);
-        p.pop();
-    } else if (std::strcmp(el, "linearGradient") == 0) {
-        parse_gradient(p, attr, kLinear);
-    } else if (std::strcmp(el, "radialGradient") == 0) {
-        parse_gradient(p, attr, kRadial);
-    } else if (std::strcmp(el, "stop") == 0) {
-        parse_stop(p, attr);
-    } else if (std::strcmp(el, "defs") == 0) {
-        p.defs_flag = true;
-    } else if (std::strcmp(el, "svg") == 0) {
-        parse_svg(p, attr);
-    }
+// --- elements ----------------------------------------------------------------------------------
+// What each element does when it opens and closes.  Inside <defs> only gradients and their stops
+// open.  A shape element reads its attributes into a state of its own (pushed, then popped);
+// <g> pushes a state that its closing tag pops.
+void parse_shape(Parser &p, const char **attr, void (*read)(Parser &, const char **)) {
+    p.push();
+    read(p, attr);
+    p.pop();
 }
 
-void end_element(Parser &p, const char *el) {
-    if (std::strcmp(el, "g") == 0) p.pop();
-    else if (std::strcmp(el, "path") == 0) p.path_flag = false;
-    else if (std::strcmp(el, "defs") == 0) p.defs_flag = false;
+struct ElementRule {
+    const char *name;
+    bool in_defs;                                   // also read inside <defs>
+    void (*open)(Parser &, const char **);
+    void (*close)(Parser &);                        // null: nothing to do
+};
+
+const ElementRule kElements[] = {  // sorted by name (strcmp)
+    {"circle", false, [](Parser &p, const char **a) { parse_shape(p, a, parse_circle); }, nullptr},
+    {"defs", false, [](Parser &p, const char **) { p.defs_flag = true; }, [](Parser &p) { p.defs_flag = false; }},
+    {"ellipse", false, [](Parser &p, const char **a) { parse_shape(p, a, parse_ellipse); }, nullptr},
+    {"g", false, [](Parser &p, const char **a) {
+         p.push();
+         parse_attribs(p, a);
+     }, [](Parser &p) { p.pop(); }},
+    {"line", false, [](Parser &p, const char **a) { parse_shape(p, a, parse_line); }, nullptr},
+    {"linearGradient", true, [](Parser &p, const char **a) { parse_gradient(p, a, kLinear); }, nullptr},
+    {"path", false, [](Parser &p, const char **a) { parse_shape(p, a, parse_path); }, nullptr},
+    {"polygon", false, [](Parser &p, const char **a) {
+         parse_shape(p, a, [](Parser &q, const char **b) { parse_poly(q, b, true); });
+     }, nullptr},
+    {"polyline", false, [](Parser &p, const char **a) {
+         parse_shape(p, a, [](Parser &q, const char **b) { parse_poly(q, b, false); });
+     }, nullptr},
+    {"radialGradient", true, [](Parser &p, const char **a) { parse_gradient(p, a, kRadial); }, nullptr},
+    {"rect", false, [](Parser &p, const char **a) { parse_shape(p, a, parse_rect); }, nullptr},
+    {"stop", true, [](Parser &p, const char **a) { parse_stop(p, a); }, nullptr},
+    {"svg", false, [](Parser &p, const char **a) { parse_svg(p, a); }, nullptr},
+};
+
+const ElementRule *element_rule(const char *name) {
+    const ElementRule *end = kElements + sizeof kElements / sizeof kElements[0];
+    const ElementRule *r = std::lower_bound(kElements, end, name,
+                                            [](const ElementRule &e, const char *n) { return std::strcmp(e.name, n) < 0; });
+    return r != end && std::strcmp(r->name, name) == 0 ? r : nullptr;
 }
 
-// nsvg__parseElement on a mutable tag body
-void parse_element(Parser &p, char *s) {
-    const char *attr[kMaxXmlAttribs];
-    int nattr = 0;
-    bool start = false, end = false;
-    while (*s && is_space(*s)) s++;
-    if (*s == '/') {
-        s++;
-        end = true;
+// --- XML -----------------------------------------------------------------------------------------
+// The document is cut into tags the way the reference's parser (nanosvg) cuts it, so that every
+// document gives the reference's scene, quirks included: text outside tags is skipped; a tag runs
+// from a '<' to the next '>' (quotes do not hide a '>'), and one left open at the end is dropped;
+// "<?...>", "<!...>" and empty tags are skipped; after an optional '/' (a closing tag) the name runs
+// to the first white space; in an opening tag, attributes follow until a '/' (which also closes
+// it): a name ends at white space or '=', and its value is the next quoted string (single or
+// double quotes) - so an unquoted value takes the next attribute's.  At most 127 attributes.
+constexpr int kMaxTagAttrs = 127;
+
+struct Tag {
+    std::string name;
+    bool opens = false, closes = false;
+    std::vector<std::string> kv;     // name, value, name, value, ...
+    std::vector<const char *> argv;  // the same as C strings, then two null pointers
+};
+
+// Reads the tag whose text (between '<' and '>') is [b, e); false for one that is skipped.
+bool read_tag(const char *b, const char *e, Tag &t) {
+    t.name.clear();
+    t.kv.clear();
+    t.opens = t.closes = false;
+    const char *q = b;
+    while (q < e && is_space(*q)) q++;
+    if (q < e && *q == '/') {
+        t.closes = true;
+        q++;
     } else {
-        start = true;
+        t.opens = true;
     }
-    if (!*s || *s == '?' || *s == '!') return;
-    char *name = s;
-    while (*s && !is_space(*s)) s++;
-    if (*s) *s++ = '\0';
-    while (!end && *s && nattr < kMaxXmlAttribs - 3) {
-        while (*s && is_space(*s)) s++;
-        if (!*s) break;
-        if (*s == '/') {
-            end = true;
+    if (q == e || *q == '?' || *q == '!') return false;
+    const char *nb = q;
+    while (q < e && !is_space(*q)) q++;
+    t.name.assign(nb, q);
+    if (q < e) q++;  // the white space after the name
+    while (!t.closes && q < e && (int)t.kv.size() < 2 * kMaxTagAttrs) {
+        while (q < e && is_space(*q)) q++;
+        if (q == e) break;
+        if (*q == '/') {
+            t.closes = true;
             break;
         }
-        char *an = s;
-        while (*s && !is_space(*s) && *s != '=') s++;
-        if (*s) *s++ = '\0';
-        while (*s && *s != '\"' && *s != '\'') s++;
-        if (!*s) break;
-        const char quote = *s;
-        s++;
-        char *av = s;
-        while (*s && *s != quote) s++;
-        if (*s) *s++ = '\0';
-        attr[nattr++] = an;
-        attr[nattr++] = av;
+        const char *ab = q;
+        while (q < e && !is_space(*q) && *q != '=') q++;
+        const char *ae = q;
+        if (q < e) q++;  // the '=' or white space after the name
+        while (q < e && *q != '"' && *q != '\'') q++;
+        if (q == e) break;
+        const char quote = *q++;
+        const char *vb = q;
+        while (q < e && *q != quote) q++;
+        t.kv.emplace_back(ab, ae);
+        t.kv.emplace_back(vb, q);
+        if (q < e) q++;  // the closing quote
     }
-    attr[nattr++] = nullptr;
-    attr[nattr++] = nullptr;
-    if (start) start_element(p, name, attr);
-    if (end) end_element(p, name);
+    t.argv.clear();
+    for (const std::string &x : t.kv) t.argv.push_back(x.c_str());
+    t.argv.push_back(nullptr);
+    t.argv.push_back(nullptr);
+    return true;
 }
 
-void parse_xml(Parser &p, char *input) {
-    char *s = input, *mark = s;
-    bool tag = false;
-    while (*s) {
-        if (*s == '<' && !tag) {
-            *s++ = '\0';
-            mark = s;
-            tag = true;
-        } else if (*s == '>' && tag) {
-            *s++ = '\0';
-            parse_element(p, mark);
-            mark = s;
-            tag = false;
-        } else {
-            s++;
-        }
+void parse_document(Parser &p, const char *text, size_t n) {
+    Tag t;
+    const char *q = text, *end = text + n;
+    while (q < end) {
+        const char *lt = static_cast<const char *>(std::memchr(q, '<', size_t(end - q)));
+        if (!lt) break;
+        const char *gt = static_cast<const char *>(std::memchr(lt + 1, '>', size_t(end - lt - 1)));
+        if (!gt) break;
+        q = gt + 1;
+        if (!read_tag(lt + 1, gt, t)) continue;
+        const ElementRule *r = element_rule(t.name.c_str());
+        if (!r) continue;
+        if (t.opens && (r->in_defs || !p.defs_flag)) r->open(p, t.argv.data());
+        if (t.closes && r->close) r->close(p);  // closing tags act inside <defs> too
     }
 }
 
@@ -1617,7 +1676,6 @@ extern "C" {
 int pf_svg_parse(const char *text, size_t length, float dpi, pf_svg **out) {
     if (!text || !out) return PF_ERR_INVALID_ARGUMENT;
     *out = nullptr;
-    std::string copy(text, length);
     Parser *p = new (std::nothrow) Parser();
     pf_svg *svg = new (std::nothrow) pf_svg();
     if (!p || !svg) {
@@ -1626,7 +1684,7 @@ int pf_svg_parse(const char *text, size_t length, float dpi, pf_svg **out) {
         return PF_ERR_OUT_OF_MEMORY;
     }
     p->dpi = dpi;
-    parse_xml(*p, &copy[0]);
+    parse_document(*p, text, strnlen(text, length));  // the text ends at its first NUL, as C text does
     scale_to_viewbox(*p);
     SceneOut &o = svg->out;
     o.width = p->width;
