@@ -8,6 +8,9 @@
 //     renderer = std::make_shared<RendererCuda>(device, queue);
 //     scene_builder = std::make_shared<SceneBuilderCuda>();
 //
+// On a host with no graphics API the device and queue are the headless DeviceCuda::create()
+// and QueueCuda of device_cuda.h.
+//
 // Canvas::draw (pathfinder/core/canvas.cpp:557-567) then calls
 // scene_builder->build(scene, renderer) and renderer->draw(scene_builder, clear) as it does
 // for the other modes.

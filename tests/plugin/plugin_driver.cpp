@@ -8,10 +8,49 @@
 
 #include "core/path2d.h"
 #include "core/scene.h"
+#include "device_cuda.h"
 #include "pf_oracle.h"
 #include "renderer_cuda.h"
 
 using namespace Pathfinder;
+
+// The headless device: transfers through staging buffers round-trip, the Renderer base class
+// and the palette's metadata upload run on it, and RendererCuda::draw without a CUDA device
+// logs an error and leaves the destination as it was (the reference logs and continues).
+static int check_headless_device(Scene &scene) {
+    auto device = DeviceCuda::create(0);
+    auto queue = std::make_shared<QueueCuda>();
+    auto tex = device->create_texture({{7, 5}, TextureFormat::Rgba8Unorm}, "t");
+    std::vector<uint8_t> in(7 * 5 * 4), out(7 * 5 * 4, 0), part(3 * 2 * 4, 0);
+    for (size_t i = 0; i < in.size(); i++) in[i] = uint8_t(i * 7 + 3);
+    auto enc = device->create_command_encoder("transfers");
+    enc->write_texture(tex, {}, in.data());
+    enc->read_texture(tex, {}, out.data());
+    enc->read_texture(tex, RectI({2, 1}, {5, 3}), part.data());
+    auto buf = device->create_buffer({BufferType::Storage, 64, MemoryProperty::DeviceLocal}, "b");
+    std::vector<uint8_t> bin(40), bout(40, 0);
+    for (size_t i = 0; i < bin.size(); i++) bin[i] = uint8_t(255 - i);
+    enc->write_buffer(buf, 16, 40, bin.data());
+    enc->read_buffer(buf, 16, 40, bout.data());
+    queue->submit(enc, device->create_fence("f"));
+    if (out != in || bout != bin) return std::printf("FAIL transfers\n"), 1;
+    for (int y = 0; y < 2; y++)
+        if (std::memcmp(&part[y * 12], &in[((1 + y) * 7 + 2) * 4], 12)) return std::printf("FAIL region\n"), 1;
+    auto renderer = std::make_shared<RendererCuda>(device, queue);  // Renderer::Renderer on DeviceCuda
+    auto dest = device->create_texture({{300, 200}, TextureFormat::Rgba8Unorm}, "dest");
+    renderer->set_dest_texture(dest);
+    auto meta = scene.palette.build_paint_info(renderer.get());  // the metadata upload
+    if (meta.size() != 8) return std::printf("FAIL palette %zu\n", meta.size()), 1;
+    auto builder = std::make_shared<SceneBuilderCuda>();
+    builder->build(&scene, renderer.get());
+    if (builder->view().width != 300.f || builder->view().height != 200.f) return std::printf("FAIL dest size\n"), 1;
+    auto &px = static_cast<TextureCuda *>(dest.get())->pixels();
+    std::fill(px.begin(), px.end(), uint8_t(9));
+    renderer->draw(builder, true);  // no CUDA device in this process: logged, destination untouched
+    for (uint8_t v : px)
+        if (v != 9) return std::printf("FAIL draw without a device touched the destination\n"), 1;
+    return 0;
+}
 
 int main() {
     // a view box with an origin: tiles and lines are clipped to it (Scene::set_view_box rounds
@@ -89,6 +128,8 @@ int main() {
     uint64_t clipped = 0;
     for (uint64_t t = 0; t < a.n_tiles; t++) clipped += a.tile_mask[t] != 0;
     same = same && clipped > 0;
-    std::printf("%s %llu\n", same ? "OK" : "FAIL", (unsigned long long)a.n_fills);
-    return same ? 0 : 1;
+    if (!same) return std::printf("FAIL %llu\n", (unsigned long long)a.n_fills), 1;
+    if (check_headless_device(scene)) return 1;
+    std::printf("OK %llu\n", (unsigned long long)a.n_fills);
+    return 0;
 }

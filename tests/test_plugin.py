@@ -1,9 +1,13 @@
 """The reference-side drop-in (pathfinder-cpp_gb300/plugin) against the reference's own types.
 
-Compiles SceneBuilderCuda / RendererCuda with the reference's headers, links them with the
-reference's compiled Scene, Path2d and paint code (oracle/_ref), builds a scene through the
-reference API and checks the packed scene against the reference tiler.  Needs the reference
-tree; skipped where it is absent.
+Compiles SceneBuilderCuda / RendererCuda and the headless DeviceCuda / QueueCuda with the
+reference's headers, links them with the reference's compiled Scene, Path2d, paint and Renderer
+code (oracle/_ref), builds a scene through the reference API (with a view box that has an
+origin) and checks the packed scene against the reference tiler; then runs the reference's
+Renderer base class and Palette::build_paint_info on the headless device, checks its transfers,
+and that RendererCuda::draw without a CUDA device logs and leaves the destination alone.  Needs
+the reference tree (so it does not run where the GPU is: the reference's headers are not there);
+skipped where it is absent.
 """
 import glob
 import os
@@ -27,7 +31,8 @@ def test_plugin_packs_reference_scene(tmp_path, oracle_mod, pf):
            f"-I{ref}/pathfinder", f"-I{ref}/third_party", f"-I{ref}/third_party/umHalf",
            f"-I{ROOT}/include", f"-I{ROOT}/oracle", f"-I{ROOT}/pathfinder-cpp_gb300/plugin", "-w",
            os.path.join(ROOT, "tests", "plugin", "plugin_driver.cpp"),
-           os.path.join(ROOT, "pathfinder-cpp_gb300", "plugin", "renderer_cuda.cpp"), *objs,
+           os.path.join(ROOT, "pathfinder-cpp_gb300", "plugin", "renderer_cuda.cpp"),
+           os.path.join(ROOT, "pathfinder-cpp_gb300", "plugin", "device_cuda.cpp"), *objs,
            os.path.join(ROOT, "oracle", "_ref", "libpfref.so"), os.path.join(ROOT, "oracle", "_build", "libpforacle.so"),
            pf.LIB_PATH, "-lpthread", "-o", exe]
     subprocess.run(cmd, check=True, capture_output=True)
