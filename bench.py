@@ -110,6 +110,9 @@ def parse_args(argv=None):
                          "document log-uniform 16-1024) parsed on the host by pf_svg_parse; the line adds an "
                          "svg_stage whose end-to-end step parses the documents' text too")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tuning", default=None,
+                    help="launch parameters to set over the built-in or tuned ones, as JSON (pf_tuning fields, "
+                         "e.g. '{\"bin_sorted\": 1}')")
     ap.add_argument("--profile-frames", action="store_true",
                     help="only the exact, learned and default frames (warm-up + steps each), a short summary "
                          "line instead of the benchmark line: the command the committed launch lists profile")
@@ -511,6 +514,23 @@ def main():
     learned = os.path.exists(pfcuda.DEFAULT_WEIGHTS)
     if learned:
         r.sizer_load(pfcuda.DEFAULT_WEIGHTS)
+    # the launch parameters the autotuner (tune.py) found for the batched configuration on this
+    # GPU; the built-in ones are timed beside them (an A/B in this run)
+    tuning = None
+    if args.config == 4 and os.path.exists(pfcuda.DEFAULT_RENDER_CONFIG):
+        builtin = r.tuning()
+        frame0 = r.render_auto if learned else r.render
+        for _ in range(max(args.warmup, 6)):
+            frame0()
+        ms_builtin, _ = timed(frame0, args.steps)
+        cfg = r.load_render_config()
+        tuning = {"source": "weights/render_config.json (tune.py: pf_autotune on this configuration)",
+                  "params": r.tuning(), "builtin_params": builtin, "frame_ms_builtin": ms_builtin,
+                  "tuned_on": cfg.get("gpu"), "tune_frame_ms": cfg.get("frame_ms"),
+                  "tune_start_frame_ms": cfg.get("start_frame_ms")}
+    if args.tuning:
+        r.set_tuning({**r.tuning(), **json.loads(args.tuning)})
+        tuning = dict(tuning or {}, params=r.tuning(), override=json.loads(args.tuning))
 
     # 1. the exact two-pass frame, inputs resident
     for _ in range(args.warmup):
@@ -546,7 +566,7 @@ def main():
         if rank == 0:
             print(json.dumps({"profile_frames": True, "exact_ms": ms_exact, "learned_ms": ms_learned,
                               "frame_ms": ms_frame, "exact_stats": stats_e[-1], "frame_stats": st,
-                              "sizer": sizer}), flush=True)
+                              "sizer": sizer, "tuning": tuning}), flush=True)
         r.close()
         return
 
@@ -758,6 +778,7 @@ def main():
                         if learned else None),
             **({"plain": plain, "speedup_vs_plain": plain["ms_per_step"] / ms_frame} if plain else {}),
             "sizer": sizer,
+            "tuning": dict(tuning, frame_ms_tuned=ms_frame) if tuning else None,
             **({"stroke_stage": stroke_stage} if stroke_stage else {}),
             **({"svg_stage": svg_stage} if svg_stage else {}),
             "e2e": {"value": world * n_scenes / (ms_e2e * 1e-3), "unit": UNIT, "ms_per_step": ms_e2e,

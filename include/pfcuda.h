@@ -326,6 +326,35 @@ int pf_render_auto(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_
 int pf_auto_choice(void *ctx, int *last, int *choice, float *exact_ms, float *learned_ms);
 
 /*
+ * Launch parameters of the frame's kernels (the configuration the autotuner searches; no
+ * counterpart in the reference, whose dispatch sizes are fixed in its shaders).  Zero-initialise
+ * and pf_tuning_get for the defaults.  Output never depends on them.
+ */
+typedef struct pf_tuning {
+    uint32_t bin_ctas_per_sm[3]; /* binning CTAs resident per SM for the three CTA classes (paths
+                                    whose rect plus a row of column sums takes <= 1088, 4352,
+                                    16896 words); 0: as many as fit */
+    float long_line;             /* lines spanning more tiles than this are walked by a whole warp */
+    uint32_t bin_concurrent;     /* 1: the three binning classes run at once on side streams */
+    uint32_t seg_sorted;         /* 1: the flatten takes segments ordered by subdivision depth */
+    uint32_t bin_sorted;         /* 1: binning's count walk takes each window of 2048 lines in order
+                                    of the tiles they span (warps get lines of like length) */
+    uint32_t reserved[8];
+} pf_tuning;
+int pf_tuning_get(void *ctx, pf_tuning *out);
+int pf_tuning_set(void *ctx, const pf_tuning *tuning);
+/*
+ * Search the launch parameters on the uploaded scenes [first_scene, first_scene + n_scenes):
+ * coordinate descent from the current parameters, each trial the default frame
+ * (pf_render_auto's choice) run `frames` times and timed on the device (median), until no
+ * parameter improves the frame by more than 1%.  The best parameters are left set; *best_ms and
+ * *start_ms (the current parameters' time) may be NULL.  The caller persists them
+ * (pathfinder-cpp_gb300/tune.py writes a RenderConfig JSON file).
+ */
+int pf_autotune(void *ctx, uint32_t first_scene, uint32_t n_scenes, uint32_t frames, pf_tuning *best, float *best_ms,
+                float *start_ms);
+
+/*
  * Learned sizer: features (12 per path) -> 64 -> 64 -> (log1p leaf lines, log1p fills),
  * bf16 weights, fp32 accumulation, trained on the GPU with the library's own forward,
  * backward and Adam kernels.  It replaces the reference's buffer sizing by readback and

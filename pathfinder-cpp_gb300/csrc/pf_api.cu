@@ -78,7 +78,7 @@ struct Ctx {
 
     // inputs
     DevBuf points, pflags, cstart, pstart, fill_rule, color, scenes, scene_path_first, scene_contour_first,
-        scene_fb_first;
+        scene_fb_first, fb_scene;
     std::vector<SceneDev> h_scenes;
     std::vector<uint32_t> h_scene_fb_first;
     // clip paths: per uploaded path its scene-local clip path (PF_NO_CLIP) and whether it is one;
@@ -182,6 +182,11 @@ struct Ctx {
         int last = PF_FRAME_EXACT;     // the frame the last auto call ran
     } au;
     cudaEvent_t au_ev[2] = {};
+
+    // launch parameters (pf_tuning) and the side streams of concurrent binning classes
+    Tuning tune;
+    BinStreams bs{};
+    bool bs_ready = false;
 };
 
 thread_local std::string g_last_error;
@@ -809,6 +814,8 @@ int upload(Ctx *c, const pf_scene_view *scenes, uint32_t n) {
     for (CopyPlan *cp : {&pts, &fl, &csp, &psp, &fr, &col}) PF_CUDA(cp->run(c->stream));
     PF_CUDA(cudaMemcpyAsync(c->scene_fb_first.p, c->h_scene_fb_first.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
                             c->stream));
+    PF_CUDA(c->fb_scene.ensure(size_t(fb) * 4 + 16));
+    PF_CUDA(launch_fb_scene(c->scene_fb_first.as<uint32_t>(), n, c->fb_scene.as<uint32_t>(), c->stream));
     PF_CUDA(cudaMemcpyAsync(c->scene_row_first.p, c->h_scene_row_first.data(), (n + 1) * 4, cudaMemcpyHostToDevice,
                             c->stream));
     if (strokes) {
@@ -844,6 +851,7 @@ Batch make_batch(Ctx *c) {
     b.scene_path_first = c->scene_path_first.as<uint32_t>();
     b.scene_contour_first = c->scene_contour_first.as<uint32_t>();
     b.scene_fb_first = c->scene_fb_first.as<uint32_t>();
+    b.fb_scene = c->fb_scene.as<uint32_t>();
     b.scene_row_first = c->scene_row_first.as<uint32_t>();
     const bool clips = !c->h_path_clip.empty();
     b.path_clip_cat = clips ? c->path_clip.as<uint32_t>() : nullptr;
@@ -906,6 +914,9 @@ Batch make_batch(Ctx *c) {
     b.image = c->host_img_dev ? c->host_img_dev : c->image.as<uint8_t>();
     b.status = c->status.as<uint32_t>();
     b.counters = (c->flags & PF_CONFIG_FRAME_COUNTERS) ? 1u : 0u;
+    b.long_line = c->tune.long_line;
+    b.bin_sorted = c->tune.bin_sorted ? 1u : 0u;
+    if (!c->tune.seg_sorted) b.seg_order = nullptr;
     return b;
 }
 
@@ -984,7 +995,7 @@ int begin_frame(Ctx *c, uint32_t first, uint32_t count) {
     PF_CUDA(c->bin_list.ensure(size_t(N) * 20 + 16));
     PF_CUDA(c->path_fill.ensure(size_t(N) * 4 + 16));
     size_t stage_bytes = 0;
-    PF_CUDA(bin_stage_bytes(&stage_bytes));
+    PF_CUDA(bin_stage_bytes(c->tune, &stage_bytes));
     PF_CUDA(c->bin_stage.ensure(stage_bytes));
     PF_CUDA(c->path_cls.ensure(size_t(N) + 16));
     PF_CUDA(c->bin_ctl.ensure(1024));
@@ -1062,7 +1073,13 @@ int bin_and_composite(Ctx *c, Batch b, bool learned) {
         PF_CUDA(cudaMemsetAsync(b.bin_ctl, 0, 1024, st));
         PF_CUDA(cudaMemsetAsync(b.status + kStFill64, 0, 8, st));
         PF_CUDA(launch_bin_classify(b, learned, st));
-        PF_CUDA(launch_bin_paths(b, st));
+        if (c->tune.bin_concurrent && !c->bs_ready) {
+            for (auto &s : c->bs.side) PF_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+            PF_CUDA(cudaEventCreateWithFlags(&c->bs.fork, cudaEventDisableTiming));
+            for (auto &e : c->bs.join) PF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            c->bs_ready = true;
+        }
+        PF_CUDA(launch_bin_paths(b, c->tune, c->bs_ready ? &c->bs : nullptr, st));
         record(c, 3);
         record(c, 4);
         record(c, 5);
@@ -1142,7 +1159,7 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     Batch b = make_batch(c);
     PF_CUDA(launch_contour_segments(b, true, st));
     PF_CUDA(launch_rows(b, true, st));
-    PF_CUDA(launch_seg_order(b, c->n_segs, c->seg_ctl.as<uint32_t>(), st));
+    if (c->tune.seg_sorted) PF_CUDA(launch_seg_order(b, c->n_segs, c->seg_ctl.as<uint32_t>(), st));
     PF_CUDA(cudaMemsetAsync(b.seg_leaves + c->n_segs, 0, 4, st));
     PF_CUDA(launch_flatten(b, c->n_segs, false, st));
     if (int e = scan(c, b.seg_leaves, c->n_segs + 1, kStLeaves)) return e;
@@ -1195,7 +1212,7 @@ int render_learned_frame(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats 
     b.pool_idx = c->pool_idx.as<uint32_t>();
     PF_CUDA(launch_contour_segments(b, true, st));
     PF_CUDA(launch_rows(b, true, st));
-    PF_CUDA(launch_seg_order(b, c->n_segs, c->seg_ctl.as<uint32_t>(), st));
+    if (c->tune.seg_sorted) PF_CUDA(launch_seg_order(b, c->n_segs, c->seg_ctl.as<uint32_t>(), st));
     PF_CUDA(launch_flatten_budget(b, c->n_segs, st));
     record(c, 2);
     // the spill pool's lines listed by path, so each path's CTA finds them
@@ -1815,7 +1832,7 @@ int pf_ctx_destroy(void *ctx) {
                       &c->path_leaf_budget, &c->path_leaf_cursor, &c->path_fill_budget, &c->path_bounds,
                       &c->bin_list, &c->bin_ctl, &c->path_leaf_range,
                       &c->points, &c->pflags, &c->cstart, &c->pstart, &c->fill_rule, &c->color, &c->scenes,
-                      &c->scene_path_first, &c->scene_contour_first, &c->scene_fb_first, &c->contour_point_first,
+                      &c->scene_path_first, &c->scene_contour_first, &c->scene_fb_first, &c->fb_scene, &c->contour_point_first,
                       &c->contour_path, &c->paths, &c->path_tiles, &c->path_cols, &c->contour_segs,
                       &c->path_contours, &c->segs, &c->seg_leaves, &c->seg_order, &c->seg_ctl, &c->leaves, &c->pool_path, &c->pool_cnt,
                       &c->pool_idx, &c->tile_fills, &c->path_fill, &c->path_cls, &c->tile_state, &c->col_above,
@@ -1836,6 +1853,11 @@ int pf_ctx_destroy(void *ctx) {
         if (e) cudaEventDestroy(e);
     for (auto &e : c->au_ev)
         if (e) cudaEventDestroy(e);
+    if (c->bs_ready) {
+        for (auto &s : c->bs.side) cudaStreamDestroy(s);
+        cudaEventDestroy(c->bs.fork);
+        for (auto &e : c->bs.join) cudaEventDestroy(e);
+    }
     c->canon_state.release();
     c->canon_clip.release();
     if (c->h_status) cudaFreeHost(c->h_status);
@@ -2327,6 +2349,127 @@ int pf_render_auto(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_
     if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
     cudaSetDevice(c->device);
     return render_auto(c, first_scene, n_scenes, stats);
+}
+
+static void tuning_out(const Tuning &t, pf_tuning *o) {
+    std::memset(o, 0, sizeof *o);
+    for (int k = 0; k < 3; k++) o->bin_ctas_per_sm[k] = t.bin_ctas_per_sm[k];
+    o->long_line = t.long_line;
+    o->bin_concurrent = t.bin_concurrent;
+    o->seg_sorted = t.seg_sorted;
+    o->bin_sorted = t.bin_sorted;
+}
+
+int pf_tuning_get(void *ctx, pf_tuning *out) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !out) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    tuning_out(c->tune, out);
+    return PF_OK;
+}
+
+int pf_tuning_set(void *ctx, const pf_tuning *t) {
+    Ctx *c = as_ctx(ctx);
+    if (!c || !t) return fail(c, PF_ERR_INVALID_ARGUMENT, "null argument");
+    if (!(t->long_line >= 1.0f && t->long_line <= 4096.0f))
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "long_line must lie in [1, 4096]");
+    for (uint32_t v : t->bin_ctas_per_sm)
+        if (v > 64) return fail(c, PF_ERR_INVALID_ARGUMENT, "bin_ctas_per_sm must lie in [0, 64]");
+    if (t->bin_concurrent > 1 || t->seg_sorted > 1 || t->bin_sorted > 1)
+        return fail(c, PF_ERR_INVALID_ARGUMENT, "flags must be 0 or 1");
+    cudaSetDevice(c->device);
+    PF_CUDA(cudaStreamSynchronize(c->stream));
+    Tuning n;
+    for (int k = 0; k < 3; k++) n.bin_ctas_per_sm[k] = t->bin_ctas_per_sm[k];
+    n.long_line = t->long_line;
+    n.bin_concurrent = t->bin_concurrent != 0;
+    n.seg_sorted = t->seg_sorted != 0;
+    n.bin_sorted = t->bin_sorted != 0;
+    c->tune = n;
+    forget_learned(c);  // the recorded frame has the old parameters in its launches
+    c->au.exact_ms = c->au.learned_ms = -1.0f;
+    c->au.exact_runs = c->au.learned_runs = 0;
+    return PF_OK;
+}
+
+int pf_autotune(void *ctx, uint32_t first, uint32_t count, uint32_t frames, pf_tuning *best, float *best_ms,
+                float *start_ms) {
+    Ctx *c = as_ctx(ctx);
+    if (!c) return fail(nullptr, PF_ERR_INVALID_ARGUMENT, "ctx is null");
+    if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
+    if (frames == 0 || frames > 100) return fail(c, PF_ERR_INVALID_ARGUMENT, "frames must lie in [1, 100]");
+    cudaSetDevice(c->device);
+    int max_ctas[3] = {1, 1, 1};
+    PF_CUDA(bin_class_max_ctas(max_ctas));
+    // the default frame settles first (it times the exact and the learned frame), then each
+    // trial: set the parameters, warm up (buffers, the learned frame's graph), time `frames`
+    pf_frame_stats st;
+    for (int k = 0; k < 6; k++)
+        if (int e = render_auto(c, first, count, &st)) return e;
+    const bool learned = c->sz_ready && c->au.learned_ms >= 0.0f && c->au.learned_ms < c->au.exact_ms;
+    auto trial = [&](const pf_tuning &t, float *ms) -> int {
+        if (int e = pf_tuning_set(c, &t)) return e;
+        std::vector<float> v;
+        for (uint32_t k = 0; k < frames + 3; k++) {
+            float m = 0.0f;
+            const int e = timed_frame(c, &m, [&] {
+                return learned ? render_learned(c, first, count, &st) : render_exact(c, first, count, &st);
+            });
+            if (e) return e;
+            if (k >= 3) v.push_back(m);
+        }
+        std::sort(v.begin(), v.end());
+        *ms = v[v.size() / 2];
+        return PF_OK;
+    };
+    pf_tuning cur;
+    tuning_out(c->tune, &cur);
+    float cur_ms = 0.0f;
+    if (int e = trial(cur, &cur_ms)) return e;
+    if (start_ms) *start_ms = cur_ms;
+    // the candidates of each parameter
+    std::vector<std::pair<int, std::vector<float>>> space = {
+        {0, {0, 1, 2, 3, 4, 5, 6}},   // bin_ctas_per_sm[0]
+        {1, {0, 1, 2, 3, 4, 6, 8}},   // bin_ctas_per_sm[1]
+        {2, {0, 1, 2, 3}},            // bin_ctas_per_sm[2]
+        {3, {4, 6, 8, 12, 16, 32}},   // long_line
+        {4, {0, 1}},                  // bin_concurrent
+        {5, {0, 1}},                  // seg_sorted
+        {6, {0, 1}},                  // bin_sorted
+    };
+    auto get = [](const pf_tuning &t, int i) -> float {
+        return i < 3 ? (float)t.bin_ctas_per_sm[i] : i == 3 ? t.long_line : i == 4 ? (float)t.bin_concurrent
+               : i == 5 ? (float)t.seg_sorted : (float)t.bin_sorted;
+    };
+    auto put = [](pf_tuning &t, int i, float v) {
+        if (i < 3) t.bin_ctas_per_sm[i] = (uint32_t)v;
+        else if (i == 3) t.long_line = v;
+        else if (i == 4) t.bin_concurrent = (uint32_t)v;
+        else if (i == 5) t.seg_sorted = (uint32_t)v;
+        else t.bin_sorted = (uint32_t)v;
+    };
+    for (int pass = 0; pass < 3; pass++) {
+        bool improved = false;
+        for (auto &dim : space) {
+            for (float v : dim.second) {
+                if (dim.first < 3 && v > (float)max_ctas[dim.first]) continue;
+                if (v == get(cur, dim.first)) continue;
+                pf_tuning t = cur;
+                put(t, dim.first, v);
+                float ms = 0.0f;
+                if (int e = trial(t, &ms)) return e;
+                if (ms < cur_ms * 0.99f) {
+                    cur = t;
+                    cur_ms = ms;
+                    improved = true;
+                }
+            }
+        }
+        if (!improved) break;
+    }
+    if (int e = pf_tuning_set(c, &cur)) return e;
+    if (best) *best = cur;
+    if (best_ms) *best_ms = cur_ms;
+    return PF_OK;
 }
 
 int pf_auto_choice(void *ctx, int *last, int *choice, float *exact_ms, float *learned_ms) {

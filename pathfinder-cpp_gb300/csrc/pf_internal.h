@@ -95,6 +95,7 @@ struct Batch {
     const uint32_t *scene_path_first;    // [n_scenes_all + 1]
     const uint32_t *scene_contour_first; // [n_scenes_all + 1]
     const uint32_t *scene_fb_first;      // [n_scenes_all + 1]
+    const uint32_t *fb_scene;            // [framebuffer tiles of all scenes] the scene of each
     const uint32_t *scene_row_first;     // [n_scenes_all + 1]
     uint32_t n_scenes_all;               // scenes uploaded
     // the scenes rendered by this frame: a contiguous range of the uploaded ones.
@@ -168,6 +169,19 @@ struct Batch {
     uint8_t *image;                      // batch image buffer
     uint32_t *status;                    // [kStCount] error bits and totals
     uint32_t counters;                   // nonzero: the composite adds its work counters to status
+    // launch parameters (pf_tuning): lines spanning more tiles than long_line are walked by a
+    // whole warp; bin_sorted: the count walk takes each window of lines in order of span
+    float long_line;
+    uint32_t bin_sorted;
+};
+
+// The launch parameters of a frame (pf_tuning), as the kernels and launchers read them.
+struct Tuning {
+    uint32_t bin_ctas_per_sm[3] = {0, 0, 0};  // 0: as many as fit
+    float long_line = 8.0f;
+    bool bin_concurrent = false;
+    bool seg_sorted = true;
+    bool bin_sorted = false;
 };
 
 // status word slots: error bits, then the totals the scans produce
@@ -282,6 +296,8 @@ cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st)
 cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st);
 cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_composite(const Batch &b, cudaStream_t st);
+// fb_scene[t] = the scene of framebuffer tile t, for every uploaded scene (at upload).
+cudaError_t launch_fb_scene(const uint32_t *scene_fb_first, uint32_t n_scenes, uint32_t *fb_scene, cudaStream_t st);
 // Frame counters: alpha and visible tiles of the draw paths into the status words.
 cudaError_t launch_tile_counts(const Batch &b, cudaStream_t st);
 cudaError_t launch_list_dump(const Batch &b, bool write, cudaStream_t st);
@@ -304,10 +320,18 @@ size_t seg_ctl_bytes();  // the per-block bucket counts launch_seg_order keeps i
 // backdrops, fill offsets, fills).  A learned frame first lists its pooled lines by path:
 // count, scan pool_cnt, scatter.
 cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st);
-cudaError_t launch_bin_paths(const Batch &b, cudaStream_t st);
+// side[0..1], fork, join[0..1]: streams and events for running the CTA classes concurrently
+// (tuning.bin_concurrent), or null.
+struct BinStreams {
+    cudaStream_t side[2];
+    cudaEvent_t fork, join[2];
+};
+cudaError_t launch_bin_paths(const Batch &b, const Tuning &t, const BinStreams *bs, cudaStream_t st);
+// The most CTAs of each binning class one SM holds.
+cudaError_t bin_class_max_ctas(int out[3]);
 cudaError_t launch_pool_lists(const Batch &b, bool scatter, cudaStream_t st);
-// Bytes of the binning CTAs' fill stage on the current device.
-cudaError_t bin_stage_bytes(size_t *bytes);
+// Bytes of the binning CTAs' fill stage on the current device for these launch parameters.
+cudaError_t bin_stage_bytes(const Tuning &t, size_t *bytes);
 cudaError_t launch_mlp_predict(const __nv_bfloat16 *w, const float *feat, uint32_t n, float *out, cudaStream_t st);
 cudaError_t launch_mlp_grad(const __nv_bfloat16 *w, const float *feat, const float *target, const uint32_t *index,
                             uint32_t n, float *grad, float *loss, cudaStream_t st);

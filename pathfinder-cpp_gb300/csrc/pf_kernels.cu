@@ -1010,11 +1010,20 @@ __global__ void k_bin_scatter(Batch b) {
 }
 
 // Tiles a line's walk visits at most (its end points' tile distance, before clipping, plus one):
-// lines above kLongLine are walked by a whole warp.
-constexpr float kLongLine = 8.0f;
+// lines above Batch::long_line (8 unless tuned) are walked by a whole warp.
 __device__ __forceinline__ float line_span(const float4 &f) {
     return fabsf(floorf(f.z * 0.0625f) - floorf(f.x * 0.0625f)) + fabsf(floorf(f.w * 0.0625f) - floorf(f.y * 0.0625f)) +
            1.0f;
+}
+
+// Span-sorted count walk (Batch::bin_sorted): windows of this many lines, lines bucketed by the
+// tiles they span (1 .. 7, 8 or more up to the long-line threshold, then the long lines).
+constexpr uint32_t kSortWin = 2048;
+constexpr int kSortBuckets = 10;
+__device__ __forceinline__ int sort_bucket(const float4 &f, float long_line) {
+    const float s = line_span(f);
+    if (!(s <= long_line)) return kSortBuckets - 1;  // long lines (and non-finite ones) last
+    return min((int)s, kSortBuckets - 2) - 1 + (s >= 1.0f ? 0 : 1);
 }
 
 // A staged fill: the four 12-bit coordinates of the packed u16 fill and the tile (< 2^16).
@@ -1039,6 +1048,8 @@ __global__ void __launch_bounds__(class_threads(kCls), class_min_ctas(kCls)) k_b
     __shared__ int32_t s_seg[kThr];
     __shared__ uint32_t s_warp[kWarps];
     __shared__ unsigned long long s_wsum[kWarps];
+    __shared__ uint32_t s_bucket[kSortBuckets];
+    __shared__ uint16_t s_order[kSortWin];
     const uint32_t tid = threadIdx.x;
     const int lane = (int)(tid & 31), warp = (int)(tid >> 5);
     const uint32_t *list = b.bin_list + (size_t)kCls * b.n_paths;
@@ -1077,25 +1088,55 @@ __global__ void __launch_bounds__(class_threads(kCls), class_min_ctas(kCls)) k_b
             if (where >= 0) atomicAdd(&cnt[where], (uint32_t)d << 24);
             else atomicAdd(&above[-1 - where], d);
         };
-        for (;;) {
-            uint32_t k0 = 0;
-            if (lane == 0) k0 = atomicAdd(&s_next, 32u);
-            k0 = __shfl_sync(0xffffffffu, k0, 0);
-            if (k0 >= L.n) break;
-            const uint32_t k = k0 + (uint32_t)lane;
-            float4 f = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            bool along = false;
-            if (k < L.n) {
-                f = b.leaves[L.index(b, k)];
-                along = line_span(f) > kLongLine;
-                if (!along) walk_line(w, f.x, f.y, f.z, f.w, on_fill, on_delta, err);
+        // With b.bin_sorted the lines go in windows of kSortWin, each window's lines ordered by the
+        // tiles they span (a counting sort in shared memory), so the 32 lines a warp takes at a
+        // time run for like numbers of steps.  Fills and deltas are counted in any order.
+        const bool sorted = b.bin_sorted && L.n > 64;
+        for (uint32_t w0 = 0; w0 < L.n; w0 += sorted ? kSortWin : L.n) {
+            const uint32_t wn = sorted ? min(kSortWin, L.n - w0) : L.n;
+            if (sorted) {
+                if (tid < kSortBuckets) s_bucket[tid] = 0;
+                __syncthreads();
+                for (uint32_t k = tid; k < wn; k += kThr)
+                    atomicAdd(&s_bucket[sort_bucket(b.leaves[L.index(b, w0 + k)], b.long_line)], 1u);
+                __syncthreads();
+                if (tid == 0) {
+                    uint32_t run = 0;
+                    for (int j = 0; j < kSortBuckets; j++) {
+                        const uint32_t v = s_bucket[j];
+                        s_bucket[j] = run;
+                        run += v;
+                    }
+                    s_next = 0;
+                }
+                __syncthreads();
+                for (uint32_t k = tid; k < wn; k += kThr) {
+                    const int bk = sort_bucket(b.leaves[L.index(b, w0 + k)], b.long_line);
+                    s_order[atomicAdd(&s_bucket[bk], 1u)] = (uint16_t)k;
+                }
+                __syncthreads();
             }
-            for (unsigned m = __ballot_sync(0xffffffffu, along); m; m &= m - 1) {
-                const int l = __ffs(m) - 1;
-                const float4 g = make_float4(__shfl_sync(0xffffffffu, f.x, l), __shfl_sync(0xffffffffu, f.y, l),
-                                             __shfl_sync(0xffffffffu, f.z, l), __shfl_sync(0xffffffffu, f.w, l));
-                walk_line_warp(w, g, on_fill, on_delta, err);
+            for (;;) {
+                uint32_t k0 = 0;
+                if (lane == 0) k0 = atomicAdd(&s_next, 32u);
+                k0 = __shfl_sync(0xffffffffu, k0, 0);
+                if (k0 >= wn) break;
+                const uint32_t k = k0 + (uint32_t)lane;
+                float4 f = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                bool along = false;
+                if (k < wn) {
+                    f = b.leaves[L.index(b, w0 + (sorted ? s_order[k] : k))];
+                    along = line_span(f) > b.long_line;
+                    if (!along) walk_line(w, f.x, f.y, f.z, f.w, on_fill, on_delta, err);
+                }
+                for (unsigned m = __ballot_sync(0xffffffffu, along); m; m &= m - 1) {
+                    const int l = __ffs(m) - 1;
+                    const float4 g = make_float4(__shfl_sync(0xffffffffu, f.x, l), __shfl_sync(0xffffffffu, f.y, l),
+                                                 __shfl_sync(0xffffffffu, f.z, l), __shfl_sync(0xffffffffu, f.w, l));
+                    walk_line_warp(w, g, on_fill, on_delta, err);
+                }
             }
+            if (sorted) __syncthreads();  // the window's order is read until its last claim
         }
         __syncthreads();
 
@@ -1519,15 +1560,17 @@ __device__ __forceinline__ void raster_column(const FillPrep &fp, int i, int *D)
 // Fills are rasterised as (fill, pixel column) work items spread over the lanes, 32 fills
 // at a time, so a tile of a few wide fills still keeps the warp busy.
 // backdrop + the fills' area sums (fixed point) of the warp's 8 pixels per lane, before the fill rule
-__device__ __forceinline__ void coverage_raw(const Batch &b, uint32_t f0, uint32_t f1, int8_t bd, int *D,
-                                             FillPrep *prep, int raw[8]) {
+// src: the tile's n fills (global memory, or the warp's shared-memory stage).
+__device__ __forceinline__ void coverage_raw(const uint2 *src, uint32_t n, int8_t bd, int *D, FillPrep *prep,
+                                             int raw[8]) {
     const int lane = threadIdx.x & 31;
+    const uint32_t f0 = 0, f1 = n;
     for (uint32_t base = f0; base < f1; base += 32) {
         const uint32_t f = base + lane;
         int items = 0;
         FillPrep fp;
         if (f < f1) {
-            const uint2 q = b.fills[f];
+            const uint2 q = src[f];
             const float x0 = (float)(q.x & 0xffffu) * (1.0f / 256.0f), y0 = (float)(q.x >> 16) * (1.0f / 256.0f);
             const float x1 = (float)(q.y & 0xffffu) * (1.0f / 256.0f), y1 = (float)(q.y >> 16) * (1.0f / 256.0f);
             fp.s = x0 > x1 ? 1.0f : -1.0f;
@@ -1594,7 +1637,7 @@ __device__ __forceinline__ void coverage_rule(const int raw[8], bool eo, float c
 __device__ __forceinline__ void alpha_coverage(const Batch &b, uint32_t f0, uint32_t f1, int8_t bd, bool eo, int *D,
                                                FillPrep *prep, float cov[8]) {
     int raw[8];
-    coverage_raw(b, f0, f1, bd, D, prep, raw);
+    coverage_raw(b.fills + f0, f1 - f0, bd, D, prep, raw);
     coverage_rule(raw, eo, cov);
 }
 
@@ -1619,7 +1662,7 @@ struct Cand {
     uint32_t p, gt, st, flags;  // st: the tile state, with a clipped tile's mask source in bits 9-10
                                 // and (kMaskBoth) the draw tile's own backdrop in bits 16-23
     uint32_t f0, f1, color;     // kFetch only (kMaskClip: the clip tile's fills)
-    uint32_t gc;                // kMaskBoth: the clip tile
+    uint32_t gc;                // kMaskClip, kMaskBoth: the clip tile
 };
 
 __device__ __forceinline__ uint32_t mask_mode(uint32_t st) { return (st >> 9) & 3u; }
@@ -1661,7 +1704,7 @@ __device__ __forceinline__ void walk_fb_tile(const Batch &b, uint32_t row, uint3
     for (uint32_t top = k_hi; top > k_lo; top = top > k_lo + 32 ? top - 32 : k_lo) {
         chunks++;
         const int64_t k = (int64_t)top - 1 - lane;
-        Cand c{0, 0, 0, 0, 0, 0, 0, 0};
+        Cand c{0, 0, 0, 0, 0, 0, 0, kNone};
         bool vis = false;
         if (k >= (int64_t)k_lo) {
             const uint4 e = b.row_paths[k];
@@ -1781,7 +1824,7 @@ __global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 3
     const uint32_t fb = blockIdx.x * kCompWarps + warp;
     if (fb < b.n_fb) {
         const uint32_t fbg = b.fb_base + fb;
-        const uint32_t s = upper_bound(b.scene_fb_first, b.n_scenes_all + 1, fbg) - 1;
+        const uint32_t s = b.fb_scene[fbg];
         const SceneDev &S = b.scenes[s];
         const uint32_t local = fbg - S.fb_first;
         const uint32_t fx = local % S.fbw, fy = local / S.fbw;
@@ -1822,7 +1865,7 @@ __global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 3
                 for (;;) {
                     comp_fills += f1 - f0;
                     zero_cells(D);
-                    coverage_raw(b, f0, f1, tbd, D, prep[warp], raw);
+                    coverage_raw(b.fills + f0, f1 - f0, tbd, D, prep[warp], raw);
                     __syncwarp();
                     if (!both) break;
 #pragma unroll
@@ -1948,7 +1991,7 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_list_dump(Batch b) {
     const uint32_t fb = blockIdx.x * kCompWarps + warp;
     if (fb >= b.n_fb) return;
     const uint32_t fbg = b.fb_base + fb;
-    const uint32_t s = upper_bound(b.scene_fb_first, b.n_scenes_all + 1, fbg) - 1;
+    const uint32_t s = b.fb_scene[fbg];
     const SceneDev &S = b.scenes[s];
     const uint32_t local = fbg - S.fb_first;
     const uint32_t fx = local % S.fbw, fy = local / S.fbw;
@@ -2083,9 +2126,10 @@ cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-// Grid of a CTA class: as many CTAs as fit on every SM (they take paths by ticket).
+// Grid of a CTA class: as many CTAs as fit on every SM (they take paths by ticket), or
+// per_sm_wanted per SM when that is nonzero and fits.
 template <int kCls>
-static cudaError_t fused_grid(unsigned *grid) {
+static cudaError_t fused_grid(unsigned *grid, uint32_t per_sm_wanted = 0) {
     const size_t smem = size_t(class_words(kCls)) * 4;
     static int configured_device = -1;
     int dev = 0, sms = 152;
@@ -2101,32 +2145,49 @@ static cudaError_t fused_grid(unsigned *grid) {
     const cudaError_t e =
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bin_fused<kCls>, class_threads(kCls), smem);
     if (e != cudaSuccess) return e;
-    *grid = (unsigned)std::max(1, per_sm) * (unsigned)sms;
+    per_sm = std::max(1, per_sm);
+    if (per_sm_wanted) per_sm = std::min(per_sm, (int)per_sm_wanted);
+    *grid = (unsigned)per_sm * (unsigned)sms;
     return cudaSuccess;
 }
 
 template <int kCls>
-static cudaError_t launch_fused(const Batch &b, cudaStream_t st) {
+static cudaError_t launch_fused(const Batch &b, uint32_t per_sm, cudaStream_t st) {
     unsigned grid = 0;
-    const cudaError_t e = fused_grid<kCls>(&grid);
+    const cudaError_t e = fused_grid<kCls>(&grid, per_sm);
     if (e != cudaSuccess) return e;
     PF_LAUNCH(k_bin_fused<kCls><<<grid, class_threads(kCls), size_t(class_words(kCls)) * 4, st>>>(b));
     return cudaGetLastError();
 }
 
-cudaError_t bin_stage_bytes(size_t *bytes) {
+cudaError_t bin_stage_bytes(const Tuning &t, size_t *bytes) {
     unsigned g0 = 0, g1 = 0, g2 = 0;
     cudaError_t e;
-    if ((e = fused_grid<0>(&g0)) != cudaSuccess) return e;
-    if ((e = fused_grid<1>(&g1)) != cudaSuccess) return e;
-    if ((e = fused_grid<2>(&g2)) != cudaSuccess) return e;
-    *bytes = 8 * std::max({size_t(g0) * class_stage(0), size_t(g1) * class_stage(1), size_t(g2) * class_stage(2)});
+    if ((e = fused_grid<0>(&g0, t.bin_ctas_per_sm[0])) != cudaSuccess) return e;
+    if ((e = fused_grid<1>(&g1, t.bin_ctas_per_sm[1])) != cudaSuccess) return e;
+    if ((e = fused_grid<2>(&g2, t.bin_ctas_per_sm[2])) != cudaSuccess) return e;
+    const size_t s0 = size_t(g0) * class_stage(0), s1 = size_t(g1) * class_stage(1), s2 = size_t(g2) * class_stage(2);
+    // concurrent classes each keep their own slice of the stage
+    *bytes = 8 * (t.bin_concurrent ? s0 + s1 + s2 : std::max({s0, s1, s2}));
+    return cudaSuccess;
+}
+
+cudaError_t bin_class_max_ctas(int out[3]) {
+    unsigned g[3];
+    cudaError_t e;
+    if ((e = fused_grid<0>(&g[0])) != cudaSuccess) return e;
+    if ((e = fused_grid<1>(&g[1])) != cudaSuccess) return e;
+    if ((e = fused_grid<2>(&g[2])) != cudaSuccess) return e;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    for (int c = 0; c < 3; c++) out[c] = (int)(g[c] / (unsigned)sms);
     return cudaSuccess;
 }
 
 // Class 3 (zero, count, backdrops and offsets, write; each returns at once when the class is
 // empty), then the CTA classes, largest rects first.
-cudaError_t launch_bin_paths(const Batch &b, cudaStream_t st) {
+cudaError_t launch_bin_paths(const Batch &b, const Tuning &t, const BinStreams *bs, cudaStream_t st) {
     if (!b.n_paths) return cudaSuccess;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -2136,9 +2197,31 @@ cudaError_t launch_bin_paths(const Batch &b, cudaStream_t st) {
     PF_LAUNCH(k_bin_large_prep<<<sms * 2, kPrepThreads, 0, st>>>(b));
     PF_LAUNCH(k_bin_large<true><<<sms * 8, kThreads, 0, st>>>(b));
     cudaError_t e;
-    if ((e = launch_fused<2>(b, st)) != cudaSuccess) return e;
-    if ((e = launch_fused<1>(b, st)) != cudaSuccess) return e;
-    return launch_fused<0>(b, st);
+    if (!t.bin_concurrent || !bs) {
+        if ((e = launch_fused<2>(b, t.bin_ctas_per_sm[2], st)) != cudaSuccess) return e;
+        if ((e = launch_fused<1>(b, t.bin_ctas_per_sm[1], st)) != cudaSuccess) return e;
+        return launch_fused<0>(b, t.bin_ctas_per_sm[0], st);
+    }
+    // the three classes at once: classes 1 and 0 on side streams, each with its own slice of
+    // the fill stage (the classes' grids follow each other in it), joined back before the
+    // composite; the block scheduler fills the SMs a class's tail leaves idle with the others
+    unsigned g2 = 0, g1 = 0;
+    if ((e = fused_grid<2>(&g2, t.bin_ctas_per_sm[2])) != cudaSuccess) return e;
+    if ((e = fused_grid<1>(&g1, t.bin_ctas_per_sm[1])) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(bs->fork, st)) != cudaSuccess) return e;
+    for (int k = 0; k < 2; k++)
+        if ((e = cudaStreamWaitEvent(bs->side[k], bs->fork, 0)) != cudaSuccess) return e;
+    Batch b1 = b, b0 = b;
+    b1.stage = b.stage ? b.stage + size_t(g2) * class_stage(2) : nullptr;
+    b0.stage = b.stage ? b1.stage + size_t(g1) * class_stage(1) : nullptr;
+    if ((e = launch_fused<2>(b, t.bin_ctas_per_sm[2], st)) != cudaSuccess) return e;
+    if ((e = launch_fused<1>(b1, t.bin_ctas_per_sm[1], bs->side[0])) != cudaSuccess) return e;
+    if ((e = launch_fused<0>(b0, t.bin_ctas_per_sm[0], bs->side[1])) != cudaSuccess) return e;
+    for (int k = 0; k < 2; k++) {
+        if ((e = cudaEventRecord(bs->join[k], bs->side[k])) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(st, bs->join[k], 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t launch_pool_lists(const Batch &b, bool scatter, cudaStream_t st) {
@@ -2199,6 +2282,17 @@ cudaError_t launch_composite(const Batch &b, cudaStream_t st) {
         else
             PF_LAUNCH(k_composite<false, false><<<grid, kCompWarps * 32, 0, st>>>(b));
     }
+    return cudaGetLastError();
+}
+
+// One block per scene: its framebuffer tiles get its index.
+__global__ void k_fb_scene(const uint32_t *scene_fb_first, uint32_t *fb_scene) {
+    const uint32_t s = blockIdx.x, a = scene_fb_first[s], e = scene_fb_first[s + 1];
+    for (uint32_t t = a + threadIdx.x; t < e; t += blockDim.x) fb_scene[t] = s;
+}
+
+cudaError_t launch_fb_scene(const uint32_t *scene_fb_first, uint32_t n_scenes, uint32_t *fb_scene, cudaStream_t st) {
+    if (n_scenes) PF_LAUNCH(k_fb_scene<<<n_scenes, kThreads, 0, st>>>(scene_fb_first, fb_scene));
     return cudaGetLastError();
 }
 

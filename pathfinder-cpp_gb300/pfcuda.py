@@ -16,7 +16,8 @@ from typing import Dict, List, Optional, Sequence
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libpfcuda.so")
+# PFCUDA_LIB: another build of the library to load (the in-tree build by default)
+LIB_PATH = os.environ.get("PFCUDA_LIB") or os.path.join(HERE, "_build", "libpfcuda.so")
 
 PF_OK = 0
 PF_CONFIG_STAGE_TIMING = 0x1
@@ -32,11 +33,37 @@ EXPORTS = [
     "pf_sizer_last_frame", "pf_debug_counters", "pf_ctx_set_flags", "pf_sizer_predict_noalloc",
     "pf_set_host_image", "pf_read_outline", "pf_upload_stats_get", "pf_svg_parse", "pf_svg_scene", "pf_svg_free",
     "pf_read_images_async", "pf_images_wait", "pf_write_image", "pf_render_auto", "pf_auto_choice",
+    "pf_tuning_get", "pf_tuning_set", "pf_autotune",
 ]
 
 N_FEATURES = 12
 N_OUTPUTS = 2
 DEFAULT_WEIGHTS = os.path.join(HERE, "weights", "sizer.bin")
+# launch parameters found by the autotuner (tune.py) for the batched configuration
+DEFAULT_RENDER_CONFIG = os.path.join(HERE, "weights", "render_config.json")
+
+
+class Tuning(C.Structure):
+    """pf_tuning: the launch parameters of the frame's kernels."""
+    _fields_ = [("bin_ctas_per_sm", C.c_uint32 * 3), ("long_line", C.c_float), ("bin_concurrent", C.c_uint32),
+                ("seg_sorted", C.c_uint32), ("bin_sorted", C.c_uint32), ("reserved", C.c_uint32 * 8)]
+
+    KEYS = ("bin_ctas_per_sm", "long_line", "bin_concurrent", "seg_sorted", "bin_sorted")
+
+    def to_dict(self) -> Dict[str, object]:
+        return {"bin_ctas_per_sm": list(self.bin_ctas_per_sm), "long_line": float(self.long_line),
+                "bin_concurrent": int(self.bin_concurrent), "seg_sorted": int(self.seg_sorted),
+                "bin_sorted": int(self.bin_sorted)}
+
+    @classmethod
+    def from_dict(cls, d: Dict[str, object]) -> "Tuning":
+        t = cls()
+        t.bin_ctas_per_sm[:] = [int(v) for v in d["bin_ctas_per_sm"]]
+        t.long_line = float(d["long_line"])
+        t.bin_concurrent = int(d["bin_concurrent"])
+        t.seg_sorted = int(d["seg_sorted"])
+        t.bin_sorted = int(d.get("bin_sorted", 0))
+        return t
 
 
 class Stroke(C.Structure):
@@ -122,8 +149,13 @@ def load(path: str = LIB_PATH) -> C.CDLL:
         lib.pf_last_error.restype = C.c_char_p
         lib.pf_last_error.argtypes = [C.c_void_p]
         for name in EXPORTS:
-            if name != "pf_last_error":
-                getattr(lib, name).restype = C.c_int
+            if name == "pf_last_error":
+                continue
+            if not hasattr(lib, name):
+                if path == os.path.join(HERE, "_build", "libpfcuda.so"):
+                    raise AttributeError(f"{path} does not export {name}")
+                continue  # another build (PFCUDA_LIB) of an older ABI: its entry points only
+            getattr(lib, name).restype = C.c_int
         lib.pf_svg_parse.argtypes = [C.c_char_p, C.c_size_t, C.c_float, C.POINTER(C.c_void_p)]
         lib.pf_svg_scene.argtypes = [C.c_void_p, C.c_void_p]
         lib.pf_svg_free.argtypes, lib.pf_svg_free.restype = [C.c_void_p], None
@@ -427,6 +459,35 @@ class Renderer:
         names = {0: "exact", 1: "learned"}
         return {"last": names[last.value], "choice": names.get(choice.value), "exact_ms": ems.value,
                 "learned_ms": lms.value}
+
+    # -- launch parameters and the autotuner ------------------------------------------------
+    def tuning(self) -> Dict[str, object]:
+        t = Tuning()
+        self._check(self.lib.pf_tuning_get(self.ctx, C.byref(t)), self.ctx)
+        return t.to_dict()
+
+    def set_tuning(self, d: Dict[str, object]) -> None:
+        t = Tuning.from_dict(d)
+        self._check(self.lib.pf_tuning_set(self.ctx, C.byref(t)), self.ctx)
+
+    def load_render_config(self, path: str = DEFAULT_RENDER_CONFIG) -> Dict[str, object]:
+        """Apply the launch parameters of a RenderConfig JSON file (tune.py writes it)."""
+        import json
+        with open(path) as f:
+            cfg = json.load(f)
+        self.set_tuning(cfg["tuning"])
+        return cfg
+
+    def autotune(self, first: int = 0, count: Optional[int] = None, frames: int = 5):
+        """Search the launch parameters on the uploaded scenes; returns (best, best_ms, start_ms)
+        and leaves the best set."""
+        if count is None:
+            count = len(self._sizes) - first
+        t = Tuning()
+        best, start = C.c_float(), C.c_float()
+        self._check(self.lib.pf_autotune(self.ctx, first, count, frames, C.byref(t), C.byref(best), C.byref(start)),
+                    self.ctx)
+        return t.to_dict(), best.value, start.value
 
     def sizer_init(self, seed: int = 0) -> None:
         self._check(self.lib.pf_sizer_init(self.ctx, C.c_uint64(seed)), self.ctx)

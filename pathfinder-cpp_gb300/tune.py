@@ -1,0 +1,57 @@
+"""Autotune the frame's launch parameters on the GPU and persist them as a RenderConfig.
+
+    python pathfinder-cpp_gb300/tune.py [--scenes 512] [--frames 5] [--out weights/render_config.json]
+
+Uploads the batched configuration (scenes.batched: 512 scenes, seeds 1000+i), loads the sizer,
+and runs pf_autotune: coordinate descent over the binning CTAs per SM of each CTA class, the
+long-line threshold of the tile walk, concurrent binning classes and the flatten's segment
+order, each trial the default frame (pf_render_auto's choice) timed
+on the device.  The file records the parameters, the frame time with the starting (built-in)
+parameters and with the tuned ones, the GPU, and the workload.  bench.py and
+pfcuda.Renderer.load_render_config apply it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+
+def main() -> None:
+    import pfcuda
+    import scenes as S
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--scenes", type=int, default=512)
+    ap.add_argument("--frames", type=int, default=5)
+    ap.add_argument("--out", default=pfcuda.DEFAULT_RENDER_CONFIG)
+    args = ap.parse_args()
+    scs = S.batched(n_scenes=args.scenes)
+    with pfcuda.Renderer() as r:
+        r.sizer_load()
+        r.upload(scs)
+        start = r.tuning()
+        best, best_ms, start_ms = r.autotune(frames=args.frames)
+        auto = r.last_auto_choice()
+    try:
+        import subprocess
+        gpu = subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader"], capture_output=True,
+                             text=True, timeout=30).stdout.strip().splitlines()[0]
+    except (OSError, IndexError, subprocess.SubprocessError):
+        gpu = "unknown"
+    cfg = {"tuning": best, "start": start, "frame_ms": best_ms, "start_frame_ms": start_ms,
+           "frame": "learned" if auto.get("choice") == "learned" else "exact", "gpu": gpu,
+           "workload": f"scenes.batched({args.scenes}): paths/scene log-uniform 16-4096, canvas side in "
+                       "{256,512,1024,2048}, seeds 1000+i",
+           "search": "coordinate descent, median of %d device-timed frames per trial, 1%% improvement to move"
+                     % args.frames}
+    with open(args.out, "w") as f:
+        json.dump(cfg, f, indent=1)
+    print(json.dumps(cfg))
+
+
+if __name__ == "__main__":
+    main()
