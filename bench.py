@@ -112,7 +112,10 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tuning", default=None,
                     help="launch parameters to set over the built-in or tuned ones, as JSON (pf_tuning fields, "
-                         "e.g. '{\"bin_sorted\": 1}')")
+                         "e.g. '{\"bin_concurrent\": 1}')")
+    ap.add_argument("--counters", action="store_true",
+                    help="frame counters on in every frame (composite entries and fills, alpha and visible "
+                         "tiles), for --profile-frames captures that need them")
     ap.add_argument("--profile-frames", action="store_true",
                     help="only the exact, learned and default frames (warm-up + steps each), a short summary "
                          "line instead of the benchmark line: the command the committed launch lists profile")
@@ -475,7 +478,7 @@ def main():
     n_paths = sum(s.n_paths for s in scenes_list)
     bufs, views, h2d_bytes = pack_pinned(scenes_list)
     stream = torch.cuda.Stream()
-    r = pfcuda.Renderer(device=local_rank, stream=stream.cuda_stream, stage_timing=True)
+    r = pfcuda.Renderer(device=local_rank, stream=stream.cuda_stream, stage_timing=True, counters=args.counters)
     r.upload_views(views)
     img_bytes = r.image_bytes()
     img_host = torch.empty(img_bytes, dtype=torch.uint8, pin_memory=True)

@@ -337,8 +337,9 @@ typedef struct pf_tuning {
     float long_line;             /* lines spanning more tiles than this are walked by a whole warp */
     uint32_t bin_concurrent;     /* 1: the three binning classes run at once on side streams */
     uint32_t seg_sorted;         /* 1: the flatten takes segments ordered by subdivision depth */
-    uint32_t bin_sorted;         /* 1: binning's count walk takes each window of 2048 lines in order
-                                    of the tiles they span (warps get lines of like length) */
+    uint32_t composite_ticket;   /* 0: the composite runs a warp per framebuffer tile; n > 0: its warps
+                                    stay resident and take n consecutive tiles per ticket from a
+                                    frame-wide queue (at most 4096) */
     uint32_t reserved[8];
 } pf_tuning;
 int pf_tuning_get(void *ctx, pf_tuning *out);

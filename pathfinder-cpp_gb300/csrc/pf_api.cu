@@ -915,7 +915,7 @@ Batch make_batch(Ctx *c) {
     b.status = c->status.as<uint32_t>();
     b.counters = (c->flags & PF_CONFIG_FRAME_COUNTERS) ? 1u : 0u;
     b.long_line = c->tune.long_line;
-    b.bin_sorted = c->tune.bin_sorted ? 1u : 0u;
+    b.comp_ticket = c->tune.comp_ticket;
     if (!c->tune.seg_sorted) b.seg_order = nullptr;
     return b;
 }
@@ -2357,7 +2357,7 @@ static void tuning_out(const Tuning &t, pf_tuning *o) {
     o->long_line = t.long_line;
     o->bin_concurrent = t.bin_concurrent;
     o->seg_sorted = t.seg_sorted;
-    o->bin_sorted = t.bin_sorted;
+    o->composite_ticket = t.comp_ticket;
 }
 
 int pf_tuning_get(void *ctx, pf_tuning *out) {
@@ -2374,7 +2374,8 @@ int pf_tuning_set(void *ctx, const pf_tuning *t) {
         return fail(c, PF_ERR_INVALID_ARGUMENT, "long_line must lie in [1, 4096]");
     for (uint32_t v : t->bin_ctas_per_sm)
         if (v > 64) return fail(c, PF_ERR_INVALID_ARGUMENT, "bin_ctas_per_sm must lie in [0, 64]");
-    if (t->bin_concurrent > 1 || t->seg_sorted > 1 || t->bin_sorted > 1)
+    if (t->composite_ticket > 4096) return fail(c, PF_ERR_INVALID_ARGUMENT, "composite_ticket must lie in [0, 4096]");
+    if (t->bin_concurrent > 1 || t->seg_sorted > 1)
         return fail(c, PF_ERR_INVALID_ARGUMENT, "flags must be 0 or 1");
     cudaSetDevice(c->device);
     PF_CUDA(cudaStreamSynchronize(c->stream));
@@ -2383,7 +2384,7 @@ int pf_tuning_set(void *ctx, const pf_tuning *t) {
     n.long_line = t->long_line;
     n.bin_concurrent = t->bin_concurrent != 0;
     n.seg_sorted = t->seg_sorted != 0;
-    n.bin_sorted = t->bin_sorted != 0;
+    n.comp_ticket = t->composite_ticket;
     c->tune = n;
     forget_learned(c);  // the recorded frame has the old parameters in its launches
     c->au.exact_ms = c->au.learned_ms = -1.0f;
@@ -2434,18 +2435,18 @@ int pf_autotune(void *ctx, uint32_t first, uint32_t count, uint32_t frames, pf_t
         {3, {4, 6, 8, 12, 16, 32}},   // long_line
         {4, {0, 1}},                  // bin_concurrent
         {5, {0, 1}},                  // seg_sorted
-        {6, {0, 1}},                  // bin_sorted
+        {6, {0, 1, 2, 4, 8, 16}},     // composite_ticket
     };
     auto get = [](const pf_tuning &t, int i) -> float {
         return i < 3 ? (float)t.bin_ctas_per_sm[i] : i == 3 ? t.long_line : i == 4 ? (float)t.bin_concurrent
-               : i == 5 ? (float)t.seg_sorted : (float)t.bin_sorted;
+               : i == 5 ? (float)t.seg_sorted : (float)t.composite_ticket;
     };
     auto put = [](pf_tuning &t, int i, float v) {
         if (i < 3) t.bin_ctas_per_sm[i] = (uint32_t)v;
         else if (i == 3) t.long_line = v;
         else if (i == 4) t.bin_concurrent = (uint32_t)v;
         else if (i == 5) t.seg_sorted = (uint32_t)v;
-        else t.bin_sorted = (uint32_t)v;
+        else t.composite_ticket = (uint32_t)v;
     };
     for (int pass = 0; pass < 3; pass++) {
         bool improved = false;

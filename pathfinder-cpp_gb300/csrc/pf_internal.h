@@ -170,9 +170,10 @@ struct Batch {
     uint32_t *status;                    // [kStCount] error bits and totals
     uint32_t counters;                   // nonzero: the composite adds its work counters to status
     // launch parameters (pf_tuning): lines spanning more tiles than long_line are walked by a
-    // whole warp; bin_sorted: the count walk takes each window of lines in order of span
+    // whole warp; comp_ticket > 0: the composite's warps stay resident and take that many
+    // framebuffer tiles per ticket (0: one warp per tile)
     float long_line;
-    uint32_t bin_sorted;
+    uint32_t comp_ticket;
 };
 
 // The launch parameters of a frame (pf_tuning), as the kernels and launchers read them.
@@ -181,7 +182,7 @@ struct Tuning {
     float long_line = 8.0f;
     bool bin_concurrent = false;
     bool seg_sorted = true;
-    bool bin_sorted = false;
+    uint32_t comp_ticket = 0;
 };
 
 // status word slots: error bits, then the totals the scans produce
@@ -295,7 +296,7 @@ cudaError_t launch_path_offsets(const Batch &b, cudaStream_t st);
 cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st);
 cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st);
-cudaError_t launch_composite(const Batch &b, cudaStream_t st);
+cudaError_t launch_composite(const Batch &b, cudaStream_t st);  // b.comp_ticket picks the grid
 // fb_scene[t] = the scene of framebuffer tile t, for every uploaded scene (at upload).
 cudaError_t launch_fb_scene(const uint32_t *scene_fb_first, uint32_t n_scenes, uint32_t *fb_scene, cudaStream_t st);
 // Frame counters: alpha and visible tiles of the draw paths into the status words.

@@ -859,8 +859,8 @@ enum : int { kCtlCount = 0, kCtlTicket = 4, kCtlTicketZero = 8, kCtlTicketPrep =
 // and from slot 16 the CTA classes' paths counted by log2 of their leaf lines (3 x 32), then
 // the write cursors of those buckets (3 x 32): each class's list runs from its largest paths to
 // its smallest, so the last CTAs to start take the shortest paths
-enum : int { kCtlBucket = 16, kCtlCursor = 16 + 3 * 32, kCtlWords = 16 + 6 * 32 };
-static_assert(kCtlWords * 4 <= 1024, "bin_ctl holds 1024 bytes");
+enum : int { kCtlBucket = 16, kCtlCursor = 16 + 3 * 32, kCtlWords = 16 + 6 * 32, kCtlCompTicket = kCtlWords };
+static_assert((kCtlCompTicket + 1) * 4 <= 1024, "bin_ctl holds 1024 bytes");
 constexpr uint64_t kLow40 = (1ull << 40) - 1;
 
 __device__ __forceinline__ unsigned long long *ctl3_word(const Batch &b) {
@@ -1016,16 +1016,6 @@ __device__ __forceinline__ float line_span(const float4 &f) {
            1.0f;
 }
 
-// Span-sorted count walk (Batch::bin_sorted): windows of this many lines, lines bucketed by the
-// tiles they span (1 .. 7, 8 or more up to the long-line threshold, then the long lines).
-constexpr uint32_t kSortWin = 2048;
-constexpr int kSortBuckets = 10;
-__device__ __forceinline__ int sort_bucket(const float4 &f, float long_line) {
-    const float s = line_span(f);
-    if (!(s <= long_line)) return kSortBuckets - 1;  // long lines (and non-finite ones) last
-    return min((int)s, kSortBuckets - 2) - 1 + (s >= 1.0f ? 0 : 1);
-}
-
 // A staged fill: the four 12-bit coordinates of the packed u16 fill and the tile (< 2^16).
 __device__ __forceinline__ uint2 stage_pack(uint2 q, uint32_t local) {
     const uint32_t x0 = q.x & 0xfffu, y0 = q.x >> 16, x1 = q.y & 0xfffu, y1 = q.y >> 16;
@@ -1048,8 +1038,6 @@ __global__ void __launch_bounds__(class_threads(kCls), class_min_ctas(kCls)) k_b
     __shared__ int32_t s_seg[kThr];
     __shared__ uint32_t s_warp[kWarps];
     __shared__ unsigned long long s_wsum[kWarps];
-    __shared__ uint32_t s_bucket[kSortBuckets];
-    __shared__ uint16_t s_order[kSortWin];
     const uint32_t tid = threadIdx.x;
     const int lane = (int)(tid & 31), warp = (int)(tid >> 5);
     const uint32_t *list = b.bin_list + (size_t)kCls * b.n_paths;
@@ -1088,55 +1076,25 @@ __global__ void __launch_bounds__(class_threads(kCls), class_min_ctas(kCls)) k_b
             if (where >= 0) atomicAdd(&cnt[where], (uint32_t)d << 24);
             else atomicAdd(&above[-1 - where], d);
         };
-        // With b.bin_sorted the lines go in windows of kSortWin, each window's lines ordered by the
-        // tiles they span (a counting sort in shared memory), so the 32 lines a warp takes at a
-        // time run for like numbers of steps.  Fills and deltas are counted in any order.
-        const bool sorted = b.bin_sorted && L.n > 64;
-        for (uint32_t w0 = 0; w0 < L.n; w0 += sorted ? kSortWin : L.n) {
-            const uint32_t wn = sorted ? min(kSortWin, L.n - w0) : L.n;
-            if (sorted) {
-                if (tid < kSortBuckets) s_bucket[tid] = 0;
-                __syncthreads();
-                for (uint32_t k = tid; k < wn; k += kThr)
-                    atomicAdd(&s_bucket[sort_bucket(b.leaves[L.index(b, w0 + k)], b.long_line)], 1u);
-                __syncthreads();
-                if (tid == 0) {
-                    uint32_t run = 0;
-                    for (int j = 0; j < kSortBuckets; j++) {
-                        const uint32_t v = s_bucket[j];
-                        s_bucket[j] = run;
-                        run += v;
-                    }
-                    s_next = 0;
-                }
-                __syncthreads();
-                for (uint32_t k = tid; k < wn; k += kThr) {
-                    const int bk = sort_bucket(b.leaves[L.index(b, w0 + k)], b.long_line);
-                    s_order[atomicAdd(&s_bucket[bk], 1u)] = (uint16_t)k;
-                }
-                __syncthreads();
+        for (;;) {
+            uint32_t k0 = 0;
+            if (lane == 0) k0 = atomicAdd(&s_next, 32u);
+            k0 = __shfl_sync(0xffffffffu, k0, 0);
+            if (k0 >= L.n) break;
+            const uint32_t k = k0 + (uint32_t)lane;
+            float4 f = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            bool along = false;
+            if (k < L.n) {
+                f = b.leaves[L.index(b, k)];
+                along = line_span(f) > b.long_line;
+                if (!along) walk_line(w, f.x, f.y, f.z, f.w, on_fill, on_delta, err);
             }
-            for (;;) {
-                uint32_t k0 = 0;
-                if (lane == 0) k0 = atomicAdd(&s_next, 32u);
-                k0 = __shfl_sync(0xffffffffu, k0, 0);
-                if (k0 >= wn) break;
-                const uint32_t k = k0 + (uint32_t)lane;
-                float4 f = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                bool along = false;
-                if (k < wn) {
-                    f = b.leaves[L.index(b, w0 + (sorted ? s_order[k] : k))];
-                    along = line_span(f) > b.long_line;
-                    if (!along) walk_line(w, f.x, f.y, f.z, f.w, on_fill, on_delta, err);
-                }
-                for (unsigned m = __ballot_sync(0xffffffffu, along); m; m &= m - 1) {
-                    const int l = __ffs(m) - 1;
-                    const float4 g = make_float4(__shfl_sync(0xffffffffu, f.x, l), __shfl_sync(0xffffffffu, f.y, l),
-                                                 __shfl_sync(0xffffffffu, f.z, l), __shfl_sync(0xffffffffu, f.w, l));
-                    walk_line_warp(w, g, on_fill, on_delta, err);
-                }
+            for (unsigned m = __ballot_sync(0xffffffffu, along); m; m &= m - 1) {
+                const int l = __ffs(m) - 1;
+                const float4 g = make_float4(__shfl_sync(0xffffffffu, f.x, l), __shfl_sync(0xffffffffu, f.y, l),
+                                             __shfl_sync(0xffffffffu, f.z, l), __shfl_sync(0xffffffffu, f.w, l));
+                walk_line_warp(w, g, on_fill, on_delta, err);
             }
-            if (sorted) __syncthreads();  // the window's order is read until its last claim
         }
         __syncthreads();
 
@@ -1807,9 +1765,10 @@ __device__ __forceinline__ float4 gradient_color(const Batch &b, uint32_t g, flo
     return o;
 }
 
-// kClip: the batch has clip paths; kPaint: it has gradient paints (variants of their own, so
-// that their code's registers cost batches without them nothing)
-template <bool kClip, bool kPaint>
+// kClip: the batch has clip paths; kPaint: it has gradient paints; kTicket: resident warps
+// take tiles by ticket (b.comp_ticket > 0).  Variants of their own, so that code one frame does
+// not need costs it no registers.
+template <bool kClip, bool kPaint, bool kTicket>
 __global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 32) / kCompWarps) k_composite(Batch b) {
     __shared__ int cells[kCompWarps][kCovCells];
     __shared__ FillPrep prep[kCompWarps][32];
@@ -1821,8 +1780,25 @@ __global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 3
     const int col = lane & 15, h = lane >> 4;
     const float inv255 = 1.0f / 255.0f;
     uint32_t entries = 0, comp_fills = 0, chunks = 0;
-    const uint32_t fb = blockIdx.x * kCompWarps + warp;
-    if (fb < b.n_fb) {
+    // one framebuffer tile per warp, or (kTicket) warps that stay and take comp_ticket
+    // consecutive tiles at a time from a frame-wide ticket counter
+    uint32_t next = 0, left = 0;
+    for (uint32_t round = 0;; round++) {
+        uint32_t fb;
+        if (!kTicket) {
+            if (round > 0) break;
+            fb = blockIdx.x * kCompWarps + warp;
+        } else {
+            if (left == 0) {
+                uint32_t t = 0;
+                if (lane == 0) t = atomicAdd(&b.bin_ctl[kCtlCompTicket], b.comp_ticket);
+                next = __shfl_sync(0xffffffffu, t, 0);
+                left = b.comp_ticket;
+            }
+            fb = next++;
+            left--;
+        }
+        if (fb >= b.n_fb) break;
         const uint32_t fbg = b.fb_base + fb;
         const uint32_t s = b.fb_scene[fbg];
         const SceneDev &S = b.scenes[s];
@@ -2270,19 +2246,32 @@ cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_composite(const Batch &b, cudaStream_t st) {
-    if (b.n_fb) {
-        const unsigned grid = grid_for(b.n_fb, kCompWarps);
-        if (b.path_clip_cat && b.path_grad)
-            PF_LAUNCH(k_composite<true, true><<<grid, kCompWarps * 32, 0, st>>>(b));
-        else if (b.path_clip_cat)
-            PF_LAUNCH(k_composite<true, false><<<grid, kCompWarps * 32, 0, st>>>(b));
-        else if (b.path_grad)
-            PF_LAUNCH(k_composite<false, true><<<grid, kCompWarps * 32, 0, st>>>(b));
-        else
-            PF_LAUNCH(k_composite<false, false><<<grid, kCompWarps * 32, 0, st>>>(b));
+// Grid of the composite: a warp per framebuffer tile, or (ticketed) as many resident blocks as
+// fit on every SM.
+template <bool kClip, bool kPaint>
+static cudaError_t launch_composite_variant(const Batch &b, cudaStream_t st) {
+    if (!b.comp_ticket) {
+        PF_LAUNCH(k_composite<kClip, kPaint, false><<<grid_for(b.n_fb, kCompWarps), kCompWarps * 32, 0, st>>>(b));
+        return cudaGetLastError();
     }
+    int dev = 0, sms = 152, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_composite<kClip, kPaint, true>, kCompWarps * 32, 0);
+    if (e != cudaSuccess) return e;
+    const unsigned grid =
+        std::min<unsigned>(grid_for(b.n_fb, kCompWarps), (unsigned)std::max(per_sm, 1) * (unsigned)sms);
+    PF_LAUNCH(k_composite<kClip, kPaint, true><<<grid, kCompWarps * 32, 0, st>>>(b));
     return cudaGetLastError();
+}
+
+cudaError_t launch_composite(const Batch &b, cudaStream_t st) {
+    if (!b.n_fb) return cudaSuccess;
+    if (b.path_clip_cat && b.path_grad) return launch_composite_variant<true, true>(b, st);
+    if (b.path_clip_cat) return launch_composite_variant<true, false>(b, st);
+    if (b.path_grad) return launch_composite_variant<false, true>(b, st);
+    return launch_composite_variant<false, false>(b, st);
 }
 
 // One block per scene: its framebuffer tiles get its index.

@@ -46,14 +46,14 @@ DEFAULT_RENDER_CONFIG = os.path.join(HERE, "weights", "render_config.json")
 class Tuning(C.Structure):
     """pf_tuning: the launch parameters of the frame's kernels."""
     _fields_ = [("bin_ctas_per_sm", C.c_uint32 * 3), ("long_line", C.c_float), ("bin_concurrent", C.c_uint32),
-                ("seg_sorted", C.c_uint32), ("bin_sorted", C.c_uint32), ("reserved", C.c_uint32 * 8)]
+                ("seg_sorted", C.c_uint32), ("composite_ticket", C.c_uint32), ("reserved", C.c_uint32 * 8)]
 
-    KEYS = ("bin_ctas_per_sm", "long_line", "bin_concurrent", "seg_sorted", "bin_sorted")
+    KEYS = ("bin_ctas_per_sm", "long_line", "bin_concurrent", "seg_sorted", "composite_ticket")
 
     def to_dict(self) -> Dict[str, object]:
         return {"bin_ctas_per_sm": list(self.bin_ctas_per_sm), "long_line": float(self.long_line),
                 "bin_concurrent": int(self.bin_concurrent), "seg_sorted": int(self.seg_sorted),
-                "bin_sorted": int(self.bin_sorted)}
+                "composite_ticket": int(self.composite_ticket)}
 
     @classmethod
     def from_dict(cls, d: Dict[str, object]) -> "Tuning":
@@ -62,7 +62,7 @@ class Tuning(C.Structure):
         t.long_line = float(d["long_line"])
         t.bin_concurrent = int(d["bin_concurrent"])
         t.seg_sorted = int(d["seg_sorted"])
-        t.bin_sorted = int(d.get("bin_sorted", 0))
+        t.composite_ticket = int(d.get("composite_ticket", 0))
         return t
 
 

@@ -4,9 +4,9 @@
 
 Uploads the batched configuration (scenes.batched: 512 scenes, seeds 1000+i), loads the sizer,
 and runs pf_autotune: coordinate descent over the binning CTAs per SM of each CTA class, the
-long-line threshold of the tile walk, concurrent binning classes and the flatten's segment
-order, each trial the default frame (pf_render_auto's choice) timed
-on the device.  The file records the parameters, the frame time with the starting (built-in)
+long-line threshold of the tile walk, concurrent binning classes, the flatten's segment order
+and the composite's tiles per ticket, each trial the default frame (pf_render_auto's choice)
+timed on the device.  The file records the parameters, the frame time with the starting (built-in)
 parameters and with the tuned ones, the GPU, and the workload.  bench.py and
 pfcuda.Renderer.load_render_config apply it.
 """
@@ -35,6 +35,8 @@ def main() -> None:
         r.upload(scs)
         start = r.tuning()
         best, best_ms, start_ms = r.autotune(frames=args.frames)
+        for _ in range(6):  # the default frame's choice with the tuned parameters
+            r.render_auto()
         auto = r.last_auto_choice()
     try:
         import subprocess
@@ -43,7 +45,7 @@ def main() -> None:
     except (OSError, IndexError, subprocess.SubprocessError):
         gpu = "unknown"
     cfg = {"tuning": best, "start": start, "frame_ms": best_ms, "start_frame_ms": start_ms,
-           "frame": "learned" if auto.get("choice") == "learned" else "exact", "gpu": gpu,
+           "frame": auto.get("choice"), "auto": auto, "gpu": gpu,
            "workload": f"scenes.batched({args.scenes}): paths/scene log-uniform 16-4096, canvas side in "
                        "{256,512,1024,2048}, seeds 1000+i",
            "search": "coordinate descent, median of %d device-timed frames per trial, 1%% improvement to move"

@@ -16,10 +16,10 @@ pytestmark = pytest.mark.gpu
 LIST_KEYS = ["fb_tiles", "z", "fb_list_first", "fb_list"]
 
 SETTINGS = [
-    {"bin_ctas_per_sm": [0, 0, 0], "long_line": 8.0, "bin_concurrent": 1, "seg_sorted": 1, "bin_sorted": 1},
-    {"bin_ctas_per_sm": [1, 2, 1], "long_line": 4.0, "bin_concurrent": 1, "seg_sorted": 0, "bin_sorted": 0},
-    {"bin_ctas_per_sm": [3, 1, 2], "long_line": 32.0, "bin_concurrent": 0, "seg_sorted": 1, "bin_sorted": 1},
-    {"bin_ctas_per_sm": [0, 4, 0], "long_line": 1.0, "bin_concurrent": 0, "seg_sorted": 0, "bin_sorted": 1},
+    {"bin_ctas_per_sm": [0, 0, 0], "long_line": 8.0, "bin_concurrent": 1, "seg_sorted": 1, "composite_ticket": 4},
+    {"bin_ctas_per_sm": [1, 2, 1], "long_line": 4.0, "bin_concurrent": 1, "seg_sorted": 0, "composite_ticket": 1},
+    {"bin_ctas_per_sm": [3, 1, 2], "long_line": 32.0, "bin_concurrent": 0, "seg_sorted": 1, "composite_ticket": 0},
+    {"bin_ctas_per_sm": [0, 4, 0], "long_line": 1.0, "bin_concurrent": 0, "seg_sorted": 0, "composite_ticket": 16},
 ]
 
 
@@ -70,7 +70,8 @@ def test_autotune_returns_a_setting_no_slower_than_the_start(pf):
 def test_bad_launch_parameters_are_rejected(pf):
     with pf.Renderer() as r:
         good = r.tuning()
-        for bad in ({**good, "long_line": 0.5}, {**good, "bin_concurrent": 2}, {**good, "bin_ctas_per_sm": [0, 65, 0]}):
+        for bad in ({**good, "long_line": 0.5}, {**good, "bin_concurrent": 2}, {**good, "bin_ctas_per_sm": [0, 65, 0]},
+                    {**good, "composite_ticket": 5000}):
             with pytest.raises(pf.PfError) as e:
                 r.set_tuning(bad)
             assert e.value.status == 1
