@@ -842,9 +842,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_flatten_budget(Batch b, uint32_
 // landing above the rect, summed as int32).
 constexpr int kCtaClasses = 3;
 __host__ __device__ constexpr uint32_t class_words(int c) { return c == 0 ? 1088u : c == 1 ? 4352u : 16896u; }
-__host__ __device__ constexpr int class_threads(int c) { return c == 2 ? 384 : 256; }
+// Small CTAs for the small classes: a path's barriers then hold few warps, and more paths are in
+// flight per SM (A/B on the 512-scene batch, binning: 21.56 ms with 256-thread CTAs, 6 per SM, for
+// classes 0 and 1; 20.80 ms with 128-thread CTAs, 12 per SM; 20.72 ms with class 0 at 64 threads,
+// 24 per SM).  Class 2 keeps 384 threads: its shared words allow 3 CTAs per SM (256 or 512 threads
+// ran slower).
+__host__ __device__ constexpr int class_threads(int c) { return c == 2 ? 384 : c == 1 ? 128 : 64; }
 // CTAs per SM the register budget is set for (shared memory allows 3 of class 2, 12 of class 1)
-__host__ __device__ constexpr int class_min_ctas(int c) { return c == 2 ? 3 : 6; }
+__host__ __device__ constexpr int class_min_ctas(int c) { return c == 2 ? 3 : c == 1 ? 12 : 24; }
 // Fills a CTA stages during its count walk (8 bytes each, in its own slice of a global buffer
 // that stays in L2): the fills are then placed without walking the lines again.  A path with
 // more fills than this walks its lines twice.
