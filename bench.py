@@ -51,6 +51,8 @@ UNIT = "scenes/s"
 # DRAM bytes of the hot kernels per algorithmic byte, from an ncu capture of each workload
 # (written next to the capture's summary; absent: traffic is reported as null)
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "dram_traffic.json")
+# pf_render_auto calls that always suffice for it to decide (two timed frames of each kind)
+AUTO_SETTLE = 7
 L2_FLUSH_BYTES = 256 << 20  # written between timed steps of the single-scene configurations
 
 CONFIG_DESC = {
@@ -523,7 +525,7 @@ def main():
     if args.config == 4 and os.path.exists(pfcuda.DEFAULT_RENDER_CONFIG):
         builtin = r.tuning()
         frame0 = r.render_auto if learned else r.render
-        for _ in range(max(args.warmup, 6)):
+        for _ in range(max(args.warmup, AUTO_SETTLE)):
             frame0()
         ms_builtin, _ = timed(frame0, args.steps)
         cfg = r.load_render_config()
@@ -549,10 +551,11 @@ def main():
         for _ in range(args.warmup):
             r.render_learned()
         ms_learned, stats_l = timed(lambda: r.render_learned(), args.steps)
-    # 3. the library's default frame (pf_render_auto), the headline: its first five calls over a
-    #    workload time the exact and the learned frame, so it takes at least six warm-up frames
+    # 3. the library's default frame (pf_render_auto), the headline: its first calls over a
+    #    workload time the exact and the learned frame (at most seven decide), so it takes at
+    #    least that many warm-up frames
     frame = r.render_auto if learned else r.render
-    for _ in range(max(args.warmup, 6)):
+    for _ in range(max(args.warmup, AUTO_SETTLE)):
         frame()
     ms_frame, stats_f = timed(frame, args.steps)
     st = stats_f[-1]

@@ -310,19 +310,19 @@ int pf_render_learned(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_fra
  * The frame to use by default: the learned frame where it pays, else the exact one.  The context
  * times both frames on the device over the workload (the scene range and its totals of paths,
  * contours and points: a later upload of scenes of the same size keeps what was measured) as they
- * run: the first calls run the exact frame until it is timed, the next ones the learned frame
- * until its time is known (neither frame's first run is timed, nor a learned frame that records
- * its CUDA graph; its replay is), and from then on the faster of the two, re-timing the learned
- * frame whenever it runs.  A learned frame that has
- * to be redone exactly (stats->overflow) counts as the slower one.  Without sizer weights every
- * call runs the exact frame.  Output is identical whichever runs.  No counterpart in the reference
- * (its count-then-allocate loop always runs, renderer.cpp:540-577).
+ * run: the first calls run the exact frame until it has been timed twice, the next ones the
+ * learned frame until it has been timed twice (neither frame's first run is timed, nor a learned
+ * frame that records its CUDA graph; its replay is), and from then on the one whose faster timed
+ * frame was faster: at most seven calls decide.  A learned frame that has to be redone exactly
+ * (stats->overflow) counts as the slower one.  Without sizer weights every call runs the exact
+ * frame.  Output is identical whichever runs.  No counterpart in the reference (its
+ * count-then-allocate loop always runs, renderer.cpp:540-577).
  */
 #define PF_FRAME_EXACT 0
 #define PF_FRAME_LEARNED 1
 int pf_render_auto(void *ctx, uint32_t first_scene, uint32_t n_scenes, pf_frame_stats *stats);
 /* What pf_render_auto did: the frame its last call ran (PF_FRAME_*), the settled choice (-1 while
- * it is still timing), and the two device times it measured (0 until measured). */
+ * it is still timing), and each frame's fastest timed run (0 until timed). */
 int pf_auto_choice(void *ctx, int *last, int *choice, float *exact_ms, float *learned_ms);
 
 /*

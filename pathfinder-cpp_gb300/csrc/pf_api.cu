@@ -177,8 +177,9 @@ struct Ctx {
     uint64_t upload_epoch = 0;
     struct {
         uint64_t sig[5] = {~0ull, 0, 0, 0, 0};  // first, count, paths, contours, points of the range
-        float exact_ms = -1.0f, learned_ms = -1.0f;  // < 0: not measured
-        int exact_runs = 0, learned_runs = 0;  // frames run over the workload (the first is not timed)
+        float exact_ms = -1.0f, learned_ms = -1.0f;  // fastest timed frame of each kind; < 0: none yet
+        int exact_runs = 0, learned_runs = 0;    // frames run over the workload (the first is not timed)
+        int exact_timed = 0, learned_timed = 0;  // frames timed (kAutoSamples of each decide)
         int last = PF_FRAME_EXACT;     // the frame the last auto call ran
     } au;
     cudaEvent_t au_ev[2] = {};
@@ -1393,13 +1394,27 @@ int timed_frame(Ctx *c, float *ms, F &&frame) {
     return PF_OK;
 }
 
+// Timed frames of each kind before pf_render_auto decides, and the calls that always suffice:
+// an untimed first exact frame and two timed ones, then an untimed first learned frame, the one
+// that records its graph, and two timed replays.
+constexpr int kAutoSamples = 2;
+constexpr int kAutoSettle = 2 * kAutoSamples + 3;
+
+void auto_reset(Ctx *c) {
+    auto &a = c->au;
+    a.exact_ms = a.learned_ms = -1.0f;
+    a.exact_runs = a.learned_runs = 0;
+    a.exact_timed = a.learned_timed = 0;
+}
+
 // The frame the library picks.  With sizer weights it times, on the device, the exact frame and
 // the learned frame over the workload - the scene range and the totals of its paths, contours and
 // points, so a new upload of scenes of the same size keeps what was measured - and runs the
 // faster one once both are known.  Each frame's first run over the workload is not timed (it may
-// grow buffers), nor is a learned frame that records its graph (the next one, a replay, is); a
-// learned frame that had to be redone exactly counts as the slower one.  Without weights: the
-// exact frame.
+// grow buffers), nor is a learned frame that records its graph (the next one, a replay, is).
+// Each kind is timed kAutoSamples times and its fastest frame counts, so one frame slowed by
+// something outside it does not decide; a learned frame that had to be redone exactly counts as
+// the slower one at once.  Without weights: the exact frame.
 int render_auto(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
     auto &a = c->au;
     if (!c->uploaded) return fail(c, PF_ERR_NOT_READY, "no scene uploaded");
@@ -1412,24 +1427,30 @@ int render_auto(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) {
                              uint64_t(s1.contour_end - s0.contour_first), uint64_t(s1.point_end - s0.point_first)};
     if (std::memcmp(sig, a.sig, sizeof sig) != 0) {
         std::memcpy(a.sig, sig, sizeof sig);
-        a.exact_ms = a.learned_ms = -1.0f;
-        a.exact_runs = a.learned_runs = 0;
+        auto_reset(c);
     }
     pf_frame_stats local;
     pf_frame_stats *st = stats ? stats : &local;
     float ms = 0.0f;
-    if (a.exact_ms < 0.0f) {
+    auto keep = [](float &best, int &timed, float v) {
+        best = timed == 0 ? v : std::min(best, v);
+        timed++;
+    };
+    if (a.exact_timed < kAutoSamples) {
         const int e = timed_frame(c, &ms, [&] { return render_exact(c, first, count, st); });
-        if (e == PF_OK && a.exact_runs++ > 0) a.exact_ms = ms;
+        if (e == PF_OK && a.exact_runs++ > 0) keep(a.exact_ms, a.exact_timed, ms);
         return e;
     }
-    if (a.learned_ms < 0.0f || a.learned_ms < a.exact_ms) {
+    if (a.learned_timed < kAutoSamples || a.learned_ms < a.exact_ms) {
         a.last = PF_FRAME_LEARNED;
         const int e = timed_frame(c, &ms, [&] { return render_learned(c, first, count, st); });
         if (e != PF_OK) return e;
-        if (st->overflow) a.learned_ms = 2.0f * a.exact_ms + 1.0f;  // redone exactly: the exact frame wins
-        else if (c->lg_kind == 2 || (c->lg_kind == 0 && a.learned_runs > 0))
-            a.learned_ms = ms;  // a replay, or a plain frame after the first: the frame as it runs
+        if (st->overflow) {  // redone exactly: the exact frame wins
+            a.learned_ms = 2.0f * a.exact_ms + 1.0f;
+            a.learned_timed = kAutoSamples;
+        } else if (a.learned_timed < kAutoSamples && (c->lg_kind == 2 || (c->lg_kind == 0 && a.learned_runs > 0))) {
+            keep(a.learned_ms, a.learned_timed, ms);  // a replay, or a plain frame after the first
+        }
         a.learned_runs++;
         return e;
     }
@@ -2387,8 +2408,7 @@ int pf_tuning_set(void *ctx, const pf_tuning *t) {
     n.comp_ticket = t->composite_ticket;
     c->tune = n;
     forget_learned(c);  // the recorded frame has the old parameters in its launches
-    c->au.exact_ms = c->au.learned_ms = -1.0f;
-    c->au.exact_runs = c->au.learned_runs = 0;
+    auto_reset(c);
     return PF_OK;
 }
 
@@ -2404,7 +2424,7 @@ int pf_autotune(void *ctx, uint32_t first, uint32_t count, uint32_t frames, pf_t
     // the default frame settles first (it times the exact and the learned frame), then each
     // trial: set the parameters, warm up (buffers, the learned frame's graph), time `frames`
     pf_frame_stats st;
-    for (int k = 0; k < 6; k++)
+    for (int k = 0; k < kAutoSettle; k++)
         if (int e = render_auto(c, first, count, &st)) return e;
     const bool learned = c->sz_ready && c->au.learned_ms >= 0.0f && c->au.learned_ms < c->au.exact_ms;
     auto trial = [&](const pf_tuning &t, float *ms) -> int {
@@ -2480,7 +2500,7 @@ int pf_auto_choice(void *ctx, int *last, int *choice, float *exact_ms, float *le
     if (last) *last = a.last;
     if (choice)
         *choice = !c->sz_ready ? PF_FRAME_EXACT
-                  : (a.exact_ms < 0.0f || a.learned_ms < 0.0f) ? -1
+                  : (a.exact_timed < kAutoSamples || a.learned_timed < kAutoSamples) ? -1
                   : a.learned_ms < a.exact_ms ? PF_FRAME_LEARNED : PF_FRAME_EXACT;
     if (exact_ms) *exact_ms = a.exact_ms > 0.0f ? a.exact_ms : 0.0f;
     if (learned_ms) *learned_ms = a.learned_ms > 0.0f ? a.learned_ms : 0.0f;

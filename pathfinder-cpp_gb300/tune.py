@@ -35,7 +35,7 @@ def main() -> None:
         r.upload(scs)
         start = r.tuning()
         best, best_ms, start_ms = r.autotune(frames=args.frames)
-        for _ in range(6):  # the default frame's choice with the tuned parameters
+        for _ in range(7):  # the default frame's choice with the tuned parameters (seven calls decide)
             r.render_auto()
         auto = r.last_auto_choice()
     try:

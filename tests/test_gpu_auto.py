@@ -88,16 +88,20 @@ def test_auto_frame_output_equals_exact_and_keeps_its_choice_across_uploads(pf):
         r.upload(scs)
         r.render()
         want = [(r.canon(i), r.image(i)) for i in range(len(scs))]
-        seen = set()
+        seen, choices = set(), []
         for _ in range(8):
             r.render_auto()
             seen.add(r.last_auto_choice()["last"])
+            choices.append(r.last_auto_choice()["choice"])
             for i in range(len(scs)):
                 got = r.canon(i)
                 for k in TILE_KEYS + LIST_KEYS:
                     assert np.array_equal(got[k], want[i][0][k]), k
                 assert np.array_equal(r.image(i), want[i][1])
         assert seen == {"exact", "learned"}  # both frames were timed
+        # two timed frames of each kind decide: an untimed first exact frame and two timed ones,
+        # an untimed first learned frame, the one that records its graph, two timed replays
+        assert choices[:6] == [None] * 6 and None not in choices[6:]
         settled = r.last_auto_choice()
         assert settled["choice"] is not None and settled["exact_ms"] > 0 and settled["learned_ms"] > 0
         # a new upload of the same scenes keeps the measurements: no exact frame to re-time
