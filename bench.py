@@ -36,6 +36,7 @@ from __future__ import annotations
 import argparse
 import concurrent.futures as cf
 import json
+import math
 import os
 import subprocess
 import sys
@@ -361,7 +362,11 @@ def cpu_baseline(args, scenes_list):
         k = args.cpu_sample if label == "all" else max(4, args.cpu_sample // 4)
         idx = stratified(scenes_list, k) if n > 1 else [0]
         dt = cpu_time(scenes_list, idx, threads)
-        out[label] = {"value": len(idx) / dt, "threads": threads, "scenes": len(idx), "seconds": dt}
+        reps = 1
+        if dt < 2.0:  # a short sample is repeated to about two seconds, so the clock resolves it
+            reps = min(50, int(math.ceil(2.0 / max(dt, 1e-6))))
+            dt = sum(cpu_time(scenes_list, idx, threads) for _ in range(reps)) / reps
+        out[label] = {"value": len(idx) / dt, "threads": threads, "scenes": len(idx), "seconds": dt, "repeats": reps}
     v = out["all"]
     sample = (f"{v['scenes']} of {n} scenes (stratified by paths x canvas side), a pool of {cores} threads over "
               f"the scenes" if n > 1 else f"the whole scene, {cores} threads over paths and framebuffer tiles")
@@ -369,7 +374,8 @@ def cpu_baseline(args, scenes_list):
     return {"value": v["value"], "unit": UNIT, "cores": cores, "kind": "port",
             "sample": sample + "; restated d3d9 tiler + FP64 coverage and src-over composite",
             "by_threads": {k: {"value": o["value"], "paths_per_s": o["value"] * paths_per_scene,
-                               "threads": o["threads"], "scenes": o["scenes"], "seconds": o["seconds"]}
+                               "threads": o["threads"], "scenes": o["scenes"], "seconds": o["seconds"],
+                               "repeats": o["repeats"]}
                            for k, o in out.items()},
             "paths_per_s": v["value"] * paths_per_scene}
 

@@ -390,8 +390,7 @@ int pf_set_host_image(void *ctx, void *host, size_t bytes);
  * returns, as pf_sizer_predict does.  Features and
  * predictions are staged in a fixed device array of 16384 paths (about 0.9 MB, held by every
  * GPU that loads the library until exit); larger n is rejected with PF_ERR_INVALID_ARGUMENT.
- * The first call on a device looks the array up (cudaGetSymbolAddress) - make it before any
- * stream capture.  Calls share the array: calls whose GPU work overlaps race; serialise them.
+ * Calls share the array: calls whose GPU work overlaps race; serialise them.
  * The context must already hold sizer weights.
  */
 int pf_sizer_predict_noalloc(void *ctx, const float *features, uint32_t n, float *out);

@@ -2518,15 +2518,14 @@ int pf_auto_choice(void *ctx, int *last, int *choice, float *exact_ms, float *le
 // variant of pf_sizer_predict stages features and predictions in a fixed, file-scope device
 // array instead of context buffers.  It needs a context that already holds sizer weights
 // (pf_sizer_load / pf_sizer_init, which do allocate, once).  Like pf_sizer_predict it waits
-// on the context's stream for its results before it returns.
+// on the context's stream for its results before it returns.  No counterpart in the reference.
 //
 // Limit: kNoAllocMaxPaths paths per call (the array is (12 + 2) floats per path, about
 // 0.9 MB, and every GPU that loads this library keeps it until the process exits).
 // The first call on a device looks up the array's device address (cudaGetSymbolAddress, with
-// that device current); make that first call before any stream capture.  All calls share the
-// array and it keeps the last call's contents; nothing in it has to start at zero (each call
-// overwrites the rows it uses).  Calls whose GPU work overlaps - from two threads, or on two
-// streams - race on the array: serialise them.
+// that device current).  All calls share the array and it keeps the last call's contents;
+// nothing in it has to start at zero (each call overwrites the rows it uses).  Calls whose GPU
+// work overlaps - from two threads, or on two streams - race on the array: serialise them.
 
 namespace {
 
