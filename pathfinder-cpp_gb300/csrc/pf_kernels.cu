@@ -1522,7 +1522,7 @@ __device__ __forceinline__ void raster_column(const FillPrep &fp, int i, int *D)
 }
 
 // Warp computes the coverage of the 8 pixels of every lane (column lane&15, rows
-// (lane>>4)*8 .. +7) of an alpha tile; D must be zeroed on entry and is left dirty.
+// (lane>>4)*8 .. +7) of an alpha tile; D must be zero on entry and is left zero.
 // Fills are rasterised as (fill, pixel column) work items spread over the lanes, 32 fills
 // at a time, so a tile of a few wide fills still keeps the warp busy.
 // backdrop + the fills' area sums (fixed point) of the warp's 8 pixels per lane, before the fill rule
@@ -1544,7 +1544,9 @@ __device__ __forceinline__ void coverage_raw(const uint2 *src, uint32_t n, int8_
             fp.xr = fmaxf(x0, x1);
             fp.yl = x0 < x1 ? y0 : y1;
             fp.yr = x0 < x1 ? y1 : y0;
-            fp.dydx = (fp.yr - fp.yl) / (fp.xr - fp.xl);
+            // xr - xl >= 1/256 (vertical fills are culled when quantised): the fast divide is
+            // within 2 ulp, far inside the coverage tolerance
+            fp.dydx = __fdividef(fp.yr - fp.yl, fp.xr - fp.xl);
             fp.i0 = max((int)floorf(fp.xl), 0);
             items = max(min((int)ceilf(fp.xr), 16) - fp.i0, 0);
         }
@@ -1576,7 +1578,9 @@ __device__ __forceinline__ void coverage_raw(const uint2 *src, uint32_t n, int8_
     int run = 0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-        run += D[cov_index(h * 8 + k, col)];
+        const int idx = cov_index(h * 8 + k, col);
+        run += D[idx];
+        D[idx] = 0;  // read and clear: the next tile starts from zero cells
         acc[k] = run;
     }
     const int upper = __shfl_sync(0xffffffffu, run, col);  // rows 0..7 total of this column
@@ -1785,6 +1789,7 @@ __global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 3
     if (b.status[kStErr] & (kErrOverflowLeaf | kErrOverflowFill)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int *D = cells[warp];
+    zero_cells(D);  // once: coverage_raw leaves the cells it reads zero
     const int col = lane & 15, h = lane >> 4;
     const float inv255 = 1.0f / 255.0f;
     uint32_t entries = 0, comp_fills = 0, chunks = 0;
@@ -1848,7 +1853,6 @@ __global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 3
                 int raw[8];
                 for (;;) {
                     comp_fills += f1 - f0;
-                    zero_cells(D);
                     coverage_raw(b.fills + f0, f1 - f0, tbd, D, prep[warp], raw);
                     __syncwarp();
                     if (!both) break;
