@@ -1894,24 +1894,29 @@ __global__ void __launch_bounds__(kCompWarps * 32, (kPaint ? 20 : kClip ? 24 : 3
             }
             return stop || __all_sync(0xffffffffu, opaque);
         }, chunks);
+        // the scene's image fields in registers before the stores: a store through the image
+        // pointer may alias the scene table as far as the compiler knows, and would make it
+        // load them again for every pixel
+        const uint32_t img_w = S.img_w, img_h = S.img_h, clear = S.clear;
+        const bool load_dst = S.load == PF_LOAD_LOAD;
+        uchar4 *const img = reinterpret_cast<uchar4 *>(b.image + S.img_offset);
         const uint32_t px = fx * 16 + (uint32_t)col;
-        if (px < S.img_w) {
-            float cr = (float)(S.clear & 0xffu) * inv255, cg = (float)((S.clear >> 8) & 0xffu) * inv255,
-                  cb = (float)((S.clear >> 16) & 0xffu) * inv255, ca = (float)(S.clear >> 24) * inv255;
-            uchar4 *img = reinterpret_cast<uchar4 *>(b.image + S.img_offset);
+        if (px < img_w) {
+            float cr = (float)(clear & 0xffu) * inv255, cg = (float)((clear >> 8) & 0xffu) * inv255,
+                  cb = (float)((clear >> 16) & 0xffu) * inv255, ca = (float)(clear >> 24) * inv255;
 #pragma unroll
             for (int k = 0; k < 8; k++) {
                 const uint32_t py = fy * 16 + (uint32_t)(h * 8 + k);
-                if (py < S.img_h) {
-                    if (S.load == PF_LOAD_LOAD) {
+                if (py < img_h) {
+                    if (load_dst) {
                         // LOAD_ACTION_LOAD (tile.comp:744-757): start from the pixel already there
-                        const uchar4 d = img[(size_t)py * S.img_w + px];
+                        const uchar4 d = img[(size_t)py * img_w + px];
                         cr = (float)d.x * inv255;
                         cg = (float)d.y * inv255;
                         cb = (float)d.z * inv255;
                         ca = (float)d.w * inv255;
                     }
-                    img[(size_t)py * S.img_w + px] =
+                    img[(size_t)py * img_w + px] =
                         make_uchar4((unsigned char)__float2uint_rn(__saturatef(ar[k] + tr[k] * cr) * 255.0f),
                                     (unsigned char)__float2uint_rn(__saturatef(ag[k] + tr[k] * cg) * 255.0f),
                                     (unsigned char)__float2uint_rn(__saturatef(ab[k] + tr[k] * cb) * 255.0f),
