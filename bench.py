@@ -351,22 +351,26 @@ def cpu_time(scenes_list, idx, threads: int) -> float:
     return time.perf_counter() - t0
 
 
+CPU_RUNS = 5  # timed runs of the CPU sample after one warm-up; their median is reported
+
+
 def cpu_baseline(args, scenes_list):
-    """scenes/s of the oracle port at 1 thread, 4 threads and all host threads.  The batched
-    configuration times stratified samples (all threads: --cpu-sample scenes; 1 and 4 threads:
-    a quarter of that); a single scene runs whole."""
+    """scenes/s of the oracle port at 1 thread, 4 threads and all host threads: the median of
+    CPU_RUNS timed runs after one warm-up run.  The batched configuration times stratified
+    samples (all threads: --cpu-sample scenes; 1 and 4 threads: a quarter of that); a single scene
+    runs whole, a run repeating it to at least 0.2 s when one pass is shorter."""
     n = len(scenes_list)
     cores = os.cpu_count() or 1
     out = {}
     for label, threads in (("1", 1), ("4", min(4, cores)), ("all", cores)):
         k = args.cpu_sample if label == "all" else max(4, args.cpu_sample // 4)
         idx = stratified(scenes_list, k) if n > 1 else [0]
-        dt = cpu_time(scenes_list, idx, threads)
-        reps = 1
-        if dt < 2.0:  # a short sample is repeated to about two seconds, so the clock resolves it
-            reps = min(50, int(math.ceil(2.0 / max(dt, 1e-6))))
-            dt = sum(cpu_time(scenes_list, idx, threads) for _ in range(reps)) / reps
-        out[label] = {"value": len(idx) / dt, "threads": threads, "scenes": len(idx), "seconds": dt, "repeats": reps}
+        warm = cpu_time(scenes_list, idx, threads)
+        reps = 1 if warm >= 0.2 else min(50, int(math.ceil(0.2 / max(warm, 1e-6))))
+        runs = sorted(sum(cpu_time(scenes_list, idx, threads) for _ in range(reps)) / reps for _ in range(CPU_RUNS))
+        dt = runs[len(runs) // 2]
+        out[label] = {"value": len(idx) / dt, "threads": threads, "scenes": len(idx), "seconds": dt, "repeats": reps,
+                      "runs_seconds": runs}
     v = out["all"]
     sample = (f"{v['scenes']} of {n} scenes (stratified by paths x canvas side), a pool of {cores} threads over "
               f"the scenes" if n > 1 else f"the whole scene, {cores} threads over paths and framebuffer tiles")
@@ -375,8 +379,9 @@ def cpu_baseline(args, scenes_list):
             "sample": sample + "; restated d3d9 tiler + FP64 coverage and src-over composite",
             "by_threads": {k: {"value": o["value"], "paths_per_s": o["value"] * paths_per_scene,
                                "threads": o["threads"], "scenes": o["scenes"], "seconds": o["seconds"],
-                               "repeats": o["repeats"]}
+                               "repeats": o["repeats"], "runs_seconds": o["runs_seconds"]}
                            for k, o in out.items()},
+            "method": f"median of {CPU_RUNS} timed runs after one warm-up run, per thread count",
             "paths_per_s": v["value"] * paths_per_scene}
 
 
