@@ -10,6 +10,7 @@ without a GPU raises.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 from typing import Dict, List, Optional, Sequence
 
@@ -324,7 +325,7 @@ class Renderer:
             keep.append(k)
         arr = (SceneView * len(views))(*views)
         self._check(self.lib.pf_scene_upload_batch(self.ctx, arr, len(views)), self.ctx)
-        self._sizes = [(int(np.ceil(s.width)), int(np.ceil(s.height))) for s in scenes]
+        self._sizes = [(math.ceil(s.width), math.ceil(s.height)) for s in scenes]
 
     def render(self, first: int = 0, count: Optional[int] = None) -> Dict[str, float]:
         """Exact two-pass frame over uploaded scenes [first, first + count) (default: all)."""
@@ -430,7 +431,7 @@ class Renderer:
         """Upload a batch described by ready-made SceneView structs (host pointers)."""
         arr = (SceneView * len(views))(*views)
         self._check(self.lib.pf_scene_upload_batch(self.ctx, arr, len(views)), self.ctx)
-        self._sizes = [(int(np.ceil(v.width)), int(np.ceil(v.height))) for v in views]
+        self._sizes = [(math.ceil(v.width), math.ceil(v.height)) for v in views]
 
     # -- learned frame and sizer -------------------------------------------------
     def render_learned(self, first: int = 0, count: Optional[int] = None) -> Dict[str, float]:
