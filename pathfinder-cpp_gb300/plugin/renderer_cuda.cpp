@@ -118,7 +118,9 @@ void RendererCuda::draw(const std::shared_ptr<SceneBuilder> &scene_builder, bool
     view.load_action = load ? PF_LOAD_LOAD : PF_LOAD_CLEAR;
     int st = pf_scene_upload(ctx_, &view);
     if (st == PF_OK && load) st = pf_write_image(ctx_, 0, pixels_.data(), pixels_.size());
-    if (st == PF_OK) st = learned_ ? pf_render_learned(ctx_, 0, 1, &stats_) : pf_render(ctx_, &stats_);
+    // the library's default frame: with sizer weights it times the exact and the learned frame
+    // on this scene and keeps the faster; without them it is the exact frame
+    if (st == PF_OK) st = pf_render_auto(ctx_, 0, 1, &stats_);
     if (st == PF_OK) {
         pixels_.resize(w * h * 4);
         st = pf_read_image(ctx_, pixels_.data(), pixels_.size());

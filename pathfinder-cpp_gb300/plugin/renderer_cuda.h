@@ -71,7 +71,8 @@ public:
 
     void draw(const std::shared_ptr<SceneBuilder> &scene_builder, bool clear_dst_texture) override;
 
-    /// Loads learned-sizer weights; draw() then uses the one-pass learned frame.
+    /// Loads learned-sizer weights; draw() then runs the learned one-pass frame wherever it
+    /// measures faster than the exact one (pf_render_auto).
     bool load_sizer(const std::string &path);
 
     /// Statistics of the last frame.
