@@ -412,8 +412,8 @@ __device__ __forceinline__ int seg_bucket(const Batch &b, const SegDev &sg) {
 }
 
 // A fixed grid of kSegBlocks blocks walks the segments grid-stride.  The count pass leaves
-// each block's per-bucket counts in ctl[kSegBuckets * block + bucket]; the starts kernel
-// turns them into each block's first slot per bucket (buckets deepest first); the scatter
+// each block's per-bucket counts in ctl[kSegBuckets * block + bucket]; the totals and starts
+// kernels turn them into each block's first slot per bucket (buckets deepest first); the scatter
 // pass walks the same segments and places them from those slots.  Counters live in shared
 // memory: no global atomics (one hot global counter per bucket serialised millions of them).
 constexpr int kSegBlocks = 1216;  // 8 blocks per SM of 152
@@ -441,24 +441,65 @@ __global__ void __launch_bounds__(kThreads) k_seg_buckets(Batch b, uint32_t *ctl
     if (!kScatter && threadIdx.x < kSegBuckets) ctl[kSegBuckets * blockIdx.x + threadIdx.x] = s_cnt[threadIdx.x];
 }
 
-// Every block's first slot per bucket, buckets deepest first (one thread per bucket).
-__global__ void k_seg_bucket_starts(uint32_t *ctl) {
-    __shared__ uint32_t total[kSegBuckets];
-    const int bk = threadIdx.x;
-    if (bk < kSegBuckets) {
-        uint32_t t = 0;
-        for (int blk = 0; blk < kSegBlocks; blk++) t += ctl[kSegBuckets * blk + bk];
-        total[bk] = t;
-    }
+// Each bucket's total over the blocks (one CTA per bucket), stored after the per-block counts.
+__global__ void __launch_bounds__(kThreads) k_seg_bucket_totals(uint32_t *ctl) {
+    __shared__ uint32_t red[kThreads / 32];
+    const int bk = blockIdx.x, tid = threadIdx.x;
+    uint32_t t = 0;
+    for (int blk = tid; blk < kSegBlocks; blk += kThreads) t += ctl[kSegBuckets * blk + bk];
+    t = __reduce_add_sync(0xffffffffu, t);
+    if ((tid & 31) == 0) red[tid >> 5] = t;
     __syncthreads();
-    if (bk < kSegBuckets) {
-        uint32_t run = 0;
-        for (int d = kSegBuckets - 1; d > bk; d--) run += total[d];
-        for (int blk = 0; blk < kSegBlocks; blk++) {
-            const uint32_t c = ctl[kSegBuckets * blk + bk];
-            ctl[kSegBuckets * blk + bk] = run;
-            run += c;
-        }
+    if (tid == 0) {
+        uint32_t sum = 0;
+        for (int w = 0; w < kThreads / 32; w++) sum += red[w];
+        ctl[kSegBuckets * kSegBlocks + bk] = sum;
+    }
+}
+
+// Every block's first slot per bucket, buckets deepest first (one CTA per bucket): the deeper
+// buckets' totals, then an exclusive scan of the bucket's per-block counts.
+__global__ void __launch_bounds__(kThreads) k_seg_bucket_starts(uint32_t *ctl) {
+    constexpr int kPer = (kSegBlocks + kThreads - 1) / kThreads;  // blocks per thread
+    __shared__ uint32_t red[kThreads / 32];
+    __shared__ uint32_t s_base;
+    const int bk = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t *total = ctl + kSegBuckets * kSegBlocks;
+    uint32_t deeper = 0;
+    for (int k = bk + 1 + tid; k < kSegBuckets; k += kThreads) deeper += total[k];
+    deeper = __reduce_add_sync(0xffffffffu, deeper);
+    if (lane == 0) red[warp] = deeper;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t sum = 0;
+        for (int w = 0; w < kThreads / 32; w++) sum += red[w];
+        s_base = sum;
+    }
+    uint32_t v[kPer];
+    uint32_t own = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+        const int blk = tid * kPer + j;
+        v[j] = blk < kSegBlocks ? ctl[kSegBuckets * blk + bk] : 0u;
+        own += v[j];
+    }
+    uint32_t incl = own;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    __syncthreads();  // red is reused
+    if (lane == 31) red[warp] = incl;
+    __syncthreads();
+    uint32_t before = s_base;
+    for (int w = 0; w < warp; w++) before += red[w];
+    uint32_t run = before + incl - own;
+#pragma unroll
+    for (int j = 0; j < kPer; j++) {
+        const int blk = tid * kPer + j;
+        if (blk < kSegBlocks) ctl[kSegBuckets * blk + bk] = run;
+        run += v[j];
     }
 }
 
@@ -2095,12 +2136,13 @@ cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStre
     return cudaGetLastError();
 }
 
-size_t seg_ctl_bytes() { return size_t(kSegBlocks) * kSegBuckets * 4; }
+size_t seg_ctl_bytes() { return (size_t(kSegBlocks) + 1) * kSegBuckets * 4; }
 
 cudaError_t launch_seg_order(const Batch &b, uint32_t n_segs, uint32_t *ctl, cudaStream_t st) {
     if (!n_segs) return cudaSuccess;
     PF_LAUNCH(k_seg_buckets<false><<<kSegBlocks, kThreads, 0, st>>>(b, ctl));
-    PF_LAUNCH(k_seg_bucket_starts<<<1, kSegBuckets, 0, st>>>(ctl));
+    PF_LAUNCH(k_seg_bucket_totals<<<kSegBuckets, kThreads, 0, st>>>(ctl));
+    PF_LAUNCH(k_seg_bucket_starts<<<kSegBuckets, kThreads, 0, st>>>(ctl));
     PF_LAUNCH(k_seg_buckets<true><<<kSegBlocks, kThreads, 0, st>>>(b, ctl));
     return cudaGetLastError();
 }
