@@ -2449,8 +2449,8 @@ int pf_autotune(void *ctx, uint32_t first, uint32_t count, uint32_t frames, pf_t
     if (start_ms) *start_ms = cur_ms;
     // the candidates of each parameter
     std::vector<std::pair<int, std::vector<float>>> space = {
-        {0, {0, 4, 8, 12, 16, 20, 24}},  // bin_ctas_per_sm[0]
-        {1, {0, 2, 4, 6, 8, 10, 12}},  // bin_ctas_per_sm[1]
+        {0, {0, 4, 8, 12, 16, 20}},  // bin_ctas_per_sm[0]
+        {1, {0, 2, 4, 6, 8}},        // bin_ctas_per_sm[1]
         {2, {0, 1, 2, 3}},            // bin_ctas_per_sm[2]
         {3, {4, 6, 8, 12, 16, 32}},   // long_line
         {4, {0, 1}},                  // bin_concurrent

@@ -892,8 +892,10 @@ __host__ __device__ constexpr uint32_t class_words(int c) { return c == 0 ? 1088
 // 24 per SM).  Class 2 keeps 384 threads: its shared words allow 3 CTAs per SM (256 or 512 threads
 // ran slower).
 __host__ __device__ constexpr int class_threads(int c) { return c == 2 ? 384 : c == 1 ? 128 : 64; }
-// CTAs per SM the register budget is set for (shared memory allows 3 of class 2, 12 of class 1)
-__host__ __device__ constexpr int class_min_ctas(int c) { return c == 2 ? 3 : c == 1 ? 12 : 24; }
+// CTAs per SM the register budget is set for (shared memory allows 3 of class 2, 12 of class 1):
+// class 0 at 20 (48 registers) and class 1 at 8 (64 registers, no spills) beat 24 and 12 at 40
+// registers with 148-208 B of spills (binning 20.00 -> 19.30 ms per 512-scene frame)
+__host__ __device__ constexpr int class_min_ctas(int c) { return c == 2 ? 3 : c == 1 ? 8 : 20; }
 // Fills a CTA stages during its count walk (8 bytes each, in its own slice of a global buffer
 // that stays in L2): the fills are then placed without walking the lines again.  A path with
 // more fills than this walks its lines twice.
