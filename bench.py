@@ -822,7 +822,7 @@ def main():
             "counts": {k: st[k] for k in ("paths", "points", "segments", "microlines", "tiles", "fills",
                                           "alpha_tiles", "visible_tiles", "composite_entries",
                                           "composited_fills", "framebuffer_tiles", "walk_chunks", "host_syncs")},
-            "roofline": {"kernel": "flatten + bin (k_flatten_budget or k_flatten, then k_bin_fused)", "bound": "hbm",
+            "roofline": {"kernel": "flatten + bin (k_flatten_pool or k_flatten, then k_bin_fused)", "bound": "hbm",
                          "achieved": fb_ach, "peak": peak, "unit": "GB/s",
                          "frac": (fb_ach / peak) if fb_ach else None, "traffic": fb_traffic,
                          "traffic_unit": "GB per frame: ncu dram__bytes_read.sum + dram__bytes_write.sum of the "

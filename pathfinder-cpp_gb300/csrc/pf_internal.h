@@ -206,7 +206,8 @@ enum : int {
     kStFill64 = 16,    // two words: fills reserved by the frame's paths (64-bit)
     kStPoolListed = 18,// learned frame: pooled lines listed by path
     kStVisible = 19,   // frame counters: visible tiles of the draw paths (alpha, or a nonzero backdrop)
-    kStCount = 20,
+    kStFlatTicket = 20,// learned frame: groups of 32 segments taken by the flattening warps
+    kStCount = 21,
 };
 
 // Kernels launched by this library (host-side counter, all contexts).

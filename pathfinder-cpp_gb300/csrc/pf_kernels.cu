@@ -17,7 +17,7 @@
 //                                                 writes the lists out for the canonical read-back
 //   fill.comp + tile.comp                      -> k_composite (coverage never leaves the SM)
 //   (learned frame) per-path budgets            -> pf_sizer.cu: k_features, k_mlp_predict, k_budgets;
-//                                                 here k_flatten_budget and the spill-pool lists
+//                                                 here k_flatten_pool and the spill-pool lists
 //
 // Integer outputs follow the reference's d3d9 CPU tiler bit for bit, so every float
 // operation on that path is written with __f*_rn intrinsics (no FMA contraction), in the
@@ -275,13 +275,13 @@ __device__ __forceinline__ float half_lerp(float a, float b) { return fadd(a, fm
 
 template <class Emit>
 __device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, float c1, float c2, float c3,
-                              Emit &&emit, uint32_t *status) {
+                              Emit &&emit, uint32_t *status, int depth0 = 0) {
     float4 sa[kMaxDepth];  // start x, y, first control x, y
     float2 sb[kMaxDepth];  // second control x, y
     uint32_t pending = 0;
     int sp = 0;
     float bb[4] = {b0, b1, b2, b3}, cc[4] = {c0, c1, c2, c3};
-    int depth = 0;
+    int depth = depth0;
     for (;;) {
         if (depth >= kMaxDepth - 1 || flat_cubic(bb, cc)) {
             if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
@@ -335,12 +335,12 @@ __device__ void flatten_cubic(float b0, float b1, float b2, float b3, float c0, 
 
 template <class Emit>
 __device__ void flatten_quad(float b0, float b1, float b2, float b3, float c0, float c1, Emit &&emit,
-                             uint32_t *status) {
+                             uint32_t *status, int depth0 = 0) {
     float4 sa[kMaxDepth];  // start x, y, control x, y
     uint32_t pending = 0;
     int sp = 0;
     float bb[4] = {b0, b1, b2, b3}, cc[2] = {c0, c1};
-    int depth = 0;
+    int depth = depth0;
     for (;;) {
         if (depth >= kMaxDepth - 1 || flat_quad(bb, cc)) {
             if (depth >= kMaxDepth - 1) atomicOr(status, kErrDepth);
@@ -784,90 +784,358 @@ __device__ void walk_line_warp(const WalkCtx &w, float4 f, OnFill &&on_fill, OnD
     }
 }
 
-// Learned frame: flatten one segment and store its leaf lines in the path's leaf region,
-// laid out from the sizer's budget (slots reserved four at a time); lines past the budget
-// spill into the shared pool.  An exhausted pool sets the overflow bit and the frame is
-// redone by the exact two-pass method.
-constexpr int kLeafBatch = 4;
+// Learned frame: flatten the segments and store each path's leaf lines in the path's region,
+// laid out from the sizer's budget; lines past the budget spill into the shared pool, and an
+// exhausted pool sets the overflow bit (the frame is then redone by the exact two-pass method).
+//
+// The bisection is shared by the 32 lanes of a warp.  With one segment per lane (as the exact
+// frame's k_flatten does) a warp runs the split branch and the emit branch of every step one after
+// the other, with only the lanes on one side doing work in each (13 of 32 lanes active on the
+// 512-scene batch, flattening 5.93 ms of the learned frame).  Here the lanes share the work of the
+// warp's segments instead (flattening 4.54 ms):
+//
+// * a split round: each lane takes a pending (not flat) piece from the warp's pool in shared
+//   memory, splits it at t = 0.5, and tests both halves: a flat half (or one at the depth bound)
+//   joins the warp's leaf queue, the other goes back on the pool;
+// * an emit round: each lane takes a queued leaf line and stores it in its path's region: the
+//   segment's first leaf (its leftmost piece) at the segment's own slot, the others at slots
+//   reserved with one atomic per path among the round's lines (lanes grouped by path), lines
+//   past the budget in the spill pool.
+//
+// Every piece is split with the same operations as in the depth-first walk, so the leaf lines
+// are the same lines bit for bit; only their order within a path's region differs, which no
+// output depends on (fills are counted and placed per tile, coverage sums are integers).  The
+// pool is a stack, so it stays near 32 pieces per level of the warp's deepest segments; a half
+// that finds it full is flattened depth first by its lane alone (on the 512-scene batch about
+// 0.02% of the lines).  Warps take their segments 32 at a time, in the bucketed order, from a
+// frame-wide ticket, up to kPoolSets groups in flight: a group's slot in the segment table is
+// reused once no pending piece or queued line refers to it.
+constexpr int kPoolWarps = 2;     // warps per block
+constexpr int kPoolCap = 224;     // pending pieces per warp
+constexpr int kPoolLeafCap = 96;  // queued leaf lines per warp: < 32 before a round, + 2 per lane
+constexpr int kPoolSets = 4;      // groups of 32 segments in flight per warp
+// piece and line tags: bits 0-6 the segment's table entry (group * 32 + lane), bit 7 the
+// segment's leftmost piece, bit 8 a cubic (else a quadratic), bits 9-13 the depth
+constexpr uint32_t kTagEntry = 127u, kTagLeft = 1u << 7, kTagCubic = 1u << 8;
+constexpr int kTagDepthShift = 9;
 
-__global__ void __launch_bounds__(kThreads, 4) k_flatten_budget(Batch b, uint32_t n_segs) {
-    const uint32_t t = global_tid();
-    if (t >= n_segs || t >= b.status[kStSegs]) return;
-    const uint32_t i = b.seg_order ? b.seg_order[t] : t;
-    const SegDev sg = b.segs[i];
-    const uint32_t region = b.path_leaf_first[sg.path], budget = b.path_leaf_budget[sg.path];
-    // the segment's first leaf: the slot of the segment's index within its path (the budget
-    // covers every segment), so a line segment writes without an atomic and consecutive
-    // segments of a path write consecutive slots
-    const uint32_t own = region + (i - b.contour_segs[b.path_contours[sg.path].x]);
-    bool own_done = false;
-    // pending leaves, in registers (an indexed array would live in local memory)
-    float4 q0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), q1 = q0, q2 = q0, q3 = q0;
-    uint32_t npend = 0;
+struct FlattenPool {
+    float4 pend_ends[kPoolCap];   // x0, y0, x1, y1
+    float4 pend_ctrl[kPoolCap];   // first control x, y, second control x, y (quadratic: first only)
+    uint32_t pend_tag[kPoolCap];
+    float4 leaf[kPoolLeafCap];    // x0, y0, x1, y1
+    uint32_t leaf_tag[kPoolLeafCap];
+    uint4 seg[kPoolSets * 32];    // path, region, budget, own slot
+};
+
+// Where a lane stores leaf lines by itself.
+struct LeafSink {
+    float4 *leaves;
+    uint32_t *cursor, *status, *pool_path;
+    uint32_t pool_first, pool_cap;
+};
+
+// A half that found the pool full: flattened depth first from its depth, its lines stored one
+// slot at a time.  Returns the lines it produced.
+__device__ __noinline__ uint32_t flatten_piece_alone(LeafSink out, uint4 sg, float4 ends, float4 ctrl, uint32_t tag) {
+    bool left = (tag & kTagLeft) != 0;
     uint32_t produced = 0;
-    auto flush = [&]() {
-        if (!npend) return;
-        const uint32_t slot = atomicAdd(&b.path_leaf_cursor[sg.path], npend);
-        const uint32_t in_region = slot >= budget ? 0u : min(npend, budget - slot);
-        uint32_t q = 0;
-        if (in_region < npend) {
-            if (slot <= budget && slot + npend > budget) atomicAdd(&b.status[kStPathsOver], 1u);
-            q = atomicAdd(&b.status[kStPoolUsed], npend - in_region);
-        }
-#pragma unroll
-        for (uint32_t k = 0; k < (uint32_t)kLeafBatch; k++) {
-            const float4 v = k == 0 ? q0 : k == 1 ? q1 : k == 2 ? q2 : q3;
-            if (k < in_region) {
-                b.leaves[region + slot + k] = v;
-            } else if (k < npend) {
-                const uint32_t j = q + (k - in_region);
-                if (j < b.leaf_pool_cap) {
-                    b.leaves[b.leaf_pool_first + j] = v;
-                    b.pool_path[j] = sg.path;
-                } else {
-                    atomicOr(&b.status[kStErr], kErrOverflowLeaf);
-                }
-            }
-        }
-        npend = 0;
-    };
     auto emit = [&](float x0, float y0, float x1, float y1) {
         const float4 v = make_float4(x0, y0, x1, y1);
         produced++;
-        if (!own_done) {
-            b.leaves[own] = v;
-            own_done = true;
+        if (left) {
+            out.leaves[sg.w] = v;
+            left = false;
             return;
         }
-        if (npend == 0) q0 = v;
-        else if (npend == 1) q1 = v;
-        else if (npend == 2) q2 = v;
-        else q3 = v;
-        if (++npend == (uint32_t)kLeafBatch) flush();
+        const uint32_t slot = atomicAdd(&out.cursor[sg.x], 1u);
+        if (slot < sg.z) {
+            out.leaves[sg.y + slot] = v;
+            return;
+        }
+        if (slot == sg.z) atomicAdd(&out.status[kStPathsOver], 1u);
+        const uint32_t j = atomicAdd(&out.status[kStPoolUsed], 1u);
+        if (j < out.pool_cap) {
+            out.leaves[out.pool_first + j] = v;
+            out.pool_path[j] = sg.x;
+        } else {
+            atomicOr(&out.status[kStErr], kErrOverflowLeaf);
+        }
     };
-    const float2 p0 = b.points[sg.a];
-    switch (sg.kind) {
-        case kSegLine: {
-            const float2 p1 = b.points[sg.a + 1];
-            emit(p0.x, p0.y, p1.x, p1.y);
-        } break;
-        case kSegClose: {
-            const float2 p1 = b.points[sg.b];
-            emit(p0.x, p0.y, p1.x, p1.y);
-        } break;
-        case kSegQuad: {
-            const float2 c = b.points[sg.a + 1], p2 = b.points[sg.a + 2];
-            flatten_quad(p0.x, p0.y, p2.x, p2.y, c.x, c.y, emit, &b.status[kStErr]);
-        } break;
-        default: {
-            const float2 c0 = b.points[sg.a + 1], c1 = b.points[sg.a + 2], p3 = b.points[sg.a + 3];
-            flatten_cubic(p0.x, p0.y, p3.x, p3.y, c0.x, c0.y, c1.x, c1.y, emit, &b.status[kStErr]);
-        } break;
+    const int depth = (int)(tag >> kTagDepthShift) & 31;
+    if (tag & kTagCubic)
+        flatten_cubic(ends.x, ends.y, ends.z, ends.w, ctrl.x, ctrl.y, ctrl.z, ctrl.w, emit, &out.status[kStErr],
+                      depth);
+    else
+        flatten_quad(ends.x, ends.y, ends.z, ends.w, ctrl.x, ctrl.y, emit, &out.status[kStErr], depth);
+    return produced;
+}
+
+__device__ __forceinline__ bool piece_flat(bool cubic, float4 e, float4 c) {
+    const float bb[4] = {e.x, e.y, e.z, e.w}, cc[4] = {c.x, c.y, c.z, c.w};
+    return cubic ? flat_cubic(bb, cc) : flat_quad(bb, cc);
+}
+
+__global__ void __launch_bounds__(kPoolWarps * 32) k_flatten_pool(Batch b, uint32_t n_segs) {
+    __shared__ FlattenPool pools[kPoolWarps];
+    FlattenPool &W = pools[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    uint32_t *const err = &b.status[kStErr];
+    n_segs = min(n_segs, b.status[kStSegs]);
+    const uint32_t n_groups = (n_segs + 31u) / 32u;
+    // a group of 32 segments: lane 0 takes the ticket, and the lanes read it when they need it,
+    // so the atomic's round trip overlaps the work in between
+    uint32_t ticket = lane == 0 ? atomicAdd(&b.status[kStFlatTicket], 1u) : 0u;
+    auto current_group = [&]() { return __shfl_sync(~0u, ticket, 0); };
+    int top = 0, nleaf = 0;  // pool and queue sizes (the same in every lane)
+    uint32_t produced = 0;
+
+    // An emit round reserves its lines' slots and stores them one round later: the reservation's
+    // round trip overlaps the split rounds in between.  The lines waiting for their slots:
+    bool held = false;                                   // this lane holds one
+    float4 held_line = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t held_path = 0, held_region = 0, held_budget = 0;
+    uint32_t held_first = 0;                             // the reservation's first slot (its leader lane)
+    uint32_t held_count = 0, held_rank = 0;
+    int held_leader = 0;
+    auto store_held = [&]() {
+        const unsigned held_mask = __ballot_sync(~0u, held);
+        if (!held_mask) return;
+        bool spill = false;
+        if (held) {
+            const uint32_t slot = __shfl_sync(held_mask, held_first, held_leader) + held_rank;
+            if (lane == held_leader && held_first <= held_budget && held_first + held_count > held_budget)
+                atomicAdd(&b.status[kStPathsOver], 1u);
+            spill = slot >= held_budget;
+            if (!spill) b.leaves[held_region + slot] = held_line;
+        }
+        const unsigned spill_mask = __ballot_sync(~0u, spill);
+        if (spill_mask) {
+            const int first = __ffs(spill_mask) - 1;
+            uint32_t q = 0;
+            if (lane == first) q = atomicAdd(&b.status[kStPoolUsed], (uint32_t)__popc(spill_mask));
+            q = __shfl_sync(~0u, q, first);
+            if (spill) {
+                const uint32_t j = q + __popc(spill_mask & below);
+                if (j < b.leaf_pool_cap) {
+                    b.leaves[b.leaf_pool_first + j] = held_line;
+                    b.pool_path[j] = held_path;
+                } else {
+                    atomicOr(err, kErrOverflowLeaf);
+                }
+            }
+        }
+        held = false;
+    };
+
+    // n (1..32) queued lines from the top of the queue, one per lane: a segment's leftmost line
+    // goes to the segment's own slot, the others reserve slots (one atomic per path)
+    auto emit_round = [&](int n) {
+        store_held();
+        const bool act = lane < n;
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        uint32_t tag = 0;
+        uint4 sg = make_uint4(0u, 0u, 0u, 0u);
+        if (act) {
+            const int k = nleaf - 1 - lane;
+            v = W.leaf[k];
+            tag = W.leaf_tag[k];
+            sg = W.seg[tag & kTagEntry];
+        }
+        nleaf -= n;
+        produced += act ? 1u : 0u;
+        const bool left = act && (tag & kTagLeft);
+        if (left) b.leaves[sg.w] = v;
+        held = act && !left;
+        const unsigned held_mask = __ballot_sync(~0u, held);
+        if (held) {
+            const unsigned same = __match_any_sync(held_mask, sg.x);
+            held_leader = __ffs(same) - 1;
+            held_count = __popc(same);
+            held_rank = __popc(same & below);
+            if (lane == held_leader) held_first = atomicAdd(&b.path_leaf_cursor[sg.x], held_count);
+            held_line = v;
+            held_path = sg.x;
+            held_region = sg.y;
+            held_budget = sg.z;
+        }
+        __syncwarp();
+    };
+    auto drain = [&]() {
+        while (nleaf >= 32) emit_round(32);
+    };
+
+    for (;;) {
+        drain();
+        if (top < 32 && current_group() < n_groups) {
+            // a table group that no pending piece or queued line refers to
+            uint32_t used = 0;
+            for (int k = lane; k < top; k += 32) used |= 1u << ((W.pend_tag[k] & kTagEntry) >> 5);
+            for (int k = lane; k < nleaf; k += 32) used |= 1u << ((W.leaf_tag[k] & kTagEntry) >> 5);
+            used = __reduce_or_sync(~0u, used);
+            if (used != (1u << kPoolSets) - 1u) {
+                const uint32_t set = __ffs(~used) - 1;
+                const uint32_t t = current_group() * 32u + (uint32_t)lane;
+                const bool valid = t < n_segs;
+                bool is_leaf = false, is_piece = false;
+                float4 ends = make_float4(0.0f, 0.0f, 0.0f, 0.0f), ctrl = ends;
+                uint32_t tag = set * 32u + (uint32_t)lane | kTagLeft;
+                if (valid) {
+                    const uint32_t i = b.seg_order ? b.seg_order[t] : t;
+                    const SegDev sg = b.segs[i];
+                    const uint32_t region = b.path_leaf_first[sg.path];
+                    const uint32_t own = region + (i - b.contour_segs[b.path_contours[sg.path].x]);
+                    W.seg[set * 32u + lane] = make_uint4(sg.path, region, b.path_leaf_budget[sg.path], own);
+                    const float2 p0 = b.points[sg.a];
+                    if (sg.kind == kSegLine || sg.kind == kSegClose) {
+                        const float2 p1 = b.points[sg.kind == kSegLine ? sg.a + 1 : sg.b];
+                        ends = make_float4(p0.x, p0.y, p1.x, p1.y);
+                        is_leaf = true;
+                    } else if (sg.kind == kSegQuad) {
+                        const float2 c = b.points[sg.a + 1], p2 = b.points[sg.a + 2];
+                        ends = make_float4(p0.x, p0.y, p2.x, p2.y);
+                        ctrl = make_float4(c.x, c.y, 0.0f, 0.0f);
+                    } else {
+                        const float2 c0 = b.points[sg.a + 1], c1 = b.points[sg.a + 2], p3 = b.points[sg.a + 3];
+                        ends = make_float4(p0.x, p0.y, p3.x, p3.y);
+                        ctrl = make_float4(c0.x, c0.y, c1.x, c1.y);
+                        tag |= kTagCubic;
+                    }
+                    if (!is_leaf) {
+                        is_leaf = piece_flat(tag & kTagCubic, ends, ctrl);
+                        is_piece = !is_leaf;
+                    }
+                }
+                const unsigned leaf_mask = __ballot_sync(~0u, is_leaf), piece_mask = __ballot_sync(~0u, is_piece);
+                // nleaf < 32 and top < 32 here: the group fits (checked all the same)
+                if (is_leaf) {
+                    const int k = nleaf + __popc(leaf_mask & below);
+                    if (k < kPoolLeafCap) {
+                        W.leaf[k] = ends;
+                        W.leaf_tag[k] = tag;
+                    } else {
+                        atomicOr(err, kErrOverflowLeaf);
+                    }
+                }
+                if (is_piece) {
+                    const int k = top + __popc(piece_mask & below);
+                    if (k < kPoolCap) {
+                        W.pend_ends[k] = ends;
+                        W.pend_ctrl[k] = ctrl;
+                        W.pend_tag[k] = tag;
+                    } else {
+                        atomicOr(err, kErrOverflowLeaf);
+                    }
+                }
+                nleaf = min(nleaf + __popc(leaf_mask), kPoolLeafCap);
+                top = min(top + __popc(piece_mask), kPoolCap);
+                __syncwarp();
+                if (lane == 0) ticket = atomicAdd(&b.status[kStFlatTicket], 1u);
+                drain();
+            }
+        }
+        if (top == 0) {
+            if (nleaf > 0) emit_round(nleaf);
+            if (current_group() >= n_groups) break;
+            continue;
+        }
+
+        // split round: up to 32 pieces from the top of the pool
+        const int n = min(top, 32);
+        const bool act = lane < n;
+        float4 ends = make_float4(0.0f, 0.0f, 0.0f, 0.0f), ctrl = ends;
+        uint32_t tag = 0;
+        if (act) {
+            const int k = top - 1 - lane;
+            ends = W.pend_ends[k];
+            ctrl = W.pend_ctrl[k];
+            tag = W.pend_tag[k];
+        }
+        top -= n;
+        __syncwarp();
+        const bool cubic = (tag & kTagCubic) != 0;
+        float4 e0 = ends, c0 = ctrl, e1 = ends, c1 = ctrl;  // first and second halves
+        if (cubic) {
+            const float p01x = half_lerp(ends.x, ctrl.x), p01y = half_lerp(ends.y, ctrl.y);
+            const float p12x = half_lerp(ctrl.x, ctrl.z), p12y = half_lerp(ctrl.y, ctrl.w);
+            const float p23x = half_lerp(ctrl.z, ends.z), p23y = half_lerp(ctrl.w, ends.w);
+            const float p012x = half_lerp(p01x, p12x), p012y = half_lerp(p01y, p12y);
+            const float p123x = half_lerp(p12x, p23x), p123y = half_lerp(p12y, p23y);
+            const float mx = half_lerp(p012x, p123x), my = half_lerp(p012y, p123y);
+            e0 = make_float4(ends.x, ends.y, mx, my);
+            c0 = make_float4(p01x, p01y, p012x, p012y);
+            e1 = make_float4(mx, my, ends.z, ends.w);
+            c1 = make_float4(p123x, p123y, p23x, p23y);
+        } else {
+            const float ax = fadd(ends.x, fmul(fsub(ctrl.x, ends.x), 0.5f));
+            const float ay = fadd(ends.y, fmul(fsub(ctrl.y, ends.y), 0.5f));
+            const float qx = fadd(ctrl.x, fmul(fsub(ends.z, ctrl.x), 0.5f));
+            const float qy = fadd(ctrl.y, fmul(fsub(ends.w, ctrl.y), 0.5f));
+            const float mx = fadd(ax, fmul(fsub(qx, ax), 0.5f)), my = fadd(ay, fmul(fsub(qy, ay), 0.5f));
+            e0 = make_float4(ends.x, ends.y, mx, my);
+            c0 = make_float4(ax, ay, 0.0f, 0.0f);
+            e1 = make_float4(mx, my, ends.z, ends.w);
+            c1 = make_float4(qx, qy, 0.0f, 0.0f);
+        }
+        const uint32_t depth = ((tag >> kTagDepthShift) & 31u) + 1u;
+        const bool deep = depth >= (uint32_t)(kMaxDepth - 1);
+        if (act && deep) atomicOr(err, kErrDepth);
+        const uint32_t tag0 = (tag & ~(31u << kTagDepthShift)) | depth << kTagDepthShift;
+        const uint32_t tag1 = tag0 & ~kTagLeft;
+        const bool leaf0 = act && (deep || piece_flat(cubic, e0, c0));
+        const bool leaf1 = act && (deep || piece_flat(cubic, e1, c1));
+        const unsigned l0 = __ballot_sync(~0u, leaf0), l1 = __ballot_sync(~0u, leaf1);
+        // nleaf < 32 before the round, so at most 31 + 64 lines are queued after it (the
+        // bounds checks below never fail; a failure would send the frame to the exact redo)
+        if (leaf0) {
+            const int k = nleaf + __popc(l0 & below);
+            if (k < kPoolLeafCap) {
+                W.leaf[k] = e0;
+                W.leaf_tag[k] = tag0;
+            } else {
+                atomicOr(err, kErrOverflowLeaf);
+            }
+        }
+        if (leaf1) {
+            const int k = nleaf + __popc(l0) + __popc(l1 & below);
+            if (k < kPoolLeafCap) {
+                W.leaf[k] = e1;
+                W.leaf_tag[k] = tag1;
+            } else {
+                atomicOr(err, kErrOverflowLeaf);
+            }
+        }
+        nleaf = min(nleaf + __popc(l0) + __popc(l1), kPoolLeafCap);
+        // halves that are not flat go back on the pool, the second below the first
+        const bool keep0 = act && !leaf0, keep1 = act && !leaf1;
+        const unsigned m0 = __ballot_sync(~0u, keep0), m1 = __ballot_sync(~0u, keep1);
+        const int k1 = top + __popc(m1 & below), k0 = top + __popc(m1) + __popc(m0 & below);
+        if (keep1) {
+            if (k1 < kPoolCap) {
+                W.pend_ends[k1] = e1;
+                W.pend_ctrl[k1] = c1;
+                W.pend_tag[k1] = tag1;
+            }
+        }
+        if (keep0) {
+            if (k0 < kPoolCap) {
+                W.pend_ends[k0] = e0;
+                W.pend_ctrl[k0] = c0;
+                W.pend_tag[k0] = tag0;
+            }
+        }
+        top = min(top + __popc(m0) + __popc(m1), kPoolCap);
+        if ((keep1 && k1 >= kPoolCap) || (keep0 && k0 >= kPoolCap)) {
+            const LeafSink out{b.leaves, b.path_leaf_cursor, b.status, b.pool_path, b.leaf_pool_first, b.leaf_pool_cap};
+            if (keep1 && k1 >= kPoolCap) produced += flatten_piece_alone(out, W.seg[tag1 & kTagEntry], e1, c1, tag1);
+            if (keep0 && k0 >= kPoolCap) produced += flatten_piece_alone(out, W.seg[tag0 & kTagEntry], e0, c0, tag0);
+        }
+        __syncwarp();
     }
-    flush();
-    const unsigned active = __activemask();
-    const uint32_t total = __reduce_add_sync(active, produced);
-    if ((int)(threadIdx.x & 31) == __ffs(active) - 1) atomicAdd(&b.status[kStLeafCount], total);
+    store_held();
+    const uint32_t total = __reduce_add_sync(~0u, produced);
+    if (lane == 0) atomicAdd(&b.status[kStLeafCount], total);
 }
 
 // ---------------------------------------------------------------------------
@@ -2149,8 +2417,19 @@ cudaError_t launch_seg_order(const Batch &b, uint32_t n_segs, uint32_t *ctl, cud
     return cudaGetLastError();
 }
 
+// The warp-shared flattening runs as many blocks as fit on every SM (they take segments by
+// ticket), fewer when the frame has fewer groups of 32 segments than resident warps.
 cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t st) {
-    if (n_segs) PF_LAUNCH(k_flatten_budget<<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
+    if (!n_segs) return cudaSuccess;
+    int dev = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_flatten_pool, kPoolWarps * 32, 0);
+    if (e != cudaSuccess) return e;
+    const uint64_t groups = (uint64_t(n_segs) + 31) / 32;
+    const uint64_t blocks = std::min<uint64_t>(uint64_t(std::max(1, per_sm)) * uint64_t(sms),
+                                               (groups + kPoolWarps - 1) / kPoolWarps);
+    PF_LAUNCH(k_flatten_pool<<<(unsigned)blocks, kPoolWarps * 32, 0, st>>>(b, n_segs));
     return cudaGetLastError();
 }
 

@@ -145,7 +145,7 @@ __global__ void k_features(Batch b, const uint2 *path_contours, const float4 *cf
 // Per-path leaf budget (and fill estimate) from the sizer's prediction:
 // budget = ceil(expm1(prediction) * mul + add), and at least the path's segment count: every
 // segment yields at least one leaf, and a segment's first leaf goes to the slot of its own
-// index in the path's region (k_flatten_budget), so the region's write cursor starts past them.
+// index in the path's region (k_flatten_pool), so the region's write cursor starts past them.
 __global__ void k_budgets(Batch b, const float *pred, float mul, float add, uint32_t *leaf_budget,
                           uint32_t *fill_budget, uint32_t *leaf_cursor) {
     const uint32_t p = global_tid();
