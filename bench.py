@@ -36,6 +36,7 @@ from __future__ import annotations
 
 import argparse
 import concurrent.futures as cf
+import gc
 import json
 import math
 import os
@@ -70,6 +71,18 @@ CONFIG_DESC = {
        "the canvas), canvas side in {256,512,1024,2048}, seeds 1000+i",
     5: "config 5: held-out mixed scene, 8,192 paths of the three families at 4096x4096, seed 7",
 }
+
+
+class no_gc:
+    """Python's garbage collector off for a timed region (as timeit does)."""
+
+    def __enter__(self):
+        self.was = gc.isenabled()
+        gc.disable()
+
+    def __exit__(self, *exc):
+        if self.was:
+            gc.enable()
 
 
 def replica_first_seed(rank: int) -> int:
@@ -504,31 +517,35 @@ def main():
     def timed(fn, steps):
         """Mean ms per step on the device.  Batched: the steps back to back between two events
         (the working set is far larger than L2).  Single scenes: each step between its own
-        events, with an L2 flush before each step outside them."""
+        events, with an L2 flush before each step outside them.  Python's garbage collector is
+        off inside (a collection would land in a step's host time)."""
         barrier()
         torch.cuda.synchronize()
         out = []
+        with no_gc():
+            ms = timed_steps(fn, steps, out)
+        barrier()
+        return max_over_ranks(ms, dist, "cuda"), out
+
+    def timed_steps(fn, steps, out):
         if flush is None:
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            out = [fn() for _ in range(steps)]
+            out.extend(fn() for _ in range(steps))
             e1.record(stream)
             torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / steps
-        else:
-            ms = 0.0
-            for _ in range(steps):
-                with torch.cuda.stream(stream):
-                    flush.zero_()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                out.append(fn())
-                e1.record(stream)
-                torch.cuda.synchronize()
-                ms += e0.elapsed_time(e1)
-            ms /= steps
-        barrier()
-        return max_over_ranks(ms, dist, "cuda"), out
+            return e0.elapsed_time(e1) / steps
+        ms = 0.0
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out.append(fn())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+        return ms / steps
 
     learned = os.path.exists(pfcuda.DEFAULT_WEIGHTS)
     if learned:
@@ -622,10 +639,11 @@ def main():
         barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        block(steps)
-        e1.record(stream)
-        torch.cuda.synchronize()
+        with no_gc():
+            e0.record(stream)
+            block(steps)
+            e1.record(stream)
+            torch.cuda.synchronize()
         barrier()
         return max_over_ranks(e0.elapsed_time(e1) / steps, dist, "cuda")
     # E2E_BLOCKS blocks of `steps` steps each, the fastest reported (every block is timed whole,

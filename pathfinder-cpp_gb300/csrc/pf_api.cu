@@ -1169,7 +1169,7 @@ int render_exact(Ctx *c, uint32_t first, uint32_t count, pf_frame_stats *stats) 
     c->n_leaves = c->h_status[kStLeaves];
     PF_CUDA(c->leaves.ensure(size_t(c->n_leaves) * 16 + 16));
     b = make_batch(c);
-    PF_CUDA(launch_flatten(b, c->n_segs, true, st));
+    PF_CUDA(launch_flatten(b, c->n_segs, true, st, c->n_leaves));
     record(c, 2);
 
     // 3. binning (one CTA per path: counts, backdrops, fill offsets, fills grouped by tile),

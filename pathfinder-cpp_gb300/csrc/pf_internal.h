@@ -295,7 +295,7 @@ cudaError_t launch_normalize(const Batch &b, uint2 *path_contours, cudaStream_t 
 cudaError_t launch_path_setup(const Batch &b, const uint2 *path_contours, cudaStream_t st);
 cudaError_t launch_path_offsets(const Batch &b, cudaStream_t st);
 cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st);
-cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st);
+cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st, uint64_t n_lines = 0);
 cudaError_t launch_rows(const Batch &b, bool write, cudaStream_t st);
 cudaError_t launch_composite(const Batch &b, cudaStream_t st);  // b.comp_ticket picks the grid
 // fb_scene[t] = the scene of framebuffer tile t, for every uploaded scene (at upload).

@@ -825,7 +825,8 @@ struct FlattenPool {
     uint32_t pend_tag[kPoolCap];
     float4 leaf[kPoolLeafCap];    // x0, y0, x1, y1
     uint32_t leaf_tag[kPoolLeafCap];
-    uint4 seg[kPoolSets * 32];    // path, region, budget, own slot
+    uint4 seg[kPoolSets * 32];    // learned frame: path, region, budget, own slot; exact frame:
+                                  // the segment's first leaf slot and its lines stored so far
 };
 
 // Where a lane stores leaf lines by itself.
@@ -871,17 +872,39 @@ __device__ __noinline__ uint32_t flatten_piece_alone(LeafSink out, uint4 sg, flo
     return produced;
 }
 
+// The same for the exact frame: the segment's lines go to its range of the leaf buffer (from the
+// count pass), the next slot taken from the segment's counter in the warp's table.
+__device__ __noinline__ void flatten_piece_alone_exact(float4 *leaves, uint32_t leaf_cap, uint32_t *status,
+                                                       uint32_t *stored, uint32_t first, float4 ends, float4 ctrl,
+                                                       uint32_t tag) {
+    auto emit = [&](float x0, float y0, float x1, float y1) {
+        const uint32_t idx = first + atomicAdd(stored, 1u);
+        if (idx < leaf_cap) leaves[idx] = make_float4(x0, y0, x1, y1);
+        else atomicOr(&status[kStErr], kErrOverflowLeaf);
+    };
+    const int depth = (int)(tag >> kTagDepthShift) & 31;
+    if (tag & kTagCubic)
+        flatten_cubic(ends.x, ends.y, ends.z, ends.w, ctrl.x, ctrl.y, ctrl.z, ctrl.w, emit, &status[kStErr], depth);
+    else
+        flatten_quad(ends.x, ends.y, ends.z, ends.w, ctrl.x, ctrl.y, emit, &status[kStErr], depth);
+}
+
 __device__ __forceinline__ bool piece_flat(bool cubic, float4 e, float4 c) {
     const float bb[4] = {e.x, e.y, e.z, e.w}, cc[4] = {c.x, c.y, c.z, c.w};
     return cubic ? flat_cubic(bb, cc) : flat_quad(bb, cc);
 }
 
+template <bool kExact>
 __global__ void __launch_bounds__(kPoolWarps * 32) k_flatten_pool(Batch b, uint32_t n_segs) {
     __shared__ FlattenPool pools[kPoolWarps];
     FlattenPool &W = pools[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
     uint32_t *const err = &b.status[kStErr];
+    if (kExact && b.status[kStLeaves] > b.leaf_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, kErrOverflowLeaf);
+        return;
+    }
     n_segs = min(n_segs, b.status[kStSegs]);
     const uint32_t n_groups = (n_segs + 31u) / 32u;
     // a group of 32 segments: lane 0 takes the ticket, and the lanes read it when they need it,
@@ -932,6 +955,35 @@ __global__ void __launch_bounds__(kPoolWarps * 32) k_flatten_pool(Batch b, uint3
     // n (1..32) queued lines from the top of the queue, one per lane: a segment's leftmost line
     // goes to the segment's own slot, the others reserve slots (one atomic per path)
     auto emit_round = [&](int n) {
+        if constexpr (kExact) {
+            // exact frame: each segment's lines fill its counted range, slots taken from the
+            // segment's counter by one lane per segment among the round's lines
+            const bool act = lane < n;
+            float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            uint32_t entry = 0;
+            if (act) {
+                const int k = nleaf - 1 - lane;
+                v = W.leaf[k];
+                entry = W.leaf_tag[k] & kTagEntry;
+            }
+            nleaf -= n;
+            const unsigned act_mask = __ballot_sync(~0u, act);
+            if (act) {
+                const unsigned same = __match_any_sync(act_mask, entry);
+                const int leader = __ffs(same) - 1;
+                uint32_t stored = 0;
+                if (lane == leader) {
+                    stored = W.seg[entry].y;
+                    W.seg[entry].y = stored + __popc(same);
+                }
+                stored = __shfl_sync(act_mask, stored, leader);
+                const uint32_t idx = W.seg[entry].x + stored + __popc(same & below);
+                if (idx < b.leaf_cap) b.leaves[idx] = v;
+                else atomicOr(err, kErrOverflowLeaf);
+            }
+            __syncwarp();
+            return;
+        }
         store_held();
         const bool act = lane < n;
         float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -984,9 +1036,13 @@ __global__ void __launch_bounds__(kPoolWarps * 32) k_flatten_pool(Batch b, uint3
                 if (valid) {
                     const uint32_t i = b.seg_order ? b.seg_order[t] : t;
                     const SegDev sg = b.segs[i];
-                    const uint32_t region = b.path_leaf_first[sg.path];
-                    const uint32_t own = region + (i - b.contour_segs[b.path_contours[sg.path].x]);
-                    W.seg[set * 32u + lane] = make_uint4(sg.path, region, b.path_leaf_budget[sg.path], own);
+                    if constexpr (kExact) {
+                        W.seg[set * 32u + lane] = make_uint4(b.seg_leaves[i], 0u, 0u, 0u);
+                    } else {
+                        const uint32_t region = b.path_leaf_first[sg.path];
+                        const uint32_t own = region + (i - b.contour_segs[b.path_contours[sg.path].x]);
+                        W.seg[set * 32u + lane] = make_uint4(sg.path, region, b.path_leaf_budget[sg.path], own);
+                    }
                     const float2 p0 = b.points[sg.a];
                     if (sg.kind == kSegLine || sg.kind == kSegClose) {
                         const float2 p1 = b.points[sg.kind == kSegLine ? sg.a + 1 : sg.b];
@@ -1127,15 +1183,31 @@ __global__ void __launch_bounds__(kPoolWarps * 32) k_flatten_pool(Batch b, uint3
         }
         top = min(top + __popc(m0) + __popc(m1), kPoolCap);
         if ((keep1 && k1 >= kPoolCap) || (keep0 && k0 >= kPoolCap)) {
-            const LeafSink out{b.leaves, b.path_leaf_cursor, b.status, b.pool_path, b.leaf_pool_first, b.leaf_pool_cap};
-            if (keep1 && k1 >= kPoolCap) produced += flatten_piece_alone(out, W.seg[tag1 & kTagEntry], e1, c1, tag1);
-            if (keep0 && k0 >= kPoolCap) produced += flatten_piece_alone(out, W.seg[tag0 & kTagEntry], e0, c0, tag0);
+            if constexpr (kExact) {
+                if (keep1 && k1 >= kPoolCap) {
+                    uint4 &sg = W.seg[tag1 & kTagEntry];
+                    flatten_piece_alone_exact(b.leaves, b.leaf_cap, b.status, &sg.y, sg.x, e1, c1, tag1);
+                }
+                if (keep0 && k0 >= kPoolCap) {
+                    uint4 &sg = W.seg[tag0 & kTagEntry];
+                    flatten_piece_alone_exact(b.leaves, b.leaf_cap, b.status, &sg.y, sg.x, e0, c0, tag0);
+                }
+            } else {
+                const LeafSink out{b.leaves, b.path_leaf_cursor, b.status, b.pool_path, b.leaf_pool_first,
+                                   b.leaf_pool_cap};
+                if (keep1 && k1 >= kPoolCap)
+                    produced += flatten_piece_alone(out, W.seg[tag1 & kTagEntry], e1, c1, tag1);
+                if (keep0 && k0 >= kPoolCap)
+                    produced += flatten_piece_alone(out, W.seg[tag0 & kTagEntry], e0, c0, tag0);
+            }
         }
         __syncwarp();
     }
-    store_held();
-    const uint32_t total = __reduce_add_sync(~0u, produced);
-    if (lane == 0) atomicAdd(&b.status[kStLeafCount], total);
+    if constexpr (!kExact) {
+        store_held();
+        const uint32_t total = __reduce_add_sync(~0u, produced);
+        if (lane == 0) atomicAdd(&b.status[kStLeafCount], total);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -2399,10 +2471,48 @@ cudaError_t launch_contour_segments(const Batch &b, bool write, cudaStream_t st)
     return cudaGetLastError();
 }
 
-cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st) {
+// The warp-shared flattening runs as many blocks as fit on every SM (they take segments by
+// ticket), fewer when the frame has fewer groups of 32 segments than resident warps.
+template <bool kExact>
+static cudaError_t flatten_pool_blocks(uint64_t *resident) {
+    int dev = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_flatten_pool<kExact>, kPoolWarps * 32, 0);
+    *resident = uint64_t(std::max(1, per_sm)) * uint64_t(sms);
+    return e;
+}
+
+template <bool kExact>
+static cudaError_t launch_flatten_pool(const Batch &b, uint32_t n_segs, cudaStream_t st) {
+    uint64_t resident = 0;
+    if (const cudaError_t e = flatten_pool_blocks<kExact>(&resident)) return e;
+    const uint64_t groups = (uint64_t(n_segs) + 31) / 32;
+    const uint64_t blocks = std::min<uint64_t>(resident, (groups + kPoolWarps - 1) / kPoolWarps);
+    PF_LAUNCH(k_flatten_pool<kExact><<<(unsigned)blocks, kPoolWarps * 32, 0, st>>>(b, n_segs));
+    return cudaGetLastError();
+}
+
+// Exact frame: the count pass one segment per thread (it stores nothing, so its stack stays in
+// L1).  The write pass is shared by the lanes of a warp when the segments bisect deeply enough
+// and are many enough to give every resident warp a group of 32; otherwise one segment per
+// thread keeps more of them in flight (GB300, exact frames: 512-scene batch, 51 lines per
+// segment, 38.28 -> 34.48 ms with the shared pass; 20,000 paths, 25 per segment, 2.28 -> 2.10 ms;
+// 150,000 glyphs, 2.3 per segment, 2.29 -> 2.37 ms; 240 paths, 4,062 segments, 0.445 -> 0.453 ms).
+constexpr uint64_t kPoolMinLinesPerSeg = 8;
+
+cudaError_t launch_flatten(const Batch &b, uint32_t n_segs, bool write, cudaStream_t st, uint64_t n_lines) {
     if (!n_segs) return cudaSuccess;
-    if (write) PF_LAUNCH(k_flatten<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
-    else PF_LAUNCH(k_flatten<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
+    if (write) {
+        uint64_t resident = 0;
+        if (const cudaError_t e = flatten_pool_blocks<true>(&resident)) return e;
+        if (n_lines >= kPoolMinLinesPerSeg * n_segs && n_segs >= resident * kPoolWarps * 32)
+            return launch_flatten_pool<true>(b, n_segs, st);
+        PF_LAUNCH(k_flatten<true><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
+        return cudaGetLastError();
+    }
+    PF_LAUNCH(k_flatten<false><<<grid_for(n_segs), kThreads, 0, st>>>(b, n_segs));
     return cudaGetLastError();
 }
 
@@ -2417,20 +2527,9 @@ cudaError_t launch_seg_order(const Batch &b, uint32_t n_segs, uint32_t *ctl, cud
     return cudaGetLastError();
 }
 
-// The warp-shared flattening runs as many blocks as fit on every SM (they take segments by
-// ticket), fewer when the frame has fewer groups of 32 segments than resident warps.
 cudaError_t launch_flatten_budget(const Batch &b, uint32_t n_segs, cudaStream_t st) {
     if (!n_segs) return cudaSuccess;
-    int dev = 0, sms = 152, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_flatten_pool, kPoolWarps * 32, 0);
-    if (e != cudaSuccess) return e;
-    const uint64_t groups = (uint64_t(n_segs) + 31) / 32;
-    const uint64_t blocks = std::min<uint64_t>(uint64_t(std::max(1, per_sm)) * uint64_t(sms),
-                                               (groups + kPoolWarps - 1) / kPoolWarps);
-    PF_LAUNCH(k_flatten_pool<<<(unsigned)blocks, kPoolWarps * 32, 0, st>>>(b, n_segs));
-    return cudaGetLastError();
+    return launch_flatten_pool<false>(b, n_segs, st);
 }
 
 cudaError_t launch_bin_classify(const Batch &b, bool learned, cudaStream_t st) {
