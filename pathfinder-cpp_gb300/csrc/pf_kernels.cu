@@ -784,9 +784,12 @@ __device__ void walk_line_warp(const WalkCtx &w, float4 f, OnFill &&on_fill, OnD
     }
 }
 
-// Learned frame: flatten the segments and store each path's leaf lines in the path's region,
-// laid out from the sizer's budget; lines past the budget spill into the shared pool, and an
-// exhausted pool sets the overflow bit (the frame is then redone by the exact two-pass method).
+// Flattening shared by the lanes of a warp, for both frames:
+// * learned frame (kExact false): each path's leaf lines go to the path's region, laid out from
+//   the sizer's budget; lines past the budget spill into the shared pool, and an exhausted pool
+//   sets the overflow bit (the frame is then redone by the exact two-pass method);
+// * exact frame's write pass (kExact true): each segment's lines go to its range of the leaf
+//   buffer, counted by the count pass.
 //
 // The bisection is shared by the 32 lanes of a warp.  With one segment per lane (as the exact
 // frame's k_flatten does) a warp runs the split branch and the emit branch of every step one after
@@ -797,17 +800,19 @@ __device__ void walk_line_warp(const WalkCtx &w, float4 f, OnFill &&on_fill, OnD
 // * a split round: each lane takes a pending (not flat) piece from the warp's pool in shared
 //   memory, splits it at t = 0.5, and tests both halves: a flat half (or one at the depth bound)
 //   joins the warp's leaf queue, the other goes back on the pool;
-// * an emit round: each lane takes a queued leaf line and stores it in its path's region: the
-//   segment's first leaf (its leftmost piece) at the segment's own slot, the others at slots
-//   reserved with one atomic per path among the round's lines (lanes grouped by path), lines
-//   past the budget in the spill pool.
+// * an emit round: each lane takes a queued leaf line and stores it.  Learned frame: the
+//   segment's first leaf (its leftmost piece) at the segment's own slot in its path's region, the
+//   others at slots reserved with one atomic per path among the round's lines (lanes grouped by
+//   path) and stored one round later, so that the atomic's round trip overlaps the next split
+//   round; lines past the budget go to the spill pool.  Exact frame: at the next slots of the
+//   segment's range, from a counter in the warp's segment table (no global atomics).
 //
 // Every piece is split with the same operations as in the depth-first walk, so the leaf lines
 // are the same lines bit for bit; only their order within a path's region differs, which no
 // output depends on (fills are counted and placed per tile, coverage sums are integers).  The
 // pool is a stack, so it stays near 32 pieces per level of the warp's deepest segments; a half
-// that finds it full is flattened depth first by its lane alone (on the 512-scene batch about
-// 0.02% of the lines).  Warps take their segments 32 at a time, in the bucketed order, from a
+// that finds it full is flattened depth first by its lane alone (about 0.02% of the lines of the
+// 512-scene batch, in a CPU model of this kernel).  Warps take their segments 32 at a time, in the bucketed order, from a
 // frame-wide ticket, up to kPoolSets groups in flight: a group's slot in the segment table is
 // reused once no pending piece or queued line refers to it.
 constexpr int kPoolWarps = 2;     // warps per block
